@@ -1,0 +1,157 @@
+/* supermc_gb300 -- C ABI of the GB300 (sm_103a) initial-condition engine.
+ *
+ * Drop-in boundary for superMC's per-event path.  In the reference the path
+ * sits behind two C++ classes called from main() (src/main.cpp:35-61):
+ *   MakeDensity(ParameterReader*)               src/MakeDensity.h:43
+ *     generateEccTable / generate_profile_ebe / generate_profile_average /
+ *     dumpEccentricities                         src/MakeDensity.h:53-57
+ *   MCnucl(ParameterReader*)                    src/MCnucl.h:87
+ *     generateNuclei, getBinaryCollision, CentralityCut, calculateThickness,
+ *     setDensity, getTA1/getTA2/getRho, rotateGrid, makeTable
+ *                                               src/MCnucl.h:94-130
+ * Each entry point below names the reference call(s) it replaces.  All
+ * functions return an smc_status; none calls exit() (the reference exits on
+ * a missing parameter, a zero dN/dy or a KLN table overflow,
+ * src/ParameterReader.cpp:195, src/MCnucl.cpp:812-816, :665-670).
+ *
+ * Threading: one context per host thread at a time; calls on one context
+ * are serialised on the context's CUDA stream.  Host pointers are borrowed
+ * for the duration of the call.  Device buffers are owned by the context.
+ */
+#ifndef SUPERMC_GB300_H
+#define SUPERMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int smc_status;
+enum {
+  SMC_OK = 0,
+  SMC_ERR_ARGUMENT = 1,     /* bad pointer / size / order range            */
+  SMC_ERR_CONFIG = 2,       /* unsupported or inconsistent parameters       */
+  SMC_ERR_RETRY_CAP = 3,    /* event retry loop hit its cap (reference loops
+                               forever, src/MakeDensity.cpp:2147-2162)      */
+  SMC_ERR_KLN_TABLE = 4,    /* thickness beyond the dN/dy table
+                               (src/MCnucl.cpp:424-428, :665-670)           */
+  SMC_ERR_ZERO_DNDY = 5,    /* integrated density is zero (MCnucl.cpp:812)  */
+  SMC_ERR_CAPACITY = 6,     /* a per-event buffer (collisions) overflowed   */
+  SMC_ERR_CUDA = 7,         /* CUDA runtime error                           */
+  SMC_ERR_NO_DEVICE = 8     /* no usable GPU                                */
+};
+
+/* Physics and grid configuration: the parameters.dat keys of the path
+ * (reference parameters.dat, read by src/ParameterReader.cpp), plus
+ * optional overrides for values the reference hard-codes (<= 0 keeps the
+ * reference value). */
+typedef struct smc_params {
+  int which_mc_model;       /* 5 = MC-Glauber, 1 = MC-KLN, 7 = sqrt(T_A T_B)  */
+  int sub_model;            /* Glauber: 1 classical, 2 Heinz-Qiu-Moreland;
+                               KLN: 7                                        */
+  int shape_of_nucleons;    /* 1 disk, 2 Gaussian from sigma, 4 user width  */
+  int shape_of_entropy;     /* 1 disk, 2 Gaussian                           */
+  int collision_criterion;  /* 1 disk (d^2 <= sigma/pi), 2 Gaussian profile */
+  int Aproj, Atarg;         /* mass numbers (1 = p, 2 = d, else Woods-Saxon)*/
+  int proj_deformed, targ_deformed;
+  double ecm;               /* sqrt(s) [GeV]; sigma_in from Regge fits      */
+  double alpha;             /* (1-alpha)/2 WN + alpha BC                    */
+  double gauss_nucl_width;  /* width for shape_of_nucleons = 4 [fm]        */
+  double quark_width;       /* valence-quark box width [fm]                 */
+  double lambda;            /* KLN saturation exponent                      */
+  double bmin, bmax;        /* impact-parameter range [fm]                  */
+  int npmin, npmax;         /* Npart acceptance                             */
+  double maxx, maxy, dx, dy;/* grid half-width and spacing [fm]             */
+  double final_factor;      /* finalFactor                                  */
+  int tmax, tmax_subdivision; /* KLN dN/dy table size                       */
+  int ecc_from_order, ecc_to_order;
+  /* extensions (<= 0: reference value) */
+  double proj_R, proj_a, targ_R, targ_a; /* Woods-Saxon radius/diffuseness  */
+  double proj_d_min, targ_d_min;         /* hard-core distance              */
+  double sigin_override;                 /* sigma_in [mb]                   */
+  int kln_npt, kln_nkt, kln_nphi;        /* KLN table quadrature nodes      */
+  uint64_t seed;                         /* Philox key                      */
+  int max_attempts;                      /* event retry cap (0: 100000)     */
+  int max_collisions;                    /* per-event collision capacity
+                                            (0: 4096)                       */
+} smc_params;
+
+/* Derived constants (MCnucl::MCnucl, src/MCnucl.cpp:22-154). */
+typedef struct smc_info {
+  int nx, ny;               /* Maxx, Maxy                                   */
+  double sigin;             /* inelastic NN cross section [mb]              */
+  double dsq;               /* 0.1 sigma_in / pi [fm^2]                     */
+  double width;             /* nucleon width [fm]                           */
+  double sigma_gg;          /* Gaussian-profile cross section [fm^2]        */
+  int kln_tmax;             /* subdivided table size                        */
+  double kln_dT;            /* table thickness step [fm^-2]                 */
+  int A, B;                 /* nucleons per nucleus                         */
+} smc_info;
+
+/* Per-event results.  Every pointer may be NULL (not produced).  When
+ * `device` is non-zero the pointers are device memory of the context's GPU,
+ * otherwise host memory (copied back inside the call). */
+typedef struct smc_outputs {
+  int device;
+  double *ecc;          /* [n][49]: orders 1..9 x (Re,Im r^2-weighted,
+                           Re,Im r^n-weighted, <r^n>), Npart, Ncoll,
+                           integral rho*finalFactor*dx*dy, b -- the line
+                           MakeDensity::dumpEccentricities appends to
+                           sn_ecc_eccp_10.dat (src/MakeDensity.cpp:2473-2500) */
+  float *rho;           /* [n][nx][ny] density (MCnucl::getRho)              */
+  float *ta, *tb;       /* [n][nx][ny] thickness (MCnucl::getTA1/getTA2)     */
+  int *npart;           /* [n][2] Npart1, Npart2                             */
+  int *ncoll;           /* [n]                                               */
+  double *b;            /* [n] impact parameter                              */
+  int *attempts;        /* [n] tries per accepted event                      */
+  double *positions;    /* [n][A+B][2] nucleon x,y (projectile first, each
+                           nucleus sorted by x)                              */
+  uint8_t *wounded;     /* [n][A+B] 1 = participant                          */
+} smc_outputs;
+
+/* MCnucl::MCnucl + MakeDensity::MakeDensity: validates the configuration,
+ * selects device 0 of the process, allocates device state.  For
+ * which_mc_model = 1 the dN/dy table is built on the GPU here
+ * (MCnucl::makeTable, src/MCnucl.cpp:911-960). */
+smc_status smc_create(const smc_params *params, void **ctx_out);
+void smc_destroy(void *ctx);
+smc_status smc_get_info(void *ctx, smc_info *info);
+const char *smc_status_string(smc_status s);
+/* Runs subsequent work on the given cudaStream_t (NULL: the context's own
+ * stream). */
+smc_status smc_set_stream(void *ctx, void *cuda_stream);
+smc_status smc_synchronize(void *ctx);
+
+/* Event generation, one batch: the event loop of
+ * MakeDensity::generateEccTable / generate_profile_ebe
+ * (src/MakeDensity.cpp:2143-2196, :574-694) for events
+ * [first_event, first_event + n).  Each event draws its impact parameter
+ * and nuclei (MCnucl::generateNuclei, Nucleus::populate) from Philox
+ * streams keyed by (seed, event id), retries until Ncoll > 0 and
+ * npmin <= Npart <= npmax (MCnucl::getBinaryCollision, CentralityCut),
+ * then computes thickness, density (MCnucl::calculateThickness,
+ * setDensity) and eccentricities (MakeDensity::dumpEccentricities). */
+smc_status smc_generate(void *ctx, uint64_t first_event, int n, const smc_outputs *out);
+
+/* The same pipeline from given nucleon positions (the reference's injection
+ * harness path): xy_proj [n][A][2], xy_targ [n][B][2], b [n] (may be NULL),
+ * host memory unless out->device.  Replaces getBinaryCollision +
+ * calculateThickness + setDensity + dumpEccentricities on injected
+ * nuclei. */
+smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_targ,
+                      const double *b, const smc_outputs *out);
+
+/* Plain per-event path: the same results as smc_generate, one event per
+ * kernel launch sequence (the unbatched baseline). */
+smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_outputs *out);
+
+/* MC-KLN dN/dy table (MCnucl::makeTable, src/MCnucl.cpp:911-960): copies the
+ * current table ([tmax][tmax] doubles, rapidity slice 0) to host. */
+smc_status smc_kln_table(void *ctx, double *host_table, int capacity);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

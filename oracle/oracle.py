@@ -134,6 +134,7 @@ class Oracle:
         lib.smco_kln_dndy.argtypes = [ctypes.POINTER(KLN), ctypes.c_double, ctypes.c_double,
                                       ctypes.c_int, ctypes.c_int, ctypes.c_int]
         lib.smco_gauss_legendre01.argtypes = [ctypes.c_int, _D, _D]
+        lib.smco_set_pair_stream.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
         lib.smco_run_ecc_table.restype = ctypes.c_long
         lib.smco_run_ecc_table.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Nucleus),
                                            ctypes.POINTER(Nucleus), ctypes.c_double, ctypes.c_double,

@@ -121,7 +121,12 @@ extern "C" {
 // data/, EOS/ link), parses the parameter text (one key=value per line, the
 // parameters.dat syntax) and constructs the reference MakeDensity.
 int refh_init(const char *workdir, const char *eos_dir, const char *params_text) {
-  if (g_md) { delete g_md; g_md = 0; }
+  if (g_md) {
+    // the installed dN/dy table belongs to the harness, not to MCnucl
+    if (g_table) MCAccess::set_table(mc(), 0, 0, 0.0);
+    delete g_md;
+    g_md = 0;
+  }
   if (g_par) { delete g_par; g_par = 0; }
   free_table();
   g_workdir = workdir;
@@ -295,6 +300,7 @@ int refh_populate(int which, double xc, double yc, double *xyz, int maxn) {
 // Installs a dN/dy table (row-major tmax x tmax, rapidity slice 0) with
 // thickness step dT into MCnucl, as MCnucl::makeTable would have.
 void refh_set_kln_table(const double *tab, int tmax, double dT) {
+  if (g_table) MCAccess::set_table(mc(), 0, 0, 0.0);
   free_table();
   g_table = new double **[1];
   g_table[0] = new double *[tmax];

@@ -579,6 +579,13 @@ static int hit(const smco_event *e, const nucleon_t *p1, const nucleon_t *p2, do
 static uint64_t g_pair_seed, g_pair_event;
 static int g_pair_attempt, g_pair_philox;
 
+void smco_set_pair_stream(uint64_t seed, uint64_t event, int attempt, int philox) {
+  g_pair_seed = seed;
+  g_pair_event = event;
+  g_pair_attempt = attempt;
+  g_pair_philox = philox;
+}
+
 int smco_event_pair(smco_event *e) {
   nucleon_t *P = e->nuc[0], *T = e->nuc[1];
   int nP = e->n[0], nT = e->n[1];

@@ -85,6 +85,10 @@ void smco_event_populate_philox(smco_event *e, const smco_nucleus *nA, const smc
                                 double b, uint64_t seed, uint64_t event, int attempt);
 double smco_impact_philox(uint64_t seed, uint64_t event, int attempt, double bmin, double bmax);
 
+/* random draws of the Gaussian collision criterion: libc drand48 in the
+ * reference's sweep order (philox = 0) or Philox streams keyed by the sorted
+ * pair index (philox = 1, the GPU's streams) */
+void smco_set_pair_stream(uint64_t seed, uint64_t event, int attempt, int philox);
 /* MCnucl::getBinaryCollision (MCnucl.cpp:217-308); returns Ncoll */
 int smco_event_pair(smco_event *e);
 int smco_event_npart(const smco_event *e, int which);

@@ -1,0 +1,119 @@
+"""ctypes binding of the C ABI declared in include/supermc.h.
+
+The library is the in-tree ``supermc_gb300/_build/libsupermc_gb300.so``;
+loading fails loudly when it is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsupermc_gb300.so")
+
+SMC_OK = 0
+STATUS_NAMES = {
+    0: "SMC_OK", 1: "SMC_ERR_ARGUMENT", 2: "SMC_ERR_CONFIG", 3: "SMC_ERR_RETRY_CAP",
+    4: "SMC_ERR_KLN_TABLE", 5: "SMC_ERR_ZERO_DNDY", 6: "SMC_ERR_CAPACITY", 7: "SMC_ERR_CUDA",
+    8: "SMC_ERR_NO_DEVICE",
+}
+ECC_LEN = 49
+
+# exported symbols, in the order include/supermc.h declares them
+EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "smc_set_stream",
+           "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_plain", "smc_kln_table"]
+
+
+class SmcError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: {STATUS_NAMES.get(status, status)}")
+        self.status = status
+
+
+class SmcParams(ctypes.Structure):
+    _fields_ = [
+        ("which_mc_model", ctypes.c_int), ("sub_model", ctypes.c_int),
+        ("shape_of_nucleons", ctypes.c_int), ("shape_of_entropy", ctypes.c_int),
+        ("collision_criterion", ctypes.c_int),
+        ("Aproj", ctypes.c_int), ("Atarg", ctypes.c_int),
+        ("proj_deformed", ctypes.c_int), ("targ_deformed", ctypes.c_int),
+        ("ecm", ctypes.c_double), ("alpha", ctypes.c_double), ("gauss_nucl_width", ctypes.c_double),
+        ("quark_width", ctypes.c_double), ("lambda_", ctypes.c_double),
+        ("bmin", ctypes.c_double), ("bmax", ctypes.c_double),
+        ("npmin", ctypes.c_int), ("npmax", ctypes.c_int),
+        ("maxx", ctypes.c_double), ("maxy", ctypes.c_double), ("dx", ctypes.c_double), ("dy", ctypes.c_double),
+        ("final_factor", ctypes.c_double),
+        ("tmax", ctypes.c_int), ("tmax_subdivision", ctypes.c_int),
+        ("ecc_from_order", ctypes.c_int), ("ecc_to_order", ctypes.c_int),
+        ("proj_R", ctypes.c_double), ("proj_a", ctypes.c_double),
+        ("targ_R", ctypes.c_double), ("targ_a", ctypes.c_double),
+        ("proj_d_min", ctypes.c_double), ("targ_d_min", ctypes.c_double),
+        ("sigin_override", ctypes.c_double),
+        ("kln_npt", ctypes.c_int), ("kln_nkt", ctypes.c_int), ("kln_nphi", ctypes.c_int),
+        ("seed", ctypes.c_uint64),
+        ("max_attempts", ctypes.c_int), ("max_collisions", ctypes.c_int),
+    ]
+
+
+class SmcInfo(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("sigin", ctypes.c_double), ("dsq", ctypes.c_double), ("width", ctypes.c_double),
+        ("sigma_gg", ctypes.c_double), ("kln_tmax", ctypes.c_int), ("kln_dT", ctypes.c_double),
+        ("A", ctypes.c_int), ("B", ctypes.c_int),
+    ]
+
+
+class SmcOutputs(ctypes.Structure):
+    _fields_ = [
+        ("device", ctypes.c_int),
+        ("ecc", ctypes.c_void_p), ("rho", ctypes.c_void_p), ("ta", ctypes.c_void_p), ("tb", ctypes.c_void_p),
+        ("npart", ctypes.c_void_p), ("ncoll", ctypes.c_void_p), ("b", ctypes.c_void_p),
+        ("attempts", ctypes.c_void_p), ("positions", ctypes.c_void_p), ("wounded", ctypes.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Loads the in-tree library (build it with supermc_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OSError(f"{LIB_PATH} is missing: build the CUDA extension first "
+                      "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = ctypes.CDLL(LIB_PATH)
+    vp = ctypes.c_void_p
+    lib.smc_create.argtypes = [ctypes.POINTER(SmcParams), ctypes.POINTER(vp)]
+    lib.smc_destroy.argtypes = [vp]
+    lib.smc_destroy.restype = None
+    lib.smc_get_info.argtypes = [vp, ctypes.POINTER(SmcInfo)]
+    lib.smc_status_string.argtypes = [ctypes.c_int]
+    lib.smc_status_string.restype = ctypes.c_char_p
+    lib.smc_set_stream.argtypes = [vp, vp]
+    lib.smc_synchronize.argtypes = [vp]
+    lib.smc_generate.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(SmcOutputs)]
+    lib.smc_generate_plain.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(SmcOutputs)]
+    lib.smc_inject.argtypes = [vp, ctypes.c_int, vp, vp, vp, ctypes.POINTER(SmcOutputs)]
+    lib.smc_kln_table.argtypes = [vp, vp, ctypes.c_int]
+    _lib = lib
+    return lib
+
+
+def check(status: int, what: str) -> None:
+    if status != SMC_OK:
+        raise SmcError(status, what)
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array or a torch tensor (None passes NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"]
+        return a.ctypes.data
+    return a.data_ptr()

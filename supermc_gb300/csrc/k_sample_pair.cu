@@ -1,0 +1,631 @@
+// Stage 1 of the event pipeline: nucleus sampling, participant/binary
+// pairing and construction of the splat sources, one CTA per event.
+//
+// Reference behaviour restated here:
+//   impact parameter and retry loop   src/MakeDensity.cpp:2147-2162
+//   Woods-Saxon sampling, hard core   src/Nucleus.cpp:187-317, :578-621
+//   deuteron (Hulthen)                src/Nucleus.cpp:342-359, src/HulthenFunc.cpp:27-41
+//   pairing (disk / Gaussian)         src/MCnucl.cpp:217-385
+//   binary-collision midpoints        src/MCnucl.cpp:326-352
+//   splat windows                     src/MCnucl.cpp:432-478, :688-779, :822-866
+//   eccentricity hot-spot region      src/MCnucl.cpp:1303-1323, src/MakeDensity.cpp:2341-2359
+#include "smc_device.cuh"
+#include "smc_kernels.h"
+
+#include <cfloat>
+
+namespace smc {
+
+constexpr int kNT = 256;   // threads per CTA; also the candidate batch size
+
+struct SampleSmem {
+  float cx[kNT], cy[kNT], cz[kNT];          // candidate batch (nucleus frame)
+  uint8_t valid[kNT];
+  uint32_t conflict[kNT][kNT / 32];          // intra-batch hard-core conflicts
+  int order[kNT];
+  int n_new;
+  float ax[2][kMaxA], ay[2][kMaxA], az[2][kMaxA];  // accepted (nucleus frame)
+  double X[2][kMaxA], Y[2][kMaxA];           // final positions, sorted by x
+  float Xf[2][kMaxA], Yf[2][kMaxA];
+  int hits[2][kMaxA];
+  int scan[kNT];
+  double red[kNT / 32 * 3];
+  int ired[kNT / 32 * 4];
+  double red4[kNT / 32];
+  double b;
+};
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ float sph2(float ct) { return (3.0f * ct * ct - 1.0f) * 0.31539156525252005f; }
+__device__ __forceinline__ float sph4(float ct) {
+  float c2 = ct * ct;
+  return (35.0f * c2 * c2 - 30.0f * c2 + 3.0f) * 0.10578554691520431f;
+}
+
+// Point3D::rotate (src/MathBasics.cpp:41-50)
+__device__ __forceinline__ void rotate3f(float &x, float &y, float &z, float cth, float phi) {
+  float sphi, cphi;
+  sincosf(phi, &sphi, &cphi);
+  float sth = sqrtf(fmaxf(0.f, 1.f - cth * cth));
+  float x0 = x, y0 = y, z0 = z;
+  x = cth * cphi * x0 - sphi * y0 + sth * cphi * z0;
+  y = cth * sphi * x0 + cphi * y0 + sth * sphi * z0;
+  z = -sth * x0 + cth * z0;
+}
+
+// One Woods-Saxon candidate from four uniforms (Nucleus::getDeformRandomWS)
+__device__ __forceinline__ bool ws_candidate(const NucleusDev &n, float ctr, float phir, double u0, double u1,
+                                             double u2, double u3, float &x, float &y, float &z) {
+  float R = (float)n.R, a = (float)n.a;
+  float r = (float)n.rmax_cut * powf((float)u0, 1.0f / 3.0f);
+  if (n.deformed) {
+    float cx = 1.0f - 2.0f * (float)u1;
+    float rad1 = R * (1.0f + (float)n.beta2 * sph2(cx) + (float)n.beta4 * sph4(cx));
+    float rw1 = 1.0f / (1.0f + expf(-rad1 / a));
+    if ((float)u2 * rw1 > 1.0f / (1.0f + expf((r - rad1) / a))) return false;
+    float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
+    float sp, cp;
+    sincospif(2.0f * (float)u3, &sp, &cp);
+    x = r * sx * cp; y = r * sx * sp; z = r * cx;
+    rotate3f(x, y, z, ctr, phir);
+  } else {
+    if ((float)u1 * (float)n.rw_max > 1.0f / (1.0f + expf((r - R) / a))) return false;
+    float cx = 1.0f - 2.0f * (float)u2;
+    float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
+    float sp, cp;
+    sincospif(2.0f * (float)u3, &sp, &cp);
+    x = r * sx * cp; y = r * sx * sp; z = r * cx;
+  }
+  return true;
+}
+
+// HulthenFunc::CDF (src/HulthenFunc.cpp:27-36)
+__device__ double hulthen_cdf(double r) {
+  const double alpha = .228, beta = 1.18;
+  if (r <= 0) return 0;
+  const double c = (alpha * beta * (alpha + beta)) / ((alpha - beta) * (alpha - beta));
+  return 2 * c * (2 * (exp(-r * (alpha + beta)) / (alpha + beta)) - .5 * exp(-2 * alpha * r) / alpha -
+                  .5 * exp(-2 * beta * r) / beta + .5 / alpha + .5 / beta - 2 / (alpha + beta));
+}
+// invertFunc Newton iteration as used by HulthenFunc::invCDF (src/arsenal.cpp:318-387)
+__device__ double hulthen_inv(double y) {
+  const double xL = 0, xR = 100.0, dx = 0.001, acc = 0.001 * 0.001;
+  double XX2 = 1.0, XX1 = XX2 - 10 * acc;
+  for (int it = 0; it < 61 && fabs(XX2 - XX1) > acc; it++) {
+    XX1 = XX2;
+    double F0 = hulthen_cdf(XX1) - y;
+    double X1 = (XX1 > xL + dx) ? XX1 - dx : xL;
+    double X2 = (XX1 < xR - dx) ? XX1 + dx : xR;
+    double F3 = (hulthen_cdf(X1) - hulthen_cdf(X2)) / (X1 - X2);
+    XX2 = XX1 - F0 / F3;
+  }
+  return XX2;
+}
+
+__device__ __forceinline__ double block_sum_d(double v, double *red, int slot) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[slot * (kNT / 32) + w] = v;
+  __syncthreads();
+  double s = 0;
+  for (int i = 0; i < kNT / 32; i++) s += red[slot * (kNT / 32) + i];
+  return s;
+}
+
+__device__ __forceinline__ int block_sum_i(int v, int *red, int slot) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[slot * (kNT / 32) + w] = v;
+  __syncthreads();
+  int s = 0;
+  for (int i = 0; i < kNT / 32; i++) s += red[slot * (kNT / 32) + i];
+  return s;
+}
+
+// Samples one nucleus into sm.ax/ay/az[w] (nucleus frame, centre of mass
+// not yet removed).  Candidates are consumed in order; a candidate is kept
+// iff it passes the radial test and lies at least d_min from every nucleon
+// kept before it -- the sequential rule of Nucleus::populate, evaluated a
+// batch of kNT candidates at a time.  Returns false if the candidate cap is hit.
+__device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t seed, uint64_t ev, int attempt,
+                          float ctr, float phir) {
+  const int tid = threadIdx.x;
+  const int A = n.A;
+  const float dmin2 = (float)(n.d_min * n.d_min);
+  const uint32_t sid = stream_id(attempt, w == 0 ? ST_PROJ : ST_TARG);
+  int n_acc = 0;
+  for (uint32_t base = 0; n_acc < A; base += kNT) {
+    if (base > (1u << 20)) return false;
+    uint32_t c = base + tid;
+    double u0, u1, u2, u3;
+    uniform2(seed, ev, sid, 2 * c, u0, u1);
+    uniform2(seed, ev, sid, 2 * c + 1, u2, u3);
+    float x = 0, y = 0, z = 0;
+    bool ok = ws_candidate(n, ctr, phir, u0, u1, u2, u3, x, y, z);
+    if (ok) {
+      for (int k = 0; k < n_acc; k++) {
+        float dx = x - sm.ax[w][k], dy = y - sm.ay[w][k], dz = z - sm.az[w][k];
+        if (dx * dx + dy * dy + dz * dz < dmin2) { ok = false; break; }
+      }
+    }
+    sm.cx[tid] = x; sm.cy[tid] = y; sm.cz[tid] = z;
+    sm.valid[tid] = ok;
+    __syncthreads();
+    uint32_t m[kNT / 32];
+#pragma unroll
+    for (int q = 0; q < kNT / 32; q++) m[q] = 0;
+    if (ok) {
+      for (int k = 0; k < tid; k++) {
+        if (!sm.valid[k]) continue;
+        float dx = x - sm.cx[k], dy = y - sm.cy[k], dz = z - sm.cz[k];
+        if (dx * dx + dy * dy + dz * dz < dmin2) m[k >> 5] |= 1u << (k & 31);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kNT / 32; q++) sm.conflict[tid][q] = m[q];
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t accb[kNT / 32];
+#pragma unroll
+      for (int q = 0; q < kNT / 32; q++) accb[q] = 0;
+      int k = 0;
+      for (int cc = 0; cc < kNT && n_acc + k < A; cc++) {
+        if (!sm.valid[cc]) continue;
+        bool clash = false;
+#pragma unroll
+        for (int q = 0; q < kNT / 32; q++) clash |= (sm.conflict[cc][q] & accb[q]) != 0;
+        if (clash) continue;
+        accb[cc >> 5] |= 1u << (cc & 31);
+        sm.order[k++] = cc;
+      }
+      sm.n_new = k;
+    }
+    __syncthreads();
+    int k = sm.n_new;
+    if (tid < k) {
+      int cc = sm.order[tid];
+      sm.ax[w][n_acc + tid] = sm.cx[cc];
+      sm.ay[w][n_acc + tid] = sm.cy[cc];
+      sm.az[w][n_acc + tid] = sm.cz[cc];
+    }
+    n_acc += k;
+    __syncthreads();
+  }
+  return true;
+}
+
+// Places nucleus w: nucleus-frame positions -> centre-of-mass removed in
+// FP64 -> shifted by xc along x -> sorted by x (the reference sorts by the
+// left box edge x-4w, src/Nucleus.cpp:314, the same order).
+__device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const double *inj_xy) {
+  const int tid = threadIdx.x;
+  double px = 0, py = 0;
+  if (inj_xy) {
+    if (tid < A) { px = inj_xy[2 * tid]; py = inj_xy[2 * tid + 1]; }
+  } else {
+    double sx = tid < A ? (double)sm.ax[w][tid] : 0.0;
+    double sy = tid < A ? (double)sm.ay[w][tid] : 0.0;
+    double mx = block_sum_d(sx, sm.red, 0);
+    double my = block_sum_d(sy, sm.red, 1);
+    __syncthreads();
+    if (tid < A) {
+      px = (double)sm.ax[w][tid] - mx / A + xc;
+      py = (double)sm.ay[w][tid] - my / A;
+    }
+  }
+  // stash unsorted in X/Y, then rank-sort by x
+  if (tid < A) { sm.X[w][tid] = px; sm.Y[w][tid] = py; }
+  __syncthreads();
+  int rank = 0;
+  if (tid < A) {
+    for (int j = 0; j < A; j++) {
+      double xj = sm.X[w][j];
+      rank += (xj < px) || (xj == px && j < tid);
+    }
+  }
+  __syncthreads();
+  if (tid < A) {
+    sm.X[w][rank] = px; sm.Y[w][rank] = py;
+    sm.Xf[w][rank] = (float)px; sm.Yf[w][rank] = (float)py;
+  }
+  __syncthreads();
+}
+
+// Bounding-box edges of a nucleon at x (Particle::Particle + calculateBounds,
+// src/Particle.cpp:16-24,94-99, with all quarks at the nucleon centre).
+__device__ __forceinline__ double box_lo(double x, const DevParams &P) {
+  return fmin(x - 4 * P.width, x - 4 * P.quark_width);
+}
+__device__ __forceinline__ double box_hi(double x, const DevParams &P) {
+  return fmax(x + 4 * P.width, x + 4 * P.quark_width);
+}
+
+// Target range swept for projectile i by MCnucl::getBinaryCollision
+// (src/MCnucl.cpp:244-292): from the first target whose box right edge
+// reaches the projectile box's left edge, through the first target whose
+// box left edge lies beyond the projectile box's right edge (the sweep
+// tests that one too).  Both nuclei are sorted by x, so binary searches
+// find both ends.
+__device__ __forceinline__ void sweep_range(const SampleSmem &sm, const DevParams &P, int i, int B, int &lo,
+                                            int &hi) {
+  double pxl = box_lo(sm.X[0][i], P), pxr = box_hi(sm.X[0][i], P);
+  int a = 0, b = B;
+  while (a < b) {  // first j with box_hi(xj) >= pxl
+    int m = (a + b) >> 1;
+    if (box_hi(sm.X[1][m], P) >= pxl) b = m; else a = m + 1;
+  }
+  lo = a;
+  int c = lo, d = B;
+  while (c < d) {  // first j >= lo with box_lo(xj) > pxr
+    int m = (c + d) >> 1;
+    if (box_lo(sm.X[1][m], P) > pxr) d = m; else c = m + 1;
+  }
+  // inclusive; nothing is swept when the first candidate already lies
+  // beyond the projectile box (the loop condition fails before any test)
+  hi = (c == lo) ? lo - 1 : (c < B ? c : B - 1);
+}
+
+// MCnucl::hit (src/MCnucl.cpp:357-385) for projectile i, target j.  The disk
+// test is decided in FP32 away from the threshold and in FP64, rounded as the
+// reference rounds, near it.
+__device__ __forceinline__ bool pair_hit(const SampleSmem &sm, const DevParams &P, int i, int j, float dsq_lo,
+                                         float dsq_hi, uint64_t ev, int attempt, int B, bool swept) {
+  float dx = sm.Xf[1][j] - sm.Xf[0][i], dy = sm.Yf[1][j] - sm.Yf[0][i];
+  float d2 = dx * dx + dy * dy;
+  if (swept) {
+    // y-overlap of the bounding boxes (src/MCnucl.cpp:272-274)
+    float ady = fabsf(dy), lim = 4.f * (float)(fmax(P.width, P.quark_width)) * 2.f;
+    if (ady > lim * (1.f + 1e-5f)) return false;
+    if (ady > lim * (1.f - 1e-5f)) {
+      double yi = sm.Y[0][i], yj = sm.Y[1][j];
+      if (!(box_lo(yi, P) <= box_hi(yj, P) && box_hi(yi, P) >= box_lo(yj, P))) return false;
+    }
+  }
+  if (P.collision_criterion == 1) {
+    if (d2 < dsq_lo) return true;
+    if (d2 > dsq_hi) return false;
+    double b = __dsqrt_rn(sq_dist_rn(sm.X[0][i], sm.Y[0][i], sm.X[1][j], sm.Y[1][j]));
+    return __dmul_rn(b, b) <= P.dsq;
+  }
+  // Gaussian profile: P = 1 - exp(-sigma_gg exp(-b^2/4w^2)/(4 pi w^2))
+  if (d2 > 576.f * (float)P.w2) return false;  // P < 1e-60 beyond 24 w
+  double u, unused;
+  uniform2(P.seed, ev, stream_id(attempt, ST_COLL), (uint32_t)(i * B + j), u, unused);
+  float w2 = (float)P.w2;
+  float pf = 1.f - expf(-(float)P.sigma_gg * expf(-d2 / (4.f * w2)) / (4.f * 3.14159265f * w2));
+  if ((float)u < pf - 1e-5f) return true;
+  if ((float)u > pf + 1e-5f) return false;
+  double b = __dsqrt_rn(sq_dist_rn(sm.X[0][i], sm.Y[0][i], sm.X[1][j], sm.Y[1][j]));
+  double w = P.width;
+  return u < 1. - exp(-P.sigma_gg * exp(-b * b / (4. * w * w)) / (4. * M_PI * w * w));
+}
+
+__device__ __forceinline__ void set_window(Source &s, double lo, double hi, double mn, double d, float inv_d,
+                                           int nmax, bool is_x) {
+  int l = trunc_index(lo, mn, d, inv_d), r = trunc_index(hi, mn, d, inv_d);
+  l = max(0, l);
+  r = min(nmax, r);
+  if (is_x) { s.xl = (int16_t)l; s.xr = (int16_t)r; }
+  else { s.yl = (int16_t)l; s.yr = (int16_t)r; }
+}
+
+// ----------------------------------------------------------------- kernel
+__global__ void __launch_bounds__(kNT) k_sample_pair(DevParams P, uint64_t first_event, int n_events,
+                                                     const double *inj_proj, const double *inj_targ,
+                                                     const double *inj_b, EventRec *recs, Source *srcs,
+                                                     double *out_pos, uint8_t *out_wounded) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SampleSmem &sm = *reinterpret_cast<SampleSmem *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int A = P.nuc[0].A, B = P.nuc[1].A;
+  const bool inject = inj_proj != nullptr;
+  const float dsq_lo = (float)P.dsq * (1.f - 1e-4f), dsq_hi = (float)P.dsq * (1.f + 1e-4f);
+  const float inv_dx = (float)(1.0 / P.dx), inv_dy = (float)(1.0 / P.dy);
+  // The reference only tests pairs its box sweep reaches.  For the disk test
+  // with a hit radius well inside the box width every hit pair is swept, so
+  // all pairs are tested; otherwise the sweep's tested set is reproduced.
+  const bool swept = P.collision_criterion != 1 || sqrt(P.dsq) > 7.9 * fmax(P.width, P.quark_width);
+
+  for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
+    const uint64_t ev = first_event + (uint64_t)e;
+    int status = 0, attempt = 0, ncoll = 0, np1 = 0, np2 = 0;
+    for (;; attempt++) {
+      if (attempt >= P.max_attempts) { status = 3; break; }
+      // impact parameter (MakeDensity.cpp:2149)
+      if (tid == 0) {
+        if (inject) sm.b = inj_b ? inj_b[e] : 0.0;
+        else {
+          double u, unused;
+          uniform2(P.seed, ev, stream_id(attempt, ST_EVENT), 0, u, unused);
+          sm.b = sqrt((P.bmax * P.bmax - P.bmin * P.bmin) * u + P.bmin * P.bmin);
+        }
+      }
+      __syncthreads();
+      const double b = sm.b;
+      bool ok = true;
+      for (int w = 0; w < 2; w++) {
+        const NucleusDev &nu = P.nuc[w];
+        const double xc = (w == 0 ? b : -b) / 2.0;
+        if (inject) {
+          place_sorted(sm, w, nu.A, 0.0, (w == 0 ? inj_proj : inj_targ) + (size_t)e * 2 * nu.A);
+          continue;
+        }
+        double o0, o1;
+        uniform2(P.seed, ev, stream_id(attempt, ST_EVENT), 1 + w, o0, o1);
+        float ctr = (float)(1.0 - 2.0 * o0), phir = (float)(2 * M_PI * o1);
+        if (nu.A == 1) {
+          if (tid == 0) { sm.ax[w][0] = 0.f; sm.ay[w][0] = 0.f; sm.az[w][0] = 0.f; }
+          __syncthreads();
+        } else if (nu.A == 2) {
+          if (tid == 0) {
+            double u, unused;
+            uniform2(P.seed, ev, stream_id(attempt, ST_DEUT), (uint32_t)w, u, unused);
+            double d = hulthen_inv(u);
+            float x1 = (float)(d / 2.0), y1 = 0.f, z1 = 0.f;
+            rotate3f(x1, y1, z1, ctr, phir);
+            sm.ax[w][0] = x1; sm.ay[w][0] = y1; sm.az[w][0] = z1;
+            sm.ax[w][1] = -x1; sm.ay[w][1] = -y1; sm.az[w][1] = -z1;
+          }
+          __syncthreads();
+        } else {
+          ok = ok && sample_ws(sm, nu, w, P.seed, ev, attempt, ctr, phir);
+        }
+        place_sorted(sm, w, nu.A, xc, nullptr);
+      }
+      if (!ok) { status = 3; break; }
+      // ---- pairing: thread i tests projectile i against every target
+      if (tid < B) sm.hits[1][tid] = 0;
+      __syncthreads();
+      int cnt = 0;
+      if (tid < A) {
+        int jlo = 0, jhi = B - 1;
+        if (swept) sweep_range(sm, P, tid, B, jlo, jhi);
+        for (int j = jlo; j <= jhi; j++) {
+          if (pair_hit(sm, P, tid, j, dsq_lo, dsq_hi, ev, attempt, B, swept)) {
+            cnt++;
+            atomicAdd(&sm.hits[1][j], 1);
+          }
+        }
+        sm.hits[0][tid] = cnt;
+      }
+      __syncthreads();
+      np1 = block_sum_i(tid < A && sm.hits[0][tid] > 0, sm.ired, 0);
+      np2 = block_sum_i(tid < B && sm.hits[1][tid] > 0, sm.ired, 1);
+      ncoll = block_sum_i(cnt, sm.ired, 2);
+      __syncthreads();
+      if (inject) break;
+      int np = np1 + np2;
+      if (ncoll > 0 && np >= P.npmin && np <= P.npmax) break;   // CentralityCut
+    }
+
+    // ---- outputs: positions, wounded flags
+    const int AB = A + B;
+    if (out_pos) {
+      for (int k = tid; k < AB; k += kNT) {
+        int w = k < A ? 0 : 1, i = k < A ? k : k - A;
+        out_pos[((size_t)e * AB + k) * 2] = sm.X[w][i];
+        out_pos[((size_t)e * AB + k) * 2 + 1] = sm.Y[w][i];
+      }
+    }
+    if (out_wounded) {
+      for (int k = tid; k < AB; k += kNT) {
+        int w = k < A ? 0 : 1, i = k < A ? k : k - A;
+        out_wounded[(size_t)e * AB + k] = sm.hits[w][i] > 0;
+      }
+    }
+
+    // ---- splat sources
+    Source *S = srcs + (size_t)e * P.max_src;
+    const double d_max = P.shape_of_nucleons == 1 ? 2. * sqrt(P.dsq) : 5. * P.width;
+    const int model = P.which_mc_model;
+    const bool box_src = (model == 5 && P.sub_model == 1) || model == 7;
+    const bool coll_src = model == 5 && P.alpha > 1e-8;
+    const bool thick_src = model == 1 || P.want_ta || P.want_tb;
+    const bool disk_n = P.shape_of_nucleons == 1, disk_e = P.shape_of_entropy == 1;
+    const float peak = (float)P.peak;
+    const float disk_val = (float)(10.0 / P.sigin);
+
+    // region of the eccentricity mask: union of participant boxes and the
+    // (unset, all-zero) collision boxes
+    double rxl = ncoll > 0 ? 0.0 : DBL_MAX, rxr = ncoll > 0 ? 0.0 : -DBL_MAX;
+    double ryl = rxl, ryr = rxr;
+    {
+      double lxl = DBL_MAX, lxr = -DBL_MAX, lyl = DBL_MAX, lyr = -DBL_MAX;
+      for (int k = tid; k < AB; k += kNT) {
+        int w = k < A ? 0 : 1, i = k < A ? k : k - A;
+        if (sm.hits[w][i] == 0) continue;
+        double x = sm.X[w][i], y = sm.Y[w][i];
+        lxl = fmin(lxl, fmin(x - 4 * P.width, x - 4 * P.quark_width));
+        lxr = fmax(lxr, fmax(x + 4 * P.width, x + 4 * P.quark_width));
+        lyl = fmin(lyl, fmin(y - 4 * P.width, y - 4 * P.quark_width));
+        lyr = fmax(lyr, fmax(y + 4 * P.width, y + 4 * P.quark_width));
+      }
+      for (int o = 16; o; o >>= 1) {
+        lxl = fmin(lxl, __shfl_xor_sync(0xffffffffu, lxl, o));
+        lxr = fmax(lxr, __shfl_xor_sync(0xffffffffu, lxr, o));
+        lyl = fmin(lyl, __shfl_xor_sync(0xffffffffu, lyl, o));
+        lyr = fmax(lyr, __shfl_xor_sync(0xffffffffu, lyr, o));
+      }
+      if ((tid & 31) == 0) {
+        int w = tid >> 5;
+        sm.red[w] = lxl; sm.red[kNT / 32 + w] = lxr; sm.red[2 * (kNT / 32) + w] = lyl;
+        sm.red4[w] = lyr;
+      }
+      __syncthreads();
+      for (int q = 0; q < kNT / 32; q++) {
+        rxl = fmin(rxl, sm.red[q]);
+        rxr = fmax(rxr, sm.red[kNT / 32 + q]);
+        ryl = fmin(ryl, sm.red[2 * (kNT / 32) + q]);
+        ryr = fmax(ryr, sm.red4[q]);
+      }
+      __syncthreads();
+      if (np1 + np2 == 0 && ncoll == 0) { rxl = rxr = ryl = ryr = 0.0; }
+    }
+    const int nXp = (int)((rxr - rxl) / P.dx), nYp = (int)((ryr - ryl) / P.dy);
+    const int ioff = (int)((rxl - P.xmin) / P.dx), joff = (int)((ryl - P.ymin) / P.dy);
+
+    // participant sources in nucleon order (projectile then target)
+    int nsrc = 0;
+    int imin = P.nx, imax = 0, jmin = P.ny, jmax = 0;
+    {
+      // one box record per participant (a splat source, or mask-only when the
+      // model does not splat boxes) plus a thickness record when T_A/T_B are made
+      int per_part = 1 + (thick_src ? 1 : 0);
+      // prefix over wounded flags
+      int flag = 0;
+      for (int k = tid; k < ((AB + kNT - 1) / kNT) * kNT; k += kNT) {
+        int w = k < A ? 0 : 1, i = k < A ? k : k - A;
+        flag = (k < AB) && sm.hits[w][i] > 0;
+        // block exclusive scan of flag
+        int v = flag;
+        for (int o = 1; o < 32; o <<= 1) {
+          int t = __shfl_up_sync(0xffffffffu, v, o);
+          if ((tid & 31) >= o) v += t;
+        }
+        if ((tid & 31) == 31) sm.ired[tid >> 5] = v;
+        __syncthreads();
+        int woff = 0, tot = 0;
+        for (int q = 0; q < kNT / 32; q++) {
+          if (q < (tid >> 5)) woff += sm.ired[q];
+          tot += sm.ired[q];
+        }
+        int pos = nsrc + (woff + v - flag) * per_part;
+        if (flag) {
+          double x = sm.X[w][i], y = sm.Y[w][i];
+          {
+            Source s;
+            s.x = x; s.y = y;
+            double bxl = fmin(x - 4 * P.width, x - 4 * P.quark_width);
+            double bxr = fmax(x + 4 * P.width, x + 4 * P.quark_width);
+            double byl = fmin(y - 4 * P.width, y - 4 * P.quark_width);
+            double byr = fmax(y + 4 * P.width, y + 4 * P.quark_width);
+            if (box_src) {
+              set_window(s, bxl, bxr, P.xmin, P.dx, inv_dx, P.nx, true);
+              set_window(s, byl, byr, P.ymin, P.dy, inv_dy, P.ny, false);
+            } else {
+              s.xl = s.xr = s.yl = s.yr = 0;   // eccentricity mask only
+            }
+            int x0 = (int)((bxl - rxl) / P.dx), x1 = (int)((bxr - rxl) / P.dx);
+            int y0 = (int)((byl - ryl) / P.dy), y1 = (int)((byr - ryl) / P.dx);
+            s.mx0 = (int16_t)(max(0, x0) + ioff); s.mx1 = (int16_t)(min(nXp, x1) + ioff);
+            s.my0 = (int16_t)(max(0, y0) + joff); s.my1 = (int16_t)(min(nYp, y1) + joff);
+            s.kind = box_src ? (SRC_PART_BOX | (disk_e ? 16 : 0)) : 3;
+            s.plane = (model == 7 && w == 1) ? 1 : 0;
+            s.weight = disk_e ? disk_val * (model == 5 ? (float)((1.0 - P.alpha) / 2.) : 1.f)
+                              : peak * (model == 5 ? (float)((1.0 - P.alpha) / 2.) : 1.f);
+            s.pad = 0.f;
+            S[pos++] = s;
+          }
+          if (thick_src) {
+            Source s;
+            s.x = x; s.y = y;
+            set_window(s, x - d_max, x + d_max, P.xmin, P.dx, inv_dx, P.nx, true);
+            set_window(s, y - d_max, y + d_max, P.ymin, P.dy, inv_dy, P.ny, false);
+            s.mx0 = s.mx1 = s.my0 = s.my1 = 0;
+            s.kind = SRC_THICK | (disk_n ? 16 : 0);
+            s.plane = w == 0 ? 1 : 2;
+            s.weight = disk_n ? disk_val : peak;
+            s.pad = 0.f;
+            S[pos++] = s;
+          }
+        }
+        nsrc += tot * per_part;
+        __syncthreads();
+      }
+    }
+    // collision sources, ordered by (projectile, target) index
+    int ncs = 0;
+    if (coll_src && ncoll > 0) {
+      // exclusive scan of per-projectile hit counts
+      int c = tid < A ? sm.hits[0][tid] : 0;
+      int v = c;
+      for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if ((tid & 31) >= o) v += t;
+      }
+      if ((tid & 31) == 31) sm.ired[tid >> 5] = v;
+      __syncthreads();
+      int woff = 0;
+      for (int q = 0; q < (tid >> 5); q++) woff += sm.ired[q];
+      __syncthreads();
+      int pos = woff + v - c;
+      ncs = min(ncoll, P.max_coll);
+      if (ncoll > P.max_coll) status = 6;
+      if (tid < A && c > 0) {
+        int jlo = 0, jhi = B - 1;
+        if (swept) sweep_range(sm, P, tid, B, jlo, jhi);
+        for (int j = jlo; j <= jhi && pos < ncs; j++) {
+          if (!pair_hit(sm, P, tid, j, dsq_lo, dsq_hi, ev, attempt, B, swept)) continue;
+          Source s;
+          s.x = (sm.X[0][tid] + sm.X[1][j]) / 2.0;
+          s.y = (sm.Y[0][tid] + sm.Y[1][j]) / 2.0;
+          set_window(s, s.x - d_max, s.x + d_max, P.xmin, P.dx, inv_dx, P.nx, true);
+          set_window(s, s.y - d_max, s.y + d_max, P.ymin, P.dy, inv_dy, P.ny, false);
+          s.mx0 = s.mx1 = s.my0 = s.my1 = 0;
+          s.kind = SRC_COLL | (disk_e ? 16 : 0);
+          s.plane = 0;
+          double aw = 0.;
+          if (model == 5 && P.sub_model == 2) aw = (double)(1 / c) + (double)(1 / sm.hits[1][j]);
+          double fw = P.alpha + (1. - P.alpha) * aw;
+          s.weight = (float)((disk_e ? 10.0 / P.sigin : P.peak) * fw);
+          s.pad = 0.f;
+          S[nsrc + pos] = s;
+          pos++;
+        }
+      }
+    }
+    __syncthreads();
+    nsrc += ncs;
+    // bounding box of all windows
+    for (int k = tid; k < nsrc; k += kNT) {
+      Source s = S[k];
+      if (s.xr > s.xl && s.yr > s.yl) {
+        imin = min(imin, (int)s.xl); imax = max(imax, (int)s.xr);
+        jmin = min(jmin, (int)s.yl); jmax = max(jmax, (int)s.yr);
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      imin = min(imin, __shfl_xor_sync(0xffffffffu, imin, o));
+      imax = max(imax, __shfl_xor_sync(0xffffffffu, imax, o));
+      jmin = min(jmin, __shfl_xor_sync(0xffffffffu, jmin, o));
+      jmax = max(jmax, __shfl_xor_sync(0xffffffffu, jmax, o));
+    }
+    if ((tid & 31) == 0) {
+      int w = tid >> 5;
+      sm.scan[w] = imin; sm.scan[8 + w] = imax; sm.scan[16 + w] = jmin; sm.scan[24 + w] = jmax;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int q = 0; q < kNT / 32; q++) {
+        imin = min(imin, sm.scan[q]); imax = max(imax, sm.scan[8 + q]);
+        jmin = min(jmin, sm.scan[16 + q]); jmax = max(jmax, sm.scan[24 + q]);
+      }
+      EventRec r;
+      r.b = sm.b;
+      r.npart1 = np1; r.npart2 = np2; r.ncoll = ncoll; r.nsrc = nsrc;
+      r.attempts = attempt + 1; r.status = status;
+      r.imin = imin; r.imax = imax; r.jmin = jmin; r.jmax = jmax;
+      recs[e] = r;
+    }
+    __syncthreads();
+  }
+}
+
+size_t sample_pair_smem() { return sizeof(SampleSmem); }
+
+cudaError_t launch_sample_pair(const DevParams &P, uint64_t first_event, int n_events, const double *inj_proj,
+                               const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
+                               double *out_pos, uint8_t *out_wounded, int grid, cudaStream_t st) {
+  size_t smem = sizeof(SampleSmem);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_sample_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  k_sample_pair<<<grid, kNT, smem, st>>>(P, first_event, n_events, inj_proj, inj_targ, inj_b, recs, srcs, out_pos,
+                                         out_wounded);
+  return cudaGetLastError();
+}
+
+}  // namespace smc

@@ -1,0 +1,532 @@
+// Host runtime behind the C ABI of include/supermc.h: configuration and
+// derived constants (MCnucl::MCnucl, src/MCnucl.cpp:22-154), device buffers,
+// batching and the two-stage launch sequence.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/supermc.h"
+#include "smc_kernels.h"
+
+namespace {
+
+using smc::DevParams;
+using smc::EventRec;
+using smc::Source;
+
+// ------------------------------------------------------------ constants
+// sigma_in = sigma_tot - sigma_el for pp from the PDG-96 Regge fits
+// (hadronxsec::totalXsection / elasticXsection, src/Regge96.cpp:27-50).
+double sigma_inelastic(double ecm) {
+  double s = ecm * ecm;
+  double sig = 22.0 * std::pow(s, 0.079) + 56.1 * std::pow(s, -0.46);
+  double bel = 2.0 * 2.3 + 2.0 * 2.3 + 4.0 * std::pow(s, 0.0808) - 4.2;
+  return sig - 0.0511 * sig * sig / bel;
+}
+
+// 38-point Gauss-Legendre abscissae/weights on [0,1] from the published
+// table the reference uses (Nucleus::Gauss38, src/Nucleus.cpp:697-751).
+void gauss38_unit(double *xn, double *wn) {
+  static const double xp[19] = {
+      4.078514790458e-2, 1.220840253379e-1, 2.025704538921e-1, 2.817088097902e-1, 3.589724404794e-1,
+      4.338471694324e-1, 5.058347179279e-1, 5.744560210478e-1, 6.392544158297e-1, 6.997986803792e-1,
+      7.556859037540e-1, 8.065441676053e-1, 8.520350219324e-1, 8.918557390046e-1, 9.257413320486e-1,
+      9.534663309335e-1, 9.748463285902e-1, 9.897394542664e-1, 9.980499305357e-1};
+  static const double wp[19] = {
+      8.152502928039e-2, 8.098249377060e-2, 7.990103324353e-2, 7.828784465821e-2, 7.615366354845e-2,
+      7.351269258474e-2, 7.038250706690e-2, 6.678393797914e-2, 6.274093339213e-2, 5.828039914700e-2,
+      5.343201991033e-2, 4.822806186076e-2, 4.270315850467e-2, 3.689408159400e-2, 3.083950054518e-2,
+      2.457973973823e-2, 1.815657770961e-2, 1.161344471647e-2, 5.002880749632e-3};
+  for (int k = 0; k < 19; k++) {
+    xn[19 + k] = (1.0 * xp[k]) / 2.0 + 0.5;
+    wn[19 + k] = (1.0 * wp[k]) / 2.0;
+    xn[18 - k] = (1.0 * -xp[k]) / 2.0 + 0.5;
+    wn[18 - k] = (1.0 * wp[k]) / 2.0;
+  }
+}
+
+// sigma_gg from sigma_in = int d^2b [1 - exp(-sigma_gg T_pp(b))] by Newton
+// iteration (GaussianNucleonsCal::getSigEff, src/GaussianNucleonsCal.cpp:130-163).
+double sigma_gg_from(double siginNN, double width) {
+  double xg[38], wg[38];
+  gauss38_unit(xg, wg);
+  double sigin = siginNN * 0.1, Bmax = 5.0 * width, sigeff = 10.0, prev;
+  int guard = 0;
+  do {
+    prev = sigeff;
+    double sum = 0.0, dN = 0.0;
+    for (int ib = 0; ib < 38; ib++) {
+      double b = xg[ib] * Bmax, db = wg[ib] * Bmax;
+      double Tpp = std::exp(-b * b / (4. * width * width)) / (M_PI * (4. * width * width));
+      sum += 2 * M_PI * b * db * (1.0 - std::exp(-sigeff * Tpp));
+      dN += 2 * M_PI * b * db * Tpp * std::exp(-sigeff * Tpp);
+    }
+    sigeff -= (sum - sigin) / dN;
+  } while (std::fabs(sigeff - prev) > 1e-4 && ++guard < 1000);
+  return sigeff;
+}
+
+// Gauss-Legendre rule on [0,1] (Newton iteration on P_n from the
+// asymptotic initial guess).
+void gauss_legendre01(int n, std::vector<double> &x, std::vector<double> &w) {
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  for (int i = 0; i < (n + 1) / 2; i++) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 0;
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1.0, p1 = 0.0;
+      for (int j = 1; j <= n; j++) {
+        double p2 = p1;
+        p1 = p0;
+        p0 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p2) / j;
+      }
+      dp = n * (z * p0 - p1) / (z * z - 1.0);
+      double z1 = z;
+      z = z1 - p0 / dp;
+      if (std::fabs(z - z1) < 1e-15) break;
+    }
+    x[i] = 0.5 * (1.0 - z);
+    x[n - 1 - i] = 0.5 * (1.0 + z);
+    w[i] = w[n - 1 - i] = 1.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+// Nucleus::Nucleus radius/diffuseness/deformation table (src/Nucleus.cpp:58-148)
+smc::NucleusDev make_nucleus(int A, int deformed, double R_ov, double a_ov, double dmin_ov) {
+  smc::NucleusDev n{};
+  n.A = A;
+  n.deformed = deformed;
+  double Ad = A;
+  double rad = 1.12 * std::pow(Ad, 0.333333) - 0.86 / std::pow(Ad, 0.333333), dr = 0.54;
+  if (A == 197) { rad = 6.42; dr = 0.45; }
+  else if (A == 63) { rad = 4.28; dr = 0.5; }
+  else if (A == 238) { rad = 6.86; dr = 0.44; }
+  else if (A == 208) { rad = 6.67; dr = 0.44; }
+  else if (A == 129) { rad = 5.36; dr = 0.590; }
+  if (R_ov > 0) rad = R_ov;
+  if (a_ov > 0) dr = a_ov;
+  n.R = rad;
+  n.a = dr;
+  n.d_min = dmin_ov > 0 ? dmin_ov : 0.9;
+  if (deformed) {
+    if (A == 197) { n.beta2 = -0.13; n.beta4 = -0.03; }
+    else if (A == 63) { n.beta2 = 0.162; n.beta4 = 0.006; }
+    else if (A == 129) { n.beta2 = 0.162; n.beta4 = -0.003; }
+    else if (A == 238) { n.beta2 = 0.28; n.beta4 = 0.093; }
+  }
+  n.rmax_cut = rad + 2.5;
+  n.rw_max = 1.0 / (1.0 + std::exp(-rad / dr));
+  return n;
+}
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t want) {
+    if (want <= n) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * want);
+    if (e == cudaSuccess) n = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct Ctx {
+  smc_params prm{};
+  DevParams P{};
+  smc_info info{};
+  int device = 0, sms = 0;
+  cudaStream_t own = nullptr, st = nullptr;
+  int occ1 = 1, occ2 = 1;
+  int chunk = 4096;
+  DevBuf<EventRec> recs;
+  DevBuf<Source> srcs;
+  DevBuf<double> ecc, pos, bvec, inj_p, inj_t, inj_b;
+  DevBuf<float> rho, ta, tb, scratch;
+  DevBuf<int> status, npart, ncoll, attempts;
+  DevBuf<uint8_t> wounded;
+  DevBuf<double> kln64;
+  DevBuf<float> kln32;
+  std::vector<int> h_status;
+  std::vector<EventRec> h_recs;
+};
+
+#define CK(x)                                   \
+  do {                                          \
+    cudaError_t _e = (x);                       \
+    if (_e != cudaSuccess) return SMC_ERR_CUDA; \
+  } while (0)
+
+smc_status validate(const smc_params &p) {
+  if (p.which_mc_model != 5 && p.which_mc_model != 1 && p.which_mc_model != 7) return SMC_ERR_CONFIG;
+  if (p.which_mc_model == 5 && p.sub_model != 1 && p.sub_model != 2) return SMC_ERR_CONFIG;
+  if (p.shape_of_nucleons != 1 && p.shape_of_nucleons != 2 && p.shape_of_nucleons != 4) return SMC_ERR_CONFIG;
+  if (p.shape_of_entropy != 1 && p.shape_of_entropy != 2) return SMC_ERR_CONFIG;
+  if (p.collision_criterion != 1 && p.collision_criterion != 2) return SMC_ERR_CONFIG;
+  if (p.Aproj < 1 || p.Atarg < 1 || p.Aproj > smc::kMaxA || p.Atarg > smc::kMaxA) return SMC_ERR_CONFIG;
+  if (!(p.dx > 0) || !(p.dy > 0) || !(p.maxx > 0) || !(p.maxy > 0)) return SMC_ERR_CONFIG;
+  if (p.ecc_from_order < 1 || p.ecc_to_order > 9 || p.ecc_from_order > p.ecc_to_order) return SMC_ERR_CONFIG;
+  if (p.bmax < p.bmin || p.bmin < 0) return SMC_ERR_CONFIG;
+  return SMC_OK;
+}
+
+smc_status build_kln_table(Ctx *c) {
+  const smc_params &p = c->prm;
+  int npt = p.kln_npt > 0 ? p.kln_npt : 48, nkt = p.kln_nkt > 0 ? p.kln_nkt : 64,
+      nphi = p.kln_nphi > 0 ? p.kln_nphi : 32;
+  std::vector<double> xp, wp, xk, wk, xf, wf;
+  gauss_legendre01(npt, xp, wp);
+  gauss_legendre01(nkt, xk, wk);
+  gauss_legendre01(nphi, xf, wf);
+  std::vector<double> nodes;
+  for (auto *v : {&xp, &wp, &xk, &wk, &xf, &wf}) nodes.insert(nodes.end(), v->begin(), v->end());
+  double *d_nodes = nullptr;
+  CK(cudaMalloc(&d_nodes, sizeof(double) * nodes.size()));
+  CK(cudaMemcpyAsync(d_nodes, nodes.data(), sizeof(double) * nodes.size(), cudaMemcpyHostToDevice, c->st));
+  smc::KlnDev K{};
+  K.ecm = p.ecm;
+  K.lambda = p.lambda;
+  K.y = 0.0;
+  K.ptmin = 0.1;
+  K.ptmax = 12.0;
+  K.lambda_qcd2 = 0.2 * 0.2;
+  K.alpha_max = 0.5;
+  K.beta0 = (33.0 - 2.0 * 3.0) / (12 * M_PI);
+  double CF = (3.0 * 3.0 - 1.0) / (2 * 3.0);
+  K.fac = CF * 2. / (3. * M_PI * M_PI);
+  const double hbarC = 0.197327053;
+  K.prefactor = 1.0 * 2.0 * (2. / CF / (hbarC * hbarC)) * 9. / 32.;
+  K.npt = npt; K.nkt = nkt; K.nphi = nphi;
+  K.xp = d_nodes; K.wp = d_nodes + npt; K.xk = K.wp + npt; K.wk = K.xk + nkt; K.xf = K.wk + nkt;
+  K.wf = K.xf + nphi;
+  int tmax = c->info.kln_tmax;
+  CK(c->kln64.ensure((size_t)tmax * tmax));
+  CK(c->kln32.ensure((size_t)tmax * tmax));
+  CK(smc::launch_kln_table(K, tmax, c->info.kln_dT, c->kln64.p, c->kln32.p, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  cudaFree(d_nodes);
+  c->P.kln_table = c->kln32.p;
+  return SMC_OK;
+}
+
+smc_status ensure_buffers(Ctx *c, int n, const smc_outputs *out) {
+  const DevParams &P = c->P;
+  CK(c->recs.ensure(n));
+  CK(c->srcs.ensure((size_t)n * P.max_src));
+  CK(c->status.ensure(n));
+  if (!out->device) {
+    size_t g = (size_t)P.nx * P.ny;
+    if (out->ecc) CK(c->ecc.ensure((size_t)n * smc::kEccLen));
+    if (out->rho) CK(c->rho.ensure((size_t)n * g));
+    if (out->ta) CK(c->ta.ensure((size_t)n * g));
+    if (out->tb) CK(c->tb.ensure((size_t)n * g));
+    if (out->positions) CK(c->pos.ensure((size_t)n * 2 * (c->info.A + c->info.B)));
+    if (out->wounded) CK(c->wounded.ensure((size_t)n * (c->info.A + c->info.B)));
+  }
+  if (!out->ecc || out->device == 0) CK(c->ecc.ensure((size_t)n * smc::kEccLen));
+  return SMC_OK;
+}
+
+// Gathers the small per-event scalars out of the event records.
+__global__ void k_scalars(const EventRec *r, int n, int *npart, int *ncoll, double *b, int *attempts) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  if (npart) { npart[2 * e] = r[e].npart1; npart[2 * e + 1] = r[e].npart2; }
+  if (ncoll) ncoll[e] = r[e].ncoll;
+  if (b) b[e] = r[e].b;
+  if (attempts) attempts[e] = r[e].attempts;
+}
+
+// One chunk of events through both stages.  Device outputs land directly in
+// the caller's buffers at offset `off`; host outputs are staged and copied.
+smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_outputs *out,
+                     const double *inj_p, const double *inj_t, const double *inj_b, bool plain) {
+  const DevParams &P = c->P;
+  const size_t g = (size_t)P.nx * P.ny;
+  const int AB = c->info.A + c->info.B;
+  const bool dev = out->device != 0;
+  double *ecc = dev && out->ecc ? out->ecc + (size_t)off * smc::kEccLen : c->ecc.p;
+  float *rho = out->rho ? (dev ? out->rho + (size_t)off * g : c->rho.p) : nullptr;
+  float *ta = out->ta ? (dev ? out->ta + (size_t)off * g : c->ta.p) : nullptr;
+  float *tb = out->tb ? (dev ? out->tb + (size_t)off * g : c->tb.p) : nullptr;
+  double *pos = out->positions ? (dev ? out->positions + (size_t)off * 2 * AB : c->pos.p) : nullptr;
+  uint8_t *wnd = out->wounded ? (dev ? out->wounded + (size_t)off * AB : c->wounded.p) : nullptr;
+  int grid1 = std::max(1, std::min(n, c->sms * c->occ1));
+  int grid2 = std::max(1, std::min(n, c->sms * c->occ2));
+  if (!rho) CK(c->scratch.ensure((size_t)(plain ? 1 : grid2) * g));
+  if (plain) {
+    for (int e = 0; e < n; e++) {
+      CK(smc::launch_sample_pair(P, first_event + e, 1, inj_p ? inj_p + (size_t)e * 2 * c->info.A : nullptr,
+                                 inj_t ? inj_t + (size_t)e * 2 * c->info.B : nullptr, inj_b ? inj_b + e : nullptr,
+                                 c->recs.p + e, c->srcs.p + (size_t)e * P.max_src, pos ? pos + (size_t)e * 2 * AB : nullptr,
+                                 wnd ? wnd + (size_t)e * AB : nullptr, 1, c->st));
+      CK(smc::launch_grid(P, 1, c->recs.p + e, c->srcs.p + (size_t)e * P.max_src, rho ? rho + (size_t)e * g : nullptr,
+                          ta ? ta + (size_t)e * g : nullptr, tb ? tb + (size_t)e * g : nullptr, c->scratch.p,
+                          ecc + (size_t)e * smc::kEccLen, c->status.p + e, 1, c->st));
+    }
+  } else {
+    CK(smc::launch_sample_pair(P, first_event, n, inj_p, inj_t, inj_b, c->recs.p, c->srcs.p, pos, wnd, grid1, c->st));
+    CK(smc::launch_grid(P, n, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p, grid2, c->st));
+  }
+  int *np = out->npart ? (dev ? out->npart + 2 * off : nullptr) : nullptr;
+  int *nc = out->ncoll ? (dev ? out->ncoll + off : nullptr) : nullptr;
+  double *bb = out->b ? (dev ? out->b + off : nullptr) : nullptr;
+  int *at = out->attempts ? (dev ? out->attempts + off : nullptr) : nullptr;
+  if (dev && (np || nc || bb || at)) {
+    k_scalars<<<(n + 255) / 256, 256, 0, c->st>>>(c->recs.p, n, np, nc, bb, at);
+    CK(cudaGetLastError());
+  }
+  // status of every event of the chunk (also carries stage-1 failures)
+  c->h_status.resize(n);
+  CK(cudaMemcpyAsync(c->h_status.data(), c->status.p, sizeof(int) * n, cudaMemcpyDeviceToHost, c->st));
+  if (!dev) {
+    if (out->ecc)
+      CK(cudaMemcpyAsync(out->ecc + (size_t)off * smc::kEccLen, ecc, sizeof(double) * n * smc::kEccLen,
+                         cudaMemcpyDeviceToHost, c->st));
+    if (out->rho) CK(cudaMemcpyAsync(out->rho + (size_t)off * g, rho, sizeof(float) * n * g, cudaMemcpyDeviceToHost, c->st));
+    if (out->ta) CK(cudaMemcpyAsync(out->ta + (size_t)off * g, ta, sizeof(float) * n * g, cudaMemcpyDeviceToHost, c->st));
+    if (out->tb) CK(cudaMemcpyAsync(out->tb + (size_t)off * g, tb, sizeof(float) * n * g, cudaMemcpyDeviceToHost, c->st));
+    if (out->positions)
+      CK(cudaMemcpyAsync(out->positions + (size_t)off * 2 * AB, pos, sizeof(double) * n * 2 * AB,
+                         cudaMemcpyDeviceToHost, c->st));
+    if (out->wounded)
+      CK(cudaMemcpyAsync(out->wounded + (size_t)off * AB, wnd, (size_t)n * AB, cudaMemcpyDeviceToHost, c->st));
+    if (out->npart || out->ncoll || out->b || out->attempts) {
+      c->h_recs.resize(n);
+      CK(cudaMemcpyAsync(c->h_recs.data(), c->recs.p, sizeof(EventRec) * n, cudaMemcpyDeviceToHost, c->st));
+    }
+  }
+  CK(cudaStreamSynchronize(c->st));
+  if (!dev) {
+    for (int e = 0; e < n; e++) {
+      const EventRec &r = c->h_recs.empty() ? EventRec{} : c->h_recs[std::min<size_t>(e, c->h_recs.size() - 1)];
+      if (out->npart) { out->npart[2 * (off + e)] = r.npart1; out->npart[2 * (off + e) + 1] = r.npart2; }
+      if (out->ncoll) out->ncoll[off + e] = r.ncoll;
+      if (out->b) out->b[off + e] = r.b;
+      if (out->attempts) out->attempts[off + e] = r.attempts;
+    }
+  }
+  int worst = 0;
+  for (int e = 0; e < n; e++) worst = std::max(worst, c->h_status[e]);
+  switch (worst) {
+    case 0: return SMC_OK;
+    case 3: return SMC_ERR_RETRY_CAP;
+    case 4: return SMC_ERR_KLN_TABLE;
+    case 5: return SMC_ERR_ZERO_DNDY;
+    case 6: return SMC_ERR_CAPACITY;
+    default: return SMC_ERR_CUDA;
+  }
+}
+
+smc_status run(Ctx *c, uint64_t first_event, int n, const smc_outputs *out, const double *inj_p,
+               const double *inj_t, const double *inj_b, bool plain) {
+  if (n < 0 || !out) return SMC_ERR_ARGUMENT;
+  if (n == 0) return SMC_OK;
+  CK(cudaSetDevice(c->device));
+  smc_status worst = SMC_OK;
+  for (int off = 0; off < n; off += c->chunk) {
+    int m = std::min(c->chunk, n - off);
+    smc_status s = ensure_buffers(c, m, out);
+    if (s) return s;
+    const double *ip = nullptr, *it = nullptr, *ib = nullptr;
+    if (inj_p) {
+      // injected positions are staged on the device
+      size_t np = (size_t)m * 2 * c->info.A, nt = (size_t)m * 2 * c->info.B;
+      CK(c->inj_p.ensure(np));
+      CK(c->inj_t.ensure(nt));
+      cudaMemcpyKind kind = out->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+      CK(cudaMemcpyAsync(c->inj_p.p, inj_p + (size_t)off * 2 * c->info.A, sizeof(double) * np, kind, c->st));
+      CK(cudaMemcpyAsync(c->inj_t.p, inj_t + (size_t)off * 2 * c->info.B, sizeof(double) * nt, kind, c->st));
+      ip = c->inj_p.p;
+      it = c->inj_t.p;
+      if (inj_b) {
+        CK(c->inj_b.ensure(m));
+        CK(cudaMemcpyAsync(c->inj_b.p, inj_b + off, sizeof(double) * m, kind, c->st));
+        ib = c->inj_b.p;
+      }
+    }
+    s = run_chunk(c, first_event + off, off, m, out, ip, it, ib, plain);
+    if (s && s != SMC_ERR_ZERO_DNDY) return s;
+    if (s) worst = s;
+  }
+  return worst;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *smc_status_string(smc_status s) {
+  switch (s) {
+    case SMC_OK: return "ok";
+    case SMC_ERR_ARGUMENT: return "invalid argument";
+    case SMC_ERR_CONFIG: return "unsupported or inconsistent configuration";
+    case SMC_ERR_RETRY_CAP: return "event retry cap reached";
+    case SMC_ERR_KLN_TABLE: return "thickness beyond the KLN dN/dy table";
+    case SMC_ERR_ZERO_DNDY: return "integrated density is zero";
+    case SMC_ERR_CAPACITY: return "per-event collision capacity exceeded";
+    case SMC_ERR_CUDA: return "CUDA runtime error";
+    case SMC_ERR_NO_DEVICE: return "no usable GPU";
+    default: return "unknown status";
+  }
+}
+
+smc_status smc_create(const smc_params *params, void **ctx_out) {
+  if (!params || !ctx_out) return SMC_ERR_ARGUMENT;
+  *ctx_out = nullptr;
+  smc_status v = validate(*params);
+  if (v) return v;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SMC_ERR_NO_DEVICE;
+  Ctx *c = new (std::nothrow) Ctx;
+  if (!c) return SMC_ERR_ARGUMENT;
+  c->prm = *params;
+  const smc_params &p = c->prm;
+  cudaGetDevice(&c->device);
+  cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
+  if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) { delete c; return SMC_ERR_CUDA; }
+  c->st = c->own;
+
+  DevParams &P = c->P;
+  double sigin = p.sigin_override > 0 ? p.sigin_override : sigma_inelastic(p.ecm);
+  double width = 0;
+  if (p.shape_of_nucleons == 1) width = std::sqrt(0.1 * sigin / M_PI) / 2.0;
+  else if (p.shape_of_nucleons == 2) width = std::sqrt(0.1 * sigin / M_PI) / std::sqrt(8.0);
+  else width = p.gauss_nucl_width;
+  P.nx = (int)((p.maxx - (-p.maxx)) / p.dx + 0.1) + 1;   // MCnucl.cpp:39-40
+  P.ny = (int)((p.maxy - (-p.maxy)) / p.dy + 0.1) + 1;
+  P.xmin = -p.maxx; P.ymin = -p.maxy; P.dx = p.dx; P.dy = p.dy;
+  P.width = width; P.w2 = width * width; P.quark_width = p.quark_width;
+  P.peak = 1 / (2 * M_PI * width * width);
+  P.dsq = 0.1 * sigin / M_PI / 1;                       // MCnucl.cpp:120 (overSample = 1)
+  P.sigin = sigin;
+  P.sigma_gg = sigma_gg_from(sigin, width);
+  P.alpha = p.alpha; P.final_factor = p.final_factor;
+  P.which_mc_model = p.which_mc_model; P.sub_model = p.sub_model;
+  P.shape_of_nucleons = p.shape_of_nucleons; P.shape_of_entropy = p.shape_of_entropy;
+  P.collision_criterion = p.collision_criterion;
+  P.npmin = p.npmin; P.npmax = p.npmax; P.bmin = p.bmin; P.bmax = p.bmax;
+  P.nuc[0] = make_nucleus(p.Aproj, p.proj_deformed, p.proj_R, p.proj_a, p.proj_d_min);
+  P.nuc[1] = make_nucleus(p.Atarg, p.targ_deformed, p.targ_R, p.targ_a, p.targ_d_min);
+  P.seed = p.seed;
+  P.max_attempts = p.max_attempts > 0 ? p.max_attempts : 100000;
+  P.max_coll = p.max_collisions > 0 ? p.max_collisions : 4096;
+  P.max_src = 2 * (p.Aproj + p.Atarg) + P.max_coll;
+  P.ecc_from = p.ecc_from_order; P.ecc_to = p.ecc_to_order;
+  P.want_ta = P.want_tb = 0;
+  double d_max = p.shape_of_nucleons == 1 ? 2. * std::sqrt(P.dsq) : 5. * width;
+  double span = std::max(2 * d_max, 8 * std::max(width, p.quark_width));
+  P.splat_mw = (int)(span / std::min(p.dx, p.dy)) + 3;
+  if (p.which_mc_model == 1) {
+    int sub = p.tmax_subdivision > 0 ? p.tmax_subdivision : 3;
+    int tmax = p.tmax > 1 ? p.tmax : 71;
+    P.kln_tmax = (p.shape_of_nucleons >= 2) ? sub * (tmax - 1) + 1 : tmax;   // MCnucl.cpp:915-919
+    P.kln_dT = 10.0 / sigin / 1 / ((p.shape_of_nucleons >= 2) ? sub : 1);
+  }
+  smc_info &I = c->info;
+  I.nx = P.nx; I.ny = P.ny; I.sigin = sigin; I.dsq = P.dsq; I.width = width; I.sigma_gg = P.sigma_gg;
+  I.kln_tmax = P.kln_tmax; I.kln_dT = P.kln_dT; I.A = p.Aproj; I.B = p.Atarg;
+
+  size_t smem2 = smc::grid_smem(P);
+  int dev_smem = 0;
+  cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  if ((int)smem2 > dev_smem) { smc_destroy(c); return SMC_ERR_CONFIG; }
+  // persistent grid sizes from the occupancy the kernels reach
+  c->occ1 = std::max(1, (int)(227 * 1024 / (smc::sample_pair_smem() + 1024)));
+  c->occ1 = std::min(c->occ1, 8);
+  c->occ2 = std::max(1, (int)(228 * 1024 / (smem2 + 1024)));
+  c->occ2 = std::min(c->occ2, 4);
+  if (p.which_mc_model == 1) {
+    smc_status s = build_kln_table(c);
+    if (s) { smc_destroy(c); return s; }
+  }
+  *ctx_out = c;
+  return SMC_OK;
+}
+
+void smc_destroy(void *ctx) {
+  Ctx *c = static_cast<Ctx *>(ctx);
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  c->recs.release(); c->srcs.release(); c->ecc.release(); c->pos.release(); c->bvec.release();
+  c->inj_p.release(); c->inj_t.release(); c->inj_b.release(); c->rho.release(); c->ta.release();
+  c->tb.release(); c->scratch.release(); c->status.release(); c->npart.release(); c->ncoll.release();
+  c->attempts.release(); c->wounded.release(); c->kln64.release(); c->kln32.release();
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+}
+
+smc_status smc_get_info(void *ctx, smc_info *info) {
+  if (!ctx || !info) return SMC_ERR_ARGUMENT;
+  *info = static_cast<Ctx *>(ctx)->info;
+  return SMC_OK;
+}
+
+smc_status smc_set_stream(void *ctx, void *cuda_stream) {
+  if (!ctx) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  c->st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : c->own;
+  return SMC_OK;
+}
+
+smc_status smc_synchronize(void *ctx) {
+  if (!ctx) return SMC_ERR_ARGUMENT;
+  return cudaStreamSynchronize(static_cast<Ctx *>(ctx)->st) == cudaSuccess ? SMC_OK : SMC_ERR_CUDA;
+}
+
+static smc_status set_thickness_flags(Ctx *c, const smc_outputs *out) {
+  c->P.want_ta = out->ta != nullptr;
+  c->P.want_tb = out->tb != nullptr;
+  if ((out->ta || out->tb) && c->P.which_mc_model == 7) return SMC_ERR_CONFIG;
+  return SMC_OK;
+}
+
+smc_status smc_generate(void *ctx, uint64_t first_event, int n, const smc_outputs *out) {
+  if (!ctx || !out) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  smc_status s = set_thickness_flags(c, out);
+  if (s) return s;
+  return run(c, first_event, n, out, nullptr, nullptr, nullptr, false);
+}
+
+smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_outputs *out) {
+  if (!ctx || !out) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  smc_status s = set_thickness_flags(c, out);
+  if (s) return s;
+  return run(c, first_event, n, out, nullptr, nullptr, nullptr, true);
+}
+
+smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_targ, const double *b,
+                      const smc_outputs *out) {
+  if (!ctx || !out || !xy_proj || !xy_targ) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  smc_status s = set_thickness_flags(c, out);
+  if (s) return s;
+  return run(c, 0, n, out, xy_proj, xy_targ, b, false);
+}
+
+smc_status smc_kln_table(void *ctx, double *host_table, int capacity) {
+  if (!ctx || !host_table) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  if (c->P.which_mc_model != 1 || !c->kln64.p) return SMC_ERR_CONFIG;
+  size_t n = (size_t)c->info.kln_tmax * c->info.kln_tmax;
+  if ((size_t)capacity < n) return SMC_ERR_ARGUMENT;
+  CK(cudaMemcpyAsync(host_table, c->kln64.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return SMC_OK;
+}
+
+}  // extern "C"

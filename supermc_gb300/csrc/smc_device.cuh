@@ -1,0 +1,126 @@
+// Device-side definitions shared by the sm_103a kernels of supermc_gb300.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace smc {
+
+constexpr int kMaxA = 256;          // nucleons per nucleus held on chip
+constexpr int kEccLen = 49;         // dumpEccentricities line length
+constexpr int kMaxOrder = 10;
+
+// Source kinds of the splat (which window rule and weight apply).
+enum SrcKind : int {
+  SRC_PART_BOX = 0,   // participant, bounding-box window, r <= 5w cut (MCnucl::addDensity)
+  SRC_COLL = 1,       // binary collision, +-d_max window, dc <= 25 w^2 (MCnucl::setDensity)
+  SRC_THICK = 2,      // participant, +-d_max window, r <= 5w (MCnucl::setThickness)
+};
+
+// One source of the density/thickness splat.  Windows are grid index
+// half-open ranges computed exactly as the reference's (int) casts.
+struct Source {
+  double x, y;        // FP64 position
+  int16_t xl, xr, yl, yr;  // splat window [xl,xr) x [yl,yr)
+  int16_t mx0, mx1, my0, my1;  // eccentricity-mask window (participant boxes)
+  int16_t kind, plane;   // SrcKind, accumulator plane
+  float weight;          // multiplies exp(-r^2/2w^2)
+  float pad;
+};
+static_assert(sizeof(Source) == 48, "Source layout");
+
+struct NucleusDev {
+  int A, deformed;
+  double R, a, beta2, beta4, d_min, rmax_cut, rw_max;
+};
+
+// Per-context constants passed by value to every kernel.
+struct DevParams {
+  int nx, ny;
+  double xmin, ymin, dx, dy;
+  double width, w2, quark_width, peak;   // nucleon width, width^2, 1/(2 pi w^2)
+  double dsq, sigin, sigma_gg;
+  double alpha, final_factor;
+  int which_mc_model, sub_model, shape_of_nucleons, shape_of_entropy, collision_criterion;
+  int npmin, npmax;
+  double bmin, bmax;
+  NucleusDev nuc[2];
+  uint64_t seed;
+  int max_attempts, max_coll, max_src;
+  int ecc_from, ecc_to;
+  int kln_tmax;
+  double kln_dT;
+  const float *kln_table;   // [tmax][tmax] (device)
+  int want_ta, want_tb;     // thickness planes requested
+  int splat_mw;             // widest splat window in columns (+ margin)
+};
+
+// Per-event record written by the sampling/pairing stage.
+struct EventRec {
+  double b;
+  int npart1, npart2, ncoll, nsrc;
+  int attempts, status;
+  int imin, imax, jmin, jmax;   // bounding box of all splat windows (grid idx)
+};
+
+// ---------------------------------------------------------------- Philox
+__host__ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+#ifdef __CUDA_ARCH__
+    uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+#else
+    uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+    uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+  }
+}
+
+__host__ __device__ __forceinline__ double u53(uint32_t lo, uint32_t hi) {
+  uint64_t v = ((uint64_t)hi << 32) | lo;
+  return ((double)(v >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+// Two uniforms in (0,1): counter {slot, stream, event_lo, event_hi},
+// key {seed_lo, seed_hi}.
+__host__ __device__ __forceinline__ void uniform2(uint64_t seed, uint64_t event, uint32_t stream,
+                                                  uint32_t slot, double &u0, double &u1) {
+  uint32_t c[4] = {slot, stream, (uint32_t)event, (uint32_t)(event >> 32)};
+  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  u0 = u53(c[0], c[1]);
+  u1 = u53(c[2], c[3]);
+}
+
+enum StreamId : uint32_t { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4 };
+__host__ __device__ __forceinline__ uint32_t stream_id(int attempt, uint32_t sid) {
+  return ((uint32_t)attempt << 8) | sid;
+}
+
+// ------------------------------------------------------- exact helpers
+// (int)((v - mn)/d) as the reference computes it in FP64 (C++ truncation
+// toward zero).  FP64 division is slow on this part, so the FP32 estimate
+// is used whenever it is provably on the same side of every integer.
+__device__ __forceinline__ int trunc_index(double v, double mn, double d, float inv_d) {
+  float t = (float)(v - mn) * inv_d;      // |error| < ~4e-5 for |t| < 400
+  float f = floorf(t);
+  float fr = t - f;
+  if (fr > 1e-3f && fr < 1.f - 1e-3f) {
+    int i = (int)f;
+    // truncation toward zero differs from floor for negative non-integers
+    return (t < 0.f) ? i + 1 : i;
+  }
+  double e = __ddiv_rn(__dadd_rn(v, -mn), d);
+  return (int)e;
+}
+
+// exact FP64 distance tests with explicit rounding (no contraction)
+__device__ __forceinline__ double sq_dist_rn(double x1, double y1, double x2, double y2) {
+  double dx = __dadd_rn(x2, -x1), dy = __dadd_rn(y2, -y1);
+  return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+}
+
+}  // namespace smc

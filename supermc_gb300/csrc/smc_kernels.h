@@ -1,0 +1,25 @@
+// Launchers of the sm_103a kernels (one translation unit each).
+#pragma once
+#include "smc_device.cuh"
+
+namespace smc {
+
+// MC-KLN quadrature description (KLNModel::func, src/KLNModel.cpp:219-277)
+struct KlnDev {
+  double ecm, lambda, y, ptmin, ptmax, lambda_qcd2, alpha_max, beta0, fac, prefactor;
+  int npt, nkt, nphi;
+  const double *xp, *wp, *xk, *wk, *xf, *wf;   // Gauss-Legendre nodes on [0,1]
+};
+
+size_t sample_pair_smem();
+cudaError_t launch_sample_pair(const DevParams &P, uint64_t first_event, int n_events, const double *inj_proj,
+                               const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
+                               double *out_pos, uint8_t *out_wounded, int grid, cudaStream_t st);
+size_t grid_smem(const DevParams &P);
+cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs, float *out_rho,
+                        float *out_ta, float *out_tb, float *scratch, double *out_ecc, int *status, int grid,
+                        cudaStream_t st);
+cudaError_t launch_kln_table(const KlnDev &K, int tmax, double dT, double *table64, float *table32,
+                             cudaStream_t st);
+
+}  // namespace smc

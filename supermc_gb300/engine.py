@@ -1,0 +1,140 @@
+"""Python host interface over the C ABI (include/supermc.h).
+
+``Engine`` owns one library context.  It is built from the superMC
+``parameters.dat`` key set (see :mod:`supermc_gb300.params`) and exposes the
+batched event generator, the injected-positions path and the plain
+per-event path.  Results come back as numpy arrays (host buffers) or are
+written into caller-provided device tensors.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .params import DEFAULTS, EXTENSION_KEYS, read_parameters
+
+
+def smc_params_from(vals: dict[str, float], seed: int = 1) -> _lib.SmcParams:
+    v = dict(DEFAULTS)
+    v.update(EXTENSION_KEYS)
+    v.update({k.lower(): x for k, x in vals.items()})
+    p = _lib.SmcParams()
+    p.which_mc_model = int(v["which_mc_model"])
+    p.sub_model = int(v["sub_model"])
+    p.shape_of_nucleons = int(v["shape_of_nucleons"])
+    p.shape_of_entropy = int(v["shape_of_entropy"])
+    p.collision_criterion = int(v["collision_criterion"])
+    p.Aproj, p.Atarg = int(v["aproj"]), int(v["atarg"])
+    p.proj_deformed, p.targ_deformed = int(v["proj_deformed"]), int(v["targ_deformed"])
+    p.ecm, p.alpha = v["ecm"], v["alpha"]
+    p.gauss_nucl_width, p.quark_width, p.lambda_ = v["gauss_nucl_width"], v["quark_width"], v["lambda"]
+    p.bmin, p.bmax = v["bmin"], v["bmax"]
+    p.npmin, p.npmax = int(v["npmin"]), int(v["npmax"])
+    p.maxx, p.maxy, p.dx, p.dy = v["maxx"], v["maxy"], v["dx"], v["dy"]
+    p.final_factor = v["finalfactor"]
+    p.tmax, p.tmax_subdivision = int(v["tmax"]), int(v["tmax_subdivision"])
+    p.ecc_from_order, p.ecc_to_order = int(v["ecc_from_order"]), int(v["ecc_to_order"])
+    p.proj_R, p.proj_a, p.targ_R, p.targ_a = v["proj_r"], v["proj_a"], v["targ_r"], v["targ_a"]
+    p.proj_d_min, p.targ_d_min = v["proj_d_min"], v["targ_d_min"]
+    p.sigin_override = v["sigininn_override"]
+    p.kln_npt, p.kln_nkt, p.kln_nphi = int(v["kln_npt"]), int(v["kln_nkt"]), int(v["kln_nphi"])
+    p.seed = int(seed) & ((1 << 64) - 1)
+    p.max_attempts = int(v["max_attempts"])
+    p.max_collisions = int(v["max_collisions"])
+    return p
+
+
+OUTPUT_NAMES = ("ecc", "rho", "ta", "tb", "npart", "ncoll", "b", "attempts", "positions", "wounded")
+
+
+class Engine:
+    def __init__(self, params: dict[str, float] | None = None, seed: int = 1, **overrides):
+        vals = read_parameters(None, [f"{k}={v}" for k, v in (params or {}).items()])
+        vals.update({k.lower(): float(x) for k, x in overrides.items()})
+        self.values = vals
+        self.lib = _lib.load()
+        self.params = smc_params_from(vals, seed)
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.smc_create(ctypes.byref(self.params), ctypes.byref(h)), "smc_create")
+        self.h = h
+        info = _lib.SmcInfo()
+        _lib.check(self.lib.smc_get_info(self.h, ctypes.byref(info)), "smc_get_info")
+        self.info = info
+        self.nx, self.ny, self.A, self.B = info.nx, info.ny, info.A, info.B
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.smc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------
+    def _host_buffers(self, n: int, want) -> dict[str, np.ndarray]:
+        g = (n, self.nx, self.ny)
+        AB = self.A + self.B
+        shapes = {"ecc": ((n, _lib.ECC_LEN), np.float64), "rho": (g, np.float32), "ta": (g, np.float32),
+                  "tb": (g, np.float32), "npart": ((n, 2), np.int32), "ncoll": ((n,), np.int32),
+                  "b": ((n,), np.float64), "attempts": ((n,), np.int32),
+                  "positions": ((n, AB, 2), np.float64), "wounded": ((n, AB), np.uint8)}
+        return {k: np.zeros(*shapes[k]) for k in want}
+
+    @staticmethod
+    def _outputs(bufs: dict, device: bool) -> _lib.SmcOutputs:
+        o = _lib.SmcOutputs()
+        o.device = 1 if device else 0
+        for k in OUTPUT_NAMES:
+            setattr(o, k, _lib.ptr(bufs.get(k)))
+        return o
+
+    def generate(self, first_event: int, n: int, want=("ecc", "npart", "ncoll", "b")) -> dict[str, np.ndarray]:
+        """Batched event generation into host arrays."""
+        bufs = self._host_buffers(n, want)
+        o = self._outputs(bufs, False)
+        _lib.check(self.lib.smc_generate(self.h, first_event, n, ctypes.byref(o)), "smc_generate")
+        return bufs
+
+    def generate_plain(self, first_event: int, n: int, want=("ecc", "npart", "ncoll", "b")) -> dict[str, np.ndarray]:
+        """The unbatched path: one event per launch sequence."""
+        bufs = self._host_buffers(n, want)
+        o = self._outputs(bufs, False)
+        _lib.check(self.lib.smc_generate_plain(self.h, first_event, n, ctypes.byref(o)), "smc_generate_plain")
+        return bufs
+
+    def generate_into(self, first_event: int, n: int, device_bufs: dict, plain: bool = False) -> None:
+        """Writes into caller-owned device tensors (keys of OUTPUT_NAMES)."""
+        o = self._outputs(device_bufs, True)
+        fn = self.lib.smc_generate_plain if plain else self.lib.smc_generate
+        _lib.check(fn(self.h, first_event, n, ctypes.byref(o)), "smc_generate")
+
+    def inject(self, xy_proj, xy_targ, b=None, want=("ecc", "npart", "ncoll", "rho")) -> dict[str, np.ndarray]:
+        """Pairing, grids and eccentricities from given nucleon positions
+        (xy_proj [n,A,2], xy_targ [n,B,2], b [n])."""
+        xp = np.ascontiguousarray(xy_proj, dtype=np.float64)
+        xt = np.ascontiguousarray(xy_targ, dtype=np.float64)
+        if xp.ndim == 2:
+            xp, xt = xp[None], xt[None]
+        n = xp.shape[0]
+        if xp.shape[1:] != (self.A, 2) or xt.shape[1:] != (self.B, 2) or xt.shape[0] != n:
+            raise ValueError("positions must be [n,A,2] and [n,B,2]")
+        bb = None if b is None else np.ascontiguousarray(np.broadcast_to(b, (n,)), dtype=np.float64)
+        bufs = self._host_buffers(n, want)
+        o = self._outputs(bufs, False)
+        _lib.check(self.lib.smc_inject(self.h, n, _lib.ptr(xp), _lib.ptr(xt), _lib.ptr(bb), ctypes.byref(o)),
+                   "smc_inject")
+        return bufs
+
+    def kln_table(self) -> np.ndarray:
+        t = self.info.kln_tmax
+        out = np.zeros((t, t))
+        _lib.check(self.lib.smc_kln_table(self.h, _lib.ptr(out), t * t), "smc_kln_table")
+        return out
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        _lib.check(self.lib.smc_set_stream(self.h, stream_handle), "smc_set_stream")

@@ -46,6 +46,8 @@ EXTENSION_KEYS: dict[str, float] = {
     "proj_d_min": 0.0, "targ_d_min": 0.0, "sigininn_override": 0.0,
     # MC-KLN table quadrature (p_T x k_T x phi Gauss-Legendre nodes)
     "kln_npt": 48, "kln_nkt": 64, "kln_nphi": 32,
+    # event retry cap and per-event collision capacity (0: library defaults)
+    "max_attempts": 0, "max_collisions": 0,
 }
 
 

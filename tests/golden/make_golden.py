@@ -1,0 +1,184 @@
+"""Generates the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a container that holds the reference source tree (default
+/root/reference): it builds oracle/_ref/libsmc_ref.so from those sources
+(oracle/Makefile.ref) and drives the reference's own code through the
+injection harness (oracle/ref_harness.cpp).  The fixtures then pin the
+oracle and the GPU path on machines without the reference.
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from oracle.oracle import Reference, build_reference  # noqa: E402
+from supermc_gb300.params import parameters_text, read_parameters  # noqa: E402
+
+# parameter sets (parameters.dat keys) of the fixtures
+SYSTEMS = {
+    "auau200": ["which_mc_model=5", "sub_model=1", "shape_of_nucleons=4", "gauss_nucl_width=0.5",
+                "collision_criterion=1", "shape_of_entropy=2", "alpha=0.118", "ecm=200", "maxx=13", "maxy=13",
+                "dx=0.1", "dy=0.1", "cc_fluctuation_model=0", "Aproj=197", "Atarg=197", "operation=0",
+                "use_ed=0", "finalFactor=40", "Npmin=2", "Npmax=500", "bmin=0", "bmax=20",
+                "ecc_from_order=1", "ecc_to_order=9"],
+    "pbpb2760": ["which_mc_model=5", "sub_model=1", "shape_of_nucleons=4", "gauss_nucl_width=0.5",
+                 "collision_criterion=1", "shape_of_entropy=2", "alpha=0.118", "ecm=2760", "maxx=13",
+                 "maxy=13", "dx=0.1", "dy=0.1", "cc_fluctuation_model=0", "Aproj=208", "Atarg=208",
+                 "operation=0", "use_ed=0", "finalFactor=40", "Npmin=2", "Npmax=500", "bmin=0", "bmax=20",
+                 "ecc_from_order=1", "ecc_to_order=9"],
+}
+
+
+EOS_DIR = "/root/reference/EOS"
+
+
+def ref_for(args, extra=()):
+    vals = read_parameters(None, list(SYSTEMS[args[0]]) + list(extra), strict=False)
+    return Reference(parameters_text(vals), eos_dir=EOS_DIR), vals
+
+
+def grid_digest(g: np.ndarray, rng: np.random.Generator, ncell: int = 1500):
+    nz = np.argwhere(g != 0)
+    pick = nz[rng.choice(len(nz), size=min(ncell, len(nz)), replace=False)] if len(nz) else np.zeros((0, 2), int)
+    return {"cells": pick.astype(np.int16), "values": g[pick[:, 0], pick[:, 1]] if len(pick) else np.zeros(0),
+            "rowsum": g.sum(axis=1), "colsum": g.sum(axis=0), "total": np.array(g.sum())}
+
+
+def sample_positions(ref: Reference, b: float):
+    """Both nuclei from the reference's own sampler (Nucleus::populate)."""
+    a = ref.populate(0, b / 2.0)[:, :2].copy()
+    t = ref.populate(1, -b / 2.0)[:, :2].copy()
+    return a, t
+
+
+def make_inject(out):
+    rng = np.random.default_rng(20261203)
+    data = {}
+    for name in SYSTEMS:
+        ref, vals = ref_for([name])
+        ev_pos_a, ev_pos_b, ev_b, ecc, np1, np2, nc, partA, partB, colls = [], [], [], [], [], [], [], [], [], []
+        digests = {}
+        for k, b in enumerate([0.7, 3.1, 5.6, 8.2, 10.9, 13.4]):
+            ref.srand(1000 + k)
+            xa, xb = sample_positions(ref, b)
+            n1, n2, c = ref.inject(xa, xb)
+            e = ref.eccentricities(1, 9, n1 + n2, c, b)
+            ev_pos_a.append(xa); ev_pos_b.append(xb); ev_b.append(b)
+            ecc.append(e); np1.append(n1); np2.append(n2); nc.append(c)
+            partA.append(ref.participants(0)); partB.append(ref.participants(1)); colls.append(ref.collisions())
+            if k in (1, 3):
+                for w, gname in enumerate(("ta", "tb", "rho")):
+                    for kk, vv in grid_digest(ref.grid(w), rng).items():
+                        digests[f"ev{k}_{gname}_{kk}"] = vv
+        pre = f"{name}_"
+        data.update({pre + "pos_a": np.array(ev_pos_a), pre + "pos_b": np.array(ev_pos_b),
+                     pre + "b": np.array(ev_b), pre + "ecc": np.array(ecc), pre + "npart1": np.array(np1),
+                     pre + "npart2": np.array(np2), pre + "ncoll": np.array(nc)})
+        for k in range(len(ev_b)):
+            data[pre + f"ev{k}_partA"] = partA[k]
+            data[pre + f"ev{k}_partB"] = partB[k]
+            data[pre + f"ev{k}_coll"] = colls[k]
+        data.update({pre + k: v for k, v in digests.items()})
+        c = ref.constants()
+        data[pre + "constants"] = np.array([c["dsq"], c["width"], c["sigma_gg"], c["sigin"]])
+        # averaged-mode rotation of the event with b = 8.2 fm (orders 2, 3)
+        xa, xb = ev_pos_a[3], ev_pos_b[3]
+        ref.inject(xa, xb)
+        for order in (2, 3):
+            ref.rotate_resplat(order)
+            for kk, vv in grid_digest(ref.grid(2), rng).items():
+                data[pre + f"rot{order}_rho_{kk}"] = vv
+    np.savez_compressed(os.path.join(out, "glauber_inject.npz"), **data)
+
+
+def make_sampler(out):
+    data = {}
+    for A, deformed in [(208, 0), (197, 0), (238, 1), (63, 0), (2, 0), (1, 0)]:
+        ref, _ = ref_for(["pbpb2760"], [f"Aproj={A}", f"Atarg={A}", f"proj_deformed={deformed}",
+                                        f"targ_deformed={deformed}"])
+        for seed in (3, 11):
+            ref.srand(seed)
+            data[f"A{A}_d{deformed}_s{seed}"] = ref.populate(0, 2.5)
+    np.savez_compressed(os.path.join(out, "sampler_drand48.npz"), **data)
+
+
+def make_native_tables(out, nev):
+    data = {}
+    for name in SYSTEMS:
+        ref, _ = ref_for([name], ["ecc_from_order=2", "ecc_to_order=5"])
+        ref.srand(7)
+        tab = ref.generate_ecc_table(nev)
+        data[name] = tab
+    np.savez_compressed(os.path.join(out, "ecc_native.npz"), **data)
+
+
+def make_kln(out):
+    ref, vals = ref_for(["pbpb2760"], ["which_mc_model=1", "sub_model=7", "lambda=0.288"])
+    ref.lib.refh_kln_setup(2760.0, 0.288)
+    rng = np.random.default_rng(5)
+    pts, vals_out, nodes, bases = [], [], [], []
+    for ta, tb in [(0.3, 0.9), (1.7, 2.2), (4.4, 0.5), (9.0, 7.5)]:
+        ref.lib.refh_kln_prepare(0.0, ta, tb)
+        for _ in range(40):
+            x = rng.random(3)
+            pts.append([ta, tb, *x])
+            vals_out.append(ref.lib.refh_kln_integrand(0.0, ta, tb, *x))
+        nodes.append([ta, tb])
+        bases.append(ref.lib.refh_kln_dndy(0.0, ta, tb))
+    # per-cell lookup: an analytic table installed into the reference's MCnucl
+    sig = ref.constants()["sigin"]
+    tmax, dT = 211, 10.0 / sig / 3
+    I, J = np.meshgrid(np.arange(tmax), np.arange(tmax), indexing="ij")
+    table = np.where((I > 0) & (J > 0), np.sqrt(I * dT * J * dT) * 3.0 + 0.1 * (I * dT) ** 2, 0.0)
+    ref.set_kln_table(table, dT)
+    grng = np.random.default_rng(9)
+    ref.srand(21)
+    xa, xb = sample_positions(ref, 6.0)
+    ref.inject(xa, xb)
+    dig = grid_digest(ref.grid(2), grng)
+    np.savez_compressed(os.path.join(out, "kln.npz"), points=np.array(pts), integrand=np.array(vals_out),
+                        nodes=np.array(nodes), bases=np.array(bases), table_dT=np.array(dT),
+                        lookup_pos_a=xa, lookup_pos_b=xb, sigin=np.array(sig),
+                        **{"lookup_rho_" + k: v for k, v in dig.items()})
+
+
+def make_constants(out):
+    ref, _ = ref_for(["auau200"])
+    c = {"sigma_in": {str(e): ref.lib.refh_sigma_in(e) for e in (62.4, 200.0, 2760.0, 3670.0, 5020.0, 5520.0)},
+         "six_point": [[0.3, 0.7, 1, 2, 3, 4, 5, 6, ref.lib.refh_six_point(0.3, 0.7, 1, 2, 3, 4, 5, 6)],
+                       [0.9, 0.1, -1, 0.5, 2, 7, 1, 3, ref.lib.refh_six_point(0.9, 0.1, -1, 0.5, 2, 7, 1, 3)]],
+         "hulthen_cdf": {str(r): ref.lib.refh_hulthen_cdf(r) for r in (0.5, 1.0, 2.0, 4.0, 7.0, 15.0)},
+         "hulthen_inv": {str(u): ref.lib.refh_hulthen_inv(u) for u in (0.05, 0.3, 0.5, 0.77, 0.95)}}
+    with open(os.path.join(out, "constants.json"), "w") as f:
+        json.dump(c, f, indent=1)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--nev", type=int, default=1500)
+    a = ap.parse_args()
+    if build_reference(a.ref) is None:
+        sys.exit(f"reference tree not found at {a.ref}")
+    global EOS_DIR
+    EOS_DIR = os.path.join(a.ref, "EOS")
+    make_constants(HERE)
+    make_sampler(HERE)
+    make_inject(HERE)
+    make_kln(HERE)
+    make_native_tables(HERE, a.nev)
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,40 @@
+"""Parameter sets shared by the tests (parameters.dat keys) and helpers to
+build the oracle's parameter struct from them."""
+import math
+
+from supermc_gb300.params import derive, read_parameters
+
+BASE = dict(which_mc_model=5, sub_model=1, shape_of_nucleons=4, gauss_nucl_width=0.5, collision_criterion=1,
+            shape_of_entropy=2, alpha=0.118, maxx=13, maxy=13, dx=0.1, dy=0.1, cc_fluctuation_model=0,
+            finalFactor=40, Npmin=2, Npmax=500, bmin=0, bmax=20, ecc_from_order=1, ecc_to_order=9,
+            quark_width=0.3)
+AUAU200 = dict(BASE, Aproj=197, Atarg=197, ecm=200)
+PBPB2760 = dict(BASE, Aproj=208, Atarg=208, ecm=2760)
+SYSTEMS = {"auau200": AUAU200, "pbpb2760": PBPB2760}
+
+
+def values(system: dict, **over) -> dict:
+    d = dict(system)
+    d.update(over)
+    return read_parameters(None, [f"{k}={v}" for k, v in d.items()])
+
+
+def oracle_params(vals: dict, sigma_gg: float | None = None):
+    from oracle.oracle import Params
+    from oracle.oracle import Oracle
+    d = derive(vals)
+    if sigma_gg is None:
+        sigma_gg = Oracle().lib.smco_sigeff(d.sigin, d.width)
+    return Params(nx=d.nx, ny=d.ny, xmax=vals["maxx"], ymax=vals["maxy"], dx=vals["dx"], dy=vals["dy"],
+                  width=d.width, quark_width=vals["quark_width"], dsq=d.dsq, sigin=d.sigin, sigma_gg=sigma_gg,
+                  alpha=vals["alpha"], which_mc_model=int(vals["which_mc_model"]),
+                  sub_model=int(vals["sub_model"]), shape_of_nucleons=int(vals["shape_of_nucleons"]),
+                  shape_of_entropy=int(vals["shape_of_entropy"]),
+                  collision_criterion=int(vals["collision_criterion"]), final_factor=vals["finalfactor"],
+                  npmin=int(vals["npmin"]), npmax=int(vals["npmax"]))
+
+
+def fmt8(a):
+    """Round like the reference's text output (setprecision(8))."""
+    import numpy as np
+    return np.vectorize(lambda v: float("%.8g" % v))(a)
