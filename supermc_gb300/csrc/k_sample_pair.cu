@@ -13,6 +13,7 @@
 #include "smc_kernels.h"
 
 #include <cfloat>
+#include <climits>
 
 namespace smc {
 
@@ -21,7 +22,7 @@ constexpr int kNT = 256;   // threads per CTA; also the candidate batch size
 struct SampleSmem {
   float cx[kNT], cy[kNT], cz[kNT];          // candidate batch (nucleus frame)
   uint8_t valid[kNT];
-  uint32_t conflict[kNT][kNT / 32];          // intra-batch hard-core conflicts
+  uint32_t keep[kNT / 32], drop[kNT / 32];   // batch resolution state
   int order[kNT];
   int n_new;
   float ax[2][kMaxA], ay[2][kMaxA], az[2][kMaxA];  // accepted (nucleus frame)
@@ -30,8 +31,10 @@ struct SampleSmem {
   int hits[2][kMaxA];
   int scan[kNT];
   double red[kNT / 32 * 3];
+  float2 red2[kNT / 32 * 2];
   int ired[kNT / 32 * 4];
   double red4[kNT / 32];
+  long long lred[32];
   double b;
 };
 
@@ -102,13 +105,22 @@ __device__ double hulthen_inv(double y) {
   return XX2;
 }
 
-__device__ __forceinline__ double block_sum_d(double v, double *red, int slot) {
-  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+// Sum over the block of FP32 values, exact to double precision for the
+// sums that occur here (double-float pairs; no FP64 arithmetic).
+__device__ __forceinline__ double block_sum_f(float v, float2 *red, int slot) {
+  float hi = v, lo = 0.f;
+  for (int o = 16; o; o >>= 1) {
+    float bh = __shfl_xor_sync(0xffffffffu, hi, o), bl = __shfl_xor_sync(0xffffffffu, lo, o);
+    float s2 = hi + bh, bb = s2 - hi;
+    float e = (hi - (s2 - bb)) + (bh - bb) + (lo + bl);
+    hi = s2 + e;
+    lo = e - (hi - s2);
+  }
   int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) red[slot * (kNT / 32) + w] = v;
+  if (l == 0) red[slot * (kNT / 32) + w] = make_float2(hi, lo);
   __syncthreads();
   double s = 0;
-  for (int i = 0; i < kNT / 32; i++) s += red[slot * (kNT / 32) + i];
+  for (int i = 0; i < kNT / 32; i++) s += (double)red[slot * (kNT / 32) + i].x + (double)red[slot * (kNT / 32) + i].y;
   return s;
 }
 
@@ -151,34 +163,60 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
     sm.cx[tid] = x; sm.cy[tid] = y; sm.cz[tid] = z;
     sm.valid[tid] = ok;
     __syncthreads();
+    // conflicts with earlier candidates of the batch, one 32-bit word per warp
     uint32_t m[kNT / 32];
 #pragma unroll
-    for (int q = 0; q < kNT / 32; q++) m[q] = 0;
-    if (ok) {
-      for (int k = 0; k < tid; k++) {
-        if (!sm.valid[k]) continue;
-        float dx = x - sm.cx[k], dy = y - sm.cy[k], dz = z - sm.cz[k];
-        if (dx * dx + dy * dy + dz * dz < dmin2) m[k >> 5] |= 1u << (k & 31);
+    for (int q = 0; q < kNT / 32; q++) {
+      uint32_t bits = 0;
+      if (ok) {
+        const int kmax = min(32, tid - q * 32);
+        for (int kk = 0; kk < kmax; kk++) {
+          const int k = q * 32 + kk;
+          if (!sm.valid[k]) continue;
+          float dx = x - sm.cx[k], dy = y - sm.cy[k], dz = z - sm.cz[k];
+          if (dx * dx + dy * dy + dz * dz < dmin2) bits |= 1u << kk;
+        }
       }
+      m[q] = bits;
     }
-#pragma unroll
-    for (int q = 0; q < kNT / 32; q++) sm.conflict[tid][q] = m[q];
+    // Sequential rule "keep candidate c iff it conflicts with no earlier kept
+    // candidate", resolved in parallel rounds: a candidate is kept once all
+    // its earlier conflicting candidates are decided dropped, and dropped as
+    // soon as one of them is kept.  Rounds end when every candidate is
+    // decided (the longest conflict chain is a few links).
+    if (tid < kNT / 32) { sm.keep[tid] = 0u; sm.drop[tid] = 0u; }
     __syncthreads();
-    if (tid == 0) {
-      uint32_t accb[kNT / 32];
+    bool decided = !ok;
+    for (int round = 0; round < kNT; round++) {
+      bool keep = false, drop = false;
+      if (!decided) {
+        bool all_dropped = true;
 #pragma unroll
-      for (int q = 0; q < kNT / 32; q++) accb[q] = 0;
-      int k = 0;
-      for (int cc = 0; cc < kNT && n_acc + k < A; cc++) {
-        if (!sm.valid[cc]) continue;
-        bool clash = false;
-#pragma unroll
-        for (int q = 0; q < kNT / 32; q++) clash |= (sm.conflict[cc][q] & accb[q]) != 0;
-        if (clash) continue;
-        accb[cc >> 5] |= 1u << (cc & 31);
-        sm.order[k++] = cc;
+        for (int q = 0; q < kNT / 32; q++) {
+          uint32_t cm = m[q];
+          if (cm & sm.keep[q]) drop = true;
+          if (cm & ~sm.drop[q]) all_dropped = false;
+        }
+        keep = !drop && all_dropped;
       }
-      sm.n_new = k;
+      __syncthreads();
+      if (keep) atomicOr(&sm.keep[tid >> 5], 1u << (tid & 31));
+      if (drop) atomicOr(&sm.drop[tid >> 5], 1u << (tid & 31));
+      if (keep || drop) decided = true;
+      int pending = __syncthreads_count(!decided);
+      if (!pending) break;
+    }
+    // kept candidates in candidate order, up to the nucleons still missing
+    {
+      uint32_t kw = sm.keep[tid >> 5];
+      int before = 0;
+      for (int q = 0; q < (tid >> 5); q++) before += __popc(sm.keep[q]);
+      before += __popc(kw & ((1u << (tid & 31)) - 1u));
+      bool kept = (kw >> (tid & 31)) & 1u;
+      if (kept && n_acc + before < A) sm.order[before] = tid;
+      int total = 0;
+      for (int q = 0; q < kNT / 32; q++) total += __popc(sm.keep[q]);
+      if (tid == 0) sm.n_new = min(total, A - n_acc);
     }
     __syncthreads();
     int k = sm.n_new;
@@ -203,24 +241,28 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
   if (inj_xy) {
     if (tid < A) { px = inj_xy[2 * tid]; py = inj_xy[2 * tid + 1]; }
   } else {
-    double sx = tid < A ? (double)sm.ax[w][tid] : 0.0;
-    double sy = tid < A ? (double)sm.ay[w][tid] : 0.0;
-    double mx = block_sum_d(sx, sm.red, 0);
-    double my = block_sum_d(sy, sm.red, 1);
+    double mx = block_sum_f(tid < A ? sm.ax[w][tid] : 0.f, sm.red2, 0);
+    double my = block_sum_f(tid < A ? sm.ay[w][tid] : 0.f, sm.red2, 1);
     __syncthreads();
     if (tid < A) {
       px = (double)sm.ax[w][tid] - mx / A + xc;
       py = (double)sm.ay[w][tid] - my / A;
     }
   }
-  // stash unsorted in X/Y, then rank-sort by x
-  if (tid < A) { sm.X[w][tid] = px; sm.Y[w][tid] = py; }
+  // stash unsorted, then rank-sort by x: FP32 keys order the FP64 values
+  // exactly except between equal keys, where the FP64 values decide
+  const float pxf = (float)px;
+  if (tid < A) { sm.X[w][tid] = px; sm.Y[w][tid] = py; sm.Xf[w][tid] = pxf; }
   __syncthreads();
   int rank = 0;
   if (tid < A) {
     for (int j = 0; j < A; j++) {
-      double xj = sm.X[w][j];
-      rank += (xj < px) || (xj == px && j < tid);
+      float xf = sm.Xf[w][j];
+      if (xf < pxf) rank++;
+      else if (xf == pxf) {
+        double xj = sm.X[w][j];
+        rank += (xj < px) || (xj == px && j < tid);
+      }
     }
   }
   __syncthreads();
@@ -234,10 +276,19 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
 // Bounding-box edges of a nucleon at x (Particle::Particle + calculateBounds,
 // src/Particle.cpp:16-24,94-99, with all quarks at the nucleon centre).
 __device__ __forceinline__ double box_lo(double x, const DevParams &P) {
-  return fmin(x - 4 * P.width, x - 4 * P.quark_width);
+  return x - 4 * fmax(P.width, P.quark_width);   // = min(x - 4w, x - 4 w_q), exactly
 }
 __device__ __forceinline__ double box_hi(double x, const DevParams &P) {
-  return fmax(x + 4 * P.width, x + 4 * P.quark_width);
+  return x + 4 * fmax(P.width, P.quark_width);
+}
+
+// signed-integer key with the order of the FP64 values
+__device__ __forceinline__ long long order_key(double d) {
+  long long b = __double_as_longlong(d);
+  return b >= 0 ? b : b ^ 0x7fffffffffffffffLL;
+}
+__device__ __forceinline__ double from_order_key(long long k) {
+  return __longlong_as_double(k >= 0 ? k : k ^ 0x7fffffffffffffffLL);
 }
 
 // Target range swept for projectile i by MCnucl::getBinaryCollision
@@ -310,7 +361,7 @@ __device__ __forceinline__ void set_window(Source &s, double lo, double hi, doub
 }
 
 // ----------------------------------------------------------------- kernel
-__global__ void __launch_bounds__(kNT) k_sample_pair(DevParams P, uint64_t first_event, int n_events,
+__global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P, uint64_t first_event, int n_events,
                                                      const double *inj_proj, const double *inj_targ,
                                                      const double *inj_b, EventRec *recs, Source *srcs,
                                                      double *out_pos, uint8_t *out_wounded) {
@@ -426,40 +477,46 @@ __global__ void __launch_bounds__(kNT) k_sample_pair(DevParams P, uint64_t first
     const float disk_val = (float)(10.0 / P.sigin);
 
     // region of the eccentricity mask: union of participant boxes and the
-    // (unset, all-zero) collision boxes
-    double rxl = ncoll > 0 ? 0.0 : DBL_MAX, rxr = ncoll > 0 ? 0.0 : -DBL_MAX;
-    double ryl = rxl, ryr = rxr;
+    // (unset, all-zero) collision boxes.  Box edges are x -+ c with
+    // c = 4 max(w, quark_width), monotone in x, so the region follows from
+    // the extreme participant coordinates, found with integer order keys
+    // of the FP64 values (no FP64 arithmetic).
+    const double cbox = 4 * fmax(P.width, P.quark_width);
+    double rxl, rxr, ryl, ryr;
     {
-      double lxl = DBL_MAX, lxr = -DBL_MAX, lyl = DBL_MAX, lyr = -DBL_MAX;
+      long long kx0 = LLONG_MAX, kx1 = LLONG_MIN, ky0 = LLONG_MAX, ky1 = LLONG_MIN;
       for (int k = tid; k < AB; k += kNT) {
         int w = k < A ? 0 : 1, i = k < A ? k : k - A;
         if (sm.hits[w][i] == 0) continue;
-        double x = sm.X[w][i], y = sm.Y[w][i];
-        lxl = fmin(lxl, fmin(x - 4 * P.width, x - 4 * P.quark_width));
-        lxr = fmax(lxr, fmax(x + 4 * P.width, x + 4 * P.quark_width));
-        lyl = fmin(lyl, fmin(y - 4 * P.width, y - 4 * P.quark_width));
-        lyr = fmax(lyr, fmax(y + 4 * P.width, y + 4 * P.quark_width));
+        long long kx = order_key(sm.X[w][i]), ky = order_key(sm.Y[w][i]);
+        kx0 = min(kx0, kx); kx1 = max(kx1, kx); ky0 = min(ky0, ky); ky1 = max(ky1, ky);
       }
       for (int o = 16; o; o >>= 1) {
-        lxl = fmin(lxl, __shfl_xor_sync(0xffffffffu, lxl, o));
-        lxr = fmax(lxr, __shfl_xor_sync(0xffffffffu, lxr, o));
-        lyl = fmin(lyl, __shfl_xor_sync(0xffffffffu, lyl, o));
-        lyr = fmax(lyr, __shfl_xor_sync(0xffffffffu, lyr, o));
+        kx0 = min(kx0, __shfl_xor_sync(0xffffffffu, kx0, o));
+        kx1 = max(kx1, __shfl_xor_sync(0xffffffffu, kx1, o));
+        ky0 = min(ky0, __shfl_xor_sync(0xffffffffu, ky0, o));
+        ky1 = max(ky1, __shfl_xor_sync(0xffffffffu, ky1, o));
       }
+      __syncthreads();
       if ((tid & 31) == 0) {
         int w = tid >> 5;
-        sm.red[w] = lxl; sm.red[kNT / 32 + w] = lxr; sm.red[2 * (kNT / 32) + w] = lyl;
-        sm.red4[w] = lyr;
+        sm.lred[w] = kx0; sm.lred[8 + w] = kx1; sm.lred[16 + w] = ky0; sm.lred[24 + w] = ky1;
       }
       __syncthreads();
       for (int q = 0; q < kNT / 32; q++) {
-        rxl = fmin(rxl, sm.red[q]);
-        rxr = fmax(rxr, sm.red[kNT / 32 + q]);
-        ryl = fmin(ryl, sm.red[2 * (kNT / 32) + q]);
-        ryr = fmax(ryr, sm.red4[q]);
+        kx0 = min(kx0, sm.lred[q]); kx1 = max(kx1, sm.lred[8 + q]);
+        ky0 = min(ky0, sm.lred[16 + q]); ky1 = max(ky1, sm.lred[24 + q]);
       }
       __syncthreads();
-      if (np1 + np2 == 0 && ncoll == 0) { rxl = rxr = ryl = ryr = 0.0; }
+      if (np1 + np2 == 0) {
+        rxl = rxr = ryl = ryr = 0.0;
+      } else {
+        rxl = from_order_key(kx0) - cbox; rxr = from_order_key(kx1) + cbox;
+        ryl = from_order_key(ky0) - cbox; ryr = from_order_key(ky1) + cbox;
+        if (ncoll > 0) {
+          rxl = fmin(rxl, 0.0); rxr = fmax(rxr, 0.0); ryl = fmin(ryl, 0.0); ryr = fmax(ryr, 0.0);
+        }
+      }
     }
     const int nXp = (int)((rxr - rxl) / P.dx), nYp = (int)((ryr - ryl) / P.dy);
     const int ioff = (int)((rxl - P.xmin) / P.dx), joff = (int)((ryl - P.ymin) / P.dy);
@@ -495,18 +552,16 @@ __global__ void __launch_bounds__(kNT) k_sample_pair(DevParams P, uint64_t first
           {
             Source s;
             s.x = x; s.y = y;
-            double bxl = fmin(x - 4 * P.width, x - 4 * P.quark_width);
-            double bxr = fmax(x + 4 * P.width, x + 4 * P.quark_width);
-            double byl = fmin(y - 4 * P.width, y - 4 * P.quark_width);
-            double byr = fmax(y + 4 * P.width, y + 4 * P.quark_width);
+            const double bxl = x - cbox, bxr = x + cbox, byl = y - cbox, byr = y + cbox;
             if (box_src) {
               set_window(s, bxl, bxr, P.xmin, P.dx, inv_dx, P.nx, true);
               set_window(s, byl, byr, P.ymin, P.dy, inv_dy, P.ny, false);
             } else {
               s.xl = s.xr = s.yl = s.yr = 0;   // eccentricity mask only
             }
-            int x0 = (int)((bxl - rxl) / P.dx), x1 = (int)((bxr - rxl) / P.dx);
-            int y0 = (int)((byl - ryl) / P.dy), y1 = (int)((byr - ryl) / P.dx);
+            // mask lattice of MakeDensity.cpp:2356-2358 (its y upper bound divides by dx)
+            int x0 = trunc_index(bxl, rxl, P.dx, inv_dx), x1 = trunc_index(bxr, rxl, P.dx, inv_dx);
+            int y0 = trunc_index(byl, ryl, P.dy, inv_dy), y1 = trunc_index(byr, ryl, P.dx, inv_dx);
             s.mx0 = (int16_t)(max(0, x0) + ioff); s.mx1 = (int16_t)(min(nXp, x1) + ioff);
             s.my0 = (int16_t)(max(0, y0) + joff); s.my1 = (int16_t)(min(nYp, y1) + joff);
             s.kind = box_src ? (SRC_PART_BOX | (disk_e ? 16 : 0)) : 3;
@@ -523,7 +578,7 @@ __global__ void __launch_bounds__(kNT) k_sample_pair(DevParams P, uint64_t first
             set_window(s, y - d_max, y + d_max, P.ymin, P.dy, inv_dy, P.ny, false);
             s.mx0 = s.mx1 = s.my0 = s.my1 = 0;
             s.kind = SRC_THICK | (disk_n ? 16 : 0);
-            s.plane = w == 0 ? 1 : 2;
+            s.plane = model == 1 ? w : 1 + w;   // MC-KLN splats T_A, T_B only
             s.weight = disk_n ? disk_val : peak;
             s.pad = 0.f;
             S[pos++] = s;

@@ -425,6 +425,7 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
   P.max_src = 2 * (p.Aproj + p.Atarg) + P.max_coll;
   P.ecc_from = p.ecc_from_order; P.ecc_to = p.ecc_to_order;
   P.want_ta = P.want_tb = 0;
+  P.n_planes = p.which_mc_model == 5 ? 3 : 2;   // largest layout, checked below
   double d_max = p.shape_of_nucleons == 1 ? 2. * std::sqrt(P.dsq) : 5. * width;
   double span = std::max(2 * d_max, 8 * std::max(width, p.quark_width));
   P.splat_mw = (int)(span / std::min(p.dx, p.dy)) + 3;
@@ -445,8 +446,7 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
   // persistent grid sizes from the occupancy the kernels reach
   c->occ1 = std::max(1, (int)(227 * 1024 / (smc::sample_pair_smem() + 1024)));
   c->occ1 = std::min(c->occ1, 8);
-  c->occ2 = std::max(1, (int)(228 * 1024 / (smem2 + 1024)));
-  c->occ2 = std::min(c->occ2, 4);
+  c->occ2 = 1;
   if (p.which_mc_model == 1) {
     smc_status s = build_kln_table(c);
     if (s) { smc_destroy(c); return s; }
@@ -487,9 +487,15 @@ smc_status smc_synchronize(void *ctx) {
 }
 
 static smc_status set_thickness_flags(Ctx *c, const smc_outputs *out) {
-  c->P.want_ta = out->ta != nullptr;
-  c->P.want_tb = out->tb != nullptr;
-  if ((out->ta || out->tb) && c->P.which_mc_model == 7) return SMC_ERR_CONFIG;
+  DevParams &P = c->P;
+  P.want_ta = out->ta != nullptr;
+  P.want_tb = out->tb != nullptr;
+  if ((out->ta || out->tb) && P.which_mc_model == 7) return SMC_ERR_CONFIG;
+  // splat planes: Glauber rho (+ T_A, T_B on request); MC-KLN T_A, T_B;
+  // sqrt(T_A T_B) scaling rho_A, rho_B
+  P.n_planes = P.which_mc_model == 5 ? ((P.want_ta || P.want_tb) ? 3 : 1) : 2;
+  size_t smem2 = smc::grid_smem(P);
+  c->occ2 = std::max(1, std::min(4, (int)(228 * 1024 / (smem2 + 1024))));
   return SMC_OK;
 }
 

@@ -52,6 +52,7 @@ struct DevParams {
   const float *kln_table;   // [tmax][tmax] (device)
   int want_ta, want_tb;     // thickness planes requested
   int splat_mw;             // widest splat window in columns (+ margin)
+  int n_planes;             // accumulator planes of the splat (1..3)
 };
 
 // Per-event record written by the sampling/pairing stage.
