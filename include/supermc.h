@@ -147,6 +147,21 @@ smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_
  * kernel launch sequence (the unbatched baseline). */
 smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_outputs *out);
 
+/* Counters and kernel timing of a context (no reference counterpart; the
+ * reference only times the whole run with clock(), src/main.cpp:40-68).
+ * With timing enabled, CUDA events bracket every launch of the two event
+ * kernels on the context's stream and their durations are summed. */
+typedef struct smc_stats {
+  uint64_t events;          /* events produced                              */
+  uint64_t attempts;        /* sampling attempts (retries included)         */
+  uint64_t launches;        /* kernels launched                             */
+  uint64_t sample_launches, grid_launches;
+  double sample_ms, grid_ms;/* summed kernel durations (timing enabled)     */
+} smc_stats;
+smc_status smc_set_timing(void *ctx, int enabled);
+smc_status smc_get_stats(void *ctx, smc_stats *stats);
+smc_status smc_reset_stats(void *ctx);
+
 /* MC-KLN dN/dy table (MCnucl::makeTable, src/MCnucl.cpp:911-960): copies the
  * current table ([tmax][tmax] doubles, rapidity slice 0) to host. */
 smc_status smc_kln_table(void *ctx, double *host_table, int capacity);

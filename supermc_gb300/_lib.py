@@ -11,7 +11,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libsupermc_gb300.so")
+LIB_PATH = os.environ.get("SUPERMC_GB300_LIB") or os.path.join(HERE, "_build", "libsupermc_gb300.so")
 
 SMC_OK = 0
 STATUS_NAMES = {
@@ -23,7 +23,8 @@ ECC_LEN = 49
 
 # exported symbols, in the order include/supermc.h declares them
 EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "smc_set_stream",
-           "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_plain", "smc_kln_table"]
+           "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_plain", "smc_set_timing",
+           "smc_get_stats", "smc_reset_stats", "smc_kln_table"]
 
 
 class SmcError(RuntimeError):
@@ -66,6 +67,12 @@ class SmcInfo(ctypes.Structure):
     ]
 
 
+class SmcStats(ctypes.Structure):
+    _fields_ = [("events", ctypes.c_uint64), ("attempts", ctypes.c_uint64), ("launches", ctypes.c_uint64),
+                ("sample_launches", ctypes.c_uint64), ("grid_launches", ctypes.c_uint64),
+                ("sample_ms", ctypes.c_double), ("grid_ms", ctypes.c_double)]
+
+
 class SmcOutputs(ctypes.Structure):
     _fields_ = [
         ("device", ctypes.c_int),
@@ -100,6 +107,9 @@ def load() -> ctypes.CDLL:
     lib.smc_generate_plain.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(SmcOutputs)]
     lib.smc_inject.argtypes = [vp, ctypes.c_int, vp, vp, vp, ctypes.POINTER(SmcOutputs)]
     lib.smc_kln_table.argtypes = [vp, vp, ctypes.c_int]
+    lib.smc_set_timing.argtypes = [vp, ctypes.c_int]
+    lib.smc_get_stats.argtypes = [vp, ctypes.POINTER(SmcStats)]
+    lib.smc_reset_stats.argtypes = [vp]
     _lib = lib
     return lib
 

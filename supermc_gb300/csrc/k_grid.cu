@@ -507,6 +507,16 @@ __global__ void __launch_bounds__(kGT) k_grid(DevParams P, int n_events, const E
 
 size_t grid_smem(const DevParams &P) { return grid_layout(P.nx, P.ny, P.splat_mw, P.n_planes).total; }
 
+int grid_blocks_per_sm(const DevParams &P) {
+  const bool narrow = P.ecc_from >= 2 && P.ecc_to <= 5;
+  const void *k = narrow ? (const void *)k_grid<2, 5> : (const void *)k_grid<1, 9>;
+  size_t smem = grid_smem(P);
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
+  int nb = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kGT, smem) != cudaSuccess) return 1;
+  return nb > 0 ? nb : 1;
+}
+
 cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs, float *out_rho,
                         float *out_ta, float *out_tb, float *scratch, double *out_ecc, int *status, int grid,
                         cudaStream_t st) {

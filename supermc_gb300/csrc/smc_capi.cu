@@ -160,7 +160,55 @@ struct Ctx {
   DevBuf<float> kln32;
   std::vector<int> h_status;
   std::vector<EventRec> h_recs;
+  // counters and optional kernel timing
+  smc_stats stats{};
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;   // kind, (start, stop)
+  size_t ev_next = 0;
 };
+
+cudaEvent_t next_event(Ctx *c) {
+  if (c->ev_next == c->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    c->ev_pool.push_back(e);
+  }
+  return c->ev_pool[c->ev_next++];
+}
+
+// brackets one kernel launch with events when timing is on
+template <typename F>
+cudaError_t timed(Ctx *c, int kind, F &&launch) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (c->timing) {
+    a = next_event(c);
+    b = next_event(c);
+    if (a) cudaEventRecord(a, c->st);
+  }
+  cudaError_t e = launch();
+  if (c->timing && a && b) {
+    cudaEventRecord(b, c->st);
+    c->pending.push_back({kind, {a, b}});
+  }
+  c->stats.launches++;
+  if (kind == 0) c->stats.sample_launches++;
+  else c->stats.grid_launches++;
+  return e;
+}
+
+// folds recorded kernel durations into the counters (after a stream sync)
+void collect_timing(Ctx *c) {
+  for (auto &p : c->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
+      if (p.first == 0) c->stats.sample_ms += ms;
+      else c->stats.grid_ms += ms;
+    }
+  }
+  c->pending.clear();
+  c->ev_next = 0;
+}
 
 #define CK(x)                                   \
   do {                                          \
@@ -267,17 +315,28 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
   if (!rho) CK(c->scratch.ensure((size_t)(plain ? 1 : grid2) * g));
   if (plain) {
     for (int e = 0; e < n; e++) {
-      CK(smc::launch_sample_pair(P, first_event + e, 1, inj_p ? inj_p + (size_t)e * 2 * c->info.A : nullptr,
-                                 inj_t ? inj_t + (size_t)e * 2 * c->info.B : nullptr, inj_b ? inj_b + e : nullptr,
-                                 c->recs.p + e, c->srcs.p + (size_t)e * P.max_src, pos ? pos + (size_t)e * 2 * AB : nullptr,
-                                 wnd ? wnd + (size_t)e * AB : nullptr, 1, c->st));
-      CK(smc::launch_grid(P, 1, c->recs.p + e, c->srcs.p + (size_t)e * P.max_src, rho ? rho + (size_t)e * g : nullptr,
-                          ta ? ta + (size_t)e * g : nullptr, tb ? tb + (size_t)e * g : nullptr, c->scratch.p,
-                          ecc + (size_t)e * smc::kEccLen, c->status.p + e, 1, c->st));
+      CK(timed(c, 0, [&] {
+        return smc::launch_sample_pair(P, first_event + e, 1, inj_p ? inj_p + (size_t)e * 2 * c->info.A : nullptr,
+                                       inj_t ? inj_t + (size_t)e * 2 * c->info.B : nullptr,
+                                       inj_b ? inj_b + e : nullptr, c->recs.p + e,
+                                       c->srcs.p + (size_t)e * P.max_src, pos ? pos + (size_t)e * 2 * AB : nullptr,
+                                       wnd ? wnd + (size_t)e * AB : nullptr, 1, c->st);
+      }));
+      CK(timed(c, 1, [&] {
+        return smc::launch_grid(P, 1, c->recs.p + e, c->srcs.p + (size_t)e * P.max_src,
+                                rho ? rho + (size_t)e * g : nullptr, ta ? ta + (size_t)e * g : nullptr,
+                                tb ? tb + (size_t)e * g : nullptr, c->scratch.p, ecc + (size_t)e * smc::kEccLen,
+                                c->status.p + e, 1, c->st);
+      }));
     }
   } else {
-    CK(smc::launch_sample_pair(P, first_event, n, inj_p, inj_t, inj_b, c->recs.p, c->srcs.p, pos, wnd, grid1, c->st));
-    CK(smc::launch_grid(P, n, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p, grid2, c->st));
+    CK(timed(c, 0, [&] {
+      return smc::launch_sample_pair(P, first_event, n, inj_p, inj_t, inj_b, c->recs.p, c->srcs.p, pos, wnd, grid1,
+                                     c->st);
+    }));
+    CK(timed(c, 1, [&] {
+      return smc::launch_grid(P, n, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p, grid2, c->st);
+    }));
   }
   int *np = out->npart ? (dev ? out->npart + 2 * off : nullptr) : nullptr;
   int *nc = out->ncoll ? (dev ? out->ncoll + off : nullptr) : nullptr;
@@ -286,6 +345,7 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
   if (dev && (np || nc || bb || at)) {
     k_scalars<<<(n + 255) / 256, 256, 0, c->st>>>(c->recs.p, n, np, nc, bb, at);
     CK(cudaGetLastError());
+    c->stats.launches++;
   }
   // status of every event of the chunk (also carries stage-1 failures)
   c->h_status.resize(n);
@@ -308,6 +368,8 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
     }
   }
   CK(cudaStreamSynchronize(c->st));
+  collect_timing(c);
+  c->stats.events += n;
   if (!dev) {
     for (int e = 0; e < n; e++) {
       const EventRec &r = c->h_recs.empty() ? EventRec{} : c->h_recs[std::min<size_t>(e, c->h_recs.size() - 1)];
@@ -464,6 +526,7 @@ void smc_destroy(void *ctx) {
   c->inj_p.release(); c->inj_t.release(); c->inj_b.release(); c->rho.release(); c->ta.release();
   c->tb.release(); c->scratch.release(); c->status.release(); c->npart.release(); c->ncoll.release();
   c->attempts.release(); c->wounded.release(); c->kln64.release(); c->kln32.release();
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
 }
@@ -494,8 +557,8 @@ static smc_status set_thickness_flags(Ctx *c, const smc_outputs *out) {
   // splat planes: Glauber rho (+ T_A, T_B on request); MC-KLN T_A, T_B;
   // sqrt(T_A T_B) scaling rho_A, rho_B
   P.n_planes = P.which_mc_model == 5 ? ((P.want_ta || P.want_tb) ? 3 : 1) : 2;
-  size_t smem2 = smc::grid_smem(P);
-  c->occ2 = std::max(1, std::min(4, (int)(228 * 1024 / (smem2 + 1024))));
+  if (P.ny > 512) return SMC_ERR_CONFIG;
+  c->occ2 = smc::grid_blocks_per_sm(P);
   return SMC_OK;
 }
 
@@ -522,6 +585,24 @@ smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_
   smc_status s = set_thickness_flags(c, out);
   if (s) return s;
   return run(c, 0, n, out, xy_proj, xy_targ, b, false);
+}
+
+smc_status smc_set_timing(void *ctx, int enabled) {
+  if (!ctx) return SMC_ERR_ARGUMENT;
+  static_cast<Ctx *>(ctx)->timing = enabled != 0;
+  return SMC_OK;
+}
+
+smc_status smc_get_stats(void *ctx, smc_stats *stats) {
+  if (!ctx || !stats) return SMC_ERR_ARGUMENT;
+  *stats = static_cast<Ctx *>(ctx)->stats;
+  return SMC_OK;
+}
+
+smc_status smc_reset_stats(void *ctx) {
+  if (!ctx) return SMC_ERR_ARGUMENT;
+  static_cast<Ctx *>(ctx)->stats = smc_stats{};
+  return SMC_OK;
 }
 
 smc_status smc_kln_table(void *ctx, double *host_table, int capacity) {

@@ -16,6 +16,7 @@ cudaError_t launch_sample_pair(const DevParams &P, uint64_t first_event, int n_e
                                const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
                                double *out_pos, uint8_t *out_wounded, int grid, cudaStream_t st);
 size_t grid_smem(const DevParams &P);
+int grid_blocks_per_sm(const DevParams &P);
 cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs, float *out_rho,
                         float *out_ta, float *out_tb, float *scratch, double *out_ecc, int *status, int grid,
                         cudaStream_t st);

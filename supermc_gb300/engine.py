@@ -136,5 +136,16 @@ class Engine:
         _lib.check(self.lib.smc_kln_table(self.h, _lib.ptr(out), t * t), "smc_kln_table")
         return out
 
+    def set_timing(self, enabled: bool) -> None:
+        _lib.check(self.lib.smc_set_timing(self.h, 1 if enabled else 0), "smc_set_timing")
+
+    def stats(self) -> dict:
+        st = _lib.SmcStats()
+        _lib.check(self.lib.smc_get_stats(self.h, ctypes.byref(st)), "smc_get_stats")
+        return {k: getattr(st, k) for k, _ in _lib.SmcStats._fields_}
+
+    def reset_stats(self) -> None:
+        _lib.check(self.lib.smc_reset_stats(self.h), "smc_reset_stats")
+
     def set_stream(self, stream_handle: int | None) -> None:
         _lib.check(self.lib.smc_set_stream(self.h, stream_handle), "smc_set_stream")
