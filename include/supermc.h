@@ -40,7 +40,9 @@ enum {
   SMC_ERR_ZERO_DNDY = 5,    /* integrated density is zero (MCnucl.cpp:812)  */
   SMC_ERR_CAPACITY = 6,     /* a per-event buffer (collisions) overflowed   */
   SMC_ERR_CUDA = 7,         /* CUDA runtime error                           */
-  SMC_ERR_NO_DEVICE = 8     /* no usable GPU                                */
+  SMC_ERR_NO_DEVICE = 8,    /* no usable GPU                                */
+  SMC_ERR_SCRATCH_LIMIT = 9 /* request larger than smc_inject_noalloc's
+                               fixed scratch                                */
 };
 
 /* Physics and grid configuration: the parameters.dat keys of the path
@@ -165,6 +167,29 @@ smc_status smc_reset_stats(void *ctx);
 /* MC-KLN dN/dy table (MCnucl::makeTable, src/MCnucl.cpp:911-960): copies the
  * current table ([tmax][tmax] doubles, rapidity slice 0) to host. */
 smc_status smc_kln_table(void *ctx, double *host_table, int capacity);
+
+/* smc_inject without any device allocation.  No counterpart in the
+ * reference (which allocates host arrays freely); it exists for callers that
+ * may not call cudaMalloc -- a host framework that owns all device memory
+ * through its own pool, or a code path that must not change the allocation
+ * state (e.g. around stream capture).  The caller passes device buffers:
+ * positions d_xy_proj [n][A][2], d_xy_targ [n][B][2], d_b [n] (may be NULL),
+ * and the outputs d_ecc [n][49], d_rho [n][nx][ny], d_status [n] (per-event
+ * smc_status).  Work is queued on cuda_stream (NULL: the legacy default
+ * stream) and is complete when that stream is.
+ *   - Intermediate data use one static 24 MiB device array: each event needs
+ *     64 + 48 * (2 (A + B) + max_collisions) bytes (max_collisions defaults to
+ *     2048 here), e.g. at most 180 Pb+Pb events per call; larger n returns
+ *     SMC_ERR_SCRATCH_LIMIT.
+ *   - All calls share that array: calls that overlap on the GPU (other
+ *     streams, other threads) race.  Nothing in it needs clearing.
+ *   - The first call on a device looks up the array's device address with
+ *     that device current; make it before any stream capture.
+ *   - MC-Glauber (which_mc_model 5) and sqrt(T_A T_B) (7) only.
+ * Allocates nothing: no cudaMalloc, cudaFree or allocating library call. */
+smc_status smc_inject_noalloc(const smc_params *params, int n, const double *d_xy_proj,
+                              const double *d_xy_targ, const double *d_b, double *d_ecc,
+                              float *d_rho, int *d_status, void *cuda_stream);
 
 #ifdef __cplusplus
 }

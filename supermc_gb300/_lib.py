@@ -17,14 +17,14 @@ SMC_OK = 0
 STATUS_NAMES = {
     0: "SMC_OK", 1: "SMC_ERR_ARGUMENT", 2: "SMC_ERR_CONFIG", 3: "SMC_ERR_RETRY_CAP",
     4: "SMC_ERR_KLN_TABLE", 5: "SMC_ERR_ZERO_DNDY", 6: "SMC_ERR_CAPACITY", 7: "SMC_ERR_CUDA",
-    8: "SMC_ERR_NO_DEVICE",
+    8: "SMC_ERR_NO_DEVICE", 9: "SMC_ERR_SCRATCH_LIMIT",
 }
 ECC_LEN = 49
 
 # exported symbols, in the order include/supermc.h declares them
 EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "smc_set_stream",
            "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_plain", "smc_set_timing",
-           "smc_get_stats", "smc_reset_stats", "smc_kln_table"]
+           "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_inject_noalloc"]
 
 
 class SmcError(RuntimeError):
@@ -110,6 +110,7 @@ def load() -> ctypes.CDLL:
     lib.smc_set_timing.argtypes = [vp, ctypes.c_int]
     lib.smc_get_stats.argtypes = [vp, ctypes.POINTER(SmcStats)]
     lib.smc_reset_stats.argtypes = [vp]
+    lib.smc_inject_noalloc.argtypes = [ctypes.POINTER(SmcParams), ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]
     _lib = lib
     return lib
 

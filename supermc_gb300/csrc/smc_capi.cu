@@ -440,6 +440,7 @@ const char *smc_status_string(smc_status s) {
     case SMC_ERR_CAPACITY: return "per-event collision capacity exceeded";
     case SMC_ERR_CUDA: return "CUDA runtime error";
     case SMC_ERR_NO_DEVICE: return "no usable GPU";
+    case SMC_ERR_SCRATCH_LIMIT: return "request exceeds the fixed scratch of smc_inject_noalloc";
     default: return "unknown status";
   }
 }
