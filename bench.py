@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Throughput benchmark of the superMC initial-condition path on GB300.
 
-Workload (configs[1] of the benchmark description): MC-KLN Pb+Pb, A=B=208,
+Workload: MC-KLN Pb+Pb at 2.76 TeV, A=B=208,
 Woods-Saxon R=6.62 fm, a=0.546 fm, sigma_NN=64 mb, b^2 uniform on
 [0,400] fm^2, 261x261 grid at dx=0.1 fm, saturation exponent 0.288;
 eccentricities eps_2..eps_5.  One step = one batch of events generated

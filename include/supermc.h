@@ -149,6 +149,24 @@ smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_
  * kernel launch sequence (the unbatched baseline). */
 smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_outputs *out);
 
+/* Averaged profiles: MakeDensity::generate_profile_average
+ * (src/MakeDensity.cpp:736-2103, per-event loop :1240-1577).  For events
+ * [first_event, first_event + n) -- generated, or injected when xy_proj /
+ * xy_targ (host, [n][A][2], [n][B][2]) are given -- and every order
+ * n_ord = from_order..to_order in turn, the sources are rotated to the
+ * order-n_ord participant plane about the density's centre of mass
+ * (MCnucl::rotateGrid, src/MCnucl.cpp:1152-1174) and re-splatted; with
+ * reaction_plane != 0 they are first recentred only
+ * (MCnucl::recenterGrid, :1119-1150; the reaction-plane-frame average).
+ * mean / mean_rp [to-from+1][nx][ny] (host) receive the event averages of
+ * the entropy density getRho * finalFactor (MakeDensity::setSd,
+ * :2514-2522) over the events with a binary collision (their count in
+ * *n_used, may be NULL; injected events without one are left out).  The
+ * moves accumulate across orders as in the reference. */
+smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_proj,
+                       const double *xy_targ, const double *b, int from_order, int to_order,
+                       int reaction_plane, double *mean, double *mean_rp, int *n_used);
+
 /* Counters and kernel timing of a context (no reference counterpart; the
  * reference only times the whole run with clock(), src/main.cpp:40-68).
  * With timing enabled, CUDA events bracket every launch of the two event

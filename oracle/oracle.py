@@ -127,6 +127,7 @@ class Oracle:
                                                   ctypes.c_double, _D]
         lib.smco_event_cm_angle.argtypes = [ctypes.c_void_p, ctypes.c_int, _D, _D, _D]
         lib.smco_event_rotate_resplat.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.smco_event_recenter_resplat.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.smco_kln_init.argtypes = [ctypes.POINTER(KLN), ctypes.c_double, ctypes.c_double]
         lib.smco_kln_integrand.restype = ctypes.c_double
         lib.smco_kln_integrand.argtypes = [ctypes.POINTER(KLN), ctypes.c_double, ctypes.c_double, _D]
@@ -237,6 +238,9 @@ class OracleEvent:
     def rotate_resplat(self, order):
         return self.lib.smco_event_rotate_resplat(self.h, order)
 
+    def recenter_resplat(self, order):
+        return self.lib.smco_event_recenter_resplat(self.h, order)
+
     def populate_drand48(self, nA, nB, b):
         self.lib.smco_event_populate_drand48(self.h, ctypes.byref(nA), ctypes.byref(nB), b)
 
@@ -262,6 +266,8 @@ class Reference:
         lib.refh_eccentricities.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_double, _D]
         lib.refh_rotate_and_resplat.argtypes = [ctypes.c_int]
+        lib.refh_recenter_and_resplat.argtypes = [ctypes.c_int]
+        lib.refh_density.argtypes = []
         lib.refh_generate_ecc_table.argtypes = [ctypes.c_int]
         lib.refh_sample_event.argtypes = [ctypes.c_double, _I, _I, _I]
         lib.refh_populate.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, _D, ctypes.c_int]
@@ -335,6 +341,9 @@ class Reference:
     def rotate_resplat(self, order):
         self.lib.refh_rotate_and_resplat(order)
 
+    def recenter_resplat(self, order):
+        self.lib.refh_recenter_and_resplat(order)
+
     def srand(self, seed):
         self.lib.refh_srand(seed)
 
@@ -342,6 +351,9 @@ class Reference:
         out = np.zeros((400, 3))
         n = self.lib.refh_populate(which, xc, yc, _ptr(out), 400)
         return out[:n].copy()
+
+    def density(self):
+        self.lib.refh_density()
 
     def sample_event(self, b):
         n1, n2, nc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

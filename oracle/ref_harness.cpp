@@ -264,6 +264,23 @@ void refh_rotate_and_resplat(int order) {
   m->setDensity(0, -1);
 }
 
+// calculateThickness + setDensity of the current event (after
+// refh_sample_event), as the averaged mode does first (src/MakeDensity.cpp:1264,1275).
+void refh_density() {
+  MCnucl *m = mc();
+  m->calculateThickness();
+  m->setDensity(0, -1);
+}
+
+// Reaction-plane-frame step of the averaged mode (src/MakeDensity.cpp:1291-1293):
+// recenter the sources on the density's centre of mass, recompute.
+void refh_recenter_and_resplat(int order) {
+  MCnucl *m = mc();
+  m->recenterGrid(0, order);
+  m->calculateThickness();
+  m->setDensity(0, -1);
+}
+
 // The op-9 event loop of the reference with its native sampler
 // (MakeDensity::generateEccTable); results are appended by the reference to
 // data/sn_ecc_eccp_*.dat in the working directory.

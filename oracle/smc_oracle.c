@@ -482,8 +482,10 @@ void smco_event_populate_drand48(smco_event *e, const smco_nucleus *nA, const sm
  * four uniforms (slots 2c, 2c+1 of the nucleus's stream); a rejected
  * candidate is simply skipped.  The nucleus orientation comes from the
  * event stream. Positions are built exactly as the GPU sampler builds them:
- * candidate in the nucleus frame, centre of mass removed, shifted by +-b/2;
- * boxes are centred on the final positions. */
+ * candidate in the nucleus frame, centre of mass removed, shifted by +-b/2.
+ * As in Nucleus::populate (Nucleus.cpp:274-309) a Woods-Saxon nucleon is
+ * constructed at its nucleus-frame point and then moved, so its base box
+ * stays there; light nuclei are constructed in place (:199-236). */
 static int populate_philox(smco_event *e, int w, const smco_nucleus *n, double xc, double yc,
                            uint64_t seed, uint64_t event, int attempt) {
   double o[2];
@@ -530,10 +532,15 @@ static int populate_philox(smco_event *e, int w, const smco_nucleus *n, double x
     double xcm = 0, ycm = 0, zcm = 0;
     for (int i = 0; i < cnt; i++) { xcm += px[i]; ycm += py[i]; zcm += pz[i]; }
     for (int i = 0; i < cnt; i++) {
-      px[i] = px[i] - xcm / A;
-      py[i] = py[i] - ycm / A;
-      pz[i] = pz[i] - zcm / A;
+      nucleon_t *q = &e->nuc[w][i];
+      construct(e, q, px[i], py[i], pz[i]);
+      set_x(q, px[i] - xcm / A + xc);
+      set_y(q, py[i] - ycm / A + yc);
+      q->z = pz[i] - zcm / A;
     }
+    e->n[w] = cnt;
+    qsort(e->nuc[w], cnt, sizeof(nucleon_t), cmp_xleft);
+    return 0;
   }
   for (int i = 0; i < cnt; i++) construct(e, &e->nuc[w][i], px[i] + xc, py[i] + yc, pz[i]);
   e->n[w] = cnt;
@@ -1047,6 +1054,30 @@ void smco_event_cm_angle(const smco_event *e, int n, double *xcm, double *ycm, d
   *xcm = X;
   *ycm = Y;
   *angle = -atan2(-ni, -nr) / n;
+}
+
+/* MCnucl::recenterGrid (MCnucl.cpp:1119-1150): shifts every source by the
+ * density's centre of mass (the boxes move with Box2D::setCenter), then
+ * calculateThickness and setDensity -- the reaction-plane-frame step of
+ * MakeDensity.cpp:1291-1293 */
+int smco_event_recenter_resplat(smco_event *e, int order) {
+  double X, Y, ang;
+  smco_event_cm_angle(e, order, &X, &Y, &ang);
+  for (int w = 0; w < 2; w++)
+    for (int k = 0; k < e->npart[w]; k++) {
+      nucleon_t *q = &e->nuc[w][e->part[w][k]];
+      set_x(q, q->x - X);
+      set_y(q, q->y - Y);
+    }
+  for (int c = 0; c < e->ncoll; c++) {
+    e->cx[c] = e->cx[c] - X;
+    box_set_center_xy(&e->cbox[c], e->cx[c], e->cbox[c].yc);
+    e->cy[c] = e->cy[c] - Y;
+    box_set_center_xy(&e->cbox[c], e->cbox[c].xc, e->cy[c]);
+  }
+  int rc = smco_event_thickness(e);
+  if (rc) return rc;
+  return smco_event_density(e);
 }
 
 /* MCnucl::recenterGrid + rotateGrid (MCnucl.cpp:1119-1174), then

@@ -120,6 +120,9 @@ void smco_event_cm_angle(const smco_event *e, int n, double *xcm, double *ycm, d
 /* MCnucl::rotateGrid (MCnucl.cpp:1152-1174) + calculateThickness +
  * setDensity, i.e. one averaged-mode step (MakeDensity.cpp:1331-1333) */
 int smco_event_rotate_resplat(smco_event *e, int order);
+/* MCnucl::recenterGrid (MCnucl.cpp:1119-1150) + calculateThickness +
+ * setDensity: the reaction-plane-frame step (MakeDensity.cpp:1291-1293) */
+int smco_event_recenter_resplat(smco_event *e, int order);
 
 /* ------------------------------------------------------------------ */
 /* MC-KLN                                                               */

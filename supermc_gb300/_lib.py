@@ -24,7 +24,7 @@ ECC_LEN = 49
 # exported symbols, in the order include/supermc.h declares them
 EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "smc_set_stream",
            "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_plain", "smc_set_timing",
-           "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_inject_noalloc"]
+           "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_inject_noalloc", "smc_average"]
 
 
 class SmcError(RuntimeError):
@@ -110,6 +110,8 @@ def load() -> ctypes.CDLL:
     lib.smc_set_timing.argtypes = [vp, ctypes.c_int]
     lib.smc_get_stats.argtypes = [vp, ctypes.POINTER(SmcStats)]
     lib.smc_reset_stats.argtypes = [vp]
+    lib.smc_average.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int, vp, vp, ctypes.POINTER(ctypes.c_int)]
     lib.smc_inject_noalloc.argtypes = [ctypes.POINTER(SmcParams), ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]
     _lib = lib
     return lib

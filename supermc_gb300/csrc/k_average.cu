@@ -1,0 +1,242 @@
+// Averaged-profile mode (MakeDensity::generate_profile_average,
+// src/MakeDensity.cpp:736-2103; per-event loop :1240-1577).
+//
+// Per event and order n the reference recomputes the density, optionally
+// recentres the sources on the density's centre of mass and re-splats
+// (reaction-plane frame, :1291-1293), then rotates the sources to the
+// order-n participant plane and re-splats (:1331-1333); the densities are
+// averaged over all accepted events.  Here:
+//   k_avg_init      per-source state: construction position and bounding box;
+//   k_avg_transform centre of mass and angle of one event's grid
+//                   (GlueDensity::calcCMAngle, src/GlueDensity.cpp:87-144) and
+//                   the source transform of MCnucl::recenterGrid / rotateGrid
+//                   (src/MCnucl.cpp:1119-1174) in FP64 with the reference's
+//                   rounding, including Box2D's move arithmetic and the reset of
+//                   a participant's box to its construction-time box
+//                   (Particle::calculateBounds, src/Particle.cpp:94-99);
+//   k_avg_accum     sum of the chunk's grids into FP64 accumulators.
+// The splat itself is k_grid (without the eccentricity pass).
+#include "smc_device.cuh"
+#include "smc_kernels.h"
+
+#include <algorithm>
+
+namespace smc {
+
+constexpr int kAT = 256;
+
+__global__ void k_avg_init(DevParams P, int n_events, const EventRec *recs, const Source *srcs, AvgSrc *state) {
+  const double c = 4 * fmax(P.width, P.quark_width);
+  for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
+    const int ns = recs[e].nsrc;
+    for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+      const Source &s = srcs[(size_t)e * P.max_src + k];
+      AvgSrc a;
+      if (s.kind & SRC_RAW_BASE) {
+        // built at (bx, by): box = base U quark box there, then
+        // Particle::setX / setY move it by Box2D::setCenter
+        a.x0 = s.bx;
+        a.y0 = s.by;
+        const double xl = a.x0 - c, xr = a.x0 + c, yl = a.y0 - c, yr = a.y0 + c;
+        const double xc = (xl + xr) / 2.0, yc = (yl + yr) / 2.0;
+        a.bxl = xl + (s.x - xc); a.bxr = xr + (s.x - xc); a.bxc = s.x;
+        a.byl = yl + (s.y - yc); a.byr = yr + (s.y - yc); a.byc = s.y;
+      } else {
+        a.x0 = s.x;
+        a.y0 = s.y;
+        a.bxl = s.x - c; a.bxr = s.x + c; a.byl = s.y - c; a.byr = s.y + c;   // Particle::Particle box
+        a.bxc = (a.bxl + a.bxr) / 2.0;                                        // Box2D::overUnion centre
+        a.byc = (a.byl + a.byr) / 2.0;
+      }
+      state[(size_t)e * P.max_src + k] = a;
+    }
+  }
+}
+
+struct DFs {
+  float hi, lo;
+};
+__device__ __forceinline__ DFs dfs_add(DFs a, DFs b) {
+  float s = a.hi + b.hi, bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb) + (a.lo + b.lo);
+  float h = s + e;
+  return {h, e - (h - s)};
+}
+__device__ double block_sum_df(float v, float c, float2 *red) {
+  DFs x{v, -c};
+  for (int o = 16; o; o >>= 1)
+    x = dfs_add(x, DFs{__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)});
+  const int w = threadIdx.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[w] = make_float2(x.hi, x.lo);
+  __syncthreads();
+  double s = 0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += (double)red[i].x + (double)red[i].y;
+  return s;
+}
+
+struct Kahan {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float y = x - c, t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+};
+
+// mode 0: recenter (MCnucl::recenterGrid); mode 1: rotate (MCnucl::rotateGrid)
+__global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events, EventRec *recs, Source *srcs,
+                                                       AvgSrc *state, const float *rho, int order, int mode) {
+  __shared__ float2 red[kAT / 32];
+  __shared__ double s_par[4];   // X, Y, cos, sin
+  __shared__ int s_box[4];      // the event's new window bounds: imin, imax, jmin, jmax
+  const int tid = threadIdx.x;
+  const int nx = P.nx, ny = P.ny;
+  const float inv_dx = (float)(1.0 / P.dx), inv_dy = (float)(1.0 / P.dy);
+  const double d_max = P.shape_of_nucleons == 1 ? 2. * sqrt(P.dsq) : 5. * P.width;
+  for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
+    const EventRec rec = recs[e];
+    const float *g = rho + (size_t)e * nx * ny;
+    // ---- centre of mass over the full grid (weights rho dx dy; dx dy cancels)
+    Kahan sw, sx, sy;
+    for (int c = tid; c < nx * ny; c += kAT) {
+      const float v = g[c];
+      if (v == 0.f) continue;
+      const int i = c / ny, j = c - i * ny;
+      sw.add(v);
+      sx.add((float)(P.xmin + i * P.dx) * v);
+      sy.add((float)(P.ymin + j * P.dy) * v);
+    }
+    const double W = block_sum_df(sw.s, sw.c, red);
+    const double SX = block_sum_df(sx.s, sx.c, red);
+    const double SY = block_sum_df(sy.s, sy.c, red);
+    if (!(W > 0)) continue;   // empty density: nothing to move (uniform over the block)
+    const double X = SX / W, Y = SY / W;
+    // ---- order-n angle: sum r^n e^{in theta} rho about the centre (full grid)
+    Kahan sr, si;
+    const float Xf = (float)X, Yf = (float)Y;
+    for (int c = tid; c < nx * ny; c += kAT) {
+      const float v = g[c];
+      if (v == 0.f) continue;
+      const int i = c / ny, j = c - i * ny;
+      const float x = (float)(P.xmin + i * P.dx) - Xf, y = (float)(P.ymin + j * P.dy) - Yf;
+      float zr = x, zi = y;
+      for (int k = 1; k < order; k++) {
+        const float t = zr * x - zi * y;
+        zi = zr * y + zi * x;
+        zr = t;
+      }
+      sr.add(zr * v);
+      si.add(zi * v);
+    }
+    const double NR = block_sum_df(sr.s, sr.c, red);
+    const double NI = block_sum_df(si.s, si.c, red);
+    if (tid == 0) {
+      const double ang = -atan2(-NI, -NR) / order;   // GlueDensity.cpp:140
+      s_par[0] = X;
+      s_par[1] = Y;
+      s_par[2] = cos(ang);
+      s_par[3] = sin(ang);
+      s_box[0] = nx; s_box[1] = 0; s_box[2] = ny; s_box[3] = 0;
+    }
+    __syncthreads();
+    const double cx = s_par[0], cy = s_par[1], cphi = s_par[2], sphi = s_par[3];
+    // ---- transform the sources (FP64, reference rounding)
+    const double c4w = 4 * P.width, c4q = 4 * P.quark_width;
+    for (int k = tid; k < rec.nsrc; k += kAT) {
+      Source &s = srcs[(size_t)e * P.max_src + k];
+      AvgSrc &a = state[(size_t)e * P.max_src + k];
+      const int kind = s.kind & 15;
+      // recenterGrid: setX(x - X) then setY(y - Y); boxes move by Box2D::setCenter
+      double x = __dadd_rn(s.x, -cx);
+      a.bxl = __dadd_rn(a.bxl, __dadd_rn(x, -a.bxc));
+      a.bxr = __dadd_rn(a.bxr, __dadd_rn(x, -a.bxc));
+      a.bxc = x;
+      double y = __dadd_rn(s.y, -cy);
+      a.byl = __dadd_rn(a.byl, __dadd_rn(y, -a.byc));
+      a.byr = __dadd_rn(a.byr, __dadd_rn(y, -a.byc));
+      a.byc = y;
+      if (mode == 1) {
+        // Point3D::rotate(cos(0), phi): x' = cphi x - sphi y, y' = sphi x + cphi y
+        const double xr = __dadd_rn(__dmul_rn(cphi, x), -__dmul_rn(sphi, y));
+        const double yr = __dadd_rn(__dmul_rn(sphi, x), __dmul_rn(cphi, y));
+        x = xr;
+        y = yr;
+        // Particle::calculateBounds: construction box U quark box at the new position
+        a.bxl = fmin(__dadd_rn(a.x0, -c4w), __dadd_rn(x, -c4q));
+        a.bxr = fmax(__dadd_rn(a.x0, c4w), __dadd_rn(x, c4q));
+        a.byl = fmin(__dadd_rn(a.y0, -c4w), __dadd_rn(y, -c4q));
+        a.byr = fmax(__dadd_rn(a.y0, c4w), __dadd_rn(y, c4q));
+        a.bxc = (a.bxl + a.bxr) / 2.0;
+        a.byc = (a.byl + a.byr) / 2.0;
+      }
+      s.x = x;
+      s.y = y;
+      // splat windows from the new geometry (src/MCnucl.cpp:829-832, :732-735, :450-453);
+      // mask-only records keep their empty window
+      if (kind == 3) continue;
+      int xl, xr, yl, yr;
+      if (kind == SRC_PART_BOX) {
+        xl = trunc_index(a.bxl, P.xmin, P.dx, inv_dx); xr = trunc_index(a.bxr, P.xmin, P.dx, inv_dx);
+        yl = trunc_index(a.byl, P.ymin, P.dy, inv_dy); yr = trunc_index(a.byr, P.ymin, P.dy, inv_dy);
+        // After a rotation the box (construction box U quark box) can be far
+        // wider than the splat's column table; only cells within the
+        // inclusion radius of the source count (r <= 5w, or dc <= dsq for a
+        // disk), so the window is cut to the rows / columns that can hold
+        // one -- a superset, the per-cell test stays exact.
+        const double R = (s.kind & 16) ? sqrt(P.dsq) : 5.0 * P.width;
+        xl = max(xl, (int)floor((x - R - P.xmin) / P.dx - 0.01));
+        xr = min(xr, (int)floor((x + R - P.xmin) / P.dx + 0.01) + 1);
+        yl = max(yl, (int)floor((y - R - P.ymin) / P.dy - 0.01));
+        yr = min(yr, (int)floor((y + R - P.ymin) / P.dy + 0.01) + 1);
+      } else {
+        xl = trunc_index(__dadd_rn(x, -d_max), P.xmin, P.dx, inv_dx);
+        xr = trunc_index(__dadd_rn(x, d_max), P.xmin, P.dx, inv_dx);
+        yl = trunc_index(__dadd_rn(y, -d_max), P.ymin, P.dy, inv_dy);
+        yr = trunc_index(__dadd_rn(y, d_max), P.ymin, P.dy, inv_dy);
+      }
+      xl = max(0, xl); xr = min(nx, xr);
+      yl = max(0, yl); yr = min(ny, yr);
+      s.xl = (int16_t)xl; s.xr = (int16_t)xr;
+      s.yl = (int16_t)yl; s.yr = (int16_t)yr;
+      if (xr > xl && yr > yl) {
+        atomicMin(&s_box[0], xl); atomicMax(&s_box[1], xr);
+        atomicMin(&s_box[2], yl); atomicMax(&s_box[3], yr);
+      }
+    }
+    __syncthreads();
+    // the splat visits only the rows of the event's window bounds
+    if (tid == 0) {
+      recs[e].imin = s_box[0]; recs[e].imax = s_box[1];
+      recs[e].jmin = s_box[2]; recs[e].jmax = s_box[3];
+    }
+  }
+}
+
+// acc[cell] += sum over the chunk's events of rho_e[cell] (Kahan in FP32 over
+// the chunk, then one FP64 add per cell)
+__global__ void k_avg_accum(const float *rho, int n_events, size_t cells, double *acc) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (size_t)gridDim.x * blockDim.x) {
+    Kahan k;
+    for (int e = 0; e < n_events; e++) k.add(rho[(size_t)e * cells + c]);
+    acc[c] += (double)k.s - (double)k.c;
+  }
+}
+
+cudaError_t launch_avg_init(const DevParams &P, int n, const EventRec *recs, const Source *srcs, AvgSrc *state,
+                            int grid, cudaStream_t st) {
+  k_avg_init<<<grid, kAT, 0, st>>>(P, n, recs, srcs, state);
+  return cudaGetLastError();
+}
+cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Source *srcs, AvgSrc *state,
+                                 const float *rho, int order, int mode, int grid, cudaStream_t st) {
+  k_avg_transform<<<grid, kAT, 0, st>>>(P, n, recs, srcs, state, rho, order, mode);
+  return cudaGetLastError();
+}
+cudaError_t launch_avg_accum(const float *rho, int n, size_t cells, double *acc, cudaStream_t st) {
+  int blocks = (int)std::min<size_t>((cells + 255) / 256, 4096);
+  k_avg_accum<<<blocks, 256, 0, st>>>(rho, n, cells, acc);
+  return cudaGetLastError();
+}
+
+}  // namespace smc

@@ -379,7 +379,9 @@ __global__ void __launch_bounds__(kGT) k_grid(DevParams P, int n_events, const E
               const Source &s = S[list[g0 + t]];
               GroupSrc g;
               g.x = s.x; g.y = s.y; g.xf = (float)s.x; g.yf = (float)s.y; g.weight = s.weight;
-              g.xl = s.xl; g.xr = s.xr; g.yl = s.yl; g.yr = s.yr; g.kind = s.kind; g.plane = s.plane;
+              // the column table holds mw columns per source: a window never reaches past it
+              g.xl = s.xl; g.xr = s.xr; g.yl = s.yl; g.yr = (int16_t)min((int)s.yr, (int)s.yl + mw);
+              g.kind = s.kind; g.plane = s.plane;
               grp[t] = g;
             }
             __syncthreads();
@@ -498,8 +500,9 @@ __global__ void __launch_bounds__(kGT) k_grid(DevParams P, int n_events, const E
     for (int i = tid; i < nx; i += kGT) xo[i] = (float)((P.xmin + i * P.dx) - xc);
     for (int j = tid; j < ny; j += kGT) yo[j] = (float)((P.ymin + j * P.dy) - yc);
     __syncthreads();
-    moments<LO, HI>(P, rec, S, rho, reinterpret_cast<uint32_t *>(acc), xo, yo, red, tot0,
-                    out_ecc + (size_t)e * kEccLen);
+    if (!P.no_moments)
+      moments<LO, HI>(P, rec, S, rho, reinterpret_cast<uint32_t *>(acc), xo, yo, red, tot0,
+                      out_ecc + (size_t)e * kEccLen);
     if (tid == 0 && status) status[e] = s_status;
     __syncthreads();
   }

@@ -238,6 +238,7 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
 __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const double *inj_xy) {
   const int tid = threadIdx.x;
   double px = 0, py = 0;
+  float rx = 0.f, ry = 0.f;
   if (inj_xy) {
     if (tid < A) { px = inj_xy[2 * tid]; py = inj_xy[2 * tid + 1]; }
   } else {
@@ -245,8 +246,10 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
     double my = block_sum_f(tid < A ? sm.ay[w][tid] : 0.f, sm.red2, 1);
     __syncthreads();
     if (tid < A) {
-      px = (double)sm.ax[w][tid] - mx / A + xc;
-      py = (double)sm.ay[w][tid] - my / A;
+      rx = sm.ax[w][tid];
+      ry = sm.ay[w][tid];
+      px = (double)rx - mx / A + xc;
+      py = (double)ry - my / A;
     }
   }
   // stash unsorted, then rank-sort by x: FP32 keys order the FP64 values
@@ -269,6 +272,7 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
   if (tid < A) {
     sm.X[w][rank] = px; sm.Y[w][rank] = py;
     sm.Xf[w][rank] = (float)px; sm.Yf[w][rank] = (float)py;
+    if (!inj_xy) { sm.ax[w][rank] = rx; sm.ay[w][rank] = ry; }   // nucleus-frame positions, same order
   }
   __syncthreads();
 }
@@ -568,7 +572,17 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P, uint64_t fi
             s.plane = (model == 7 && w == 1) ? 1 : 0;
             s.weight = disk_e ? disk_val * (model == 5 ? (float)((1.0 - P.alpha) / 2.) : 1.f)
                               : peak * (model == 5 ? (float)((1.0 - P.alpha) / 2.) : 1.f);
-            s.pad = 0.f;
+            // a Woods-Saxon nucleon is constructed at its nucleus-frame
+            // position and then moved (Nucleus::populate,
+            // src/Nucleus.cpp:274-309, Particle::setX/setY): its base box
+            // stays there, and the averaged mode's rotation brings it back
+            if (!inject && (w == 0 ? A : B) > 2) {
+              s.kind |= SRC_RAW_BASE;
+              s.bx = sm.ax[w][i];
+              s.by = sm.ay[w][i];
+            } else {
+              s.bx = s.by = 0.f;
+            }
             S[pos++] = s;
           }
           if (thick_src) {
@@ -580,7 +594,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P, uint64_t fi
             s.kind = SRC_THICK | (disk_n ? 16 : 0);
             s.plane = model == 1 ? w : 1 + w;   // MC-KLN splats T_A, T_B only
             s.weight = disk_n ? disk_val : peak;
-            s.pad = 0.f;
+            s.bx = s.by = 0.f;
             S[pos++] = s;
           }
         }
@@ -623,7 +637,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P, uint64_t fi
           if (model == 5 && P.sub_model == 2) aw = (double)(1 / c) + (double)(1 / sm.hits[1][j]);
           double fw = P.alpha + (1. - P.alpha) * aw;
           s.weight = (float)((disk_e ? 10.0 / P.sigin : P.peak) * fw);
-          s.pad = 0.f;
+          s.bx = s.by = 0.f;
           S[nsrc + pos] = s;
           pos++;
         }

@@ -158,6 +158,9 @@ struct Ctx {
   DevBuf<uint8_t> wounded;
   DevBuf<double> kln64;
   DevBuf<float> kln32;
+  DevBuf<smc::AvgSrc> avg_state;
+  DevBuf<float> avg_rho;
+  DevBuf<double> avg_acc;
   std::vector<int> h_status;
   std::vector<EventRec> h_recs;
   // counters and optional kernel timing
@@ -298,6 +301,18 @@ __global__ void k_scalars(const EventRec *r, int n, int *npart, int *ncoll, doub
 
 // One chunk of events through both stages.  Device outputs land directly in
 // the caller's buffers at offset `off`; host outputs are staged and copied.
+// per-event status codes written by the kernels -> API status
+smc_status status_error(int worst) {
+  switch (worst) {
+    case 0: return SMC_OK;
+    case 3: return SMC_ERR_RETRY_CAP;
+    case 4: return SMC_ERR_KLN_TABLE;
+    case 5: return SMC_ERR_ZERO_DNDY;
+    case 6: return SMC_ERR_CAPACITY;
+    default: return SMC_ERR_CUDA;
+  }
+}
+
 smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_outputs *out,
                      const double *inj_p, const double *inj_t, const double *inj_b, bool plain) {
   const DevParams &P = c->P;
@@ -381,14 +396,7 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
   }
   int worst = 0;
   for (int e = 0; e < n; e++) worst = std::max(worst, c->h_status[e]);
-  switch (worst) {
-    case 0: return SMC_OK;
-    case 3: return SMC_ERR_RETRY_CAP;
-    case 4: return SMC_ERR_KLN_TABLE;
-    case 5: return SMC_ERR_ZERO_DNDY;
-    case 6: return SMC_ERR_CAPACITY;
-    default: return SMC_ERR_CUDA;
-  }
+  return status_error(worst);
 }
 
 smc_status run(Ctx *c, uint64_t first_event, int n, const smc_outputs *out, const double *inj_p,
@@ -527,6 +535,7 @@ void smc_destroy(void *ctx) {
   c->inj_p.release(); c->inj_t.release(); c->inj_b.release(); c->rho.release(); c->ta.release();
   c->tb.release(); c->scratch.release(); c->status.release(); c->npart.release(); c->ncoll.release();
   c->attempts.release(); c->wounded.release(); c->kln64.release(); c->kln32.release();
+  c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -586,6 +595,113 @@ smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_
   smc_status s = set_thickness_flags(c, out);
   if (s) return s;
   return run(c, 0, n, out, xy_proj, xy_targ, b, false);
+}
+
+smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_proj, const double *xy_targ,
+                       const double *b, int from_order, int to_order, int reaction_plane, double *mean,
+                       double *mean_rp, int *n_used) {
+  if (!ctx || !mean || n < 0 || from_order < 1 || to_order < from_order || (xy_proj && !xy_targ))
+    return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  if (n_used) *n_used = 0;
+  if (n == 0) return SMC_OK;
+  CK(cudaSetDevice(c->device));
+  smc_outputs none{};
+  smc_status s = set_thickness_flags(c, &none);
+  if (s) return s;
+  DevParams P = c->P;
+  P.no_moments = 1;
+  const size_t g = (size_t)P.nx * P.ny;
+  const int norders = to_order - from_order + 1;
+  const bool rp = reaction_plane != 0 && mean_rp;
+  CK(c->avg_acc.ensure(g * norders * 2));
+  CK(cudaMemsetAsync(c->avg_acc.p, 0, sizeof(double) * g * norders * 2, c->st));
+  double *acc = c->avg_acc.p, *acc_rp = c->avg_acc.p + g * norders;
+  int used = 0;
+  for (int off = 0; off < n; off += c->chunk) {
+    const int m = std::min(c->chunk, n - off);
+    CK(c->recs.ensure(m));
+    CK(c->srcs.ensure((size_t)m * P.max_src));
+    CK(c->status.ensure(m));
+    CK(c->avg_state.ensure((size_t)m * P.max_src));
+    CK(c->avg_rho.ensure((size_t)m * g));
+    CK(c->ecc.ensure((size_t)m * smc::kEccLen));
+    const double *ip = nullptr, *it = nullptr, *ib = nullptr;
+    if (xy_proj) {
+      size_t np = (size_t)m * 2 * c->info.A, nt = (size_t)m * 2 * c->info.B;
+      CK(c->inj_p.ensure(np));
+      CK(c->inj_t.ensure(nt));
+      CK(cudaMemcpyAsync(c->inj_p.p, xy_proj + (size_t)off * 2 * c->info.A, sizeof(double) * np,
+                         cudaMemcpyHostToDevice, c->st));
+      CK(cudaMemcpyAsync(c->inj_t.p, xy_targ + (size_t)off * 2 * c->info.B, sizeof(double) * nt,
+                         cudaMemcpyHostToDevice, c->st));
+      ip = c->inj_p.p;
+      it = c->inj_t.p;
+      if (b) {
+        CK(c->inj_b.ensure(m));
+        CK(cudaMemcpyAsync(c->inj_b.p, b + off, sizeof(double) * m, cudaMemcpyHostToDevice, c->st));
+        ib = c->inj_b.p;
+      }
+    }
+    const int grid1 = std::max(1, std::min(m, c->sms * c->occ1));
+    const int grid2 = std::max(1, std::min(m, c->sms * c->occ2));
+    const int grid3 = std::max(1, std::min(m, c->sms * 4));
+    auto splat = [&]() {
+      return timed(c, 1, [&] {
+        return smc::launch_grid(P, m, c->recs.p, c->srcs.p, c->avg_rho.p, nullptr, nullptr, nullptr, c->ecc.p,
+                                c->status.p, grid2, c->st);
+      });
+    };
+    CK(timed(c, 0, [&] {
+      return smc::launch_sample_pair(P, xy_proj ? 0 : first_event + off, m, ip, it, ib, c->recs.p, c->srcs.p,
+                                     nullptr, nullptr, grid1, c->st);
+    }));
+    CK(smc::launch_avg_init(P, m, c->recs.p, c->srcs.p, c->avg_state.p, grid3, c->st));
+    CK(splat());   // MakeDensity.cpp:1275
+    for (int q = 0; q < norders; q++) {
+      const int order = from_order + q;
+      if (rp) {    // MakeDensity.cpp:1289-1300
+        CK(smc::launch_avg_transform(P, m, c->recs.p, c->srcs.p, c->avg_state.p, c->avg_rho.p, order, 0, grid3,
+                                     c->st));
+        CK(splat());
+        CK(smc::launch_avg_accum(c->avg_rho.p, m, g, acc_rp + q * g, c->st));
+      }
+      // MakeDensity.cpp:1331-1340
+      CK(smc::launch_avg_transform(P, m, c->recs.p, c->srcs.p, c->avg_state.p, c->avg_rho.p, order, 1, grid3,
+                                   c->st));
+      CK(splat());
+      CK(smc::launch_avg_accum(c->avg_rho.p, m, g, acc + q * g, c->st));
+      c->stats.launches += rp ? 4 : 2;
+    }
+    c->stats.launches += 1;
+    c->h_status.resize(m);
+    c->h_recs.resize(m);
+    CK(cudaMemcpyAsync(c->h_status.data(), c->status.p, sizeof(int) * m, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(c->h_recs.data(), c->recs.p, sizeof(EventRec) * m, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    collect_timing(c);
+    c->stats.events += m;
+    int worst = 0;
+    for (int e = 0; e < m; e++) {
+      // only events with a collision enter the mean; an injected event
+      // without one has an empty density, which is not an error here
+      const bool hit = c->h_recs[e].ncoll > 0;
+      used += hit;
+      worst = std::max(worst, (!hit && c->h_status[e] == 5) ? 0 : c->h_status[e]);
+    }
+    if (worst) return status_error(worst);
+  }
+  if (n_used) *n_used = used;
+  if (used == 0) return SMC_OK;
+  std::vector<double> h(g * norders * (rp ? 2 : 1));
+  CK(cudaMemcpyAsync(h.data(), c->avg_acc.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  // MakeDensity::setSd (src/MakeDensity.cpp:2514-2522): entropy = rho * finalFactor
+  const double ff = c->P.final_factor;
+  for (size_t k = 0; k < g * norders; k++) mean[k] = h[k] / used * ff;
+  if (rp)
+    for (size_t k = 0; k < g * norders; k++) mean_rp[k] = h[g * norders + k] / used * ff;
+  return SMC_OK;
 }
 
 smc_status smc_set_timing(void *ctx, int enabled) {

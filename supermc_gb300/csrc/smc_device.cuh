@@ -14,6 +14,7 @@ enum SrcKind : int {
   SRC_PART_BOX = 0,   // participant, bounding-box window, r <= 5w cut (MCnucl::addDensity)
   SRC_COLL = 1,       // binary collision, +-d_max window, dc <= 25 w^2 (MCnucl::setDensity)
   SRC_THICK = 2,      // participant, +-d_max window, r <= 5w (MCnucl::setThickness)
+  SRC_RAW_BASE = 32,  // flag: participant box built at (bx, by), then moved
 };
 
 // One source of the density/thickness splat.  Windows are grid index
@@ -24,9 +25,16 @@ struct Source {
   int16_t mx0, mx1, my0, my1;  // eccentricity-mask window (participant boxes)
   int16_t kind, plane;   // SrcKind, accumulator plane
   float weight;          // multiplies exp(-r^2/2w^2)
-  float pad;
+  float bx, by;          // construction point of a participant box (kind bit SRC_RAW_BASE)
 };
 static_assert(sizeof(Source) == 48, "Source layout");
+
+// Averaged-mode state of one source: construction position and the
+// current bounding box with Box2D's centre (src/Box2D.h:16-63).
+struct AvgSrc {
+  double x0, y0;
+  double bxl, bxr, byl, byr, bxc, byc;
+};
 
 struct NucleusDev {
   int A, deformed;
@@ -53,6 +61,7 @@ struct DevParams {
   int want_ta, want_tb;     // thickness planes requested
   int splat_mw;             // widest splat window in columns (+ margin)
   int n_planes;             // accumulator planes of the splat (1..3)
+  int no_moments;           // skip the eccentricity pass (averaged mode)
 };
 
 // Per-event record written by the sampling/pairing stage.

@@ -20,6 +20,11 @@ int grid_blocks_per_sm(const DevParams &P);
 cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs, float *out_rho,
                         float *out_ta, float *out_tb, float *scratch, double *out_ecc, int *status, int grid,
                         cudaStream_t st);
+cudaError_t launch_avg_init(const DevParams &P, int n, const EventRec *recs, const Source *srcs, AvgSrc *state,
+                            int grid, cudaStream_t st);
+cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Source *srcs, AvgSrc *state,
+                                 const float *rho, int order, int mode, int grid, cudaStream_t st);
+cudaError_t launch_avg_accum(const float *rho, int n, size_t cells, double *acc, cudaStream_t st);
 cudaError_t launch_kln_table(const KlnDev &K, int tmax, double dT, double *table64, float *table32,
                              cudaStream_t st);
 

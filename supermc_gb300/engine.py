@@ -130,6 +130,29 @@ class Engine:
                    "smc_inject")
         return bufs
 
+    def average(self, first_event: int, n: int, from_order: int = 2, to_order: int = 3,
+                reaction_plane: bool = True, xy_proj=None, xy_targ=None, b=None):
+        """Event-averaged entropy densities (rho * finalFactor) rotated to each
+        order's participant plane (and, with reaction_plane, recentred only).
+        Returns (mean, mean_rp), each [orders][nx][ny]; the number of events
+        with a collision that entered them is left in last_average_events."""
+        no = to_order - from_order + 1
+        mean = np.zeros((no, self.nx, self.ny))
+        mean_rp = np.zeros((no, self.nx, self.ny)) if reaction_plane else None
+        xp = xt = bb = None
+        if xy_proj is not None:
+            xp = np.ascontiguousarray(xy_proj, dtype=np.float64)
+            xt = np.ascontiguousarray(xy_targ, dtype=np.float64)
+            n = xp.shape[0]
+            if b is not None:
+                bb = np.ascontiguousarray(np.broadcast_to(b, (n,)), dtype=np.float64)
+        used = ctypes.c_int(0)
+        _lib.check(self.lib.smc_average(self.h, first_event, n, _lib.ptr(xp), _lib.ptr(xt), _lib.ptr(bb),
+                                        from_order, to_order, 1 if reaction_plane else 0, _lib.ptr(mean),
+                                        _lib.ptr(mean_rp), ctypes.byref(used)), "smc_average")
+        self.last_average_events = used.value
+        return mean, mean_rp
+
     def kln_table(self) -> np.ndarray:
         t = self.info.kln_tmax
         out = np.zeros((t, t))

@@ -101,6 +101,40 @@ def make_inject(out):
     np.savez_compressed(os.path.join(out, "glauber_inject.npz"), **data)
 
 
+AVG_EVENTS = [(3001, 2.4), (3002, 6.5), (3003, 9.8), (3004, 4.1)]   # (drand48 seed, b)
+
+
+def make_average(out):
+    """MakeDensity::generate_profile_average's per-event sequence on events
+    from the reference's own sampler: density, then for orders 2 and 3 the
+    reaction-plane recentre + re-splat and the rotation + re-splat; the
+    event means of getRho * finalFactor are digested."""
+    rng = np.random.default_rng(77)
+    data = {}
+    for name in SYSTEMS:
+        ref, vals = ref_for([name])
+        ff = float(vals["finalfactor"])
+        acc = {(o, m): 0.0 for o in (2, 3) for m in ("rp", "rot")}
+        used = []
+        for seed, b in AVG_EVENTS:
+            ref.srand(seed)
+            n1, n2, nc = ref.sample_event(b)
+            if nc == 0:
+                continue
+            used.append((seed, b))
+            ref.density()
+            for o in (2, 3):
+                ref.recenter_resplat(o)
+                acc[(o, "rp")] = acc[(o, "rp")] + ref.grid(2)
+                ref.rotate_resplat(o)
+                acc[(o, "rot")] = acc[(o, "rot")] + ref.grid(2)
+        data[name + "_events"] = np.array(used)
+        for (o, m), g in acc.items():
+            for kk, vv in grid_digest(g / len(used) * ff, rng).items():
+                data[f"{name}_{m}{o}_{kk}"] = vv
+    np.savez_compressed(os.path.join(out, "average.npz"), **data)
+
+
 def make_sampler(out):
     data = {}
     for A, deformed in [(208, 0), (197, 0), (238, 1), (63, 0), (2, 0), (1, 0)]:
@@ -167,16 +201,19 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--nev", type=int, default=1500)
+    ap.add_argument("--only", choices=["constants", "sampler", "inject", "average", "kln", "native"],
+                    help="regenerate one fixture only")
     a = ap.parse_args()
     if build_reference(a.ref) is None:
         sys.exit(f"reference tree not found at {a.ref}")
     global EOS_DIR
     EOS_DIR = os.path.join(a.ref, "EOS")
-    make_constants(HERE)
-    make_sampler(HERE)
-    make_inject(HERE)
-    make_kln(HERE)
-    make_native_tables(HERE, a.nev)
+    steps = {"constants": lambda: make_constants(HERE), "sampler": lambda: make_sampler(HERE),
+             "inject": lambda: make_inject(HERE), "average": lambda: make_average(HERE),
+             "kln": lambda: make_kln(HERE), "native": lambda: make_native_tables(HERE, a.nev)}
+    for k, f in steps.items():
+        if a.only in (None, k):
+            f()
     print("fixtures written to", HERE)
 
 

@@ -38,3 +38,27 @@ def fmt8(a):
     """Round like the reference's text output (setprecision(8))."""
     import numpy as np
     return np.vectorize(lambda v: float("%.8g" % v))(a)
+
+
+def oracle_average(oracle, vals, fill, n, orders=(2, 3), params=None):
+    """The oracle through MakeDensity::generate_profile_average's per-event
+    sequence (src/MakeDensity.cpp:1264-1340): density, then per order the
+    reaction-plane recentre + re-splat and the rotation + re-splat.
+    fill(ev, k) populates event k (False skips it); events without a
+    collision are skipped.  Returns ({("rp"|"rot", order): mean grid of
+    rho * finalFactor}, events used)."""
+    ev = oracle.event(params if params is not None else oracle_params(vals))
+    acc, used = {}, 0
+    for k in range(n):
+        if not fill(ev, k) or ev.pair() == 0:
+            continue
+        used += 1
+        if ev.thickness() or ev.density():
+            raise RuntimeError("oracle thickness/density failed")
+        for o in orders:
+            ev.recenter_resplat(o)
+            acc[("rp", o)] = acc.get(("rp", o), 0.0) + ev.grid(2)
+            ev.rotate_resplat(o)
+            acc[("rot", o)] = acc.get(("rot", o), 0.0) + ev.grid(2)
+    ff = vals["finalfactor"]
+    return {key: g / used * ff for key, g in acc.items()}, used
