@@ -354,6 +354,19 @@ def run_gpu(args, vals) -> dict | None:
             dist.destroy_process_group()
         return None
 
+    # ---- batched path with the CUDA-core splat instead of the tensor cores
+    eng.set_grid_path(False)
+    eng.generate_into(10 ** 8, n, bufs)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    eng.generate_into(10 ** 8 + n, n, bufs)
+    b.record(stream)
+    torch.cuda.synchronize()
+    cuda_core = n / (a.elapsed_time(b) / 1e3)
+    eng.set_grid_path(True)
+
     # ---- plain per-event path, same workload (sample)
     m = args.plain_events
     pb = {k: v[:m] for k, v in bufs.items()}
@@ -378,7 +391,7 @@ def run_gpu(args, vals) -> dict | None:
     achieved = flops_per_event * events_per_launch / (grid_launch_ms / 1e3) / 1e12
     roof = {"bound": "tensor", "achieved": achieved, "peak": tf_peak, "unit": "TFLOP/s",
             "frac": achieved / tf_peak, "traffic": None,
-            "kernel": "k_grid (thickness splat, KLN lookup, eps_n)",
+            "kernel": "k_grid_tc (tcgen05 split-TF32 thickness contraction, KLN lookup, eps_n)",
             "work": "2*Nx*Ny*N_src FLOP per event (dense separable contraction), N_src = Npart",
             "peak_kind": f"bf16 dense, {peak_kind}",
             "sample_kernel_ms_per_launch": st["sample_ms"] / max(1, st["sample_launches"]),
@@ -406,6 +419,8 @@ def run_gpu(args, vals) -> dict | None:
             "clocks": clk, "roofline": roof, "cpu_baseline": base,
             "plain_gpu": {"value": plain, "unit": "events/s", "events": m,
                           "batched_over_plain": value / plain},
+            "batched_cuda_core_splat": {"value": cuda_core, "unit": "events/s", "events": n,
+                                        "note": "same batched path, FP32 CUDA-core splat (smc_set_grid_path 0)"},
             "eps_abs_err_vs_fp64_oracle": err, "init_s": t_init}
     print(json.dumps(line), flush=True)
     if world > 1:

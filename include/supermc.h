@@ -179,6 +179,16 @@ typedef struct smc_stats {
   double sample_ms, grid_ms;/* summed kernel durations (timing enabled)     */
 } smc_stats;
 smc_status smc_set_timing(void *ctx, int enabled);
+/* Splat implementation of the batched entry points (smc_generate,
+ * smc_inject, smc_average); no reference counterpart (the reference has
+ * one CPU loop, src/MCnucl.cpp:432-478, :688-866).  tensor_cores != 0
+ * (default): the separable contraction Gx diag(w) Gy^T on the tcgen05
+ * tensor cores in split-TF32 (three-term) precision with FP32
+ * accumulation, plus an exact subtraction of the window cells beyond the
+ * reference's cut; used for Gaussian profiles (shape_of_nucleons != 1,
+ * shape_of_entropy != 1).  0: the FP32 CUDA-core splat.  The plain path
+ * (smc_generate_plain) always uses the CUDA-core splat. */
+smc_status smc_set_grid_path(void *ctx, int tensor_cores);
 smc_status smc_get_stats(void *ctx, smc_stats *stats);
 smc_status smc_reset_stats(void *ctx);
 

@@ -1,0 +1,345 @@
+// Device helpers shared by the two grid kernels (the CUDA-core splat in
+// k_grid.cu and the tensor-core contraction in k_grid_tc.cu): double-float
+// reductions, the reference's exact per-cell inclusion rules, the six-point
+// table interpolation and the eccentricity moments.
+//
+//   per-cell cuts       src/Particle.cpp:122-132, src/MCnucl.cpp:732-756
+//   six-point lookup    src/arsenal.cpp:33-54 (used at src/MCnucl.cpp:654-687)
+//   eps_n, <r^n>        src/MakeDensity.cpp:2244-2511, hot-spot mask src/MCnucl.cpp:1303-1323
+#pragma once
+#include "smc_device.cuh"
+
+namespace smc {
+
+struct GroupSrc {
+  double x, y;
+  float xf, yf, weight;
+  int16_t xl, xr, yl, yr;
+  int16_t kind, plane;
+};
+
+// ---------------------------------------------------- double-float sums
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s = a.hi + b.hi;
+  float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);   // TwoSum error
+  e += a.lo + b.lo;
+  float h = s + e;
+  return {h, e - (h - s)};
+}
+__device__ __forceinline__ DF df_warp_sum(DF v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    DF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = df_add(v, w);
+  }
+  return v;
+}
+// Kahan-compensated FP32 accumulator
+struct KSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ DF df() const { return {s, -c}; }
+};
+
+// exact per-cell inclusion, FP64 as the reference evaluates it
+static __device__ __noinline__ bool cell_in_exact(const DevParams &P, double sx, double sy, int kind, int i, int j) {
+  double xg = __dadd_rn(P.xmin, __dmul_rn((double)i, P.dx));
+  double yg = __dadd_rn(P.ymin, __dmul_rn((double)j, P.dy));
+  double dc = sq_dist_rn(sx, sy, xg, yg);
+  if (kind & 16) return !(dc > P.dsq);                        // disk nucleons / entropy
+  if ((kind & 15) == SRC_COLL) return dc <= __dmul_rn(25., P.w2);  // MCnucl.cpp:754
+  double r = __dsqrt_rn(dc);                                  // Particle::getSmoothTn
+  return !(r > __dmul_rn(5., P.width));
+}
+
+__device__ __forceinline__ float six_point(float x, float y, float v00, float v01, float v02, float v10, float v11,
+                                           float v20) {
+  float axx = 0.5f * (v00 - 2.f * v10 + v20);
+  float axy = v00 - v01 - v10 + v11;
+  float ayy = 0.5f * (v00 - 2.f * v01 + v02);
+  float bx = 0.5f * (-3.f * v00 + 4.f * v10 - v20);
+  float by = 0.5f * (-3.f * v00 + 4.f * v01 - v02);
+  return axx * x * x + axy * x * y + ayy * y * y + bx * x + by * y + v00;
+}
+
+// Per-cell post-op of the splat planes a0..a2 (np planes): the density v and
+// the thickness outputs t1, t2 (MCnucl::setDensity, src/MCnucl.cpp:654-811).
+//   model 5 (Glauber): v = a0; planes 1, 2 are T_A, T_B when requested
+//   model 7: v = sqrt(T_A T_B)
+//   model 1 (MC-KLN): planes are T_A, T_B; v = dN/dy from the six-point
+//     interpolation in the table; false when the thickness lies beyond it
+//     (the reference exits there, src/MCnucl.cpp:665-670)
+__device__ __forceinline__ bool post_cell(const DevParams &P, int np, float a0, float a1, float a2, float &v,
+                                          float &t1, float &t2) {
+  v = t1 = t2 = 0.f;
+  const int model = P.which_mc_model;
+  if (model == 5) {
+    v = a0;
+    if (np > 2) { t1 = a1; t2 = a2; }
+  } else if (model == 7) {
+    v = sqrtf(a0 * a1);
+  } else {
+    t1 = a0; t2 = a1;
+    // a zero thickness reads the zero first row / column of the table
+    // (src/MCnucl.cpp:937-944): the interpolation is exactly 0 there
+    if (t1 == 0.f || t2 == 0.f) return true;
+    const float dT = (float)P.kln_dT;
+    float di = t1 / dT, dj = t2 / dT;
+    const int tm = P.kln_tmax;
+    if (di < 0.f || di >= tm - 2 || dj < 0.f || dj >= tm - 2) return false;
+    int ii = (int)floorf(di), jj = (int)floorf(dj);
+    const float *T = P.kln_table + ii * tm + jj;
+    v = six_point(di - ii, dj - jj, __ldg(T), __ldg(T + 1), __ldg(T + 2), __ldg(T + tm), __ldg(T + tm + 1),
+                  __ldg(T + 2 * tm));
+  }
+  return true;
+}
+
+// Column interval [ja, jb) of row i that the reference includes for source
+// g.  dc(j) is convex in j, so the included cells form one interval around
+// the column nearest the source.
+static __device__ __noinline__ void row_interval(const DevParams &P, const GroupSrc &g, int i, float dx2, float lo,
+                                             float hi, const float *yg, float inv_dy, float ymin_f, int &ja,
+                                             int &jb) {
+  const int wl = g.yl, wr = g.yr;
+  auto dcf = [&](int j) {
+    float dy = yg[j] - g.yf;
+    return fmaf(dy, dy, dx2);
+  };
+  auto inside = [&](int j) {
+    float d = dcf(j);
+    if (d < lo) return true;
+    if (d > hi) return false;
+    return cell_in_exact(P, g.x, g.y, g.kind, i, j);
+  };
+  ja = jb = wl;
+  if (wr <= wl) return;
+  float h2 = lo - dx2;
+  int a, b;
+  if (h2 > 0.f) {
+    float h = sqrtf(h2);
+    a = (int)ceilf((g.yf - h - ymin_f) * inv_dy);
+    b = (int)floorf((g.yf + h - ymin_f) * inv_dy) + 1;
+    a = max(a, wl);
+    b = min(b, wr);
+    // shrink to cells certainly inside (rounding of the estimate)
+    while (a < b && !(dcf(a) < lo)) a++;
+    while (b > a && !(dcf(b - 1) < lo)) b--;
+  } else {
+    a = b = 0;
+  }
+  if (a >= b) {
+    // no certainly-inside cell: only the cells nearest the source can be in
+    int jc = (int)floorf((g.yf - ymin_f) * inv_dy);
+    a = b = -1;
+    for (int j = max(wl, jc - 1); j <= min(wr - 1, jc + 2); j++) {
+      if (inside(j)) {
+        if (a < 0) a = j;
+        b = j + 1;
+      }
+    }
+    if (a < 0) return;
+  }
+  // extend by cells decided inside at the FP32 error scale
+  while (a - 1 >= wl && inside(a - 1)) a--;
+  while (b < wr && inside(b)) b++;
+  ja = a;
+  jb = b;
+}
+
+// Column interval [ja, jb) of row i inside the cut of a Gaussian source at
+// (sxf, syf) (FP32 copy of the FP64 position *sxy) within the window
+// columns [wl, wr): the same decision as row_interval, with scalar
+// arguments so that it inlines.  dc(j) is convex in j, so the included
+// cells form one interval around the column nearest the source; the FP32
+// distance decides every cell except those within its error of the cut,
+// which take the reference's FP64 test.
+__device__ __forceinline__ void cut_interval(const DevParams &P, const double *sxy, int kind, float syf, int i,
+                                             float dx2, float lo, float hi, const float *yg, float inv_dy,
+                                             float ymin_f, int wl, int wr, int &ja, int &jb) {
+  auto dcf = [&](int j) {
+    const float dy = yg[j] - syf;
+    return fmaf(dy, dy, dx2);
+  };
+  auto inside = [&](int j) {
+    const float d = dcf(j);
+    if (d < lo) return true;
+    if (d > hi) return false;
+    return cell_in_exact(P, sxy[0], sxy[1], kind, i, j);
+  };
+  ja = jb = wl;
+  if (wr <= wl) return;
+  int a, b;
+  const float h2 = lo - dx2;
+  if (h2 > 0.f) {
+    const float h = sqrtf(h2);
+    a = max((int)ceilf((syf - h - ymin_f) * inv_dy), wl);
+    b = min((int)floorf((syf + h - ymin_f) * inv_dy) + 1, wr);
+    while (a < b && !(dcf(a) < lo)) a++;
+    while (b > a && !(dcf(b - 1) < lo)) b--;
+  } else {
+    a = b = 0;
+  }
+  if (a >= b) {
+    const int jc = (int)floorf((syf - ymin_f) * inv_dy);
+    a = b = -1;
+    for (int j = max(wl, jc - 1); j <= min(wr - 1, jc + 2); j++) {
+      if (inside(j)) {
+        if (a < 0) a = j;
+        b = j + 1;
+      }
+    }
+    if (a < 0) return;
+  }
+  while (a - 1 >= wl && inside(a - 1)) a--;
+  while (b < wr && inside(b)) b++;
+  ja = a;
+  jb = b;
+}
+
+template <int LO, int HI, int NT>
+__device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, const Source *S, const float *rho, uint32_t *mask,
+                        const float *xo, const float *yo, float2 *red, double tot0, double *ecc_out) {
+  const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+  const int nx = P.nx, ny = P.ny;
+  const int nw = (ny + 31) / 32;
+  // ---- eccentricity mask from the participant boxes
+  for (int k = tid; k < nx * nw; k += NT) mask[k] = 0;
+  __syncthreads();
+  for (int s = tid; s < rec.nsrc; s += NT) {
+    const Source &src = S[s];
+    int kd = src.kind & 15;
+    if (kd != SRC_PART_BOX && kd != 3) continue;
+    int r0 = max(0, (int)src.mx0), r1 = min(nx, (int)src.mx1);
+    int c0 = max(0, (int)src.my0), c1 = min(ny, (int)src.my1);
+    if (r1 <= r0 || c1 <= c0) continue;
+    int w0 = c0 >> 5, w1 = (c1 - 1) >> 5;
+    for (int row = r0; row < r1; row++)
+      for (int wd = w0; wd <= w1; wd++) {
+        int lo = max(c0, wd * 32), hi = min(c1, wd * 32 + 32);
+        uint32_t bits = (hi - lo >= 32) ? 0xffffffffu : (((1u << (hi - lo)) - 1u) << (lo - wd * 32));
+        atomicOr(&mask[row * nw + wd], bits);
+      }
+  }
+  __syncthreads();
+
+  constexpr int NO = HI - LO + 1;
+  float a_rn[10];
+  float a_norm = 0.f;
+  float a_re2[NO], a_im2[NO], a_ren[NO], a_imn[NO], a_np[NO];
+#pragma unroll
+  for (int k = 0; k < 10; k++) a_rn[k] = 0.f;
+#pragma unroll
+  for (int k = 0; k < NO; k++) a_re2[k] = a_im2[k] = a_ren[k] = a_imn[k] = a_np[k] = 0.f;
+  const int from = P.ecc_from, to = P.ecc_to;
+  // warps take (row, 32-column block) items of the bounding box, lanes the columns
+  const int nbj = rec.jmax > rec.jmin ? (rec.jmax - rec.jmin + 31) >> 5 : 0;
+  const int nitem = rec.imax > rec.imin ? (rec.imax - rec.imin) * nbj : 0;
+  for (int c = wid; c < nitem; c += NT / 32) {
+    const int ib = c / nbj;
+    const int i = rec.imin + ib, j = rec.jmin + ((c - ib * nbj) << 5) + lane;
+    if (j >= rec.jmax) continue;
+    float d = rho[(size_t)i * ny + j];
+    if (d == 0.f) continue;
+    float x = xo[i], y = yo[j];
+    float r2 = x * x + y * y;
+    float r = sqrtf(r2);
+    float rp[10];
+    rp[0] = 1.f;
+#pragma unroll
+    for (int k = 1; k < 10; k++) rp[k] = rp[k - 1] * r;
+#pragma unroll
+    for (int k = 1; k < 10; k++) a_rn[k] += rp[k] * d;
+    bool imp = (mask[i * nw + (j >> 5)] >> (j & 31)) & 1u;
+    if (!imp) continue;
+    float inv_r = r > 0.f ? 1.f / r : 0.f;
+    a_norm += r2 * d;
+    float zr = x, zi = y;   // z^n
+#pragma unroll
+    for (int n = 1; n <= HI; n++) {
+      if (n > 1) {
+        float t = zr * x - zi * y;
+        zi = zr * y + zi * x;
+        zr = t;
+      }
+      if (n >= LO && n >= from && n <= to) {
+        const int q = n - LO;
+        // r^2 e^{in theta} = z^n r^{2-n};  r^n e^{in theta} = z^n (r^3 e^{i theta} for n = 1)
+        float s2 = n == 1 ? r : 1.f;
+#pragma unroll
+        for (int k = 2; k < n; k++) s2 *= inv_r;
+        a_re2[q] += zr * s2 * d;
+        a_im2[q] += zi * s2 * d;
+        if (n == 1) {
+          a_ren[q] += zr * r2 * d;
+          a_imn[q] += zi * r2 * d;
+          a_np[q] += rp[3] * d;
+        } else {
+          a_ren[q] += zr * d;
+          a_imn[q] += zi * d;
+          a_np[q] += rp[n] * d;
+        }
+      }
+    }
+  }
+  // ---- block reduction in double-float (each accumulator retires as it is reduced)
+  constexpr int NV = 10 + 5 * NO;
+  auto put = [&](int k, float x) {
+    DF t = df_warp_sum(DF{x, 0.f});
+    if (lane == 0) red[wid * 64 + k] = make_float2(t.hi, t.lo);
+  };
+#pragma unroll
+  for (int k = 1; k < 10; k++) put(k - 1, a_rn[k]);
+  put(9, a_norm);
+#pragma unroll
+  for (int q = 0; q < NO; q++) {
+    put(10 + 5 * q, a_re2[q]);
+    put(11 + 5 * q, a_im2[q]);
+    put(12 + 5 * q, a_ren[q]);
+    put(13 + 5 * q, a_imn[q]);
+    put(14 + 5 * q, a_np[q]);
+  }
+  __syncthreads();
+  __shared__ double s_tot[64];
+  if (tid < NV) {
+    double t = 0;
+    for (int w = 0; w < NT / 32; w++) t += (double)red[w * 64 + tid].x + (double)red[w * 64 + tid].y;
+    s_tot[tid] = t;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const double *tot = s_tot;
+    const double ff = P.final_factor, eps = 1e-15;
+    double *out = ecc_out;
+    const double dn = tot0;
+    for (int n = 1; n < 10; n++) {
+      double *o = out + 5 * (n - 1);
+      o[0] = o[1] = o[2] = o[3] = 0.0;
+      o[4] = (tot[n - 1] * ff) / (dn * ff);
+      if (n >= LO && n <= HI && n >= from && n <= to) {
+        int q = n - LO;
+        o[0] = -(tot[10 + 5 * q] * ff) / (tot[9] * ff + eps);
+        o[1] = -(tot[11 + 5 * q] * ff) / (tot[9] * ff + eps);
+        o[2] = -(tot[12 + 5 * q] * ff) / (tot[14 + 5 * q] * ff + eps);
+        o[3] = -(tot[13 + 5 * q] * ff) / (tot[14 + 5 * q] * ff + eps);
+      }
+    }
+    out[45] = (double)(rec.npart1 + rec.npart2);
+    out[46] = (double)rec.ncoll;
+    out[47] = tot0 * ff * P.dx * P.dy;
+    out[48] = rec.b;
+  }
+  __syncthreads();
+}
+
+
+}  // namespace smc

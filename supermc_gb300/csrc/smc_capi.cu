@@ -148,13 +148,15 @@ struct Ctx {
   smc_info info{};
   int device = 0, sms = 0;
   cudaStream_t own = nullptr, st = nullptr;
-  int occ1 = 1, occ2 = 1;
+  int occ1 = 1, occ2 = 1, occ_tc = 1;
+  bool use_tc = true;   // tensor-core splat for the batched paths (when the profile allows it)
   int chunk = 4096;
   DevBuf<EventRec> recs;
   DevBuf<Source> srcs;
   DevBuf<double> ecc, pos, bvec, inj_p, inj_t, inj_b;
   DevBuf<float> rho, ta, tb, scratch;
   DevBuf<int> status, npart, ncoll, attempts;
+  DevBuf<int> corr_scratch;   // corner corrections of the tensor-core splat, per CTA
   DevBuf<uint8_t> wounded;
   DevBuf<double> kln64;
   DevBuf<float> kln32;
@@ -299,6 +301,20 @@ __global__ void k_scalars(const EventRec *r, int n, int *npart, int *ncoll, doub
   if (attempts) attempts[e] = r[e].attempts;
 }
 
+// Batched splat of one chunk: the tensor-core contraction where the profile
+// allows it, else the CUDA-core splat.
+cudaError_t launch_splat(Ctx *c, const DevParams &P, int n, const EventRec *recs, const Source *srcs, float *rho,
+                         float *ta, float *tb, float *scratch, double *ecc, int *status) {
+  if (c->use_tc && smc::grid_tc_supported(P)) {
+    const int grid = std::max(1, std::min(n, c->sms * c->occ_tc));
+    cudaError_t e = c->corr_scratch.ensure((size_t)grid * P.n_planes * P.nx * P.ny);
+    if (e != cudaSuccess) return e;
+    return smc::launch_grid_tc(P, n, recs, srcs, rho, ta, tb, scratch, c->corr_scratch.p, ecc, status, grid, c->st);
+  }
+  const int grid = std::max(1, std::min(n, c->sms * c->occ2));
+  return smc::launch_grid(P, n, recs, srcs, rho, ta, tb, scratch, ecc, status, grid, c->st);
+}
+
 // One chunk of events through both stages.  Device outputs land directly in
 // the caller's buffers at offset `off`; host outputs are staged and copied.
 // per-event status codes written by the kernels -> API status
@@ -327,7 +343,8 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
   uint8_t *wnd = out->wounded ? (dev ? out->wounded + (size_t)off * AB : c->wounded.p) : nullptr;
   int grid1 = std::max(1, std::min(n, c->sms * c->occ1));
   int grid2 = std::max(1, std::min(n, c->sms * c->occ2));
-  if (!rho) CK(c->scratch.ensure((size_t)(plain ? 1 : grid2) * g));
+  const int grid_tc = std::max(1, std::min(n, c->sms * c->occ_tc));
+  if (!rho) CK(c->scratch.ensure((size_t)(plain ? 1 : std::max(grid2, grid_tc)) * g));
   if (plain) {
     for (int e = 0; e < n; e++) {
       CK(timed(c, 0, [&] {
@@ -350,7 +367,7 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
                                      c->st);
     }));
     CK(timed(c, 1, [&] {
-      return smc::launch_grid(P, n, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p, grid2, c->st);
+      return launch_splat(c, P, n, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p);
     }));
   }
   int *np = out->npart ? (dev ? out->npart + 2 * off : nullptr) : nullptr;
@@ -534,7 +551,7 @@ void smc_destroy(void *ctx) {
   c->recs.release(); c->srcs.release(); c->ecc.release(); c->pos.release(); c->bvec.release();
   c->inj_p.release(); c->inj_t.release(); c->inj_b.release(); c->rho.release(); c->ta.release();
   c->tb.release(); c->scratch.release(); c->status.release(); c->npart.release(); c->ncoll.release();
-  c->attempts.release(); c->wounded.release(); c->kln64.release(); c->kln32.release();
+  c->attempts.release(); c->wounded.release(); c->corr_scratch.release(); c->kln64.release(); c->kln32.release();
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
@@ -569,8 +586,10 @@ static smc_status set_thickness_flags(Ctx *c, const smc_outputs *out) {
   P.n_planes = P.which_mc_model == 5 ? ((P.want_ta || P.want_tb) ? 3 : 1) : 2;
   if (P.ny > 512) return SMC_ERR_CONFIG;
   c->occ2 = smc::grid_blocks_per_sm(P);
+  c->occ_tc = smc::grid_tc_supported(P) ? smc::grid_tc_blocks_per_sm(P) : 1;
   return SMC_OK;
 }
+
 
 smc_status smc_generate(void *ctx, uint64_t first_event, int n, const smc_outputs *out) {
   if (!ctx || !out) return SMC_ERR_ARGUMENT;
@@ -644,12 +663,11 @@ smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_
       }
     }
     const int grid1 = std::max(1, std::min(m, c->sms * c->occ1));
-    const int grid2 = std::max(1, std::min(m, c->sms * c->occ2));
     const int grid3 = std::max(1, std::min(m, c->sms * 4));
     auto splat = [&]() {
       return timed(c, 1, [&] {
-        return smc::launch_grid(P, m, c->recs.p, c->srcs.p, c->avg_rho.p, nullptr, nullptr, nullptr, c->ecc.p,
-                                c->status.p, grid2, c->st);
+        return launch_splat(c, P, m, c->recs.p, c->srcs.p, c->avg_rho.p, nullptr, nullptr, nullptr, c->ecc.p,
+                            c->status.p);
       });
     };
     CK(timed(c, 0, [&] {
@@ -701,6 +719,12 @@ smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_
   for (size_t k = 0; k < g * norders; k++) mean[k] = h[k] / used * ff;
   if (rp)
     for (size_t k = 0; k < g * norders; k++) mean_rp[k] = h[g * norders + k] / used * ff;
+  return SMC_OK;
+}
+
+smc_status smc_set_grid_path(void *ctx, int tensor_cores) {
+  if (!ctx) return SMC_ERR_ARGUMENT;
+  static_cast<Ctx *>(ctx)->use_tc = tensor_cores != 0;
   return SMC_OK;
 }
 

@@ -20,6 +20,13 @@ int grid_blocks_per_sm(const DevParams &P);
 cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs, float *out_rho,
                         float *out_ta, float *out_tb, float *scratch, double *out_ecc, int *status, int grid,
                         cudaStream_t st);
+size_t grid_tc_smem(const DevParams &P);
+bool grid_tc_supported(const DevParams &P);
+int grid_tc_blocks_per_sm(const DevParams &P);
+// corr_scratch: per-CTA corner-correction grids, grid x n_planes x nx x ny ints
+cudaError_t launch_grid_tc(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs,
+                           float *out_rho, float *out_ta, float *out_tb, float *scratch, int *corr_scratch,
+                           double *out_ecc, int *status, int grid, cudaStream_t st);
 cudaError_t launch_avg_init(const DevParams &P, int n, const EventRec *recs, const Source *srcs, AvgSrc *state,
                             int grid, cudaStream_t st);
 cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Source *srcs, AvgSrc *state,

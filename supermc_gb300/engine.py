@@ -159,6 +159,10 @@ class Engine:
         _lib.check(self.lib.smc_kln_table(self.h, _lib.ptr(out), t * t), "smc_kln_table")
         return out
 
+    def set_grid_path(self, tensor_cores: bool) -> None:
+        """Batched splat on the tcgen05 tensor cores (default) or the FP32 CUDA cores."""
+        _lib.check(self.lib.smc_set_grid_path(self.h, 1 if tensor_cores else 0), "smc_set_grid_path")
+
     def set_timing(self, enabled: bool) -> None:
         _lib.check(self.lib.smc_set_timing(self.h, 1 if enabled else 0), "smc_set_timing")
 

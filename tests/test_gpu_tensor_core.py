@@ -1,0 +1,117 @@
+"""The tensor-core splat (tcgen05 split-TF32 contraction plus exact removal
+of the window cells beyond the reference's cut) against the FP32 CUDA-core
+splat and the FP64 oracle, through the C ABI.
+
+Bars: Npart / Ncoll identical; grids within 2e-5 of the grid maximum;
+eps_n within 1e-6 absolute (MC-KLN: the bars of its oracle test, see
+test_tensor_core_generated_kln_vs_cuda_core).
+"""
+import numpy as np
+import pytest
+
+from systems import SYSTEMS, oracle_params, values
+from test_gpu_parity import GRID_RTOL, _oracle_events, assert_ecc_close, engine
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = [
+    ("pbpb2760", {}),
+    ("auau200", {}),
+    ("auau200", dict(sub_model=2)),
+    ("auau200", dict(which_mc_model=7)),
+    ("auau200", dict(alpha=0.0)),
+    ("pbpb2760", dict(shape_of_nucleons=2)),
+    ("pbpb2760", dict(collision_criterion=2)),
+]
+
+
+def _both_paths(vals, pa, pb, bs, want):
+    eng = engine(vals, seed=0)
+    eng.set_grid_path(True)
+    tc = eng.inject(pa, pb, bs, want=want)
+    eng.set_grid_path(False)
+    cc = eng.inject(pa, pb, bs, want=want)
+    return tc, cc
+
+
+@pytest.mark.parametrize("name,over", VARIANTS)
+def test_tensor_core_equals_cuda_core_splat(oracle, name, over):
+    base = values(SYSTEMS[name])
+    pa, pb, bs, _ = _oracle_events(oracle, base, 16, 23)
+    vals = values(SYSTEMS[name], **over)
+    tc, cc = _both_paths(vals, pa, pb, bs, ("ecc", "npart", "ncoll", "rho"))
+    np.testing.assert_array_equal(tc["npart"], cc["npart"])
+    np.testing.assert_array_equal(tc["ncoll"], cc["ncoll"])
+    for k in range(len(bs)):
+        scale = np.abs(cc["rho"][k]).max()
+        assert np.abs(tc["rho"][k] - cc["rho"][k]).max() <= GRID_RTOL * scale
+    assert_ecc_close(tc["ecc"], cc["ecc"])
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_thickness_planes_vs_oracle(oracle, name):
+    """Glauber with T_A, T_B requested: three accumulator planes, beyond the
+    tensor-core kernel's shared memory, so the batched call takes the
+    CUDA-core splat; the injected events still match the oracle."""
+    vals = values(SYSTEMS[name])
+    pa, pb, bs, res = _oracle_events(oracle, vals, 12, 31)
+    eng = engine(vals)
+    eng.set_grid_path(True)
+    out = eng.inject(pa, pb, bs, want=("ecc", "rho", "ta", "tb"))
+    ev = oracle.event(oracle_params(vals))
+    for k in range(len(bs)):
+        ev.inject(pa[k], pb[k])
+        ev.pair()
+        assert ev.thickness() == 0 and ev.density() == 0
+        for plane, key in ((0, "ta"), (1, "tb"), (2, "rho")):
+            ref = ev.grid(plane)
+            assert np.abs(out[key][k] - ref).max() <= GRID_RTOL * ref.max(), (k, key)
+        assert_ecc_close(out["ecc"][k], res[k][3])
+
+
+def test_tensor_core_central_events_many_sources(oracle):
+    """Head-on Pb+Pb: ~1800 binary collisions, several source windows and
+    operand chunks per tile."""
+    vals = values(SYSTEMS["pbpb2760"])
+    p = oracle_params(vals)
+    ev = oracle.event(p)
+    nuc = oracle.nucleus(208)
+    pa, pb, res = [], [], []
+    for k in range(6):
+        ev.populate_philox(nuc, nuc, 0.3 * k, 3, k, 0)
+        xa, xb = ev.nucleons(0)[:, :2], ev.nucleons(1)[:, :2]
+        ev.inject(xa, xb)
+        nc = ev.pair()
+        ev.thickness(); ev.density()
+        pa.append(xa); pb.append(xb)
+        res.append((nc, ev.grid(2), ev.eccentricities(1, 9, 0.3 * k)))
+    eng = engine(vals)
+    eng.set_grid_path(True)
+    out = eng.inject(np.array(pa), np.array(pb), 0.3 * np.arange(6), want=("ecc", "ncoll", "rho"))
+    assert max(r[0] for r in res) > 1000
+    for k, (nc, rho, ecc) in enumerate(res):
+        assert out["ncoll"][k] == nc
+        assert np.abs(out["rho"][k] - rho).max() <= GRID_RTOL * rho.max()
+        assert_ecc_close(out["ecc"][k], ecc)
+
+
+def test_tensor_core_generated_kln_vs_cuda_core():
+    """MC-KLN generated batch (the benchmark workload's model): the same
+    events through both splats."""
+    vals = values(SYSTEMS["pbpb2760"], which_mc_model=1, sub_model=7, ecc_from_order=2, ecc_to_order=5,
+                  sigininn_override=64.0)
+    eng = engine(vals, seed=5)
+    eng.set_grid_path(True)
+    tc = eng.generate(0, 256, want=("ecc", "npart", "ncoll", "rho"))
+    eng.set_grid_path(False)
+    cc = eng.generate(0, 256, want=("ecc", "npart", "ncoll", "rho"))
+    np.testing.assert_array_equal(tc["npart"], cc["npart"])
+    np.testing.assert_array_equal(tc["ncoll"], cc["ncoll"])
+    # dN/dy is the reference's piecewise six-point interpolation in the
+    # table: a thickness that differs in its last bits can select the next
+    # stencil, so grids and eps get the MC-KLN bars of test_kln_events_vs_oracle
+    scale = np.abs(cc["rho"]).max(axis=(1, 2))
+    assert (np.abs(tc["rho"] - cc["rho"]).max(axis=(1, 2)) <= 1e-4 * scale).all()
+    np.testing.assert_allclose(tc["ecc"], cc["ecc"], rtol=1e-5, atol=1e-5)
+    eps25 = [5 * (n - 1) + c for n in range(2, 6) for c in range(4)]
+    assert np.median(np.abs(tc["ecc"][:, eps25] - cc["ecc"][:, eps25]).max(axis=1)) < 1e-6
