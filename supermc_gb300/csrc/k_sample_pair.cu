@@ -18,16 +18,22 @@
 namespace smc {
 
 constexpr int kNT = 256;   // threads per CTA; also the candidate batch size
+static_assert(kMaxA % 4 == 0, "float4 rows");
 
-struct SampleSmem {
+struct alignas(16) SampleSmem {
   float cx[kNT], cy[kNT], cz[kNT];          // candidate batch (nucleus frame)
   uint8_t valid[kNT];
-  uint32_t keep[kNT / 32], drop[kNT / 32];   // batch resolution state
+  uint32_t keep[kNT / 32], conf[kNT / 32];   // batch resolution state: kept, conflicted
+  uint32_t cmask[kNT][kNT / 32];             // earlier batch candidates each one conflicts with
   int order[kNT];
   int n_new;
-  float ax[2][kMaxA], ay[2][kMaxA], az[2][kMaxA];  // accepted (nucleus frame)
+  // read four at a time (float4): 16-byte aligned rows of kMaxA (a multiple of 4)
+  alignas(16) float ax[2][kMaxA];
+  alignas(16) float ay[2][kMaxA];
+  alignas(16) float az[2][kMaxA];            // accepted (nucleus frame)
   double X[2][kMaxA], Y[2][kMaxA];           // final positions, sorted by x
-  float Xf[2][kMaxA], Yf[2][kMaxA];
+  alignas(16) float Xf[2][kMaxA];
+  float Yf[2][kMaxA];
   int hits[2][kMaxA];
   int scan[kNT];
   double red[kNT / 32 * 3];
@@ -153,22 +159,55 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
     uniform2(seed, ev, sid, 2 * c, u0, u1);
     uniform2(seed, ev, sid, 2 * c + 1, u2, u3);
     float x = 0, y = 0, z = 0;
-    bool ok = ws_candidate(n, ctr, phir, u0, u1, u2, u3, x, y, z);
+    const bool ws = ws_candidate(n, ctr, phir, u0, u1, u2, u3, x, y, z);
+    // the radially accepted candidates, compacted in candidate order: the
+    // hard-core tests below then run on full warps
+    const int lane = tid & 31, wid = tid >> 5;
+    const unsigned bal = __ballot_sync(0xffffffffu, ws);
+    if (lane == 0) sm.ired[wid] = __popc(bal);
+    __syncthreads();
+    int off = 0, nv = 0;
+#pragma unroll
+    for (int q = 0; q < kNT / 32; q++) {
+      const int cq = sm.ired[q];
+      off += q < wid ? cq : 0;
+      nv += cq;
+    }
+    if (ws) {
+      const int v = off + __popc(bal & ((1u << lane) - 1u));
+      sm.cx[v] = x; sm.cy[v] = y; sm.cz[v] = z;
+    }
+    __syncthreads();
+    // candidate tid (< nv): hard core against the nucleons accepted so far
+    bool ok = tid < nv;
     if (ok) {
-      for (int k = 0; k < n_acc; k++) {
+      x = sm.cx[tid]; y = sm.cy[tid]; z = sm.cz[tid];
+      // four accepted nucleons per step (the arrays are 16-byte aligned;
+      // entries past n_acc are never compared)
+      int k = 0;
+      for (; k + 4 <= n_acc && ok; k += 4) {
+        const float4 ax = *reinterpret_cast<const float4 *>(&sm.ax[w][k]);
+        const float4 ay = *reinterpret_cast<const float4 *>(&sm.ay[w][k]);
+        const float4 az = *reinterpret_cast<const float4 *>(&sm.az[w][k]);
+        const float d0 = (x - ax.x) * (x - ax.x) + (y - ay.x) * (y - ay.x) + (z - az.x) * (z - az.x);
+        const float d1 = (x - ax.y) * (x - ax.y) + (y - ay.y) * (y - ay.y) + (z - az.y) * (z - az.y);
+        const float d2 = (x - ax.z) * (x - ax.z) + (y - ay.z) * (y - ay.z) + (z - az.z) * (z - az.z);
+        const float d3 = (x - ax.w) * (x - ax.w) + (y - ay.w) * (y - ay.w) + (z - az.w) * (z - az.w);
+        if (fminf(fminf(d0, d1), fminf(d2, d3)) < dmin2) ok = false;
+      }
+      for (; k < n_acc && ok; k++) {
         float dx = x - sm.ax[w][k], dy = y - sm.ay[w][k], dz = z - sm.az[w][k];
-        if (dx * dx + dy * dy + dz * dz < dmin2) { ok = false; break; }
+        if (dx * dx + dy * dy + dz * dz < dmin2) ok = false;
       }
     }
-    sm.cx[tid] = x; sm.cy[tid] = y; sm.cz[tid] = z;
     sm.valid[tid] = ok;
     __syncthreads();
     // conflicts with earlier candidates of the batch, one 32-bit word per warp
-    uint32_t m[kNT / 32];
+    bool conflicted = false;
 #pragma unroll
     for (int q = 0; q < kNT / 32; q++) {
       uint32_t bits = 0;
-      if (ok) {
+      if (ok && q * 32 < tid) {
         const int kmax = min(32, tid - q * 32);
         for (int kk = 0; kk < kmax; kk++) {
           const int k = q * 32 + kk;
@@ -177,35 +216,36 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
           if (dx * dx + dy * dy + dz * dz < dmin2) bits |= 1u << kk;
         }
       }
-      m[q] = bits;
+      sm.cmask[tid][q] = bits;
+      conflicted |= bits != 0;
     }
     // Sequential rule "keep candidate c iff it conflicts with no earlier kept
-    // candidate", resolved in parallel rounds: a candidate is kept once all
-    // its earlier conflicting candidates are decided dropped, and dropped as
-    // soon as one of them is kept.  Rounds end when every candidate is
-    // decided (the longest conflict chain is a few links).
-    if (tid < kNT / 32) { sm.keep[tid] = 0u; sm.drop[tid] = 0u; }
-    __syncthreads();
-    bool decided = !ok;
-    for (int round = 0; round < kNT; round++) {
-      bool keep = false, drop = false;
-      if (!decided) {
-        bool all_dropped = true;
-#pragma unroll
-        for (int q = 0; q < kNT / 32; q++) {
-          uint32_t cm = m[q];
-          if (cm & sm.keep[q]) drop = true;
-          if (cm & ~sm.drop[q]) all_dropped = false;
-        }
-        keep = !drop && all_dropped;
+    // candidate": a valid candidate without such conflicts is kept; the few
+    // with conflicts (a 0.9 fm hard core in a nucleus) are then decided one
+    // by one in candidate order.
+    {
+      const unsigned kb = __ballot_sync(0xffffffffu, ok && !conflicted);
+      const unsigned cb = __ballot_sync(0xffffffffu, ok && conflicted);
+      if ((tid & 31) == 0) {
+        sm.keep[tid >> 5] = kb;
+        sm.conf[tid >> 5] = cb;
       }
-      __syncthreads();
-      if (keep) atomicOr(&sm.keep[tid >> 5], 1u << (tid & 31));
-      if (drop) atomicOr(&sm.drop[tid >> 5], 1u << (tid & 31));
-      if (keep || drop) decided = true;
-      int pending = __syncthreads_count(!decided);
-      if (!pending) break;
     }
+    __syncthreads();
+    if (tid == 0) {
+      for (int q = 0; q < kNT / 32; q++) {
+        uint32_t pend = sm.conf[q];
+        while (pend) {
+          const int c = q * 32 + __ffs(pend) - 1;
+          pend &= pend - 1;
+          bool kept = true;
+          for (int r = 0; r <= q; r++)
+            if (sm.cmask[c][r] & sm.keep[r]) kept = false;
+          if (kept) sm.keep[q] |= 1u << (c & 31);
+        }
+      }
+    }
+    __syncthreads();
     // kept candidates in candidate order, up to the nucleons still missing
     {
       uint32_t kw = sm.keep[tid >> 5];
@@ -257,13 +297,21 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
   const float pxf = (float)px;
   if (tid < A) { sm.X[w][tid] = px; sm.Y[w][tid] = py; sm.Xf[w][tid] = pxf; }
   __syncthreads();
+  // keys past A read as +inf (never below a key)
+  if (tid >= A && tid < ((A + 3) & ~3)) sm.Xf[w][tid] = INFINITY;
+  __syncthreads();
   int rank = 0;
   if (tid < A) {
-    for (int j = 0; j < A; j++) {
-      float xf = sm.Xf[w][j];
-      if (xf < pxf) rank++;
-      else if (xf == pxf) {
-        double xj = sm.X[w][j];
+    int eq = 0;
+    for (int j = 0; j < A; j += 4) {
+      const float4 k4 = *reinterpret_cast<const float4 *>(&sm.Xf[w][j]);
+      rank += (k4.x < pxf) + (k4.y < pxf) + (k4.z < pxf) + (k4.w < pxf);
+      eq += (k4.x == pxf) + (k4.y == pxf) + (k4.z == pxf) + (k4.w == pxf);
+    }
+    if (eq > 1) {   // equal FP32 keys (rare): the FP64 values, then the index, decide
+      for (int j = 0; j < A; j++) {
+        if (sm.Xf[w][j] != pxf || j == tid) continue;
+        const double xj = sm.X[w][j];
         rank += (xj < px) || (xj == px && j < tid);
       }
     }
@@ -318,6 +366,27 @@ __device__ __forceinline__ void sweep_range(const SampleSmem &sm, const DevParam
   // inclusive; nothing is swept when the first candidate already lies
   // beyond the projectile box (the loop condition fails before any test)
   hi = (c == lo) ? lo - 1 : (c < B ? c : B - 1);
+}
+
+// Targets that can meet projectile i under the disk test: |x_j - x_i| <= rad
+// (rad above the hit radius with margin); the targets are sorted by x, so
+// two binary searches on the FP32 keys find the inclusive range [lo, hi].
+// Pairs outside it fail the test, so the hits (and their order) are those
+// of the full scan.
+__device__ __forceinline__ void disk_range(const SampleSmem &sm, int i, int B, float rad, int &lo, int &hi) {
+  const float xl = sm.Xf[0][i] - rad, xr = sm.Xf[0][i] + rad;
+  int a = 0, b = B;
+  while (a < b) {   // first j with x_j >= xl
+    const int m = (a + b) >> 1;
+    if (sm.Xf[1][m] >= xl) b = m; else a = m + 1;
+  }
+  int c = a, d = B;
+  while (c < d) {   // first j with x_j > xr
+    const int m = (c + d) >> 1;
+    if (sm.Xf[1][m] > xr) d = m; else c = m + 1;
+  }
+  lo = a;
+  hi = c - 1;
 }
 
 // MCnucl::hit (src/MCnucl.cpp:357-385) for projectile i, target j.  The disk
@@ -375,6 +444,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P, uint64_t fi
   const int A = P.nuc[0].A, B = P.nuc[1].A;
   const bool inject = inj_proj != nullptr;
   const float dsq_lo = (float)P.dsq * (1.f - 1e-4f), dsq_hi = (float)P.dsq * (1.f + 1e-4f);
+  const float hit_rad = sqrtf(dsq_hi) * (1.f + 1e-4f);   // |dx| beyond it: no disk hit
   const float inv_dx = (float)(1.0 / P.dx), inv_dy = (float)(1.0 / P.dy);
   // The reference only tests pairs its box sweep reaches.  For the disk test
   // with a hit radius well inside the box width every hit pair is swept, so
@@ -435,6 +505,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P, uint64_t fi
       if (tid < A) {
         int jlo = 0, jhi = B - 1;
         if (swept) sweep_range(sm, P, tid, B, jlo, jhi);
+        else if (P.collision_criterion == 1) disk_range(sm, tid, B, hit_rad, jlo, jhi);
         for (int j = jlo; j <= jhi; j++) {
           if (pair_hit(sm, P, tid, j, dsq_lo, dsq_hi, ev, attempt, B, swept)) {
             cnt++;
@@ -623,6 +694,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P, uint64_t fi
       if (tid < A && c > 0) {
         int jlo = 0, jhi = B - 1;
         if (swept) sweep_range(sm, P, tid, B, jlo, jhi);
+        else if (P.collision_criterion == 1) disk_range(sm, tid, B, hit_rad, jlo, jhi);
         for (int j = jlo; j <= jhi && pos < ncs; j++) {
           if (!pair_hit(sm, P, tid, j, dsq_lo, dsq_hi, ev, attempt, B, swept)) continue;
           Source s;
