@@ -34,19 +34,23 @@
 // interval of the reference's FP64 test and adds the window cells outside
 // it to a per-cell correction grid in 32-bit fixed point (unit 2^-39 of
 // the peak height; the CTA's own grid in global memory, L2-resident;
-// integer sums do not depend on the order of the atomic adds), which the
-// post-op subtracts, so the planes hold the reference's sums.  Exact sums
-// are non-negative, so a rounding residue below zero is cleared.  Every
-// cell of a tile has one owner thread (tile row = its TMEM lane, one
-// quarter of the columns) that adds the chunk sums and runs the post-op,
-// so results do not depend on scheduling.
+// integer sums do not depend on the order of the atomic adds).  The
+// tiles subtract the corrections, so the planes hold the reference's
+// sums; exact sums are non-negative, so a rounding residue below zero is
+// cleared.  Every cell of a tile has one owner thread (tile row = its TMEM
+// lane, one quarter of the columns) that adds the chunk sums and runs the
+// post-op, so results do not depend on scheduling.  k_grid_tc writes each
+// event's density and centre-of-mass sums; k_moments (many CTAs per SM)
+// then reduces the eccentricities.
 //
-// A kernel holding TMEM runs one CTA per SM, so the CTA has 16 warps and
-// keeps the event's splat sources in shared memory.  At most two planes
-// (MC-KLN T_A, T_B; sqrt(T_A T_B); Glauber rho) fit its shared memory.
+// k_grid_tc uses 16 warps and keeps the event's splat sources in shared
+// memory (one CTA per SM by its registers and shared memory).  At most two
+// planes (MC-KLN T_A, T_B; sqrt(T_A T_B); Glauber rho) fit.
 #include "grid_common.cuh"
 #include "smc_kernels.h"
 #include "tc_ptx.cuh"
+
+#include <algorithm>
 
 namespace smc {
 
@@ -132,11 +136,10 @@ __device__ __forceinline__ bool splat_source(const Source &s) {
   return (s.kind & 15) != 3 && s.xr > s.xl && s.yr > s.yl;
 }
 
-template <int LO, int HI>
 __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, const EventRec *recs,
                                                     const Source *srcs, float *out_rho, float *out_ta,
-                                                    float *out_tb, float *scratch, int *corr_scratch,
-                                                    double *out_ecc, int *status) {
+                                                    float *out_tb, float *rho_ev, int *corr_scratch,
+                                                    double *cm_ev, int *status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int np = P.n_planes;
   const TcLayout L = tc_layout(P.nx, P.ny, np);
@@ -186,10 +189,10 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
   for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
     const EventRec rec = recs[e];
     const Source *S = srcs + (size_t)e * P.max_src;
-    float *rho = out_rho ? out_rho + (size_t)e * nx * ny : scratch + (size_t)blockIdx.x * nx * ny;
+    float *rho = (out_rho ? out_rho : rho_ev) + (size_t)e * nx * ny;
     float *ta = out_ta ? out_ta + (size_t)e * nx * ny : nullptr;
     float *tb = out_tb ? out_tb + (size_t)e * nx * ny : nullptr;
-    int *corr = corr_scratch + (size_t)blockIdx.x * np * nx * ny;   // [plane][i][j]
+    int *corr = corr_scratch + (size_t)blockIdx.x * np * nx * ny;   // [plane][i][j], this CTA's
     const bool full = out_rho || ta || tb;
     if (tid == 0) s_status = rec.status;
     KSum cm0, cm1, cm2;
@@ -477,21 +480,50 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
       }
       __syncthreads();
     }
-    const double xc = s_cm[1], yc = s_cm[2], tot0 = s_cm[0];
-    float *xo = xg + nx;
-    float *yo = yg + nyp;
-    for (int i = tid; i < nx; i += kTT) xo[i] = (float)((P.xmin + i * P.dx) - xc);
-    for (int j = tid; j < ny; j += kTT) yo[j] = (float)((P.ymin + j * P.dy) - yc);
-    __syncthreads();
-    if (!P.no_moments)
-      moments<LO, HI, kTT>(P, rec, S, rho, reinterpret_cast<uint32_t *>(smem), xo, yo, red, tot0,
-                           out_ecc + (size_t)e * kEccLen);
+    if (tid == 0) {
+      cm_ev[3 * (size_t)e] = s_cm[0];
+      cm_ev[3 * (size_t)e + 1] = s_cm[1];
+      cm_ev[3 * (size_t)e + 2] = s_cm[2];
+    }
     if (tid == 0 && status) status[e] = s_status;
     __syncthreads();
   }
   tc::fence_before_sync();
   __syncthreads();
   if (wid == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+constexpr int kCT = 256;   // threads of k_moments
+
+// ---------------------------------------------------------------- moments
+// Eccentricities of each event from its density grid and centre-of-mass
+// sums (MakeDensity::dumpEccentricities, src/MakeDensity.cpp:2244-2511).
+template <int LO, int HI>
+__global__ void __launch_bounds__(kCT) k_moments(DevParams P, int n_events, const EventRec *recs,
+                                                 const Source *srcs, const float *rho_ev, const double *cm_ev,
+                                                 double *out_ecc) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nx = P.nx, ny = P.ny, nyp = (ny + 31) / 32 * 32;
+  uint32_t *mask = reinterpret_cast<uint32_t *>(smem);
+  float *xo = reinterpret_cast<float *>(smem + sizeof(uint32_t) * (size_t)nx * (nyp / 32));
+  float *yo = xo + nx;
+  float2 *red = reinterpret_cast<float2 *>(yo + nyp);
+  const int tid = threadIdx.x;
+  for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
+    const EventRec rec = recs[e];
+    const double tot0 = cm_ev[3 * (size_t)e], xc = cm_ev[3 * (size_t)e + 1], yc = cm_ev[3 * (size_t)e + 2];
+    for (int i = tid; i < nx; i += kCT) xo[i] = (float)((P.xmin + i * P.dx) - xc);
+    for (int j = tid; j < ny; j += kCT) yo[j] = (float)((P.ymin + j * P.dy) - yc);
+    __syncthreads();
+    moments<LO, HI, kCT>(P, rec, srcs + (size_t)e * P.max_src, rho_ev + (size_t)e * nx * ny, mask, xo, yo, red,
+                         tot0, out_ecc + (size_t)e * kEccLen);
+  }
+}
+
+size_t moments_smem(const DevParams &P) {
+  const int nyp = (P.ny + 31) / 32 * 32;
+  return sizeof(uint32_t) * (size_t)P.nx * (nyp / 32) + sizeof(float) * (P.nx + nyp) +
+         sizeof(float2) * (kCT / 32) * 64;
 }
 
 size_t grid_tc_smem(const DevParams &P) { return tc_layout(P.nx, P.ny, P.n_planes).total; }
@@ -504,19 +536,36 @@ bool grid_tc_supported(const DevParams &P) {
          P.n_planes <= kMaxPlanes && P.max_src <= 32767 && P.splat_mw <= kTM;
 }
 
-// A CTA holding TMEM is not co-resident with another: one CTA per SM.
-int grid_tc_blocks_per_sm(const DevParams &) { return 1; }
+
+template <typename K>
+static int blocks_per_sm(K kern, int threads, size_t smem) {
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
+  int nb = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem) != cudaSuccess || nb < 1) nb = 1;
+  return nb;
+}
 
 cudaError_t launch_grid_tc(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs,
-                           float *out_rho, float *out_ta, float *out_tb, float *scratch, int *corr_scratch,
-                           double *out_ecc, int *status, int grid, cudaStream_t st) {
-  const size_t smem = grid_tc_smem(P);
+                           float *out_rho, float *out_ta, float *out_tb, float *rho_ev, int *corr_scratch,
+                           double *cm_ev, double *out_ecc, int *status, int sms, cudaStream_t st) {
+  if (n_events <= 0) return cudaSuccess;
+  // contraction, post-op, centre of mass
+  {
+    const size_t smem = grid_tc_smem(P);
+    cudaError_t e = cudaFuncSetAttribute(k_grid_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_grid_tc<<<std::max(1, std::min(n_events, sms)), kTT, smem, st>>>(P, n_events, recs, srcs, out_rho, out_ta,
+                                                                       out_tb, rho_ev, corr_scratch, cm_ev, status);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (P.no_moments) return cudaSuccess;
+  const size_t smem = moments_smem(P);
   const bool narrow = P.ecc_from >= 2 && P.ecc_to <= 5;
-  auto kern = narrow ? k_grid_tc<2, 5> : k_grid_tc<1, 9>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  kern<<<grid, kTT, smem, st>>>(P, n_events, recs, srcs, out_rho, out_ta, out_tb, scratch, corr_scratch, out_ecc,
-                                status);
+  auto kern = narrow ? k_moments<2, 5> : k_moments<1, 9>;
+  const int nb = blocks_per_sm(kern, kCT, smem);
+  kern<<<std::max(1, std::min(n_events, sms * nb)), kCT, smem, st>>>(P, n_events, recs, srcs,
+                                                                    out_rho ? out_rho : rho_ev, cm_ev, out_ecc);
   return cudaGetLastError();
 }
 

@@ -148,7 +148,7 @@ struct Ctx {
   smc_info info{};
   int device = 0, sms = 0;
   cudaStream_t own = nullptr, st = nullptr;
-  int occ1 = 1, occ2 = 1, occ_tc = 1;
+  int occ1 = 1, occ2 = 1;
   bool use_tc = true;   // tensor-core splat for the batched paths (when the profile allows it)
   int chunk = 4096;
   DevBuf<EventRec> recs;
@@ -156,7 +156,11 @@ struct Ctx {
   DevBuf<double> ecc, pos, bvec, inj_p, inj_t, inj_b;
   DevBuf<float> rho, ta, tb, scratch;
   DevBuf<int> status, npart, ncoll, attempts;
-  DevBuf<int> corr_scratch;   // corner corrections of the tensor-core splat, per CTA
+  // buffers of the tensor-core splat: per-event densities (when not an
+  // output), per-CTA corner corrections, per-event centre-of-mass sums
+  DevBuf<float> rho_ev;
+  DevBuf<int> corr_ev;
+  DevBuf<double> cm_ev;
   DevBuf<uint8_t> wounded;
   DevBuf<double> kln64;
   DevBuf<float> kln32;
@@ -306,10 +310,14 @@ __global__ void k_scalars(const EventRec *r, int n, int *npart, int *ncoll, doub
 cudaError_t launch_splat(Ctx *c, const DevParams &P, int n, const EventRec *recs, const Source *srcs, float *rho,
                          float *ta, float *tb, float *scratch, double *ecc, int *status) {
   if (c->use_tc && smc::grid_tc_supported(P)) {
-    const int grid = std::max(1, std::min(n, c->sms * c->occ_tc));
-    cudaError_t e = c->corr_scratch.ensure((size_t)grid * P.n_planes * P.nx * P.ny);
+    const size_t g = (size_t)P.nx * P.ny;
+    cudaError_t e = c->corr_ev.ensure((size_t)c->sms * P.n_planes * g);
+    if (e == cudaSuccess && !rho) e = c->rho_ev.ensure((size_t)n * g);
+    if (e == cudaSuccess) e = c->cm_ev.ensure((size_t)n * 3);
     if (e != cudaSuccess) return e;
-    return smc::launch_grid_tc(P, n, recs, srcs, rho, ta, tb, scratch, c->corr_scratch.p, ecc, status, grid, c->st);
+    c->stats.launches += P.no_moments ? 0 : 1;   // k_moments besides the timed launch
+    return smc::launch_grid_tc(P, n, recs, srcs, rho, ta, tb, c->rho_ev.p, c->corr_ev.p, c->cm_ev.p, ecc, status,
+                               c->sms, c->st);
   }
   const int grid = std::max(1, std::min(n, c->sms * c->occ2));
   return smc::launch_grid(P, n, recs, srcs, rho, ta, tb, scratch, ecc, status, grid, c->st);
@@ -343,8 +351,7 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
   uint8_t *wnd = out->wounded ? (dev ? out->wounded + (size_t)off * AB : c->wounded.p) : nullptr;
   int grid1 = std::max(1, std::min(n, c->sms * c->occ1));
   int grid2 = std::max(1, std::min(n, c->sms * c->occ2));
-  const int grid_tc = std::max(1, std::min(n, c->sms * c->occ_tc));
-  if (!rho) CK(c->scratch.ensure((size_t)(plain ? 1 : std::max(grid2, grid_tc)) * g));
+  if (!rho) CK(c->scratch.ensure((size_t)(plain ? 1 : grid2) * g));
   if (plain) {
     for (int e = 0; e < n; e++) {
       CK(timed(c, 0, [&] {
@@ -551,7 +558,7 @@ void smc_destroy(void *ctx) {
   c->recs.release(); c->srcs.release(); c->ecc.release(); c->pos.release(); c->bvec.release();
   c->inj_p.release(); c->inj_t.release(); c->inj_b.release(); c->rho.release(); c->ta.release();
   c->tb.release(); c->scratch.release(); c->status.release(); c->npart.release(); c->ncoll.release();
-  c->attempts.release(); c->wounded.release(); c->corr_scratch.release(); c->kln64.release(); c->kln32.release();
+  c->attempts.release(); c->wounded.release(); c->rho_ev.release(); c->corr_ev.release(); c->cm_ev.release(); c->kln64.release(); c->kln32.release();
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
@@ -586,7 +593,6 @@ static smc_status set_thickness_flags(Ctx *c, const smc_outputs *out) {
   P.n_planes = P.which_mc_model == 5 ? ((P.want_ta || P.want_tb) ? 3 : 1) : 2;
   if (P.ny > 512) return SMC_ERR_CONFIG;
   c->occ2 = smc::grid_blocks_per_sm(P);
-  c->occ_tc = smc::grid_tc_supported(P) ? smc::grid_tc_blocks_per_sm(P) : 1;
   return SMC_OK;
 }
 

@@ -22,11 +22,14 @@ cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, 
                         cudaStream_t st);
 size_t grid_tc_smem(const DevParams &P);
 bool grid_tc_supported(const DevParams &P);
-int grid_tc_blocks_per_sm(const DevParams &P);
-// corr_scratch: per-CTA corner-correction grids, grid x n_planes x nx x ny ints
+// Tensor-core splat of a batch: contraction, corner corrections and post-op
+// (k_grid_tc, one CTA per SM), then the eccentricities (k_moments, unless
+// P.no_moments).  Buffers: rho_ev [n][nx][ny] floats (the densities when
+// out_rho is NULL), corr_scratch [sms][n_planes][nx][ny] ints (per-CTA
+// corner corrections), cm_ev [n][3] doubles (centre-of-mass sums).
 cudaError_t launch_grid_tc(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs,
-                           float *out_rho, float *out_ta, float *out_tb, float *scratch, int *corr_scratch,
-                           double *out_ecc, int *status, int grid, cudaStream_t st);
+                           float *out_rho, float *out_ta, float *out_tb, float *rho_ev, int *corr_scratch,
+                           double *cm_ev, double *out_ecc, int *status, int sms, cudaStream_t st);
 cudaError_t launch_avg_init(const DevParams &P, int n, const EventRec *recs, const Source *srcs, AvgSrc *state,
                             int grid, cudaStream_t st);
 cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Source *srcs, AvgSrc *state,
