@@ -258,6 +258,53 @@ def eps_error(eng, vals, n: int = 24) -> float:
     return worst
 
 
+# ------------------------------------------------------------------ mixed batch
+MIXED_BASE = {
+    "which_mc_model": 5, "sub_model": 1, "shape_of_nucleons": 4, "gauss_nucl_width": 0.5,
+    "collision_criterion": 1, "shape_of_entropy": 2, "quark_width": 0.3, "alpha": 0.118, "bmin": 0.0,
+    "bmax": 20.0, "npmin": 2, "npmax": 600, "maxx": 13.0, "maxy": 13.0, "dx": 0.1, "dy": 0.1,
+    "finalfactor": 40.0, "ecc_from_order": 2, "ecc_to_order": 5, "cc_fluctuation_model": 0,
+}
+MIXED_SYSTEMS = [   # (share, parameters): p+Pb, d+Au, Cu+Cu, deformed U+U, Au+Au
+    (1, {"aproj": 1, "atarg": 208, "ecm": 5020.0}),
+    (2, {"aproj": 2, "atarg": 197, "ecm": 200.0}),
+    (2, {"aproj": 63, "atarg": 63, "ecm": 200.0, "proj_r": 4.2, "proj_a": 0.596, "targ_r": 4.2, "targ_a": 0.596}),
+    (2, {"aproj": 238, "atarg": 238, "ecm": 200.0, "proj_deformed": 1, "targ_deformed": 1, "proj_r": 6.81,
+         "proj_a": 0.55, "targ_r": 6.81, "targ_a": 0.55}),
+    (3, {"aproj": 197, "atarg": 197, "ecm": 200.0, "proj_r": 6.38, "proj_a": 0.535, "targ_r": 6.38,
+         "targ_a": 0.535, "proj_d_min": 0.4, "targ_d_min": 0.4, "sigininn_override": 42.0}),
+]
+
+
+def mixed_batch(dev, stream, n: int) -> dict:
+    """events/s of one mixed-system batch of n events, events in HBM."""
+    import numpy as np
+    import torch
+    from supermc_gb300.engine import Engine
+    eng = Engine(dict(MIXED_BASE, **MIXED_SYSTEMS[-1][1]), seed=2)
+    eng.set_stream(stream.cuda_stream)
+    shares = np.array([s for s, _ in MIXED_SYSTEMS], dtype=float)
+    counts = np.floor(n * shares / shares.sum()).astype(int)
+    counts[-1] += n - counts.sum()
+    sel = np.random.default_rng(5).permutation(np.repeat(np.arange(len(counts)), counts)).astype(np.int32)
+    systems = [p for _, p in MIXED_SYSTEMS]
+    bufs = {"ecc": torch.empty((n, 49), dtype=torch.float64, device=dev),
+            "npart": torch.empty((n, 2), dtype=torch.int32, device=dev)}
+    eng.generate_mixed(systems, sel, first_event=0, device_bufs=bufs)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    eng.generate_mixed(systems, sel, first_event=n, device_bufs=bufs)
+    b.record(stream)
+    torch.cuda.synchronize()
+    rate = n / (a.elapsed_time(b) / 1e3)
+    eng.close()
+    return {"value": rate, "unit": "events/s", "events": n,
+            "systems": "p+Pb 5.02 TeV, d+Au, Cu+Cu, deformed U+U, Au+Au (200 GeV) in shares 1:2:2:2:3, "
+                       "MC-Glauber 261x261, one smc_generate_mixed call"}
+
+
 # ------------------------------------------------------------------ GPU arm
 def run_gpu(args, vals) -> dict | None:
     import numpy as np
@@ -367,6 +414,10 @@ def run_gpu(args, vals) -> dict | None:
     cuda_core = n / (a.elapsed_time(b) / 1e3)
     eng.set_grid_path(True)
 
+    # ---- mixed-system batch (p+Pb, d+Au, Cu+Cu, deformed U+U, Au+Au in the
+    # proportions 1:2:2:2:3, MC-Glauber), one smc_generate_mixed call
+    mixed = mixed_batch(dev, stream, args.mixed_events)
+
     # ---- plain per-event path, same workload (sample)
     m = args.plain_events
     pb = {k: v[:m] for k, v in bufs.items()}
@@ -419,6 +470,7 @@ def run_gpu(args, vals) -> dict | None:
             "clocks": clk, "roofline": roof, "cpu_baseline": base,
             "plain_gpu": {"value": plain, "unit": "events/s", "events": m,
                           "batched_over_plain": value / plain},
+            "mixed_batch": mixed,
             "batched_cuda_core_splat": {"value": cuda_core, "unit": "events/s", "events": n,
                                         "note": "same batched path, FP32 CUDA-core splat (smc_set_grid_path 0)"},
             "eps_abs_err_vs_fp64_oracle": err, "init_s": t_init}
@@ -437,6 +489,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--events", type=int, default=EVENTS_PER_STEP)
     ap.add_argument("--plain-events", type=int, default=200)
+    ap.add_argument("--mixed-events", type=int, default=20000)
     ap.add_argument("--ref-events", type=int, default=1600, help="reference arm: events per step (all cores)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--seed", type=int, default=1)

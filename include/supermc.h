@@ -145,6 +145,22 @@ smc_status smc_generate(void *ctx, uint64_t first_event, int n, const smc_output
 smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_targ,
                       const double *b, const smc_outputs *out);
 
+/* Mixed-system batch: events of several collision systems in one launch
+ * per stage (the reference runs one system per process, src/main.cpp:35-61,
+ * so a mixed sample there is several runs).  systems[0..nsys) are full
+ * parameter sets that may differ from the context's only in Aproj, Atarg,
+ * the deformation flags, ecm / sigin_override, the Woods-Saxon and hard-core
+ * overrides, bmin, bmax, npmin and npmax; everything else (model, nucleon
+ * and entropy shape -- shape_of_nucleons 4 --, grid, alpha, orders, seed)
+ * must equal the context's.  Event first_event + e belongs to system
+ * system_of_event[e] and draws the Philox streams it would draw in a
+ * single-system context of that system, so its results are the same.
+ * Within each chunk the heavier systems are scheduled first.  MC-Glauber
+ * and sqrt(T_A T_B) only (MC-KLN tables are per energy); out->positions and
+ * out->wounded are not produced (their shapes differ between systems). */
+smc_status smc_generate_mixed(void *ctx, const smc_params *systems, int nsys, uint64_t first_event, int n,
+                              const int *system_of_event, const smc_outputs *out);
+
 /* Plain per-event path: the same results as smc_generate, one event per
  * kernel launch sequence (the unbatched baseline). */
 smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_outputs *out);

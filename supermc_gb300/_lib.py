@@ -23,7 +23,8 @@ ECC_LEN = 49
 
 # exported symbols, in the order include/supermc.h declares them
 EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "smc_set_stream",
-           "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_plain", "smc_set_timing",
+           "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_mixed", "smc_generate_plain",
+           "smc_set_timing",
            "smc_set_grid_path", "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_inject_noalloc",
            "smc_average"]
 
@@ -106,6 +107,8 @@ def load() -> ctypes.CDLL:
     lib.smc_synchronize.argtypes = [vp]
     lib.smc_generate.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(SmcOutputs)]
     lib.smc_generate_plain.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(SmcOutputs)]
+    lib.smc_generate_mixed.argtypes = [vp, ctypes.POINTER(SmcParams), ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
+                                       vp, ctypes.POINTER(SmcOutputs)]
     lib.smc_inject.argtypes = [vp, ctypes.c_int, vp, vp, vp, ctypes.POINTER(SmcOutputs)]
     lib.smc_kln_table.argtypes = [vp, vp, ctypes.c_int]
     lib.smc_set_timing.argtypes = [vp, ctypes.c_int]

@@ -434,24 +434,49 @@ __device__ __forceinline__ void set_window(Source &s, double lo, double hi, doub
 }
 
 // ----------------------------------------------------------------- kernel
-__global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P, uint64_t first_event, int n_events,
+// systems / ev_sys (mixed batches, else NULL): the system parameters of
+// event e are systems[ev_sys[e]]; order (else NULL): the order in which the
+// CTAs take the events (heavy systems first).
+__global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t first_event, int n_events,
                                                      const double *inj_proj, const double *inj_targ,
                                                      const double *inj_b, EventRec *recs, Source *srcs,
-                                                     double *out_pos, uint8_t *out_wounded) {
+                                                     double *out_pos, uint8_t *out_wounded,
+                                                     const SystemDev *systems, const int *ev_sys,
+                                                     const int *order) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SampleSmem &sm = *reinterpret_cast<SampleSmem *>(smem_raw);
+  __shared__ DevParams s_P;   // the context's parameters with the event's system
+  const DevParams &P = s_P;
   const int tid = threadIdx.x;
-  const int A = P.nuc[0].A, B = P.nuc[1].A;
   const bool inject = inj_proj != nullptr;
-  const float dsq_lo = (float)P.dsq * (1.f - 1e-4f), dsq_hi = (float)P.dsq * (1.f + 1e-4f);
-  const float hit_rad = sqrtf(dsq_hi) * (1.f + 1e-4f);   // |dx| beyond it: no disk hit
-  const float inv_dx = (float)(1.0 / P.dx), inv_dy = (float)(1.0 / P.dy);
-  // The reference only tests pairs its box sweep reaches.  For the disk test
-  // with a hit radius well inside the box width every hit pair is swept, so
-  // all pairs are tested; otherwise the sweep's tested set is reproduced.
-  const bool swept = P.collision_criterion != 1 || sqrt(P.dsq) > 7.9 * fmax(P.width, P.quark_width);
+  const float inv_dx = (float)(1.0 / P_in.dx), inv_dy = (float)(1.0 / P_in.dy);
 
-  for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
+  for (int k_ev = blockIdx.x; k_ev < n_events; k_ev += gridDim.x) {
+    const int e = order ? order[k_ev] : k_ev;
+    __syncthreads();   // s_P of the previous event is no longer read
+    if (tid == 0) {
+      s_P = P_in;
+      if (systems) {
+        const SystemDev &sd = systems[ev_sys[e]];
+        s_P.nuc[0] = sd.nuc[0];
+        s_P.nuc[1] = sd.nuc[1];
+        s_P.dsq = sd.dsq;
+        s_P.sigma_gg = sd.sigma_gg;
+        s_P.sigin = sd.sigin;
+        s_P.bmin = sd.bmin;
+        s_P.bmax = sd.bmax;
+        s_P.npmin = sd.npmin;
+        s_P.npmax = sd.npmax;
+      }
+    }
+    __syncthreads();
+    const int A = P.nuc[0].A, B = P.nuc[1].A;
+    const float dsq_lo = (float)P.dsq * (1.f - 1e-4f), dsq_hi = (float)P.dsq * (1.f + 1e-4f);
+    const float hit_rad = sqrtf(dsq_hi) * (1.f + 1e-4f);   // |dx| beyond it: no disk hit
+    // The reference only tests pairs its box sweep reaches.  For the disk test
+    // with a hit radius well inside the box width every hit pair is swept, so
+    // all pairs are tested; otherwise the sweep's tested set is reproduced.
+    const bool swept = P.collision_criterion != 1 || sqrt(P.dsq) > 7.9 * fmax(P.width, P.quark_width);
     const uint64_t ev = first_event + (uint64_t)e;
     int status = 0, attempt = 0, ncoll = 0, np1 = 0, np2 = 0;
     for (;; attempt++) {
@@ -757,6 +782,14 @@ size_t sample_pair_smem() { return sizeof(SampleSmem); }
 cudaError_t launch_sample_pair(const DevParams &P, uint64_t first_event, int n_events, const double *inj_proj,
                                const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
                                double *out_pos, uint8_t *out_wounded, int grid, cudaStream_t st) {
+  return launch_sample_pair_mixed(P, first_event, n_events, inj_proj, inj_targ, inj_b, recs, srcs, out_pos,
+                                  out_wounded, nullptr, nullptr, nullptr, grid, st);
+}
+
+cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, int n_events, const double *inj_proj,
+                                     const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
+                                     double *out_pos, uint8_t *out_wounded, const SystemDev *systems,
+                                     const int *ev_sys, const int *order, int grid, cudaStream_t st) {
   size_t smem = sizeof(SampleSmem);
   static bool attr = false;
   if (!attr) {
@@ -765,7 +798,7 @@ cudaError_t launch_sample_pair(const DevParams &P, uint64_t first_event, int n_e
     attr = true;
   }
   k_sample_pair<<<grid, kNT, smem, st>>>(P, first_event, n_events, inj_proj, inj_targ, inj_b, recs, srcs, out_pos,
-                                         out_wounded);
+                                         out_wounded, systems, ev_sys, order);
   return cudaGetLastError();
 }
 

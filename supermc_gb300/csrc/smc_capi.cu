@@ -161,6 +161,10 @@ struct Ctx {
   DevBuf<float> rho_ev;
   DevBuf<int> corr_ev;
   DevBuf<double> cm_ev;
+  // mixed batches: system table, per-event system of the chunk, event order
+  bool mixing = false;
+  DevBuf<smc::SystemDev> mix_sys;
+  DevBuf<int> mix_ev, mix_order;
   DevBuf<uint8_t> wounded;
   DevBuf<double> kln64;
   DevBuf<float> kln32;
@@ -370,8 +374,10 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
     }
   } else {
     CK(timed(c, 0, [&] {
-      return smc::launch_sample_pair(P, first_event, n, inj_p, inj_t, inj_b, c->recs.p, c->srcs.p, pos, wnd, grid1,
-                                     c->st);
+      return smc::launch_sample_pair_mixed(P, first_event, n, inj_p, inj_t, inj_b, c->recs.p, c->srcs.p, pos, wnd,
+                                           c->mix_sys.p && c->mixing ? c->mix_sys.p : nullptr,
+                                           c->mixing ? c->mix_ev.p : nullptr, c->mixing ? c->mix_order.p : nullptr,
+                                           grid1, c->st);
     }));
     CK(timed(c, 1, [&] {
       return launch_splat(c, P, n, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p);
@@ -558,7 +564,8 @@ void smc_destroy(void *ctx) {
   c->recs.release(); c->srcs.release(); c->ecc.release(); c->pos.release(); c->bvec.release();
   c->inj_p.release(); c->inj_t.release(); c->inj_b.release(); c->rho.release(); c->ta.release();
   c->tb.release(); c->scratch.release(); c->status.release(); c->npart.release(); c->ncoll.release();
-  c->attempts.release(); c->wounded.release(); c->rho_ev.release(); c->corr_ev.release(); c->cm_ev.release(); c->kln64.release(); c->kln32.release();
+  c->attempts.release(); c->wounded.release(); c->rho_ev.release(); c->corr_ev.release(); c->cm_ev.release();
+  c->mix_sys.release(); c->mix_ev.release(); c->mix_order.release(); c->kln64.release(); c->kln32.release();
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
@@ -611,6 +618,79 @@ smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_
   smc_status s = set_thickness_flags(c, out);
   if (s) return s;
   return run(c, first_event, n, out, nullptr, nullptr, nullptr, true);
+}
+
+smc_status smc_generate_mixed(void *ctx, const smc_params *systems, int nsys, uint64_t first_event, int n,
+                              const int *system_of_event, const smc_outputs *out) {
+  if (!ctx || !out || !systems || nsys < 1 || nsys > 64 || n < 0 || (n > 0 && !system_of_event))
+    return SMC_ERR_ARGUMENT;
+  if (out->positions || out->wounded) return SMC_ERR_ARGUMENT;   // per-system shapes
+  Ctx *c = static_cast<Ctx *>(ctx);
+  const smc_params &q = c->prm;
+  if (q.which_mc_model == 1 || q.shape_of_nucleons != 4) return SMC_ERR_CONFIG;
+  std::vector<smc::SystemDev> sys(nsys);
+  std::vector<int> cost(nsys);
+  int max_ab = c->info.A + c->info.B;
+  for (int k = 0; k < nsys; k++) {
+    const smc_params &p = systems[k];
+    smc_status v = validate(p);
+    if (v) return v;
+    // everything but the nuclei, the energy / sigma_in, the impact-parameter
+    // range and the Npart cut is the context's
+    if (p.which_mc_model != q.which_mc_model || p.sub_model != q.sub_model ||
+        p.shape_of_nucleons != q.shape_of_nucleons || p.shape_of_entropy != q.shape_of_entropy ||
+        p.collision_criterion != q.collision_criterion || p.gauss_nucl_width != q.gauss_nucl_width ||
+        p.quark_width != q.quark_width || p.alpha != q.alpha || p.maxx != q.maxx || p.maxy != q.maxy ||
+        p.dx != q.dx || p.dy != q.dy || p.final_factor != q.final_factor ||
+        p.ecc_from_order != q.ecc_from_order || p.ecc_to_order != q.ecc_to_order || p.seed != q.seed)
+      return SMC_ERR_CONFIG;
+    smc::SystemDev &d = sys[k];
+    const double sigin = p.sigin_override > 0 ? p.sigin_override : sigma_inelastic(p.ecm);
+    d.nuc[0] = make_nucleus(p.Aproj, p.proj_deformed, p.proj_R, p.proj_a, p.proj_d_min);
+    d.nuc[1] = make_nucleus(p.Atarg, p.targ_deformed, p.targ_R, p.targ_a, p.targ_d_min);
+    d.dsq = 0.1 * sigin / M_PI;   // MCnucl.cpp:120
+    d.sigin = sigin;
+    d.sigma_gg = sigma_gg_from(sigin, c->P.width);
+    d.bmin = p.bmin; d.bmax = p.bmax; d.npmin = p.npmin; d.npmax = p.npmax;
+    cost[k] = p.Aproj + p.Atarg;
+    max_ab = std::max(max_ab, p.Aproj + p.Atarg);
+  }
+  for (int e = 0; e < n; e++)
+    if (system_of_event[e] < 0 || system_of_event[e] >= nsys) return SMC_ERR_ARGUMENT;
+  smc_status s = set_thickness_flags(c, out);
+  if (s) return s;
+  if (n == 0) return SMC_OK;
+  CK(cudaSetDevice(c->device));
+  CK(c->mix_sys.ensure(nsys));
+  CK(cudaMemcpyAsync(c->mix_sys.p, sys.data(), sizeof(smc::SystemDev) * nsys, cudaMemcpyHostToDevice, c->st));
+  // per-event source capacity of the largest system
+  const int saved_max_src = c->P.max_src;
+  c->P.max_src = 2 * max_ab + c->P.max_coll;
+  c->mixing = true;
+  smc_status worst = SMC_OK;
+  std::vector<int> order, evs;
+  for (int off = 0; off < n; off += c->chunk) {
+    const int m = std::min(c->chunk, n - off);
+    // the CTAs take the chunk's events heavy systems first
+    order.resize(m);
+    for (int e = 0; e < m; e++) order[e] = e;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      return cost[system_of_event[off + a]] > cost[system_of_event[off + b]];
+    });
+    s = ensure_buffers(c, m, out);
+    if (!s && (c->mix_ev.ensure(m) != cudaSuccess || c->mix_order.ensure(m) != cudaSuccess)) s = SMC_ERR_CUDA;
+    if (!s && (cudaMemcpyAsync(c->mix_ev.p, system_of_event + off, sizeof(int) * m, cudaMemcpyHostToDevice, c->st) !=
+                   cudaSuccess ||
+               cudaMemcpyAsync(c->mix_order.p, order.data(), sizeof(int) * m, cudaMemcpyHostToDevice, c->st) !=
+                   cudaSuccess))
+      s = SMC_ERR_CUDA;
+    if (!s) s = run_chunk(c, first_event + off, off, m, out, nullptr, nullptr, nullptr, false);
+    if (s) worst = s;
+    if (s && s != SMC_ERR_ZERO_DNDY) break;
+  }
+  c->mixing = false;
+  c->P.max_src = saved_max_src;
+  return worst;
 }
 
 smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_targ, const double *b,

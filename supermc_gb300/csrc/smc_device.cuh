@@ -41,6 +41,15 @@ struct NucleusDev {
   double R, a, beta2, beta4, d_min, rmax_cut, rw_max;
 };
 
+// The parameters that differ between the systems of a mixed batch (the
+// nuclei, sigma_in and its derived pairing constants, the impact-parameter
+// range and the Npart cut).
+struct SystemDev {
+  NucleusDev nuc[2];
+  double dsq, sigma_gg, sigin, bmin, bmax;
+  int npmin, npmax;
+};
+
 // Per-context constants passed by value to every kernel.
 struct DevParams {
   int nx, ny;

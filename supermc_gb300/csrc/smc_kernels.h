@@ -15,6 +15,12 @@ size_t sample_pair_smem();
 cudaError_t launch_sample_pair(const DevParams &P, uint64_t first_event, int n_events, const double *inj_proj,
                                const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
                                double *out_pos, uint8_t *out_wounded, int grid, cudaStream_t st);
+// Mixed batch: event e takes the system parameters systems[ev_sys[e]]; the
+// CTAs take the events in the given order (NULL: 0, 1, ...).
+cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, int n_events, const double *inj_proj,
+                                     const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
+                                     double *out_pos, uint8_t *out_wounded, const SystemDev *systems,
+                                     const int *ev_sys, const int *order, int grid, cudaStream_t st);
 size_t grid_smem(const DevParams &P);
 int grid_blocks_per_sm(const DevParams &P);
 cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs, float *out_rho,

@@ -47,6 +47,9 @@ def smc_params_from(vals: dict[str, float], seed: int = 1) -> _lib.SmcParams:
 
 
 OUTPUT_NAMES = ("ecc", "rho", "ta", "tb", "npart", "ncoll", "b", "attempts", "positions", "wounded")
+# keys that describe one collision system of a mixed batch
+SYSTEM_KEYS = ("aproj", "atarg", "proj_deformed", "targ_deformed", "ecm", "sigininn_override", "proj_r", "proj_a",
+               "targ_r", "targ_a", "proj_d_min", "targ_d_min")
 
 
 class Engine:
@@ -105,6 +108,35 @@ class Engine:
         bufs = self._host_buffers(n, want)
         o = self._outputs(bufs, False)
         _lib.check(self.lib.smc_generate_plain(self.h, first_event, n, ctypes.byref(o)), "smc_generate_plain")
+        return bufs
+
+    def generate_mixed(self, systems: list[dict], system_of_event, first_event: int = 0,
+                       want=("ecc", "npart", "ncoll", "b"), device_bufs: dict | None = None):
+        """Events of several collision systems in one batch.  systems are
+        parameters.dat key sets: the nucleus and energy keys (SYSTEM_KEYS)
+        start from their defaults, every other key is this engine's unless
+        given (only the impact-parameter range and the Npart cut may differ
+        besides); system_of_event[e] selects event first_event + e's system."""
+        nsys = len(systems)
+        arr = (_lib.SmcParams * nsys)()
+        for k, sysv in enumerate(systems):
+            # the nucleus and energy keys start from their defaults; the
+            # model, grid and cut keys are this engine's
+            vals = dict(self.values)
+            for key in SYSTEM_KEYS:
+                vals[key] = DEFAULTS[key] if key in DEFAULTS else EXTENSION_KEYS[key]
+            vals.update({key.lower(): float(v) for key, v in sysv.items()})
+            arr[k] = smc_params_from(vals, self.params.seed)
+        sel = np.ascontiguousarray(system_of_event, dtype=np.int32)
+        n = len(sel)
+        if device_bufs is not None:
+            o = self._outputs(device_bufs, True)
+            bufs = device_bufs
+        else:
+            bufs = self._host_buffers(n, want)
+            o = self._outputs(bufs, False)
+        _lib.check(self.lib.smc_generate_mixed(self.h, arr, nsys, first_event, n, _lib.ptr(sel), ctypes.byref(o)),
+                   "smc_generate_mixed")
         return bufs
 
     def generate_into(self, first_event: int, n: int, device_bufs: dict, plain: bool = False) -> None:
