@@ -212,6 +212,23 @@ smc_status smc_reset_stats(void *ctx);
  * current table ([tmax][tmax] doubles, rapidity slice 0) to host. */
 smc_status smc_kln_table(void *ctx, double *host_table, int capacity);
 
+/* Text outputs in the reference's layouts (host code, no GPU), so that the
+ * reference's downstream tools read the results unchanged.
+ * smc_write_ecc: MakeDensity::dumpEccentricities (src/MakeDensity.cpp:
+ *   2432-2500, non-deformed layout): for each event of ecc[n][49] appends
+ *   one line to the file of each order in [from_order, to_order] and one
+ *   line with all orders 1..9 to the file of order 10; pattern is a printf
+ *   pattern with one %d for the order ("data/sn_ecc_eccp_%d.dat").
+ * smc_write_density_block: MakeDensity::dumpDensityBlock (:2597-2609):
+ *   grid[nx][ny] as nx lines of ny values (%22.12g); the reference writes
+ *   the entropy density getRho * finalFactor.
+ * smc_write_density_4col: MakeDensity::dumpDensity4Col (:2573-2595): a
+ *   header with Npart and the grid size, then rapidity, x, y, value per cell. */
+smc_status smc_write_ecc(const double *ecc, int n, int from_order, int to_order, const char *pattern);
+smc_status smc_write_density_block(const double *grid, int nx, int ny, const char *filename);
+smc_status smc_write_density_4col(const double *grid, int nx, int ny, double xmin, double ymin, double dx, double dy,
+                                  double rapidity, double npart, const char *filename);
+
 /* smc_inject without any device allocation.  No counterpart in the
  * reference (which allocates host arrays freely); it exists for callers that
  * may not call cudaMalloc -- a host framework that owns all device memory

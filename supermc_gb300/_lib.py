@@ -25,8 +25,8 @@ ECC_LEN = 49
 EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "smc_set_stream",
            "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_mixed", "smc_generate_plain",
            "smc_set_timing",
-           "smc_set_grid_path", "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_inject_noalloc",
-           "smc_average"]
+           "smc_set_grid_path", "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_write_ecc",
+           "smc_write_density_block", "smc_write_density_4col", "smc_inject_noalloc", "smc_average"]
 
 
 class SmcError(RuntimeError):
@@ -113,6 +113,9 @@ def load() -> ctypes.CDLL:
     lib.smc_kln_table.argtypes = [vp, vp, ctypes.c_int]
     lib.smc_set_timing.argtypes = [vp, ctypes.c_int]
     lib.smc_set_grid_path.argtypes = [vp, ctypes.c_int]
+    lib.smc_write_ecc.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
+    lib.smc_write_density_block.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
+    lib.smc_write_density_4col.argtypes = [vp, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6 + [ctypes.c_char_p]
     lib.smc_get_stats.argtypes = [vp, ctypes.POINTER(SmcStats)]
     lib.smc_reset_stats.argtypes = [vp]
     lib.smc_average.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int,

@@ -1,0 +1,34 @@
+"""Writers of the reference's text files (host side, through the C ABI's
+smc_write_* functions): eccentricity tables, density blocks and 4-column
+density files, so that the reference's downstream scripts read the results
+unchanged."""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+
+
+def write_ecc(ecc, from_order: int, to_order: int, pattern: str = "data/sn_ecc_eccp_%d.dat") -> None:
+    """Appends the MakeDensity::dumpEccentricities lines of ecc[n][49]."""
+    e = np.ascontiguousarray(np.atleast_2d(ecc), dtype=np.float64)
+    lib = _lib.load()
+    _lib.check(lib.smc_write_ecc(_lib.ptr(e), e.shape[0], from_order, to_order, pattern.encode()), "smc_write_ecc")
+
+
+def write_density_block(grid, filename: str) -> None:
+    """MakeDensity::dumpDensityBlock of one [nx][ny] grid (pass the entropy
+    density getRho * finalFactor, as the reference writes)."""
+    g = np.ascontiguousarray(grid, dtype=np.float64)
+    lib = _lib.load()
+    _lib.check(lib.smc_write_density_block(_lib.ptr(g), g.shape[0], g.shape[1], filename.encode()),
+               "smc_write_density_block")
+
+
+def write_density_4col(grid, xmin: float, ymin: float, dx: float, dy: float, npart: float, filename: str,
+                       rapidity: float = 0.0) -> None:
+    """MakeDensity::dumpDensity4Col of one [nx][ny] grid."""
+    g = np.ascontiguousarray(grid, dtype=np.float64)
+    lib = _lib.load()
+    _lib.check(lib.smc_write_density_4col(_lib.ptr(g), g.shape[0], g.shape[1], xmin, ymin, dx, dy, rapidity, npart,
+                                          filename.encode()), "smc_write_density_4col")

@@ -197,11 +197,39 @@ def make_constants(out):
         json.dump(c, f, indent=1)
 
 
+def make_text(out):
+    """Raw text files of the stock reference binary: the eccentricity files of
+    operation 9 (4 Au+Au events, orders 2..5) and the block / 4-column density
+    files of operation 1 (2 events on a 13x13 grid)."""
+    import subprocess
+    import tempfile
+    ref, vals = ref_for(["auau200"])
+    exe = os.path.join(REPO, "oracle", "_ref", "superMC.e")
+    texts = {}
+    for op, args in ((9, ["nev=4", "ecc_from_order=2", "ecc_to_order=5"]),
+                     (1, ["nev=2", "maxx=3", "maxy=3", "dx=0.5", "dy=0.5", "use_block=1", "use_4col=1"])):
+        wd = tempfile.mkdtemp(prefix="smc_text_", dir=ref.workdir)
+        os.makedirs(os.path.join(wd, "data"))
+        os.symlink(os.path.join(ref.workdir, "tables"), os.path.join(wd, "tables"))
+        os.symlink(EOS_DIR, os.path.join(wd, "EOS"))
+        with open(os.path.join(wd, "parameters.dat"), "w") as f:
+            f.write(parameters_text(vals))
+        subprocess.run([exe, f"operation={op}", "randomSeed=7"] + args, cwd=wd, check=True, capture_output=True)
+        names = ([f"sn_ecc_eccp_{k}.dat" for k in (2, 3, 4, 5, 10)] if op == 9 else
+                 [f"sd_event_{e}_{kind}.dat" for e in (1, 2) for kind in ("block", "4col")])
+        for name in names:
+            with open(os.path.join(wd, "data", name)) as f:
+                texts[name] = f.read()
+    texts["grid"] = {"xmin": -3.0, "ymin": -3.0, "dx": 0.5, "dy": 0.5, "nx": 13, "ny": 13}
+    with open(os.path.join(out, "text_outputs.json"), "w") as f:
+        json.dump(texts, f, indent=0)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--nev", type=int, default=1500)
-    ap.add_argument("--only", choices=["constants", "sampler", "inject", "average", "kln", "native"],
+    ap.add_argument("--only", choices=["constants", "sampler", "inject", "average", "kln", "native", "text"],
                     help="regenerate one fixture only")
     a = ap.parse_args()
     if build_reference(a.ref) is None:
@@ -210,7 +238,8 @@ def main():
     EOS_DIR = os.path.join(a.ref, "EOS")
     steps = {"constants": lambda: make_constants(HERE), "sampler": lambda: make_sampler(HERE),
              "inject": lambda: make_inject(HERE), "average": lambda: make_average(HERE),
-             "kln": lambda: make_kln(HERE), "native": lambda: make_native_tables(HERE, a.nev)}
+             "kln": lambda: make_kln(HERE), "native": lambda: make_native_tables(HERE, a.nev),
+             "text": lambda: make_text(HERE)}
     for k, f in steps.items():
         if a.only in (None, k):
             f()

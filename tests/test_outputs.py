@@ -1,0 +1,85 @@
+"""Text outputs in the reference's layouts (smc_write_ecc,
+smc_write_density_block, smc_write_density_4col): the values read back from
+files the stock reference binary wrote (tests/golden/text_outputs.json, made by
+tests/golden/make_golden.py --only text) are written again and must give the
+same bytes.  Host code only: no GPU."""
+import io
+import json
+import os
+
+import numpy as np
+import pytest
+
+from supermc_gb300 import _lib
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "text_outputs.json")
+
+
+@pytest.fixture(scope="module")
+def texts():
+    with open(GOLDEN) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return _lib.load()
+
+
+def test_eccentricity_files(lib, texts, tmp_path):
+    ecc = np.ascontiguousarray(np.loadtxt(io.StringIO(texts["sn_ecc_eccp_10.dat"]), ndmin=2))
+    assert ecc.shape[1] == 49
+    pattern = str(tmp_path / "sn_ecc_eccp_%d.dat").encode()
+    # two calls append like the reference's per-event appends
+    first, rest = ecc[:1].copy(), ecc[1:].copy()   # kept alive across the calls
+    _lib.check(lib.smc_write_ecc(_lib.ptr(first), 1, 2, 5, pattern), "smc_write_ecc")
+    _lib.check(lib.smc_write_ecc(_lib.ptr(rest), len(rest), 2, 5, pattern), "smc_write_ecc")
+    for order in (2, 3, 4, 5, 10):
+        name = f"sn_ecc_eccp_{order}.dat"
+        assert (tmp_path / name).read_text() == texts[name], name
+
+
+@pytest.mark.parametrize("event", [1, 2])
+def test_density_block_and_4col(lib, texts, tmp_path, event):
+    g = texts["grid"]
+    block = np.ascontiguousarray(np.loadtxt(io.StringIO(texts[f"sd_event_{event}_block.dat"]), ndmin=2))
+    assert block.shape == (g["nx"], g["ny"])
+    out = str(tmp_path / "block.dat").encode()
+    _lib.check(lib.smc_write_density_block(_lib.ptr(block), g["nx"], g["ny"], out), "smc_write_density_block")
+    assert (tmp_path / "block.dat").read_text() == texts[f"sd_event_{event}_block.dat"]
+
+    four = texts[f"sd_event_{event}_4col.dat"]
+    header, body = four.split("\n", 1)
+    npart = float(header.split()[2])
+    cols = np.loadtxt(io.StringIO(body), ndmin=2)
+    grid = np.ascontiguousarray(cols[:, 3].reshape(g["nx"], g["ny"]))
+    out = str(tmp_path / "4col.dat").encode()
+    _lib.check(lib.smc_write_density_4col(_lib.ptr(grid), g["nx"], g["ny"], g["xmin"], g["ymin"], g["dx"], g["dy"],
+                                          0.0, npart, out), "smc_write_density_4col")
+    assert (tmp_path / "4col.dat").read_text() == four
+
+
+def test_writers_reject_bad_arguments(lib, tmp_path):
+    e = np.zeros((1, 49))
+    assert lib.smc_write_ecc(_lib.ptr(e), 1, 3, 2, str(tmp_path / "x%d").encode()) == 1
+    assert lib.smc_write_density_block(None, 3, 3, str(tmp_path / "b").encode()) != 0
+
+
+@pytest.mark.gpu
+def test_generated_events_round_trip_through_the_writers(tmp_path):
+    """GPU events written in the reference's layouts read back as the same
+    numbers (at the printed precision)."""
+    from supermc_gb300.engine import Engine
+    from supermc_gb300.output import write_density_block, write_ecc
+    eng = Engine({"which_mc_model": 5, "Aproj": 197, "Atarg": 197, "ecm": 200, "ecc_from_order": 2,
+                  "ecc_to_order": 5}, seed=3)
+    out = eng.generate(0, 8, want=("ecc", "rho"))
+    write_ecc(out["ecc"], 2, 5, str(tmp_path / "sn_ecc_eccp_%d.dat"))
+    back = np.loadtxt(tmp_path / "sn_ecc_eccp_10.dat", ndmin=2)
+    np.testing.assert_allclose(back, out["ecc"], rtol=1e-7, atol=1e-12)
+    for order in range(2, 6):
+        per = np.loadtxt(tmp_path / f"sn_ecc_eccp_{order}.dat", ndmin=2)
+        np.testing.assert_allclose(per[:, :5], out["ecc"][:, 5 * (order - 1):5 * order], rtol=1e-7, atol=1e-12)
+    sd = out["rho"][0].astype(np.float64) * eng.values["finalfactor"]
+    write_density_block(sd, str(tmp_path / "sd_event_1_block.dat"))
+    np.testing.assert_allclose(np.loadtxt(tmp_path / "sd_event_1_block.dat"), sd, rtol=1e-11, atol=0)
