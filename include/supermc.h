@@ -183,6 +183,35 @@ smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_
                        const double *xy_targ, const double *b, int from_order, int to_order,
                        int reaction_plane, double *mean, double *mean_rp, int *n_used);
 
+/* Reverse-mode gradients of the MC-Glauber event (no reference counterpart:
+ * the reference computes no derivatives).  For the events of smc_generate
+ * (first_event..) or of smc_inject (xy_proj / xy_targ / b given) the
+ * scalar
+ *   L = sum_e  g_eps[e][0] |eps_2(e)| + g_eps[e][1] |eps_3(e)|
+ *            + sum_cells g_rho[e][ix][iy] rho_e(ix, iy)
+ * (eps_n with r^n weighting about the centre of mass over the hot-spot
+ * region, as in columns 2-3 of the order-n block of smc_outputs.ecc;
+ * rho = getRho) is differentiated with respect to
+ *   grad[0] = dL/d width     (Gaussian nucleon width w, MCnucl::gaussCal)
+ *   grad[1] = dL/d alpha     (WN / binary-collision mixing, MCnucl.cpp:688-779)
+ *   grad[2], grad[3] = 0     (reserved: Woods-Saxon R and a)
+ * with the participants, the collisions, the splat windows, the per-cell
+ * cuts and the hot-spot region held fixed (they are piecewise constant in
+ * w and alpha).  The forward pass is recomputed inside the call.
+ * MC-Glauber (which_mc_model 5) with Gaussian entropy (shape_of_entropy 2),
+ * sub_model 1 or 2.  g_eps / g_rho may be NULL (zero cotangent);
+ * grad_events (may be NULL) receives the per-event gradients [n][4]. */
+typedef struct smc_cotangents {
+  int device;                /* g_eps, g_rho, grad_events and the injected
+                                positions are device pointers             */
+  const double *g_eps;       /* [n][2]                                    */
+  const float *g_rho;        /* [n][nx][ny]                               */
+  double *grad_events;       /* [n][4]                                    */
+} smc_cotangents;
+smc_status smc_adjoint(void *ctx, uint64_t first_event, int n, const double *xy_proj,
+                       const double *xy_targ, const double *b, const smc_cotangents *ct,
+                       double *grad);
+
 /* Counters and kernel timing of a context (no reference counterpart; the
  * reference only times the whole run with clock(), src/main.cpp:40-68).
  * With timing enabled, CUDA events bracket every launch of the two event

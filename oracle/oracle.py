@@ -125,6 +125,8 @@ class Oracle:
         lib.smco_event_rho_binary.argtypes = [ctypes.c_void_p]
         lib.smco_event_eccentricities.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                   ctypes.c_double, _D]
+        lib.smco_event_hotspot_mask.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        lib.smco_event_density_frozen.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _D]
         lib.smco_event_cm_angle.argtypes = [ctypes.c_void_p, ctypes.c_int, _D, _D, _D]
         lib.smco_event_rotate_resplat.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.smco_event_recenter_resplat.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -229,6 +231,18 @@ class OracleEvent:
         out = np.zeros(49)
         self.lib.smco_event_eccentricities(self.h, from_order, to_order, b, _ptr(out))
         return out
+
+    def hotspot_mask(self):
+        m = np.zeros((self.nx, self.ny), dtype=np.uint8)
+        self.lib.smco_event_hotspot_mask(self.h, m.ctypes.data)
+        return m.astype(bool)
+
+    def density_frozen(self, w, alpha):
+        g = np.zeros((self.nx, self.ny))
+        rc = self.lib.smco_event_density_frozen(self.h, w, alpha, _ptr(g))
+        if rc:
+            raise RuntimeError(f"smco_event_density_frozen: {rc}")
+        return g
 
     def cm_angle(self, n):
         x, y, a = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

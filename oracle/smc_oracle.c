@@ -890,6 +890,59 @@ int smco_event_density(smco_event *e) {
   return 0;
 }
 
+/* The MC-Glauber density (Gaussian entropy) of the event with its structure
+ * held fixed: the participant and collision windows, the per-cell cuts
+ * (r <= 5 w0, dc <= 25 w0^2) and the boxes are those of the width w0 =
+ * e->p.width the event was built with; the Gaussians, the peak height
+ * 1/(2 pi w^2) and the mixing weights take (w, alpha).  At w = w0 and alpha
+ * = e->p.alpha this is smco_event_density.  The function the adjoint's
+ * gradients are checked against by finite differences. */
+int smco_event_density_frozen(smco_event *e, double w, double alpha, double *rho) {
+  size_t g = (size_t)e->p.nx * e->p.ny;
+  if (e->p.which_mc_model != 5 || e->p.shape_of_entropy == 1) return 5;
+  double Xmin = -e->p.xmax, Ymin = -e->p.ymax, dx = e->p.dx, dy = e->p.dy;
+  double w0 = e->p.width;
+  double d_max = e->p.shape_of_nucleons == 1 ? 2. * sqrt(e->p.dsq) : 5. * w0;
+  memset(rho, 0, sizeof(double) * g);
+  if (e->p.sub_model == 1) {
+    double pre = (1.0 - alpha) / 2.;
+    for (int nw = 0; nw < 2; nw++)
+      for (int k = 0; k < e->npart[nw]; k++) {
+        const nucleon_t *q = &e->nuc[nw][e->part[nw][k]];
+        double x = q->x, y = q->y;
+        int xl = (int)((q->box.xl - Xmin) / dx), xr = (int)((q->box.xr - Xmin) / dx);
+        int yl = (int)((q->box.yl - Ymin) / dy), yr = (int)((q->box.yr - Ymin) / dy);
+        if (xl < 0) xl = 0;
+        if (xr > e->p.nx) xr = e->p.nx;
+        if (yl < 0) yl = 0;
+        if (yr > e->p.ny) yr = e->p.ny;
+        for (int ir = xl; ir < xr; ir++)
+          for (int jr = yl; jr < yr; jr++) {
+            double xg = Xmin + ir * dx, yg = Ymin + jr * dy;
+            double r = sqrt((xg - x) * (xg - x) + (yg - y) * (yg - y));
+            if (r > 5 * w0) continue;
+            G(rho, ir, jr) += pre * peak_height(w) * exp(-r * r / (2 * w * w));
+          }
+      }
+  } else if (e->p.sub_model != 2) {
+    return 5;
+  }
+  for (int c = 0; c < e->ncoll; c++) {
+    double x = e->cx[c], y = e->cy[c];
+    double fw = alpha + (1. - alpha) * e->caw[c];
+    int xl, xr, yl, yr;
+    window(e, x - d_max, x + d_max, Xmin, dx, e->p.nx, &xl, &xr);
+    window(e, y - d_max, y + d_max, Ymin, dy, e->p.ny, &yl, &yr);
+    for (int ir = xl; ir < xr; ir++)
+      for (int jr = yl; jr < yr; jr++) {
+        double xg = Xmin + ir * dx, yg = Ymin + jr * dy;
+        double dc = (x - xg) * (x - xg) + (y - yg) * (y - yg);
+        if (dc <= 25. * w0 * w0) G(rho, ir, jr) += peak_height(w) * exp(-dc / (2 * w * w)) * fw;
+      }
+  }
+  return 0;
+}
+
 /* MCnucl::calculate_rho_binary (MCnucl.cpp:481-531), Gaussian shapes */
 void smco_event_rho_binary(smco_event *e) {
   double Xmin = -e->p.xmax, Ymin = -e->p.ymax, dx = e->p.dx, dy = e->p.dy;
@@ -920,6 +973,54 @@ void smco_event_rho_binary(smco_event *e) {
 void smco_event_grid(const smco_event *e, int which, double *out) {
   const double *src = which == 0 ? e->TA : which == 1 ? e->TB : which == 2 ? e->rho : e->rhob;
   memcpy(out, src, sizeof(double) * e->p.nx * e->p.ny);
+}
+
+/* The hot-spot region of dumpEccentricities: MCnucl::getHotSpots
+ * (MCnucl.cpp:1303-1323) -- participant boxes of both nuclei, then the
+ * collision boxes -- marked on the lattice of their union
+ * (MakeDensity.cpp:2341-2359).  Returns the [nX][nY] flags (caller frees)
+ * and the lattice's offset on the grid. */
+static unsigned char *hotspot_region(const smco_event *e, int *nX, int *nY, int *ioff_out, int *joff_out) {
+  double Xmin = -e->p.xmax, Ymin = -e->p.ymax, dx = e->p.dx, dy = e->p.dy;
+  int nh = e->npart[0] + e->npart[1] + e->ncoll;
+  box_t *hs = (box_t *)malloc(sizeof(box_t) * (nh > 0 ? nh : 1));
+  int k = 0;
+  for (int w = 0; w < 2; w++)
+    for (int i = 0; i < e->npart[w]; i++) hs[k++] = e->nuc[w][e->part[w][i]].box;
+  for (int c = 0; c < e->ncoll; c++) hs[k++] = e->cbox[c];
+  box_t region = hs[0];
+  for (int i = 1; i < nh; i++) box_over_union(&region, &hs[i]);
+  int nYpoints = (int)((region.yr - region.yl) / dy);
+  int nXpoints = (int)((region.xr - region.xl) / dx);
+  unsigned char *imp = (unsigned char *)calloc((size_t)(nXpoints > 0 ? nXpoints : 1) *
+                                                   (nYpoints > 0 ? nYpoints : 1), 1);
+  for (int i = 0; i < nh; i++) {
+    int x0 = (int)((hs[i].xl - region.xl) / dx), x1 = (int)((hs[i].xr - region.xl) / dx);
+    int y0 = (int)((hs[i].yl - region.yl) / dy), y1 = (int)((hs[i].yr - region.yl) / dx);
+    for (int xi = x0; xi < x1; xi++)
+      for (int yi = y0; yi < y1; yi++)
+        if (xi >= 0 && xi < nXpoints && yi >= 0 && yi < nYpoints)
+          imp[(size_t)xi * nYpoints + yi] = 1;
+  }
+  *nX = nXpoints;
+  *nY = nYpoints;
+  *ioff_out = (int)((region.xl - Xmin) / dx);
+  *joff_out = (int)((region.yl - Ymin) / dy);
+  free(hs);
+  return imp;
+}
+
+void smco_event_hotspot_mask(const smco_event *e, unsigned char *mask) {
+  int nX, nY, ioff, joff;
+  unsigned char *imp = hotspot_region(e, &nX, &nY, &ioff, &joff);
+  memset(mask, 0, (size_t)e->p.nx * e->p.ny);
+  for (int iR = 0; iR < nX; iR++)
+    for (int jR = 0; jR < nY; jR++) {
+      int i = iR + ioff, j = jR + joff;
+      if (imp[(size_t)iR * nY + jR] && i >= 0 && i < e->p.nx && j >= 0 && j < e->p.ny)
+        mask[(size_t)i * e->p.ny + j] = 1;
+    }
+  free(imp);
 }
 
 /* ================================================================== */
@@ -958,29 +1059,8 @@ void smco_event_eccentricities(smco_event *e, int from_order, int to_order, doub
   }
   for (int io = 0; io < max_order; io++) rn[io] /= density_norm;
 
-  /* MCnucl::getHotSpots (MCnucl.cpp:1303-1323): participant boxes of both
-   * nuclei, then the collision boxes */
-  int nh = e->npart[0] + e->npart[1] + e->ncoll;
-  box_t *hs = (box_t *)malloc(sizeof(box_t) * (nh > 0 ? nh : 1));
-  int k = 0;
-  for (int w = 0; w < 2; w++)
-    for (int i = 0; i < e->npart[w]; i++) hs[k++] = e->nuc[w][e->part[w][i]].box;
-  for (int c = 0; c < e->ncoll; c++) hs[k++] = e->cbox[c];
-  box_t region = hs[0];
-  for (int i = 1; i < nh; i++) box_over_union(&region, &hs[i]);
-  int nYpoints = (int)((region.yr - region.yl) / dy);
-  int nXpoints = (int)((region.xr - region.xl) / dx);
-  unsigned char *imp = (unsigned char *)calloc((size_t)(nXpoints > 0 ? nXpoints : 1) *
-                                                   (nYpoints > 0 ? nYpoints : 1), 1);
-  for (int i = 0; i < nh; i++) {
-    int x0 = (int)((hs[i].xl - region.xl) / dx), x1 = (int)((hs[i].xr - region.xl) / dx);
-    int y0 = (int)((hs[i].yl - region.yl) / dy), y1 = (int)((hs[i].yr - region.yl) / dx);
-    for (int xi = x0; xi < x1; xi++)
-      for (int yi = y0; yi < y1; yi++)
-        if (xi >= 0 && xi < nXpoints && yi >= 0 && yi < nYpoints)
-          imp[(size_t)xi * nYpoints + yi] = 1;
-  }
-  int ioff = (int)((region.xl - Xmin) / dx), joff = (int)((region.yl - Ymin) / dy);
+  int nXpoints, nYpoints, ioff, joff;
+  unsigned char *imp = hotspot_region(e, &nXpoints, &nYpoints, &ioff, &joff);
   for (int order = from_order; order <= to_order; order++) {
     for (int iR = 0; iR < nXpoints; iR++)
       for (int jR = 0; jR < nYpoints; jR++) {
@@ -1022,7 +1102,6 @@ void smco_event_eccentricities(smco_event *e, int from_order, int to_order, doub
   out[47] = total * dx * dy;
   out[48] = b;
   free(imp);
-  free(hs);
   free(dens);
 }
 

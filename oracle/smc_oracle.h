@@ -115,6 +115,11 @@ void smco_event_rho_binary(smco_event *e);
  * r^n-weighted, <r^n>), then Npart, Ncoll, integral*dx*dy, b. */
 void smco_event_eccentricities(smco_event *e, int from_order, int to_order, double b,
                                double *out);
+/* the hot-spot region of the eccentricities as [nx][ny] flags */
+void smco_event_hotspot_mask(const smco_event *e, unsigned char *mask);
+/* model-5 density with windows, cuts and boxes of the event's own width and
+ * the Gaussians and weights of (w, alpha); 0 or 5 (unsupported model) */
+int smco_event_density_frozen(smco_event *e, double w, double alpha, double *rho);
 /* GlueDensity::calcCMAngle (GlueDensity.cpp:87-144) on rho */
 void smco_event_cm_angle(const smco_event *e, int n, double *xcm, double *ycm, double *angle);
 /* MCnucl::rotateGrid (MCnucl.cpp:1152-1174) + calculateThickness +

@@ -26,7 +26,8 @@ EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "sm
            "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_mixed", "smc_generate_plain",
            "smc_set_timing",
            "smc_set_grid_path", "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_write_ecc",
-           "smc_write_density_block", "smc_write_density_4col", "smc_inject_noalloc", "smc_average"]
+           "smc_write_density_block", "smc_write_density_4col", "smc_inject_noalloc", "smc_average",
+           "smc_adjoint"]
 
 
 class SmcError(RuntimeError):
@@ -84,6 +85,11 @@ class SmcOutputs(ctypes.Structure):
     ]
 
 
+class SmcCotangents(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("g_eps", ctypes.c_void_p), ("g_rho", ctypes.c_void_p),
+                ("grad_events", ctypes.c_void_p)]
+
+
 _lib = None
 
 
@@ -121,6 +127,7 @@ def load() -> ctypes.CDLL:
     lib.smc_average.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_int, vp, vp, ctypes.POINTER(ctypes.c_int)]
     lib.smc_inject_noalloc.argtypes = [ctypes.POINTER(SmcParams), ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]
+    lib.smc_adjoint.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.POINTER(SmcCotangents), vp]
     _lib = lib
     return lib
 

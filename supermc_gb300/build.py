@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libsupermc_gb300.so")
-SOURCES = ["smc_capi.cu", "k_sample_pair.cu", "k_grid.cu", "k_kln.cu", "k_average.cu", "smc_noalloc.cu", "k_grid_tc.cu", "smc_output.cpp"]
+SOURCES = ["smc_capi.cu", "k_sample_pair.cu", "k_grid.cu", "k_kln.cu", "k_average.cu", "smc_noalloc.cu", "k_grid_tc.cu", "k_adjoint.cu", "smc_output.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]

@@ -206,13 +206,15 @@ __device__ __forceinline__ void cut_interval(const DevParams &P, const double *s
   jb = b;
 }
 
-template <int LO, int HI, int NT>
-__device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, const Source *S, const float *rho, uint32_t *mask,
-                        const float *xo, const float *yo, float2 *red, double tot0, double *ecc_out) {
-  const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+// The hot-spot region of dumpEccentricities as a bit mask over the grid
+// (one bit per cell, rows of ceil(ny/32) words): the union of the
+// participant boxes on the reference's lattice (ranges mx0..my1 of the
+// participant sources, src/MakeDensity.cpp:2341-2359).
+template <int NT>
+__device__ __forceinline__ void hotspot_mask(const DevParams &P, const EventRec &rec, const Source *S, uint32_t *mask) {
+  const int tid = threadIdx.x;
   const int nx = P.nx, ny = P.ny;
   const int nw = (ny + 31) / 32;
-  // ---- eccentricity mask from the participant boxes
   for (int k = tid; k < nx * nw; k += NT) mask[k] = 0;
   __syncthreads();
   for (int s = tid; s < rec.nsrc; s += NT) {
@@ -231,6 +233,16 @@ __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, co
       }
   }
   __syncthreads();
+}
+
+template <int LO, int HI, int NT>
+__device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, const Source *S, const float *rho, uint32_t *mask,
+                        const float *xo, const float *yo, float2 *red, double tot0, double *ecc_out) {
+  const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+  const int ny = P.ny;
+  const int nw = (ny + 31) / 32;
+  // ---- eccentricity mask from the participant boxes
+  hotspot_mask<NT>(P, rec, S, mask);
 
   constexpr int NO = HI - LO + 1;
   float a_rn[10];

@@ -168,6 +168,11 @@ struct Ctx {
   DevBuf<uint8_t> wounded;
   DevBuf<double> kln64;
   DevBuf<float> kln32;
+  // adjoint: forward densities, per-CTA adjoint grids, staged cotangents,
+  // per-event gradients
+  DevBuf<float> adj_rho, adj_lam, adj_grho;
+  DevBuf<double> adj_geps, adj_out;
+  std::vector<double> h_adj;
   DevBuf<smc::AvgSrc> avg_state;
   DevBuf<float> avg_rho;
   DevBuf<double> avg_acc;
@@ -429,6 +434,28 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
   return status_error(worst);
 }
 
+// Injected positions of events [off, off + m) staged on the device (NULLs
+// when not injecting).
+smc_status stage_injection(Ctx *c, int off, int m, const double *inj_p, const double *inj_t, const double *inj_b,
+                           bool device, const double **ip, const double **it, const double **ib) {
+  *ip = *it = *ib = nullptr;
+  if (!inj_p) return SMC_OK;
+  size_t np = (size_t)m * 2 * c->info.A, nt = (size_t)m * 2 * c->info.B;
+  CK(c->inj_p.ensure(np));
+  CK(c->inj_t.ensure(nt));
+  cudaMemcpyKind kind = device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  CK(cudaMemcpyAsync(c->inj_p.p, inj_p + (size_t)off * 2 * c->info.A, sizeof(double) * np, kind, c->st));
+  CK(cudaMemcpyAsync(c->inj_t.p, inj_t + (size_t)off * 2 * c->info.B, sizeof(double) * nt, kind, c->st));
+  *ip = c->inj_p.p;
+  *it = c->inj_t.p;
+  if (inj_b) {
+    CK(c->inj_b.ensure(m));
+    CK(cudaMemcpyAsync(c->inj_b.p, inj_b + off, sizeof(double) * m, kind, c->st));
+    *ib = c->inj_b.p;
+  }
+  return SMC_OK;
+}
+
 smc_status run(Ctx *c, uint64_t first_event, int n, const smc_outputs *out, const double *inj_p,
                const double *inj_t, const double *inj_b, bool plain) {
   if (n < 0 || !out) return SMC_ERR_ARGUMENT;
@@ -440,22 +467,8 @@ smc_status run(Ctx *c, uint64_t first_event, int n, const smc_outputs *out, cons
     smc_status s = ensure_buffers(c, m, out);
     if (s) return s;
     const double *ip = nullptr, *it = nullptr, *ib = nullptr;
-    if (inj_p) {
-      // injected positions are staged on the device
-      size_t np = (size_t)m * 2 * c->info.A, nt = (size_t)m * 2 * c->info.B;
-      CK(c->inj_p.ensure(np));
-      CK(c->inj_t.ensure(nt));
-      cudaMemcpyKind kind = out->device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-      CK(cudaMemcpyAsync(c->inj_p.p, inj_p + (size_t)off * 2 * c->info.A, sizeof(double) * np, kind, c->st));
-      CK(cudaMemcpyAsync(c->inj_t.p, inj_t + (size_t)off * 2 * c->info.B, sizeof(double) * nt, kind, c->st));
-      ip = c->inj_p.p;
-      it = c->inj_t.p;
-      if (inj_b) {
-        CK(c->inj_b.ensure(m));
-        CK(cudaMemcpyAsync(c->inj_b.p, inj_b + off, sizeof(double) * m, kind, c->st));
-        ib = c->inj_b.p;
-      }
-    }
+    s = stage_injection(c, off, m, inj_p, inj_t, inj_b, out->device != 0, &ip, &it, &ib);
+    if (s) return s;
     s = run_chunk(c, first_event + off, off, m, out, ip, it, ib, plain);
     if (s && s != SMC_ERR_ZERO_DNDY) return s;
     if (s) worst = s;
@@ -567,6 +580,7 @@ void smc_destroy(void *ctx) {
   c->attempts.release(); c->wounded.release(); c->rho_ev.release(); c->corr_ev.release(); c->cm_ev.release();
   c->mix_sys.release(); c->mix_ev.release(); c->mix_order.release(); c->kln64.release(); c->kln32.release();
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
+  c->adj_rho.release(); c->adj_lam.release(); c->adj_grho.release(); c->adj_geps.release(); c->adj_out.release();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -700,6 +714,82 @@ smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_
   smc_status s = set_thickness_flags(c, out);
   if (s) return s;
   return run(c, 0, n, out, xy_proj, xy_targ, b, false);
+}
+
+smc_status smc_adjoint(void *ctx, uint64_t first_event, int n, const double *xy_proj, const double *xy_targ,
+                       const double *b, const smc_cotangents *ct, double *grad) {
+  if (!ctx || !ct || !grad || n < 0 || (xy_proj && !xy_targ)) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  for (int k = 0; k < 4; k++) grad[k] = 0.0;
+  const smc_params &p = c->prm;
+  if (p.which_mc_model != 5 || p.shape_of_entropy == 1 || (p.sub_model != 1 && p.sub_model != 2))
+    return SMC_ERR_CONFIG;
+  if (n == 0) return SMC_OK;
+  CK(cudaSetDevice(c->device));
+  smc_outputs none{};
+  smc_status s = set_thickness_flags(c, &none);
+  if (s) return s;
+  const DevParams &P = c->P;
+  const size_t g = (size_t)P.nx * P.ny;
+  const bool dev = ct->device != 0;
+  const int nb = smc::adjoint_blocks_per_sm(P);
+  smc_status worst = SMC_OK;
+  for (int off = 0; off < n; off += c->chunk) {
+    const int m = std::min(c->chunk, n - off);
+    const int grid = std::max(1, std::min(m, c->sms * nb));
+    CK(c->adj_rho.ensure((size_t)m * g));
+    CK(c->adj_lam.ensure((size_t)grid * g));
+    CK(c->adj_out.ensure((size_t)m * 4));
+    smc_outputs o{};
+    o.device = 1;
+    o.rho = c->adj_rho.p;
+    s = ensure_buffers(c, m, &o);
+    if (s) return s;
+    const double *ip, *it, *ib;
+    s = stage_injection(c, off, m, xy_proj, xy_targ, b, dev, &ip, &it, &ib);
+    if (s) return s;
+    // forward pass of the chunk (the densities are recomputed, not kept
+    // between the forward call and this one)
+    s = run_chunk(c, first_event + off, 0, m, &o, ip, it, ib, false);
+    if (s && s != SMC_ERR_ZERO_DNDY) return s;
+    if (s) worst = s;
+    const double *geps = nullptr;
+    const float *grho = nullptr;
+    if (ct->g_eps) {
+      if (dev) {
+        geps = ct->g_eps + (size_t)off * 2;
+      } else {
+        CK(c->adj_geps.ensure((size_t)m * 2));
+        CK(cudaMemcpyAsync(c->adj_geps.p, ct->g_eps + (size_t)off * 2, sizeof(double) * m * 2,
+                           cudaMemcpyHostToDevice, c->st));
+        geps = c->adj_geps.p;
+      }
+    }
+    if (ct->g_rho) {
+      if (dev) {
+        grho = ct->g_rho + (size_t)off * g;
+      } else {
+        CK(c->adj_grho.ensure((size_t)m * g));
+        CK(cudaMemcpyAsync(c->adj_grho.p, ct->g_rho + (size_t)off * g, sizeof(float) * m * g,
+                           cudaMemcpyHostToDevice, c->st));
+        grho = c->adj_grho.p;
+      }
+    }
+    CK(timed(c, 1, [&] {
+      return smc::launch_adjoint(P, m, c->recs.p, c->srcs.p, c->adj_rho.p, grho, geps, c->adj_lam.p, c->adj_out.p,
+                                 grid, c->st);
+    }));
+    c->h_adj.resize((size_t)m * 4);
+    CK(cudaMemcpyAsync(c->h_adj.data(), c->adj_out.p, sizeof(double) * m * 4, cudaMemcpyDeviceToHost, c->st));
+    if (ct->grad_events)
+      CK(cudaMemcpyAsync(ct->grad_events + (size_t)off * 4, c->adj_out.p, sizeof(double) * m * 4,
+                         dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    collect_timing(c);
+    for (int e = 0; e < m; e++)
+      for (int k = 0; k < 4; k++) grad[k] += c->h_adj[(size_t)e * 4 + k];
+  }
+  return worst;
 }
 
 smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_proj, const double *xy_targ,

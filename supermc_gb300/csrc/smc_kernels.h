@@ -41,6 +41,16 @@ cudaError_t launch_avg_init(const DevParams &P, int n, const EventRec *recs, con
 cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Source *srcs, AvgSrc *state,
                                  const float *rho, int order, int mode, int grid, cudaStream_t st);
 cudaError_t launch_avg_accum(const float *rho, int n, size_t cells, double *acc, cudaStream_t st);
+// Adjoint of a batch (k_adjoint, one CTA per event in turn): per-event
+// gradients dtheta [n][4] = (dL/dw, dL/dalpha, 0, 0) of
+// L = sum_e g_eps[e][0] |eps_2| + g_eps[e][1] |eps_3| + <g_rho[e], rho_e>
+// from the forward densities rho_ev [n][nx][ny]; g_eps, g_rho may be NULL;
+// lam_scratch [grid][nx][ny] floats.
+size_t adjoint_smem(const DevParams &P);
+int adjoint_blocks_per_sm(const DevParams &P);
+cudaError_t launch_adjoint(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs,
+                           const float *rho_ev, const float *g_grid, const double *g_eps, float *lam_scratch,
+                           double *dtheta, int grid, cudaStream_t st);
 cudaError_t launch_kln_table(const KlnDev &K, int tmax, double dT, double *table64, float *table32,
                              cudaStream_t st);
 

@@ -185,6 +185,28 @@ class Engine:
         self.last_average_events = used.value
         return mean, mean_rp
 
+    def adjoint(self, first_event: int, n: int, g_eps=None, g_rho=None, xy_proj=None, xy_targ=None, b=None):
+        """Gradients of L = sum_e g_eps[e,0] |eps_2| + g_eps[e,1] |eps_3| +
+        sum g_rho[e] * rho_e with respect to (width, alpha, R, a) for the
+        events first_event.. (or the injected positions), the structure of
+        each event (participants, windows, cuts, hot-spot region) held
+        fixed.  g_eps [n,2] and g_rho [n,nx,ny] are host arrays or None.
+        Returns (grad [4], per-event grad [n,4])."""
+        ge = None if g_eps is None else np.ascontiguousarray(g_eps, dtype=np.float64).reshape(n, 2)
+        gr = None if g_rho is None else np.ascontiguousarray(g_rho, dtype=np.float32).reshape(n, self.nx, self.ny)
+        xp = xt = bb = None
+        if xy_proj is not None:
+            xp = np.ascontiguousarray(xy_proj, dtype=np.float64).reshape(n, self.A, 2)
+            xt = np.ascontiguousarray(xy_targ, dtype=np.float64).reshape(n, self.B, 2)
+            if b is not None:
+                bb = np.ascontiguousarray(np.broadcast_to(b, (n,)), dtype=np.float64)
+        per = np.zeros((n, 4))
+        grad = np.zeros(4)
+        ct = _lib.SmcCotangents(0, _lib.ptr(ge), _lib.ptr(gr), _lib.ptr(per))
+        _lib.check(self.lib.smc_adjoint(self.h, first_event, n, _lib.ptr(xp), _lib.ptr(xt), _lib.ptr(bb),
+                                        ctypes.byref(ct), _lib.ptr(grad)), "smc_adjoint")
+        return grad, per
+
     def kln_table(self) -> np.ndarray:
         t = self.info.kln_tmax
         out = np.zeros((t, t))
