@@ -78,6 +78,12 @@ typedef struct smc_params {
   int max_attempts;                      /* event retry cap (0: 100000)     */
   int max_collisions;                    /* per-event collision capacity
                                             (0: 4096)                       */
+  int ws_inverse_cdf;                    /* 1: Woods-Saxon radii by inverse
+                                            CDF of the reference's truncated
+                                            density (r <= R + 2.5) instead of
+                                            rejection, so that positions are
+                                            differentiable in R and a
+                                            (smc_adjoint); spherical A > 2 */
 } smc_params;
 
 /* Derived constants (MCnucl::MCnucl, src/MCnucl.cpp:22-154). */
@@ -111,6 +117,9 @@ typedef struct smc_outputs {
   double *positions;    /* [n][A+B][2] nucleon x,y (projectile first, each
                            nucleus sorted by x)                              */
   uint8_t *wounded;     /* [n][A+B] 1 = participant                          */
+  double *tangents;     /* [n][A+B][4] d(x,y)/dR, d(x,y)/da of each nucleon
+                           (same order as positions; both nuclei's R, a
+                           move together; zero unless ws_inverse_cdf)        */
 } smc_outputs;
 
 /* MCnucl::MCnucl + MakeDensity::MakeDensity: validates the configuration,
@@ -194,22 +203,29 @@ smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_
  * rho = getRho) is differentiated with respect to
  *   grad[0] = dL/d width     (Gaussian nucleon width w, MCnucl::gaussCal)
  *   grad[1] = dL/d alpha     (WN / binary-collision mixing, MCnucl.cpp:688-779)
- *   grad[2], grad[3] = 0     (reserved: Woods-Saxon R and a)
+ *   grad[2] = dL/dR, grad[3] = dL/da  (Woods-Saxon radius and
+ *            diffuseness, both nuclei together: through the nucleon
+ *            positions of ws_inverse_cdf sampling, or of injected events
+ *            through the given position tangents; else 0)
  * with the participants, the collisions, the splat windows, the per-cell
- * cuts and the hot-spot region held fixed (they are piecewise constant in
- * w and alpha).  The forward pass is recomputed inside the call.
+ * cuts, the hot-spot region and the hard-core decisions held fixed (they
+ * are piecewise constant in the parameters).  The forward pass is
+ * recomputed inside the call.
  * MC-Glauber (which_mc_model 5) with Gaussian entropy (shape_of_entropy 2),
  * sub_model 1 or 2.  g_eps / g_rho may be NULL (zero cotangent);
  * grad_events (may be NULL) receives the per-event gradients [n][4]. */
-typedef struct smc_cotangents {
-  int device;                /* g_eps, g_rho, grad_events and the injected
-                                positions are device pointers             */
-  const double *g_eps;       /* [n][2]                                    */
-  const float *g_rho;        /* [n][nx][ny]                               */
-  double *grad_events;       /* [n][4]                                    */
-} smc_cotangents;
+typedef struct smc_adjoint_args {
+  int device;                /* every pointer here and the injected
+                                positions are device pointers              */
+  const double *g_eps;       /* [n][2]                                     */
+  const float *g_rho;        /* [n][nx][ny]                                */
+  const double *tangent_proj;/* injected events: [n][A][4] and [n][B][4]    */
+  const double *tangent_targ;/* position tangents d(x,y)/dR, d(x,y)/da of
+                                each nucleon, or NULL                      */
+  double *grad_events;       /* [n][4]                                     */
+} smc_adjoint_args;
 smc_status smc_adjoint(void *ctx, uint64_t first_event, int n, const double *xy_proj,
-                       const double *xy_targ, const double *b, const smc_cotangents *ct,
+                       const double *xy_targ, const double *b, const smc_adjoint_args *args,
                        double *grad);
 
 /* Counters and kernel timing of a context (no reference counterpart; the

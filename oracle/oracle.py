@@ -76,6 +76,7 @@ class Nucleus(ctypes.Structure):
         ("R", ctypes.c_double), ("a", ctypes.c_double),
         ("beta2", ctypes.c_double), ("beta4", ctypes.c_double),
         ("d_min", ctypes.c_double), ("rmax_cut", ctypes.c_double), ("rw_max", ctypes.c_double),
+        ("icdf", ctypes.c_int),
     ]
 
 
@@ -127,6 +128,17 @@ class Oracle:
                                                   ctypes.c_double, _D]
         lib.smco_event_hotspot_mask.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         lib.smco_event_density_frozen.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _D]
+        lib.smco_event_density_moved.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                                 ctypes.c_void_p, ctypes.c_void_p, _D]
+        lib.smco_ws_icdf.restype = ctypes.c_double
+        lib.smco_ws_icdf.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        lib.smco_event_icdf_displacement.argtypes = [ctypes.c_void_p, ctypes.POINTER(Nucleus),
+                                                     ctypes.POINTER(Nucleus), ctypes.c_double, ctypes.c_double,
+                                                     _D, _D]
+        lib.smco_event_icdf_tangents.argtypes = [ctypes.c_void_p, ctypes.POINTER(Nucleus),
+                                                 ctypes.POINTER(Nucleus), _D, _D]
+        lib.smco_event_nucleon_ids.argtypes = [ctypes.c_void_p, ctypes.c_int, _I, ctypes.c_int]
         lib.smco_event_cm_angle.argtypes = [ctypes.c_void_p, ctypes.c_int, _D, _D, _D]
         lib.smco_event_rotate_resplat.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.smco_event_recenter_resplat.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -145,10 +157,17 @@ class Oracle:
                                            ctypes.c_int, ctypes.c_uint64, _D]
 
     # ---- helpers ---------------------------------------------------------
-    def nucleus(self, A, deformed=0, R=0.0, a=0.0, dmin=0.0) -> Nucleus:
+    def nucleus(self, A, deformed=0, R=0.0, a=0.0, dmin=0.0, icdf=0) -> Nucleus:
         n = Nucleus()
         self.lib.smco_nucleus_init(ctypes.byref(n), A, deformed, R, a, dmin)
+        n.icdf = icdf
         return n
+
+    def ws_icdf(self, R, a, u):
+        """(r, dr/dR, dr/da) of the inverse-CDF Woods-Saxon radius."""
+        dR, da = ctypes.c_double(), ctypes.c_double()
+        r = self.lib.smco_ws_icdf(R, a, u, ctypes.byref(dR), ctypes.byref(da))
+        return r, dR.value, da.value
 
     def uniform2(self, seed, event, stream, slot):
         u = np.zeros(2)
@@ -236,6 +255,36 @@ class OracleEvent:
         m = np.zeros((self.nx, self.ny), dtype=np.uint8)
         self.lib.smco_event_hotspot_mask(self.h, m.ctypes.data)
         return m.astype(bool)
+
+    def density_moved(self, w, alpha, dA=None, dB=None):
+        g = np.zeros((self.nx, self.ny))
+        a = None if dA is None else np.ascontiguousarray(dA, dtype=np.float64)
+        b = None if dB is None else np.ascontiguousarray(dB, dtype=np.float64)
+        rc = self.lib.smco_event_density_moved(self.h, w, alpha, None if a is None else a.ctypes.data,
+                                               None if b is None else b.ctypes.data, _ptr(g))
+        if rc:
+            raise RuntimeError(f"smco_event_density_moved: {rc}")
+        return g
+
+    def icdf_displacement(self, nA, nB, dR, da):
+        """Nucleon displacements by id ([A,2], [B,2]) for (R, a) += (dR, da)."""
+        A, B = len(self.nucleons(0)), len(self.nucleons(1))
+        dA, dB = np.zeros((A, 2)), np.zeros((B, 2))
+        self.lib.smco_event_icdf_displacement(self.h, ctypes.byref(nA), ctypes.byref(nB), dR, da, _ptr(dA),
+                                              _ptr(dB))
+        return dA, dB
+
+    def icdf_tangents(self, nA, nB):
+        """(dx/dR, dy/dR, dx/da, dy/da) per nucleon by id ([A,4], [B,4])."""
+        A, B = len(self.nucleons(0)), len(self.nucleons(1))
+        tA, tB = np.zeros((A, 4)), np.zeros((B, 4))
+        self.lib.smco_event_icdf_tangents(self.h, ctypes.byref(nA), ctypes.byref(nB), _ptr(tA), _ptr(tB))
+        return tA, tB
+
+    def nucleon_ids(self, which):
+        out = np.zeros(400, dtype=np.int32)
+        n = self.lib.smco_event_nucleon_ids(self.h, which, _ptr(out, _I), 400)
+        return out[:n].copy()
 
     def density_frozen(self, w, alpha):
         g = np.zeros((self.nx, self.ny))

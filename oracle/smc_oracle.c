@@ -252,6 +252,10 @@ static void box_over_union(box_t *b, const box_t *o) {
 typedef struct {
   double x, y, z;
   box_t box, base; /* Particle::boundingBox / baseBox (Particle.h:25-26) */
+  int id;          /* index before sorting: injection / acceptance order     */
+  double nfx, nfy, nfz, u0; /* inverse-CDF sampling: nucleus-frame position
+                               before the centre-of-mass shift and the radial
+                               uniform (u0 < 0 otherwise)                   */
   int *hits;       /* who_hit_me: indices into the other nucleus, in order */
   int nhits, caphits;
 } nucleon_t;
@@ -264,6 +268,7 @@ struct smco_event {
   int *part[2]; /* wounded list (first-hit order), indices into nuc */
   int ncoll, capc;
   double *cx, *cy, *caw;
+  int *cpa, *cpb;  /* nucleon indices (sorted arrays) of each collision */
   box_t *cbox; /* CollisionPair::boundingBox, default all zero */
   double *TA, *TB, *rho, *rhob;
   double dndy;
@@ -293,7 +298,7 @@ void smco_event_free(smco_event *e) {
   if (!e) return;
   clear_nucleons(e);
   for (int w = 0; w < 2; w++) { free(e->nuc[w]); free(e->part[w]); }
-  free(e->cx); free(e->cy); free(e->caw); free(e->cbox);
+  free(e->cx); free(e->cy); free(e->caw); free(e->cbox); free(e->cpa); free(e->cpb);
   free(e->TA); free(e->TB); free(e->rho); free(e->rhob);
   free(e);
 }
@@ -321,6 +326,16 @@ static void construct(const smco_event *e, nucleon_t *n, double x, double y, dou
   box_over_union(&n->box, &q);
   n->hits = NULL;
   n->nhits = n->caphits = 0;
+  n->id = 0;
+  n->nfx = n->nfy = n->nfz = 0;
+  n->u0 = -1;
+}
+
+static int cmp_xleft(const void *a, const void *b);
+/* records each nucleon's pre-sort index, then sorts by the box's left edge */
+static void sort_nucleons(smco_event *e, int w, int n) {
+  for (int i = 0; i < n; i++) e->nuc[w][i].id = i;
+  qsort(e->nuc[w], n, sizeof(nucleon_t), cmp_xleft);
 }
 
 /* Particle::calculateBounds after a move (MCnucl.cpp:1161,1167): the box
@@ -349,8 +364,75 @@ void smco_event_inject(smco_event *e, const double *xyA, int A, const double *xy
     reserve(e, w, cnt[w] > 0 ? cnt[w] : 1);
     for (int i = 0; i < cnt[w]; i++) construct(e, &e->nuc[w][i], src[w][2 * i], src[w][2 * i + 1], 0.0);
     e->n[w] = cnt[w];
-    qsort(e->nuc[w], cnt[w], sizeof(nucleon_t), cmp_xleft);
+    sort_nucleons(e, w, cnt[w]);
   }
+}
+
+/* ================================================================== */
+/* Woods-Saxon radius by inverse CDF (differentiable sampling mode; no
+ * reference counterpart -- the reference samples radii by rejection,
+ * Nucleus.cpp:578-621).  The density is the reference's truncated one,
+ * rho(r) = 1/(1+exp((r-R)/a)) on [0, rmax], rmax = R + 2.5, with
+ * N(r) = int_0^r t^2 rho dt and F = N(r)/N(rmax).  r(u) solves F(r) = u;
+ * by the implicit function theorem
+ *   dr/dp = -(N_p(r) - u dN(rmax)/dp) / (r^2 rho(r)),  p = R, a,
+ * with N_p = int_0^r t^2 d rho/dp dt and dN(rmax)/dR including the moving
+ * end point (rmax^2 rho(rmax)).  Quadrature: 8-point Gauss-Legendre on 24
+ * panels (nodes and weights from the standard tables). */
+static const double GL8X[4] = {0.1834346424956498, 0.5255324099163290, 0.7966664774136267, 0.9602898564975363};
+static const double GL8W[4] = {0.3626837833783620, 0.3137066458778873, 0.2223810344533745, 0.1012285362903763};
+
+static void ws_integrand(double R, double a, double t, double *f, double *fR, double *fa) {
+  double rho = 1.0 / (1.0 + exp((t - R) / a));
+  double d = rho * (1.0 - rho) / a;
+  *f = t * t * rho;
+  *fR = t * t * d;
+  *fa = t * t * d * (t - R) / a;
+}
+
+static void ws_N(double R, double a, double r, double *N, double *NR, double *Na) {
+  const int panels = 24;
+  double h = r / panels, s = 0, sR = 0, sa = 0;
+  for (int p = 0; p < panels; p++) {
+    double c = (p + 0.5) * h, hh = 0.5 * h;
+    for (int k = 0; k < 4; k++)
+      for (int sg = -1; sg <= 1; sg += 2) {
+        double f, fR, fa;
+        ws_integrand(R, a, c + sg * hh * GL8X[k], &f, &fR, &fa);
+        s += GL8W[k] * hh * f;
+        sR += GL8W[k] * hh * fR;
+        sa += GL8W[k] * hh * fa;
+      }
+  }
+  *N = s;
+  *NR = sR;
+  *Na = sa;
+}
+
+double smco_ws_icdf(double R, double a, double u, double *drdR, double *drda) {
+  double rmax = R + 2.5;
+  double Nt, NtR, Nta;
+  ws_N(R, a, rmax, &Nt, &NtR, &Nta);
+  double f_end, fR_end, fa_end;
+  ws_integrand(R, a, rmax, &f_end, &fR_end, &fa_end);
+  NtR += f_end; /* d rmax / dR = 1 */
+  double target = u * Nt, lo = 0, hi = rmax;
+  for (int it = 0; it < 64; it++) {
+    double mid = 0.5 * (lo + hi), N, NR, Na;
+    ws_N(R, a, mid, &N, &NR, &Na);
+    if (N < target) lo = mid;
+    else hi = mid;
+  }
+  double r = 0.5 * (lo + hi);
+  if (drdR || drda) {
+    double N, NR, Na, f, fR, fa;
+    ws_N(R, a, r, &N, &NR, &Na);
+    ws_integrand(R, a, r, &f, &fR, &fa);
+    double F = N / Nt;
+    if (drdR) *drdR = f > 0 ? -(NR - F * NtR) / f : 0;
+    if (drda) *drda = f > 0 ? -(Na - F * Nta) / f : 0;
+  }
+  return r;
 }
 
 /* ================================================================== */
@@ -468,7 +550,7 @@ static void populate_drand48(smco_event *e, int w, const smco_nucleus *n, double
       q->z = z;
     }
   }
-  qsort(e->nuc[w], e->n[w], sizeof(nucleon_t), cmp_xleft);
+  sort_nucleons(e, w, e->n[w]);
 }
 
 void smco_event_populate_drand48(smco_event *e, const smco_nucleus *nA, const smco_nucleus *nB,
@@ -495,7 +577,7 @@ static int populate_philox(smco_event *e, int w, const smco_nucleus *n, double x
   int A = n->A;
   reserve(e, w, A);
   e->n[w] = 0;
-  double px[256], py[256], pz[256];
+  double px[256], py[256], pz[256], pu[256];
   if (A > 256) return -1;
   int cnt = 0;
   if (A == 1) {
@@ -519,7 +601,16 @@ static int populate_philox(smco_event *e, int w, const smco_nucleus *n, double x
       smco_uniform2(seed, event, sid, 2 * c, u);
       smco_uniform2(seed, event, sid, 2 * c + 1, u + 2);
       double x, y, z;
-      if (!ws_candidate(n, cx, phi, u, &x, &y, &z)) continue;
+      if (n->icdf && !n->deformed) {
+        /* inverse-CDF radius, the candidate's direction as in ws_candidate */
+        double r = smco_ws_icdf(n->R, n->a, u[0], NULL, NULL);
+        double ct = 1.0 - 2.0 * u[2], st = sqrt(1.0 - ct * ct), ph = 2 * M_PI * u[3];
+        x = r * st * cos(ph);
+        y = r * st * sin(ph);
+        z = r * ct;
+      } else if (!ws_candidate(n, cx, phi, u, &x, &y, &z)) {
+        continue;
+      }
       int conflict = 0;
       for (int i = 0; i < cnt; i++) {
         double r2 = (x - px[i]) * (x - px[i]) + (y - py[i]) * (y - py[i]) + (z - pz[i]) * (z - pz[i]);
@@ -527,6 +618,7 @@ static int populate_philox(smco_event *e, int w, const smco_nucleus *n, double x
       }
       if (conflict) continue;
       px[cnt] = x; py[cnt] = y; pz[cnt] = z;
+      pu[cnt] = (n->icdf && !n->deformed) ? u[0] : -1.0;
       cnt++;
     }
     double xcm = 0, ycm = 0, zcm = 0;
@@ -534,17 +626,18 @@ static int populate_philox(smco_event *e, int w, const smco_nucleus *n, double x
     for (int i = 0; i < cnt; i++) {
       nucleon_t *q = &e->nuc[w][i];
       construct(e, q, px[i], py[i], pz[i]);
+      q->nfx = px[i]; q->nfy = py[i]; q->nfz = pz[i]; q->u0 = pu[i];
       set_x(q, px[i] - xcm / A + xc);
       set_y(q, py[i] - ycm / A + yc);
       q->z = pz[i] - zcm / A;
     }
     e->n[w] = cnt;
-    qsort(e->nuc[w], cnt, sizeof(nucleon_t), cmp_xleft);
+    sort_nucleons(e, w, cnt);
     return 0;
   }
   for (int i = 0; i < cnt; i++) construct(e, &e->nuc[w][i], px[i] + xc, py[i] + yc, pz[i]);
   e->n[w] = cnt;
-  qsort(e->nuc[w], cnt, sizeof(nucleon_t), cmp_xleft);
+  sort_nucleons(e, w, cnt);
   return 0;
 }
 
@@ -641,6 +734,8 @@ int smco_event_pair(smco_event *e) {
     e->cy = (double *)realloc(e->cy, sizeof(double) * nc);
     e->caw = (double *)realloc(e->caw, sizeof(double) * nc);
     e->cbox = (box_t *)realloc(e->cbox, sizeof(box_t) * nc);
+    e->cpa = (int *)realloc(e->cpa, sizeof(int) * nc);
+    e->cpb = (int *)realloc(e->cpb, sizeof(int) * nc);
   }
   e->ncoll = 0;
   for (int k = 0; k < e->npart[0]; k++) {
@@ -648,6 +743,8 @@ int smco_event_pair(smco_event *e) {
     for (int j = 0; j < p->nhits; j++) {
       const nucleon_t *t = &T[p->hits[j]];
       int c = e->ncoll++;
+      e->cpa[c] = e->part[0][k];
+      e->cpb[c] = p->hits[j];
       e->cx[c] = (p->x + t->x) / 2.0;
       e->cy[c] = (p->y + t->y) / 2.0;
       double aw = 0.;
@@ -892,17 +989,22 @@ int smco_event_density(smco_event *e) {
 
 /* The MC-Glauber density (Gaussian entropy) of the event with its structure
  * held fixed: the participant and collision windows, the per-cell cuts
- * (r <= 5 w0, dc <= 25 w0^2) and the boxes are those of the width w0 =
- * e->p.width the event was built with; the Gaussians, the peak height
- * 1/(2 pi w^2) and the mixing weights take (w, alpha).  At w = w0 and alpha
- * = e->p.alpha this is smco_event_density.  The function the adjoint's
- * gradients are checked against by finite differences. */
-int smco_event_density_frozen(smco_event *e, double w, double alpha, double *rho) {
+ * (r <= 5 w0, dc <= 25 w0^2) and the boxes are those of the event as built
+ * (width w0 = e->p.width, the nucleon positions of the event); the
+ * Gaussians, the peak height 1/(2 pi w^2) and the mixing weights take
+ * (w, alpha), and each Gaussian is centred on its source displaced by
+ * dA / dB ([A][2], [B][2] by nucleon id, NULL = none; a collision moves by
+ * the mean of its two nucleons' displacements).  With no displacement, at
+ * w = w0 and alpha = e->p.alpha, this is smco_event_density.  The function
+ * the adjoint's gradients are checked against by finite differences. */
+int smco_event_density_moved(smco_event *e, double w, double alpha, const double *dA, const double *dB,
+                             double *rho) {
   size_t g = (size_t)e->p.nx * e->p.ny;
   if (e->p.which_mc_model != 5 || e->p.shape_of_entropy == 1) return 5;
   double Xmin = -e->p.xmax, Ymin = -e->p.ymax, dx = e->p.dx, dy = e->p.dy;
   double w0 = e->p.width;
   double d_max = e->p.shape_of_nucleons == 1 ? 2. * sqrt(e->p.dsq) : 5. * w0;
+  const double *disp[2] = {dA, dB};
   memset(rho, 0, sizeof(double) * g);
   if (e->p.sub_model == 1) {
     double pre = (1.0 - alpha) / 2.;
@@ -910,6 +1012,8 @@ int smco_event_density_frozen(smco_event *e, double w, double alpha, double *rho
       for (int k = 0; k < e->npart[nw]; k++) {
         const nucleon_t *q = &e->nuc[nw][e->part[nw][k]];
         double x = q->x, y = q->y;
+        double mx = x, my = y;
+        if (disp[nw]) { mx += disp[nw][2 * q->id]; my += disp[nw][2 * q->id + 1]; }
         int xl = (int)((q->box.xl - Xmin) / dx), xr = (int)((q->box.xr - Xmin) / dx);
         int yl = (int)((q->box.yl - Ymin) / dy), yr = (int)((q->box.yr - Ymin) / dy);
         if (xl < 0) xl = 0;
@@ -921,7 +1025,8 @@ int smco_event_density_frozen(smco_event *e, double w, double alpha, double *rho
             double xg = Xmin + ir * dx, yg = Ymin + jr * dy;
             double r = sqrt((xg - x) * (xg - x) + (yg - y) * (yg - y));
             if (r > 5 * w0) continue;
-            G(rho, ir, jr) += pre * peak_height(w) * exp(-r * r / (2 * w * w));
+            double r2 = (xg - mx) * (xg - mx) + (yg - my) * (yg - my);
+            G(rho, ir, jr) += pre * peak_height(w) * exp(-r2 / (2 * w * w));
           }
       }
   } else if (e->p.sub_model != 2) {
@@ -929,6 +1034,10 @@ int smco_event_density_frozen(smco_event *e, double w, double alpha, double *rho
   }
   for (int c = 0; c < e->ncoll; c++) {
     double x = e->cx[c], y = e->cy[c];
+    double mx = x, my = y;
+    const nucleon_t *pa = &e->nuc[0][e->cpa[c]], *pb = &e->nuc[1][e->cpb[c]];
+    if (dA) { mx += 0.5 * dA[2 * pa->id]; my += 0.5 * dA[2 * pa->id + 1]; }
+    if (dB) { mx += 0.5 * dB[2 * pb->id]; my += 0.5 * dB[2 * pb->id + 1]; }
     double fw = alpha + (1. - alpha) * e->caw[c];
     int xl, xr, yl, yr;
     window(e, x - d_max, x + d_max, Xmin, dx, e->p.nx, &xl, &xr);
@@ -937,10 +1046,67 @@ int smco_event_density_frozen(smco_event *e, double w, double alpha, double *rho
       for (int jr = yl; jr < yr; jr++) {
         double xg = Xmin + ir * dx, yg = Ymin + jr * dy;
         double dc = (x - xg) * (x - xg) + (y - yg) * (y - yg);
-        if (dc <= 25. * w0 * w0) G(rho, ir, jr) += peak_height(w) * exp(-dc / (2 * w * w)) * fw;
+        if (dc > 25. * w0 * w0) continue;
+        double dm = (mx - xg) * (mx - xg) + (my - yg) * (my - yg);
+        G(rho, ir, jr) += peak_height(w) * exp(-dm / (2 * w * w)) * fw;
       }
   }
   return 0;
+}
+
+int smco_event_density_frozen(smco_event *e, double w, double alpha, double *rho) {
+  return smco_event_density_moved(e, w, alpha, NULL, NULL, rho);
+}
+
+/* Inverse-CDF-sampled nuclei: the lab-frame displacement of every nucleon
+ * (by id) when (R, a) of both nuclei change by (dR, da) with the radial
+ * uniforms and directions held, the centre-of-mass shift included
+ * (positions = nucleus-frame points minus their mean, Nucleus.cpp:293-309);
+ * and the tangents d(x, y)/dR, d(x, y)/da ([n][4] by id). */
+static void icdf_moves(const smco_event *e, int w, const smco_nucleus *nu, double dR, double da, double *d,
+                       double *tan) {
+  int n = e->n[w];
+  double m[4] = {0, 0, 0, 0};
+  for (int i = 0; i < n; i++) {
+    const nucleon_t *q = &e->nuc[w][i];
+    double v[4] = {0, 0, 0, 0};
+    if (q->u0 >= 0) {
+      double drdR, drda;
+      double r0 = smco_ws_icdf(nu->R, nu->a, q->u0, &drdR, &drda);
+      double s = 0;
+      if (d) s = smco_ws_icdf(nu->R + dR, nu->a + da, q->u0, NULL, NULL) / r0 - 1.0;
+      v[0] = d ? q->nfx * s : q->nfx * drdR / r0;
+      v[1] = d ? q->nfy * s : q->nfy * drdR / r0;
+      v[2] = q->nfx * drda / r0;
+      v[3] = q->nfy * drda / r0;
+    }
+    for (int c = 0; c < 4; c++) m[c] += v[c];
+    if (d) { d[2 * q->id] = v[0]; d[2 * q->id + 1] = v[1]; }
+    if (tan) for (int c = 0; c < 4; c++) tan[4 * q->id + c] = v[c];
+  }
+  for (int i = 0; i < n; i++) {
+    int id = e->nuc[w][i].id;
+    if (d) { d[2 * id] -= m[0] / n; d[2 * id + 1] -= m[1] / n; }
+    if (tan) for (int c = 0; c < 4; c++) tan[4 * id + c] -= m[c] / n;
+  }
+}
+
+void smco_event_icdf_displacement(const smco_event *e, const smco_nucleus *nA, const smco_nucleus *nB, double dR,
+                                  double da, double *dA, double *dB) {
+  icdf_moves(e, 0, nA, dR, da, dA, NULL);
+  icdf_moves(e, 1, nB, dR, da, dB, NULL);
+}
+
+void smco_event_icdf_tangents(const smco_event *e, const smco_nucleus *nA, const smco_nucleus *nB, double *tA,
+                              double *tB) {
+  icdf_moves(e, 0, nA, 0, 0, NULL, tA);
+  icdf_moves(e, 1, nB, 0, 0, NULL, tB);
+}
+
+int smco_event_nucleon_ids(const smco_event *e, int which, int *ids, int maxn) {
+  int n = e->n[which] < maxn ? e->n[which] : maxn;
+  for (int i = 0; i < n; i++) ids[i] = e->nuc[which][i].id;
+  return n;
 }
 
 /* MCnucl::calculate_rho_binary (MCnucl.cpp:481-531), Gaussian shapes */

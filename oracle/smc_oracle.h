@@ -39,7 +39,11 @@ typedef struct {
   double d_min;         /* hard-core distance [fm] (reference: 0.9)         */
   double rmax_cut;      /* proposal sphere radius, R + 2.5                  */
   double rw_max;        /* 1/(1+exp(-R/a))                                  */
+  int icdf;             /* 1: radii by inverse CDF (spherical A > 2)        */
 } smco_nucleus;
+/* inverse-CDF Woods-Saxon radius for the uniform u, with dr/dR, dr/da
+ * (either may be NULL) */
+double smco_ws_icdf(double R, double a, double u, double *drdR, double *drda);
 /* Fills the reference's hard-coded parameters for mass number A; any of
  * R, a, d_min that is > 0 on input of the *_override arguments replaces
  * the reference value (reference behaviour when all are <= 0). */
@@ -120,6 +124,18 @@ void smco_event_hotspot_mask(const smco_event *e, unsigned char *mask);
 /* model-5 density with windows, cuts and boxes of the event's own width and
  * the Gaussians and weights of (w, alpha); 0 or 5 (unsupported model) */
 int smco_event_density_frozen(smco_event *e, double w, double alpha, double *rho);
+/* the same with the Gaussians centred on sources displaced by dA [A][2],
+ * dB [B][2] (by nucleon id, NULL = none) */
+int smco_event_density_moved(smco_event *e, double w, double alpha, const double *dA, const double *dB,
+                             double *rho);
+/* inverse-CDF events: nucleon displacements [n][2] for (R, a) += (dR, da)
+ * and tangents [n][4] = (dx/dR, dy/dR, dx/da, dy/da), by nucleon id */
+void smco_event_icdf_displacement(const smco_event *e, const smco_nucleus *nA, const smco_nucleus *nB, double dR,
+                                  double da, double *dA, double *dB);
+void smco_event_icdf_tangents(const smco_event *e, const smco_nucleus *nA, const smco_nucleus *nB, double *tA,
+                              double *tB);
+/* pre-sort index (injection / acceptance order) of each nucleon in sorted order */
+int smco_event_nucleon_ids(const smco_event *e, int which, int *ids, int maxn);
 /* GlueDensity::calcCMAngle (GlueDensity.cpp:87-144) on rho */
 void smco_event_cm_angle(const smco_event *e, int n, double *xcm, double *ycm, double *angle);
 /* MCnucl::rotateGrid (MCnucl.cpp:1152-1174) + calculateThickness +

@@ -58,6 +58,7 @@ class SmcParams(ctypes.Structure):
         ("kln_npt", ctypes.c_int), ("kln_nkt", ctypes.c_int), ("kln_nphi", ctypes.c_int),
         ("seed", ctypes.c_uint64),
         ("max_attempts", ctypes.c_int), ("max_collisions", ctypes.c_int),
+        ("ws_inverse_cdf", ctypes.c_int),
     ]
 
 
@@ -82,11 +83,13 @@ class SmcOutputs(ctypes.Structure):
         ("ecc", ctypes.c_void_p), ("rho", ctypes.c_void_p), ("ta", ctypes.c_void_p), ("tb", ctypes.c_void_p),
         ("npart", ctypes.c_void_p), ("ncoll", ctypes.c_void_p), ("b", ctypes.c_void_p),
         ("attempts", ctypes.c_void_p), ("positions", ctypes.c_void_p), ("wounded", ctypes.c_void_p),
+        ("tangents", ctypes.c_void_p),
     ]
 
 
-class SmcCotangents(ctypes.Structure):
+class SmcAdjointArgs(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("g_eps", ctypes.c_void_p), ("g_rho", ctypes.c_void_p),
+                ("tangent_proj", ctypes.c_void_p), ("tangent_targ", ctypes.c_void_p),
                 ("grad_events", ctypes.c_void_p)]
 
 
@@ -127,7 +130,7 @@ def load() -> ctypes.CDLL:
     lib.smc_average.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_int, vp, vp, ctypes.POINTER(ctypes.c_int)]
     lib.smc_inject_noalloc.argtypes = [ctypes.POINTER(SmcParams), ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]
-    lib.smc_adjoint.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.POINTER(SmcCotangents), vp]
+    lib.smc_adjoint.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.POINTER(SmcAdjointArgs), vp]
     _lib = lib
     return lib
 

@@ -1,7 +1,8 @@
 // Adjoint of the MC-Glauber event: gradients of
 //     L = sum_e [ gE[e][0] |eps_2(e)| + gE[e][1] |eps_3(e)| + sum_c gG[e][c] rho_e(c) ]
-// with respect to the nucleon width w and the mixing parameter alpha, one
-// CTA per event.  No reference counterpart (the reference computes no
+// with respect to the nucleon width w, the mixing parameter alpha and the
+// Woods-Saxon R and a (through the sources' position tangents), one CTA per
+// event.  No reference counterpart (the reference computes no
 // derivatives); the forward quantities follow
 //   rho = (1-a)/2 WN + a BC                     src/MCnucl.cpp:688-779
 //   eps_n (r^n weighting about the centre of mass, hot-spot region)
@@ -13,6 +14,7 @@
 //   W = peak (1-a)/2 (participants), peak a (binary collisions), peak = 1/2 pi w^2
 //   d rho(c)/d a = sum_s (dW_s/da) e_s(c)
 //   d rho(c)/d w = sum_s W_s e_s(c) (r^2/w^3 - 2/w)
+//   d rho(c)/d x_s = W_s e_s(c) (x_c - x_s)/w^2   (likewise y)
 // Reverse mode: lambda(c) = dL/d rho(c) (including the dependence of the
 // centre of mass on rho) is formed on the event's bounding box; then each
 // (source, row) pair recomputes its Gaussians (nothing is stored from the
@@ -58,7 +60,7 @@ __host__ __device__ inline size_t red_offset(int nx, int ny) {
 }
 
 __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, const EventRec *recs, const Source *srcs,
-                                                 const float *rho_ev, const float *g_grid, const double *g_eps,
+                                                 const float4 *src_tan, const float *rho_ev, const float *g_grid, const double *g_eps,
                                                  float *lam_scratch, double *dtheta) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nx = P.nx, ny = P.ny, nw = (ny + 31) / 32;
@@ -170,8 +172,12 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
       }
     }
     __syncthreads();
-    // ---- contraction: one (source, row) pair per thread, Gaussians recomputed
-    float dw = 0.f, da = 0.f;
+    // ---- contraction: one (source, row) pair per thread, Gaussians recomputed.
+    // With position tangents t_s = d(x_s, y_s)/d(R, a):
+    //   dL/dR += (W/w^2) sum_c lambda e (x_c - x_s, y_c - y_s) . t_s(R)
+    float dw = 0.f, da = 0.f, dR = 0.f, dA = 0.f;
+    const float4 *T = src_tan ? src_tan + (size_t)e * P.max_src : nullptr;
+    const float inv_w2 = (float)(1.0 / P.w2);
     {
       const float peak = (float)P.peak, alpha = (float)P.alpha;
       const int npair = rec.nsrc * hmax;
@@ -188,15 +194,17 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
         cut_interval(P, &s.x, s.kind, yf, i, dx2, lim_lo, lim_hi, yg, inv_dy, ymin_f, s.yl, s.yr, ja, jb);
         if (ja >= jb) continue;
         const float ex = __expf(-dx2 * inv2w2);
-        float l0 = 0.f, lr = 0.f;
+        float l0 = 0.f, lr = 0.f, ly = 0.f;
         const float *lrow = lam + (size_t)i * ny;
         for (int j = ja; j < jb; j++) {
           const float dy = yg[j] - yf, dy2 = dy * dy;
           const float t = lrow[j] * __expf(-dy2 * inv2w2);
           l0 += t;
           lr += t * dy2;
+          ly += t * dy;
         }
         l0 *= ex;
+        ly *= ex;
         lr = ex * lr + dx2 * l0;   // sum lambda e (dx^2 + dy^2)
         const float W = s.weight;
         // W = peak (1-a)/2 for participants; peak (a + (1-a) aw) for binary
@@ -208,18 +216,20 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
         }
         dw += W * (lr / (float)(w * w * w) - 2.f * l0 / (float)w);
         da += dWda * l0;
+        if (T) {
+          const float4 t = T[k];
+          const float c = W * inv_w2, lx = dx * l0;
+          dR += c * (lx * t.x + ly * t.y);
+          dA += c * (lx * t.z + ly * t.w);
+        }
       }
     }
     {
-      float v[2] = {dw, da};
-      block_sums<2>(v, red, s_tot);
+      float v[4] = {dw, da, dR, dA};
+      block_sums<4>(v, red, s_tot);
     }
-    if (tid == 0) {
-      dtheta[4 * (size_t)e] = s_tot[0];
-      dtheta[4 * (size_t)e + 1] = s_tot[1];
-      dtheta[4 * (size_t)e + 2] = 0.0;
-      dtheta[4 * (size_t)e + 3] = 0.0;
-    }
+    if (tid == 0)
+      for (int q = 0; q < 4; q++) dtheta[4 * (size_t)e + q] = s_tot[q];
     __syncthreads();
   }
 }
@@ -235,12 +245,12 @@ int adjoint_blocks_per_sm(const DevParams &P) {
 }
 
 cudaError_t launch_adjoint(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs,
-                           const float *rho_ev, const float *g_grid, const double *g_eps, float *lam_scratch,
-                           double *dtheta, int grid, cudaStream_t st) {
+                           const float4 *src_tan, const float *rho_ev, const float *g_grid, const double *g_eps,
+                           float *lam_scratch, double *dtheta, int grid, cudaStream_t st) {
   const size_t smem = adjoint_smem(P);
   cudaError_t e = cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_adjoint<<<grid, kAT, smem, st>>>(P, n_events, recs, srcs, rho_ev, g_grid, g_eps, lam_scratch, dtheta);
+  k_adjoint<<<grid, kAT, smem, st>>>(P, n_events, recs, srcs, src_tan, rho_ev, g_grid, g_eps, lam_scratch, dtheta);
   return cudaGetLastError();
 }
 

@@ -62,6 +62,80 @@ __device__ __forceinline__ void rotate3f(float &x, float &y, float &z, float cth
   z = -sth * x0 + cth * z0;
 }
 
+// ---------------------------------------------- inverse-CDF radii
+// Differentiable sampling mode (no reference counterpart; the reference
+// samples radii by rejection, src/Nucleus.cpp:578-621): r solves
+// N(r) = u N(rmax), N(r) = int_0^r t^2 rho(t) dt for the reference's
+// truncated density rho = 1/(1+exp((r-R)/a)), r <= rmax = R + 2.5.  N and
+// its R, a derivatives are tabulated on the host; between nodes they are
+// cubic Hermite interpolants whose end-point slopes are the exact integrands.
+
+// r^2 rho(r) and its derivatives in R and a
+__device__ __forceinline__ void ws_weights(const NucleusDev &n, double r, double &f, double &fR, double &fa) {
+  const double rho = 1.0 / (1.0 + exp((r - n.R) / n.a));
+  const double d = rho * (1.0 - rho) / n.a;
+  f = r * r * rho;
+  fR = r * r * d;
+  fa = fR * (r - n.R) / n.a;
+}
+
+// cubic Hermite interpolant on [r_k, r_k + h] at t in [0, 1] from the end
+// values y0, y1 and slopes (per unit r) f0, f1
+__device__ __forceinline__ double hermite(double t, double h, double y0, double y1, double f0, double f1) {
+  const double t2 = t * t, t3 = t2 * t;
+  return (2 * t3 - 3 * t2 + 1) * y0 + (t3 - 2 * t2 + t) * h * f0 + (3 * t2 - 2 * t3) * y1 + (t3 - t2) * h * f1;
+}
+
+// the radius for the uniform u: bisection over the table, then Newton
+// steps on the interval's interpolant (monotone: N increases with r)
+__device__ double icdf_radius(const NucleusDev &n, double u) {
+  const double *N = n.icdf;
+  const double T = u * n.icdf_ntot;
+  int lo = 0, hi = n.icdf_m - 1;   // N[lo] <= T < N[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (N[mid] <= T) lo = mid;
+    else hi = mid;
+  }
+  const double h = n.icdf_h, r0 = lo * h;
+  double f0, f1, g0, g1;
+  ws_weights(n, r0, f0, g0, g1);
+  ws_weights(n, r0 + h, f1, g0, g1);
+  const double y0 = N[lo], y1 = N[lo + 1];
+  double t = y1 > y0 ? (T - y0) / (y1 - y0) : 0.0;
+  for (int it = 0; it < 8; it++) {
+    const double t2 = t * t;
+    const double p = hermite(t, h, y0, y1, f0, f1) - T;
+    const double dp =
+        (6 * t2 - 6 * t) * y0 + (3 * t2 - 4 * t + 1) * h * f0 + (6 * t - 6 * t2) * y1 + (3 * t2 - 2 * t) * h * f1;
+    if (!(dp > 0)) break;
+    t = fmin(fmax(t - p / dp, 0.0), 1.0);
+  }
+  return r0 + t * h;
+}
+
+// (dr/dR)/r and (dr/da)/r at the radius r (implicit differentiation of
+// F(r) = N(r)/N(rmax) = u):  dr/dp = -(N_p(r) - F(r) dN(rmax)/dp) / (r^2 rho(r))
+__device__ void icdf_tangent(const NucleusDev &n, double r, double &sR, double &sa) {
+  sR = sa = 0.0;
+  if (!(r > 1e-9)) return;
+  const int m = n.icdf_m;
+  const double h = n.icdf_h;
+  const int k = min((int)(r / h), m - 2);
+  const double t = fmin((r - k * h) / h, 1.0);
+  double f0, fR0, fa0, f1, fR1, fa1, f, fR, fa;
+  ws_weights(n, k * h, f0, fR0, fa0);
+  ws_weights(n, (k + 1) * h, f1, fR1, fa1);
+  ws_weights(n, r, f, fR, fa);
+  const double *N = n.icdf, *NR = N + m, *Na = NR + m;
+  const double F = hermite(t, h, N[k], N[k + 1], f0, f1) / n.icdf_ntot;
+  const double nR = hermite(t, h, NR[k], NR[k + 1], fR0, fR1);
+  const double na = hermite(t, h, Na[k], Na[k + 1], fa0, fa1);
+  if (!(f > 0)) return;
+  sR = -(nR - F * n.icdf_dntot_R) / (f * r);
+  sa = -(na - F * n.icdf_dntot_a) / (f * r);
+}
+
 // One Woods-Saxon candidate from four uniforms (Nucleus::getDeformRandomWS)
 __device__ __forceinline__ bool ws_candidate(const NucleusDev &n, float ctr, float phir, double u0, double u1,
                                              double u2, double u3, float &x, float &y, float &z) {
@@ -78,7 +152,8 @@ __device__ __forceinline__ bool ws_candidate(const NucleusDev &n, float ctr, flo
     x = r * sx * cp; y = r * sx * sp; z = r * cx;
     rotate3f(x, y, z, ctr, phir);
   } else {
-    if ((float)u1 * (float)n.rw_max > 1.0f / (1.0f + expf((r - R) / a))) return false;
+    if (n.icdf) r = (float)icdf_radius(n, u0);   // every candidate passes the radial step
+    else if ((float)u1 * (float)n.rw_max > 1.0f / (1.0f + expf((r - R) / a))) return false;
     float cx = 1.0f - 2.0f * (float)u2;
     float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
     float sp, cp;
@@ -275,10 +350,36 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
 // Places nucleus w: nucleus-frame positions -> centre-of-mass removed in
 // FP64 -> shifted by xc along x -> sorted by x (the reference sorts by the
 // left box edge x-4w, src/Nucleus.cpp:314, the same order).
-__device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const double *inj_xy) {
+// With ntan (this nucleus's [A][4] rows of the per-nucleon tangents) the
+// position tangents follow the same order: injected ones as given, those
+// of inverse-CDF radii as (dr/dp)/r times the nucleus-frame point minus
+// their mean over the nucleus (the centre-of-mass shift), else zero.
+__device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const double *inj_xy,
+                             const NucleusDev &nu, const double *inj_tan, double *ntan) {
   const int tid = threadIdx.x;
   double px = 0, py = 0;
   float rx = 0.f, ry = 0.f;
+  float tg[4] = {0.f, 0.f, 0.f, 0.f};
+  if (ntan && inj_xy && inj_tan && tid < A)
+    for (int c = 0; c < 4; c++) tg[c] = (float)inj_tan[4 * tid + c];
+  if (ntan && !inj_xy && nu.icdf && !nu.deformed && A > 2) {
+    double sR = 0, sa = 0;
+    float x = 0.f, y = 0.f;
+    if (tid < A) {
+      x = sm.ax[w][tid];
+      y = sm.ay[w][tid];
+      const float z = sm.az[w][tid];
+      icdf_tangent(nu, sqrt((double)x * x + (double)y * y + (double)z * z), sR, sa);
+    }
+    float v[4] = {(float)(sR * x), (float)(sR * y), (float)(sa * x), (float)(sa * y)};
+    for (int c = 0; c < 4; c += 2) {
+      const double m0 = block_sum_f(tid < A ? v[c] : 0.f, sm.red2, 0);
+      const double m1 = block_sum_f(tid < A ? v[c + 1] : 0.f, sm.red2, 1);
+      __syncthreads();
+      tg[c] = (float)(v[c] - m0 / A);
+      tg[c + 1] = (float)(v[c + 1] - m1 / A);
+    }
+  }
   if (inj_xy) {
     if (tid < A) { px = inj_xy[2 * tid]; py = inj_xy[2 * tid + 1]; }
   } else {
@@ -321,8 +422,16 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
     sm.X[w][rank] = px; sm.Y[w][rank] = py;
     sm.Xf[w][rank] = (float)px; sm.Yf[w][rank] = (float)py;
     if (!inj_xy) { sm.ax[w][rank] = rx; sm.ay[w][rank] = ry; }   // nucleus-frame positions, same order
+    if (ntan)
+      for (int c = 0; c < 4; c++) ntan[4 * rank + c] = (double)tg[c];
   }
   __syncthreads();
+}
+
+// tangent of nucleon k (sorted order, projectile first) of event e
+__device__ __forceinline__ float4 nucleon_tangent(const double *ntan, int e, int AB, int k) {
+  const double *t = ntan + ((size_t)e * AB + k) * 4;
+  return make_float4((float)t[0], (float)t[1], (float)t[2], (float)t[3]);
 }
 
 // Bounding-box edges of a nucleon at x (Particle::Particle + calculateBounds,
@@ -442,7 +551,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
                                                      const double *inj_b, EventRec *recs, Source *srcs,
                                                      double *out_pos, uint8_t *out_wounded,
                                                      const SystemDev *systems, const int *ev_sys,
-                                                     const int *order) {
+                                                     const int *order, TangentIO tio) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SampleSmem &sm = *reinterpret_cast<SampleSmem *>(smem_raw);
   __shared__ DevParams s_P;   // the context's parameters with the event's system
@@ -496,8 +605,11 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
       for (int w = 0; w < 2; w++) {
         const NucleusDev &nu = P.nuc[w];
         const double xc = (w == 0 ? b : -b) / 2.0;
+        double *ntan = tio.ntan ? tio.ntan + ((size_t)e * (A + B) + (w == 0 ? 0 : A)) * 4 : nullptr;
         if (inject) {
-          place_sorted(sm, w, nu.A, 0.0, (w == 0 ? inj_proj : inj_targ) + (size_t)e * 2 * nu.A);
+          const double *itan = w == 0 ? tio.inj_proj : tio.inj_targ;
+          place_sorted(sm, w, nu.A, 0.0, (w == 0 ? inj_proj : inj_targ) + (size_t)e * 2 * nu.A, nu,
+                       itan ? itan + (size_t)e * 4 * nu.A : nullptr, ntan);
           continue;
         }
         double o0, o1;
@@ -520,7 +632,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
         } else {
           ok = ok && sample_ws(sm, nu, w, P.seed, ev, attempt, ctr, phir);
         }
-        place_sorted(sm, w, nu.A, xc, nullptr);
+        place_sorted(sm, w, nu.A, xc, nullptr, nu, nullptr, ntan);
       }
       if (!ok) { status = 3; break; }
       // ---- pairing: thread i tests projectile i against every target
@@ -565,8 +677,9 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
       }
     }
 
-    // ---- splat sources
+    // ---- splat sources (with their position tangents when requested)
     Source *S = srcs + (size_t)e * P.max_src;
+    float4 *stan = tio.stan ? tio.stan + (size_t)e * P.max_src : nullptr;
     const double d_max = P.shape_of_nucleons == 1 ? 2. * sqrt(P.dsq) : 5. * P.width;
     const int model = P.which_mc_model;
     const bool box_src = (model == 5 && P.sub_model == 1) || model == 7;
@@ -679,6 +792,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
             } else {
               s.bx = s.by = 0.f;
             }
+            if (stan) stan[pos] = nucleon_tangent(tio.ntan, e, AB, k);
             S[pos++] = s;
           }
           if (thick_src) {
@@ -691,6 +805,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
             s.plane = model == 1 ? w : 1 + w;   // MC-KLN splats T_A, T_B only
             s.weight = disk_n ? disk_val : peak;
             s.bx = s.by = 0.f;
+            if (stan) stan[pos] = nucleon_tangent(tio.ntan, e, AB, k);
             S[pos++] = s;
           }
         }
@@ -735,6 +850,11 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
           double fw = P.alpha + (1. - P.alpha) * aw;
           s.weight = (float)((disk_e ? 10.0 / P.sigin : P.peak) * fw);
           s.bx = s.by = 0.f;
+          if (stan) {
+            const float4 ta = nucleon_tangent(tio.ntan, e, AB, tid), tb = nucleon_tangent(tio.ntan, e, AB, A + j);
+            stan[nsrc + pos] = make_float4(0.5f * (ta.x + tb.x), 0.5f * (ta.y + tb.y), 0.5f * (ta.z + tb.z),
+                                           0.5f * (ta.w + tb.w));
+          }
           S[nsrc + pos] = s;
           pos++;
         }
@@ -789,7 +909,8 @@ cudaError_t launch_sample_pair(const DevParams &P, uint64_t first_event, int n_e
 cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, int n_events, const double *inj_proj,
                                      const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
                                      double *out_pos, uint8_t *out_wounded, const SystemDev *systems,
-                                     const int *ev_sys, const int *order, int grid, cudaStream_t st) {
+                                     const int *ev_sys, const int *order, int grid, cudaStream_t st,
+                                     const TangentIO *tio) {
   size_t smem = sizeof(SampleSmem);
   static bool attr = false;
   if (!attr) {
@@ -798,7 +919,7 @@ cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, i
     attr = true;
   }
   k_sample_pair<<<grid, kNT, smem, st>>>(P, first_event, n_events, inj_proj, inj_targ, inj_b, recs, srcs, out_pos,
-                                         out_wounded, systems, ev_sys, order);
+                                         out_wounded, systems, ev_sys, order, tio ? *tio : TangentIO{});
   return cudaGetLastError();
 }
 

@@ -122,6 +122,46 @@ smc::NucleusDev make_nucleus(int A, int deformed, double R_ov, double a_ov, doub
   return n;
 }
 
+// Inverse-CDF table of the Woods-Saxon radius (differentiable sampling
+// mode): N, dN/dR, dN/da of int_0^r t^2 rho(t) dt, rho = 1/(1+exp((t-R)/a)),
+// at r_k = k h on [0, R + 2.5], each step integrated by the 5-point
+// Gauss-Legendre rule (published nodes and weights).
+void icdf_table(smc::NucleusDev &n, std::vector<double> &tab) {
+  const int m = 2048;
+  const double rmax = n.R + 2.5, h = rmax / (m - 1);
+  static const double x5[3] = {0.0, 0.5384693101056831, 0.9061798459386640};
+  static const double w5[3] = {0.5688888888888889, 0.4786286704993665, 0.2369268850561891};
+  auto integrand = [&](double t, double &f, double &fR, double &fa) {
+    const double rho = 1.0 / (1.0 + std::exp((t - n.R) / n.a)), d = rho * (1.0 - rho) / n.a;
+    f = t * t * rho;
+    fR = t * t * d;
+    fa = fR * (t - n.R) / n.a;
+  };
+  tab.assign((size_t)3 * m, 0.0);
+  for (int k = 1; k < m; k++) {
+    const double c = (k - 0.5) * h, hh = 0.5 * h;
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int q = 0; q < 3; q++)
+      for (int sg = -1; sg <= (q == 0 ? -1 : 1); sg += 2) {
+        double f, fR, fa;
+        integrand(c + sg * hh * x5[q], f, fR, fa);
+        s0 += w5[q] * hh * f;
+        s1 += w5[q] * hh * fR;
+        s2 += w5[q] * hh * fa;
+      }
+    tab[k] = tab[k - 1] + s0;
+    tab[m + k] = tab[m + k - 1] + s1;
+    tab[2 * m + k] = tab[2 * m + k - 1] + s2;
+  }
+  double f, fR, fa;
+  integrand(rmax, f, fR, fa);
+  n.icdf_m = m;
+  n.icdf_h = h;
+  n.icdf_ntot = tab[m - 1];
+  n.icdf_dntot_R = tab[2 * m - 1] + f;   // the end point rmax = R + 2.5 moves with R
+  n.icdf_dntot_a = tab[3 * m - 1];
+}
+
 template <typename T>
 struct DevBuf {
   T *p = nullptr;
@@ -172,6 +212,12 @@ struct Ctx {
   // per-event gradients
   DevBuf<float> adj_rho, adj_lam, adj_grho;
   DevBuf<double> adj_geps, adj_out;
+  // position tangents (differentiable sampling): inverse-CDF tables, the
+  // per-nucleon and per-source tangents, injected tangents, and the set the
+  // next sampler launch uses
+  DevBuf<double> icdf_tab[2], ntan, inj_tp, inj_tt;
+  DevBuf<float4> stan;
+  smc::TangentIO tio{};
   std::vector<double> h_adj;
   DevBuf<smc::AvgSrc> avg_state;
   DevBuf<float> avg_rho;
@@ -244,6 +290,8 @@ smc_status validate(const smc_params &p) {
   if (!(p.dx > 0) || !(p.dy > 0) || !(p.maxx > 0) || !(p.maxy > 0)) return SMC_ERR_CONFIG;
   if (p.ecc_from_order < 1 || p.ecc_to_order > 9 || p.ecc_from_order > p.ecc_to_order) return SMC_ERR_CONFIG;
   if (p.bmax < p.bmin || p.bmin < 0) return SMC_ERR_CONFIG;
+  // inverse-CDF radii: spherical Woods-Saxon nuclei
+  if (p.ws_inverse_cdf && (p.Aproj < 3 || p.Atarg < 3 || p.proj_deformed || p.targ_deformed)) return SMC_ERR_CONFIG;
   return SMC_OK;
 }
 
@@ -299,6 +347,7 @@ smc_status ensure_buffers(Ctx *c, int n, const smc_outputs *out) {
     if (out->tb) CK(c->tb.ensure((size_t)n * g));
     if (out->positions) CK(c->pos.ensure((size_t)n * 2 * (c->info.A + c->info.B)));
     if (out->wounded) CK(c->wounded.ensure((size_t)n * (c->info.A + c->info.B)));
+    if (out->tangents) CK(c->ntan.ensure((size_t)n * 4 * (c->info.A + c->info.B)));
   }
   if (!out->ecc || out->device == 0) CK(c->ecc.ensure((size_t)n * smc::kEccLen));
   return SMC_OK;
@@ -358,17 +407,22 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
   float *tb = out->tb ? (dev ? out->tb + (size_t)off * g : c->tb.p) : nullptr;
   double *pos = out->positions ? (dev ? out->positions + (size_t)off * 2 * AB : c->pos.p) : nullptr;
   uint8_t *wnd = out->wounded ? (dev ? out->wounded + (size_t)off * AB : c->wounded.p) : nullptr;
+  double *tg = out->tangents ? (dev ? out->tangents + (size_t)off * 4 * AB : c->ntan.p) : nullptr;
+  smc::TangentIO tio = c->tio;
+  if (tg) tio.ntan = tg;
   int grid1 = std::max(1, std::min(n, c->sms * c->occ1));
   int grid2 = std::max(1, std::min(n, c->sms * c->occ2));
   if (!rho) CK(c->scratch.ensure((size_t)(plain ? 1 : grid2) * g));
   if (plain) {
     for (int e = 0; e < n; e++) {
+      smc::TangentIO te{};
+      te.ntan = tg ? tg + (size_t)e * 4 * AB : nullptr;
       CK(timed(c, 0, [&] {
-        return smc::launch_sample_pair(P, first_event + e, 1, inj_p ? inj_p + (size_t)e * 2 * c->info.A : nullptr,
-                                       inj_t ? inj_t + (size_t)e * 2 * c->info.B : nullptr,
-                                       inj_b ? inj_b + e : nullptr, c->recs.p + e,
-                                       c->srcs.p + (size_t)e * P.max_src, pos ? pos + (size_t)e * 2 * AB : nullptr,
-                                       wnd ? wnd + (size_t)e * AB : nullptr, 1, c->st);
+        return smc::launch_sample_pair_mixed(
+            P, first_event + e, 1, inj_p ? inj_p + (size_t)e * 2 * c->info.A : nullptr,
+            inj_t ? inj_t + (size_t)e * 2 * c->info.B : nullptr, inj_b ? inj_b + e : nullptr, c->recs.p + e,
+            c->srcs.p + (size_t)e * P.max_src, pos ? pos + (size_t)e * 2 * AB : nullptr,
+            wnd ? wnd + (size_t)e * AB : nullptr, nullptr, nullptr, nullptr, 1, c->st, &te);
       }));
       CK(timed(c, 1, [&] {
         return smc::launch_grid(P, 1, c->recs.p + e, c->srcs.p + (size_t)e * P.max_src,
@@ -382,7 +436,7 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
       return smc::launch_sample_pair_mixed(P, first_event, n, inj_p, inj_t, inj_b, c->recs.p, c->srcs.p, pos, wnd,
                                            c->mix_sys.p && c->mixing ? c->mix_sys.p : nullptr,
                                            c->mixing ? c->mix_ev.p : nullptr, c->mixing ? c->mix_order.p : nullptr,
-                                           grid1, c->st);
+                                           grid1, c->st, &tio);
     }));
     CK(timed(c, 1, [&] {
       return launch_splat(c, P, n, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p);
@@ -412,6 +466,9 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
                          cudaMemcpyDeviceToHost, c->st));
     if (out->wounded)
       CK(cudaMemcpyAsync(out->wounded + (size_t)off * AB, wnd, (size_t)n * AB, cudaMemcpyDeviceToHost, c->st));
+    if (out->tangents)
+      CK(cudaMemcpyAsync(out->tangents + (size_t)off * 4 * AB, tg, sizeof(double) * n * 4 * AB,
+                         cudaMemcpyDeviceToHost, c->st));
     if (out->npart || out->ncoll || out->b || out->attempts) {
       c->h_recs.resize(n);
       CK(cudaMemcpyAsync(c->h_recs.data(), c->recs.p, sizeof(EventRec) * n, cudaMemcpyDeviceToHost, c->st));
@@ -533,6 +590,20 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
   P.npmin = p.npmin; P.npmax = p.npmax; P.bmin = p.bmin; P.bmax = p.bmax;
   P.nuc[0] = make_nucleus(p.Aproj, p.proj_deformed, p.proj_R, p.proj_a, p.proj_d_min);
   P.nuc[1] = make_nucleus(p.Atarg, p.targ_deformed, p.targ_R, p.targ_a, p.targ_d_min);
+  if (p.ws_inverse_cdf) {
+    for (int w = 0; w < 2; w++) {
+      smc::NucleusDev &n = P.nuc[w];
+      std::vector<double> tab;
+      icdf_table(n, tab);
+      if (c->icdf_tab[w].ensure(tab.size()) != cudaSuccess ||
+          cudaMemcpy(c->icdf_tab[w].p, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice) !=
+              cudaSuccess) {
+        smc_destroy(c);
+        return SMC_ERR_CUDA;
+      }
+      n.icdf = c->icdf_tab[w].p;
+    }
+  }
   P.seed = p.seed;
   P.max_attempts = p.max_attempts > 0 ? p.max_attempts : 100000;
   P.max_coll = p.max_collisions > 0 ? p.max_collisions : 4096;
@@ -581,6 +652,8 @@ void smc_destroy(void *ctx) {
   c->mix_sys.release(); c->mix_ev.release(); c->mix_order.release(); c->kln64.release(); c->kln32.release();
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
   c->adj_rho.release(); c->adj_lam.release(); c->adj_grho.release(); c->adj_geps.release(); c->adj_out.release();
+  c->icdf_tab[0].release(); c->icdf_tab[1].release(); c->ntan.release(); c->inj_tp.release(); c->inj_tt.release();
+  c->stan.release();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -636,6 +709,8 @@ smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_
 
 smc_status smc_generate_mixed(void *ctx, const smc_params *systems, int nsys, uint64_t first_event, int n,
                               const int *system_of_event, const smc_outputs *out) {
+  if (ctx && static_cast<Ctx *>(ctx)->prm.ws_inverse_cdf) return SMC_ERR_CONFIG;
+  if (out && out->tangents) return SMC_ERR_ARGUMENT;
   if (!ctx || !out || !systems || nsys < 1 || nsys > 64 || n < 0 || (n > 0 && !system_of_event))
     return SMC_ERR_ARGUMENT;
   if (out->positions || out->wounded) return SMC_ERR_ARGUMENT;   // per-system shapes
@@ -717,8 +792,10 @@ smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_
 }
 
 smc_status smc_adjoint(void *ctx, uint64_t first_event, int n, const double *xy_proj, const double *xy_targ,
-                       const double *b, const smc_cotangents *ct, double *grad) {
+                       const double *b, const smc_adjoint_args *ct, double *grad) {
   if (!ctx || !ct || !grad || n < 0 || (xy_proj && !xy_targ)) return SMC_ERR_ARGUMENT;
+  if (!xy_proj && ct->tangent_proj) return SMC_ERR_ARGUMENT;
+  if ((ct->tangent_proj != nullptr) != (ct->tangent_targ != nullptr)) return SMC_ERR_ARGUMENT;
   Ctx *c = static_cast<Ctx *>(ctx);
   for (int k = 0; k < 4; k++) grad[k] = 0.0;
   const smc_params &p = c->prm;
@@ -733,6 +810,9 @@ smc_status smc_adjoint(void *ctx, uint64_t first_event, int n, const double *xy_
   const size_t g = (size_t)P.nx * P.ny;
   const bool dev = ct->device != 0;
   const int nb = smc::adjoint_blocks_per_sm(P);
+  const int A = c->info.A, B = c->info.B;
+  // positions depend on (R, a): inverse-CDF sampling, or injected tangents
+  const bool tangents = xy_proj ? ct->tangent_proj != nullptr : c->prm.ws_inverse_cdf != 0;
   smc_status worst = SMC_OK;
   for (int off = 0; off < n; off += c->chunk) {
     const int m = std::min(c->chunk, n - off);
@@ -748,9 +828,29 @@ smc_status smc_adjoint(void *ctx, uint64_t first_event, int n, const double *xy_
     const double *ip, *it, *ib;
     s = stage_injection(c, off, m, xy_proj, xy_targ, b, dev, &ip, &it, &ib);
     if (s) return s;
+    smc::TangentIO tio{};
+    if (tangents) {
+      CK(c->ntan.ensure((size_t)m * 4 * (A + B)));
+      CK(c->stan.ensure((size_t)m * P.max_src));
+      tio.ntan = c->ntan.p;
+      tio.stan = c->stan.p;
+      if (xy_proj) {
+        const cudaMemcpyKind kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        CK(c->inj_tp.ensure((size_t)m * 4 * A));
+        CK(c->inj_tt.ensure((size_t)m * 4 * B));
+        CK(cudaMemcpyAsync(c->inj_tp.p, ct->tangent_proj + (size_t)off * 4 * A, sizeof(double) * m * 4 * A, kind,
+                           c->st));
+        CK(cudaMemcpyAsync(c->inj_tt.p, ct->tangent_targ + (size_t)off * 4 * B, sizeof(double) * m * 4 * B, kind,
+                           c->st));
+        tio.inj_proj = c->inj_tp.p;
+        tio.inj_targ = c->inj_tt.p;
+      }
+    }
     // forward pass of the chunk (the densities are recomputed, not kept
     // between the forward call and this one)
+    c->tio = tio;
     s = run_chunk(c, first_event + off, 0, m, &o, ip, it, ib, false);
+    c->tio = smc::TangentIO{};
     if (s && s != SMC_ERR_ZERO_DNDY) return s;
     if (s) worst = s;
     const double *geps = nullptr;
@@ -776,8 +876,8 @@ smc_status smc_adjoint(void *ctx, uint64_t first_event, int n, const double *xy_
       }
     }
     CK(timed(c, 1, [&] {
-      return smc::launch_adjoint(P, m, c->recs.p, c->srcs.p, c->adj_rho.p, grho, geps, c->adj_lam.p, c->adj_out.p,
-                                 grid, c->st);
+      return smc::launch_adjoint(P, m, c->recs.p, c->srcs.p, tangents ? c->stan.p : nullptr, c->adj_rho.p, grho,
+                                 geps, c->adj_lam.p, c->adj_out.p, grid, c->st);
     }));
     c->h_adj.resize((size_t)m * 4);
     CK(cudaMemcpyAsync(c->h_adj.data(), c->adj_out.p, sizeof(double) * m * 4, cudaMemcpyDeviceToHost, c->st));

@@ -39,6 +39,23 @@ struct AvgSrc {
 struct NucleusDev {
   int A, deformed;
   double R, a, beta2, beta4, d_min, rmax_cut, rw_max;
+  // inverse-CDF radii (NULL table: rejection sampling).  icdf holds the
+  // cumulative integrals N, dN/dR, dN/da of r^2 rho(r) at r_k = k icdf_h,
+  // k < icdf_m (three rows of icdf_m); icdf_ntot = N(rmax) and its
+  // derivatives, the moving end point rmax = R + 2.5 included.
+  const double *icdf;
+  int icdf_m;
+  double icdf_h, icdf_ntot, icdf_dntot_R, icdf_dntot_a;
+};
+
+// Position tangents of the differentiable sampling mode: injected per
+// nucleon ([n][A][4], [n][B][4]: dx/dR, dy/dR, dx/da, dy/da), written per
+// nucleon in sorted order (ntan [n][A+B][4]) and per splat source
+// (stan [n][max_src]).  All NULL when unused.
+struct TangentIO {
+  const double *inj_proj, *inj_targ;
+  double *ntan;
+  float4 *stan;
 };
 
 // The parameters that differ between the systems of a mixed batch (the

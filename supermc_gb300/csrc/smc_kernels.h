@@ -20,7 +20,8 @@ cudaError_t launch_sample_pair(const DevParams &P, uint64_t first_event, int n_e
 cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, int n_events, const double *inj_proj,
                                      const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
                                      double *out_pos, uint8_t *out_wounded, const SystemDev *systems,
-                                     const int *ev_sys, const int *order, int grid, cudaStream_t st);
+                                     const int *ev_sys, const int *order, int grid, cudaStream_t st,
+                                     const TangentIO *tio = nullptr);
 size_t grid_smem(const DevParams &P);
 int grid_blocks_per_sm(const DevParams &P);
 cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs, float *out_rho,
@@ -42,15 +43,17 @@ cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Sour
                                  const float *rho, int order, int mode, int grid, cudaStream_t st);
 cudaError_t launch_avg_accum(const float *rho, int n, size_t cells, double *acc, cudaStream_t st);
 // Adjoint of a batch (k_adjoint, one CTA per event in turn): per-event
-// gradients dtheta [n][4] = (dL/dw, dL/dalpha, 0, 0) of
+// gradients dtheta [n][4] = (dL/dw, dL/dalpha, dL/dR, dL/da; the last two
+// through the source position tangents src_tan [n][max_src], zero when
+// src_tan is NULL) of
 // L = sum_e g_eps[e][0] |eps_2| + g_eps[e][1] |eps_3| + <g_rho[e], rho_e>
 // from the forward densities rho_ev [n][nx][ny]; g_eps, g_rho may be NULL;
 // lam_scratch [grid][nx][ny] floats.
 size_t adjoint_smem(const DevParams &P);
 int adjoint_blocks_per_sm(const DevParams &P);
 cudaError_t launch_adjoint(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs,
-                           const float *rho_ev, const float *g_grid, const double *g_eps, float *lam_scratch,
-                           double *dtheta, int grid, cudaStream_t st);
+                           const float4 *src_tan, const float *rho_ev, const float *g_grid, const double *g_eps,
+                           float *lam_scratch, double *dtheta, int grid, cudaStream_t st);
 cudaError_t launch_kln_table(const KlnDev &K, int tmax, double dT, double *table64, float *table32,
                              cudaStream_t st);
 

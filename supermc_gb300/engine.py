@@ -43,10 +43,11 @@ def smc_params_from(vals: dict[str, float], seed: int = 1) -> _lib.SmcParams:
     p.seed = int(seed) & ((1 << 64) - 1)
     p.max_attempts = int(v["max_attempts"])
     p.max_collisions = int(v["max_collisions"])
+    p.ws_inverse_cdf = int(v["ws_inverse_cdf"])
     return p
 
 
-OUTPUT_NAMES = ("ecc", "rho", "ta", "tb", "npart", "ncoll", "b", "attempts", "positions", "wounded")
+OUTPUT_NAMES = ("ecc", "rho", "ta", "tb", "npart", "ncoll", "b", "attempts", "positions", "wounded", "tangents")
 # keys that describe one collision system of a mixed batch
 SYSTEM_KEYS = ("aproj", "atarg", "proj_deformed", "targ_deformed", "ecm", "sigininn_override", "proj_r", "proj_a",
                "targ_r", "targ_a", "proj_d_min", "targ_d_min")
@@ -85,7 +86,8 @@ class Engine:
         shapes = {"ecc": ((n, _lib.ECC_LEN), np.float64), "rho": (g, np.float32), "ta": (g, np.float32),
                   "tb": (g, np.float32), "npart": ((n, 2), np.int32), "ncoll": ((n,), np.int32),
                   "b": ((n,), np.float64), "attempts": ((n,), np.int32),
-                  "positions": ((n, AB, 2), np.float64), "wounded": ((n, AB), np.uint8)}
+                  "positions": ((n, AB, 2), np.float64), "wounded": ((n, AB), np.uint8),
+                  "tangents": ((n, AB, 4), np.float64)}
         return {k: np.zeros(*shapes[k]) for k in want}
 
     @staticmethod
@@ -185,13 +187,15 @@ class Engine:
         self.last_average_events = used.value
         return mean, mean_rp
 
-    def adjoint(self, first_event: int, n: int, g_eps=None, g_rho=None, xy_proj=None, xy_targ=None, b=None):
+    def adjoint(self, first_event: int, n: int, g_eps=None, g_rho=None, xy_proj=None, xy_targ=None, b=None,
+                tangent_proj=None, tangent_targ=None):
         """Gradients of L = sum_e g_eps[e,0] |eps_2| + g_eps[e,1] |eps_3| +
         sum g_rho[e] * rho_e with respect to (width, alpha, R, a) for the
-        events first_event.. (or the injected positions), the structure of
-        each event (participants, windows, cuts, hot-spot region) held
-        fixed.  g_eps [n,2] and g_rho [n,nx,ny] are host arrays or None.
-        Returns (grad [4], per-event grad [n,4])."""
+        events first_event.. (or the injected positions, with optional
+        position tangents [n,A,4], [n,B,4]), the structure of each event
+        (participants, windows, cuts, hot-spot region) held fixed.  g_eps
+        [n,2] and g_rho [n,nx,ny] are host arrays or None.  Returns
+        (grad [4], per-event grad [n,4])."""
         ge = None if g_eps is None else np.ascontiguousarray(g_eps, dtype=np.float64).reshape(n, 2)
         gr = None if g_rho is None else np.ascontiguousarray(g_rho, dtype=np.float32).reshape(n, self.nx, self.ny)
         xp = xt = bb = None
@@ -200,9 +204,13 @@ class Engine:
             xt = np.ascontiguousarray(xy_targ, dtype=np.float64).reshape(n, self.B, 2)
             if b is not None:
                 bb = np.ascontiguousarray(np.broadcast_to(b, (n,)), dtype=np.float64)
+        tp = tt = None
+        if tangent_proj is not None:
+            tp = np.ascontiguousarray(tangent_proj, dtype=np.float64).reshape(n, self.A, 4)
+            tt = np.ascontiguousarray(tangent_targ, dtype=np.float64).reshape(n, self.B, 4)
         per = np.zeros((n, 4))
         grad = np.zeros(4)
-        ct = _lib.SmcCotangents(0, _lib.ptr(ge), _lib.ptr(gr), _lib.ptr(per))
+        ct = _lib.SmcAdjointArgs(0, _lib.ptr(ge), _lib.ptr(gr), _lib.ptr(tp), _lib.ptr(tt), _lib.ptr(per))
         _lib.check(self.lib.smc_adjoint(self.h, first_event, n, _lib.ptr(xp), _lib.ptr(xt), _lib.ptr(bb),
                                         ctypes.byref(ct), _lib.ptr(grad)), "smc_adjoint")
         return grad, per

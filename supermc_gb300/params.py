@@ -48,6 +48,8 @@ EXTENSION_KEYS: dict[str, float] = {
     "kln_npt": 48, "kln_nkt": 64, "kln_nphi": 32,
     # event retry cap and per-event collision capacity (0: library defaults)
     "max_attempts": 0, "max_collisions": 0,
+    # Woods-Saxon radii by inverse CDF (differentiable in R and a)
+    "ws_inverse_cdf": 0,
 }
 
 
