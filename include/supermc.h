@@ -192,6 +192,24 @@ smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_
                        const double *xy_targ, const double *b, int from_order, int to_order,
                        int reaction_plane, double *mean, double *mean_rp, int *n_used);
 
+/* Centrality-binned averaged profiles (the per-order mean of
+ * MakeDensity::generate_profile_average, src/MakeDensity.cpp:1331-1340,
+ * split into Npart classes).  Every event of [first_event, first_event + n)
+ * is recentred on its density's centre of mass and rotated to its
+ * order-`order` participant plane (GlueDensity::calcCMAngle,
+ * src/GlueDensity.cpp:87-144), then added to its bin: bin k holds the events
+ * with npart_edges[k] <= Npart1 + Npart2 < npart_edges[k + 1] (k < nbins
+ * <= 64; others are left out).
+ *   method 0: the sources are moved and re-splatted (MCnucl::rotateGrid,
+ *             src/MCnucl.cpp:1152-1174: the reference's method, exact);
+ *   method 1: each density is resampled bilinearly on the rotated frame
+ *             (one splat per event; preimages beyond the grid read zero).
+ * The bins are FP32 sums with compensation.  mean [nbins][nx][ny] (host)
+ * receives the bin averages of rho * finalFactor (MakeDensity::setSd,
+ * :2514-2522), counts [nbins] (may be NULL) the events per bin. */
+smc_status smc_average_binned(void *ctx, uint64_t first_event, int n, int order, int method, int nbins,
+                              const int *npart_edges, double *mean, int *counts);
+
 /* Reverse-mode gradients of the MC-Glauber event (no reference counterpart:
  * the reference computes no derivatives).  For the events of smc_generate
  * (first_event..) or of smc_inject (xy_proj / xy_targ / b given) the

@@ -27,7 +27,7 @@ EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "sm
            "smc_set_timing",
            "smc_set_grid_path", "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_write_ecc",
            "smc_write_density_block", "smc_write_density_4col", "smc_inject_noalloc", "smc_average",
-           "smc_adjoint"]
+           "smc_average_binned", "smc_adjoint"]
 
 
 class SmcError(RuntimeError):
@@ -130,6 +130,8 @@ def load() -> ctypes.CDLL:
     lib.smc_average.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_int, vp, vp, ctypes.POINTER(ctypes.c_int)]
     lib.smc_inject_noalloc.argtypes = [ctypes.POINTER(SmcParams), ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]
+    lib.smc_average_binned.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       vp, vp, vp]
     lib.smc_adjoint.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.POINTER(SmcAdjointArgs), vp]
     _lib = lib
     return lib

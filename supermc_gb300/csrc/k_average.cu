@@ -84,9 +84,12 @@ struct Kahan {
   }
 };
 
-// mode 0: recenter (MCnucl::recenterGrid); mode 1: rotate (MCnucl::rotateGrid)
+// mode 0: recenter (MCnucl::recenterGrid); mode 1: rotate (MCnucl::rotateGrid);
+// mode 2: only the frame.  With frame != NULL, frame[e] = (X, Y, cos, sin) of
+// the centre of mass and the rotation the sources receive.
 __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events, EventRec *recs, Source *srcs,
-                                                       AvgSrc *state, const float *rho, int order, int mode) {
+                                                       AvgSrc *state, const float *rho, int order, int mode,
+                                                       double4 *frame) {
   __shared__ float2 red[kAT / 32];
   __shared__ double s_par[4];   // X, Y, cos, sin
   __shared__ int s_box[4];      // the event's new window bounds: imin, imax, jmin, jmax
@@ -110,7 +113,10 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
     const double W = block_sum_df(sw.s, sw.c, red);
     const double SX = block_sum_df(sx.s, sx.c, red);
     const double SY = block_sum_df(sy.s, sy.c, red);
-    if (!(W > 0)) continue;   // empty density: nothing to move (uniform over the block)
+    if (!(W > 0)) {   // empty density: nothing to move (uniform over the block)
+      if (frame && tid == 0) frame[e] = make_double4(0.0, 0.0, 1.0, 0.0);
+      continue;
+    }
     const double X = SX / W, Y = SY / W;
     // ---- order-n angle: sum r^n e^{in theta} rho about the centre (full grid)
     Kahan sr, si;
@@ -141,6 +147,8 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
     }
     __syncthreads();
     const double cx = s_par[0], cy = s_par[1], cphi = s_par[2], sphi = s_par[3];
+    if (frame && tid == 0) frame[e] = make_double4(cx, cy, cphi, sphi);
+    if (mode == 2) continue;
     // ---- transform the sources (FP64, reference rounding)
     const double c4w = 4 * P.width, c4q = 4 * P.quark_width;
     for (int k = tid; k < rec.nsrc; k += kAT) {
@@ -223,14 +231,102 @@ __global__ void k_avg_accum(const float *rho, int n_events, size_t cells, double
   }
 }
 
+// ---------------------------------------------------- centrality bins
+// Events of the chunk in bin order (bin k: edges[k] <= Npart < edges[k+1]);
+// seg[k] .. seg[k+1] delimit bin k in order[], events outside every bin are
+// left out.  One thread: deterministic order, m is a chunk.
+__global__ void k_avg_bins(const EventRec *recs, int n, const int *edges, int nbins, int *order, int *seg,
+                           int *counts) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int pos = 0;
+  for (int b = 0; b < nbins; b++) {
+    seg[b] = pos;
+    for (int e = 0; e < n; e++) {
+      const int np = recs[e].npart1 + recs[e].npart2;
+      if (recs[e].ncoll > 0 && np >= edges[b] && np < edges[b + 1]) order[pos++] = e;
+    }
+    counts[b] += pos - seg[b];
+  }
+  seg[nbins] = pos;
+}
+
+// acc[b][cell] (FP32 sum, compensation) += the chunk's bin-b events at the
+// cell: with frame, the value of the event's density at the cell's preimage
+// under the recentring and rotation, R(-phi) (x', y') + (X, Y), by bilinear
+// interpolation (corners beyond the grid read zero); without, the cell's
+// value.  One thread per output cell, 16 x 16 cells per CTA, events in bin
+// order with one compensated sum in registers per bin.
+__global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const float *rho, const double4 *frame,
+                                                   const int *order, const int *seg, int nbins, float2 *acc) {
+  const int i = blockIdx.y * 16 + (threadIdx.x >> 4), j = blockIdx.x * 16 + (threadIdx.x & 15);
+  const int nx = P.nx, ny = P.ny;
+  const bool in = i < nx && j < ny;
+  const size_t g = (size_t)nx * ny;
+  const float xo = (float)(P.xmin + i * P.dx), yo = (float)(P.ymin + j * P.dy);
+  const float inv_dx = (float)(1.0 / P.dx), inv_dy = (float)(1.0 / P.dy);
+  const float xmin = (float)P.xmin, ymin = (float)P.ymin;
+  for (int b = 0; b < nbins; b++) {
+    Kahan k;
+    const int e0 = seg[b], e1 = seg[b + 1];
+    for (int q = e0; q < e1; q++) {
+      const int e = order[q];
+      const float *G = rho + (size_t)e * g;
+      float v = 0.f;
+      if (!in) continue;
+      if (frame) {
+        const double4 f = frame[e];
+        const float c = (float)f.z, s = (float)f.w;
+        // preimage in grid units
+        const float px = (c * xo + s * yo + (float)f.x - xmin) * inv_dx;
+        const float py = (-s * xo + c * yo + (float)f.y - ymin) * inv_dy;
+        const float fx = floorf(px), fy = floorf(py);
+        const int i0 = (int)fx, j0 = (int)fy;
+        const float tx = px - fx, ty = py - fy;
+        if (i0 >= -1 && i0 < nx && j0 >= -1 && j0 < ny) {
+          const bool xa = i0 >= 0, xb = i0 + 1 < nx, ya = j0 >= 0, yb = j0 + 1 < ny;
+          const float v00 = xa && ya ? G[(size_t)i0 * ny + j0] : 0.f;
+          const float v01 = xa && yb ? G[(size_t)i0 * ny + j0 + 1] : 0.f;
+          const float v10 = xb && ya ? G[(size_t)(i0 + 1) * ny + j0] : 0.f;
+          const float v11 = xb && yb ? G[(size_t)(i0 + 1) * ny + j0 + 1] : 0.f;
+          v = (1.f - tx) * ((1.f - ty) * v00 + ty * v01) + tx * ((1.f - ty) * v10 + ty * v11);
+        }
+      } else {
+        v = G[(size_t)i * ny + j];
+      }
+      k.add(v);
+    }
+    if (in && e1 > e0) {
+      // merge the chunk's compensated sum into the accumulator's
+      float2 a = acc[(size_t)b * g + (size_t)i * ny + j];
+      const float y = (k.s - k.c) - a.y, t = a.x + y;
+      a.y = (t - a.x) - y;
+      a.x = t;
+      acc[(size_t)b * g + (size_t)i * ny + j] = a;
+    }
+  }
+}
+
+cudaError_t launch_avg_bins(const EventRec *recs, int n, const int *edges, int nbins, int *order, int *seg,
+                            int *counts, cudaStream_t st) {
+  k_avg_bins<<<1, 32, 0, st>>>(recs, n, edges, nbins, order, seg, counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_avg_binned(const DevParams &P, const float *rho, const double4 *frame, const int *order,
+                              const int *seg, int nbins, float2 *acc, cudaStream_t st) {
+  dim3 grid((P.ny + 15) / 16, (P.nx + 15) / 16);
+  k_avg_binned<<<grid, 256, 0, st>>>(P, rho, frame, order, seg, nbins, acc);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_avg_init(const DevParams &P, int n, const EventRec *recs, const Source *srcs, AvgSrc *state,
                             int grid, cudaStream_t st) {
   k_avg_init<<<grid, kAT, 0, st>>>(P, n, recs, srcs, state);
   return cudaGetLastError();
 }
 cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Source *srcs, AvgSrc *state,
-                                 const float *rho, int order, int mode, int grid, cudaStream_t st) {
-  k_avg_transform<<<grid, kAT, 0, st>>>(P, n, recs, srcs, state, rho, order, mode);
+                                 const float *rho, int order, int mode, int grid, cudaStream_t st, double4 *frame) {
+  k_avg_transform<<<grid, kAT, 0, st>>>(P, n, recs, srcs, state, rho, order, mode, frame);
   return cudaGetLastError();
 }
 cudaError_t launch_avg_accum(const float *rho, int n, size_t cells, double *acc, cudaStream_t st) {

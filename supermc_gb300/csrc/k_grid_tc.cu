@@ -495,6 +495,14 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
 
 constexpr int kCT = 256;   // threads of k_moments
 
+// shared memory of k_moments: the hot-spot mask [nx][ceil(ny/32)] words, x - x_cm
+// [nx], y - y_cm [ny rounded up to 32], then the reduction slots, 16-byte aligned
+__host__ __device__ inline size_t moments_red_offset(int nx, int ny) {
+  const size_t nyp = (ny + 31) / 32 * 32;
+  const size_t b = sizeof(uint32_t) * (size_t)nx * (nyp / 32) + sizeof(float) * (nx + nyp);
+  return (b + 15) / 16 * 16;
+}
+
 // ---------------------------------------------------------------- moments
 // Eccentricities of each event from its density grid and centre-of-mass
 // sums (MakeDensity::dumpEccentricities, src/MakeDensity.cpp:2244-2511).
@@ -503,11 +511,11 @@ __global__ void __launch_bounds__(kCT) k_moments(DevParams P, int n_events, cons
                                                  const Source *srcs, const float *rho_ev, const double *cm_ev,
                                                  double *out_ecc) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int nx = P.nx, ny = P.ny, nyp = (ny + 31) / 32 * 32;
+  const int nx = P.nx, ny = P.ny;
   uint32_t *mask = reinterpret_cast<uint32_t *>(smem);
-  float *xo = reinterpret_cast<float *>(smem + sizeof(uint32_t) * (size_t)nx * (nyp / 32));
+  float *xo = reinterpret_cast<float *>(smem + sizeof(uint32_t) * (size_t)nx * ((ny + 31) / 32));
   float *yo = xo + nx;
-  float2 *red = reinterpret_cast<float2 *>(yo + nyp);
+  float2 *red = reinterpret_cast<float2 *>(smem + moments_red_offset(nx, ny));
   const int tid = threadIdx.x;
   for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
     const EventRec rec = recs[e];
@@ -520,11 +528,7 @@ __global__ void __launch_bounds__(kCT) k_moments(DevParams P, int n_events, cons
   }
 }
 
-size_t moments_smem(const DevParams &P) {
-  const int nyp = (P.ny + 31) / 32 * 32;
-  return sizeof(uint32_t) * (size_t)P.nx * (nyp / 32) + sizeof(float) * (P.nx + nyp) +
-         sizeof(float2) * (kCT / 32) * 64;
-}
+size_t moments_smem(const DevParams &P) { return moments_red_offset(P.nx, P.ny) + sizeof(float2) * (kCT / 32) * 64; }
 
 size_t grid_tc_smem(const DevParams &P) { return tc_layout(P.nx, P.ny, P.n_planes).total; }
 

@@ -186,7 +186,7 @@ struct Ctx {
   smc_params prm{};
   DevParams P{};
   smc_info info{};
-  int device = 0, sms = 0;
+  int device = 0, sms = 0, dev_smem = 0;
   cudaStream_t own = nullptr, st = nullptr;
   int occ1 = 1, occ2 = 1;
   bool use_tc = true;   // tensor-core splat for the batched paths (when the profile allows it)
@@ -220,6 +220,11 @@ struct Ctx {
   smc::TangentIO tio{};
   std::vector<double> h_adj;
   DevBuf<smc::AvgSrc> avg_state;
+  // binned averages: event frames, bin order, bin segments and counts,
+  // bin edges, per-bin compensated sums
+  DevBuf<double4> avg_frame;
+  DevBuf<int> avg_order, avg_seg, avg_count, avg_edges;
+  DevBuf<float2> avg_bins;
   DevBuf<float> avg_rho;
   DevBuf<double> avg_acc;
   std::vector<int> h_status;
@@ -610,7 +615,7 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
   P.max_src = 2 * (p.Aproj + p.Atarg) + P.max_coll;
   P.ecc_from = p.ecc_from_order; P.ecc_to = p.ecc_to_order;
   P.want_ta = P.want_tb = 0;
-  P.n_planes = p.which_mc_model == 5 ? 3 : 2;   // largest layout, checked below
+  P.n_planes = p.which_mc_model == 5 ? 1 : 2;   // smallest layout, checked below; T_A/T_B requests at each call
   double d_max = p.shape_of_nucleons == 1 ? 2. * std::sqrt(P.dsq) : 5. * width;
   double span = std::max(2 * d_max, 8 * std::max(width, p.quark_width));
   P.splat_mw = (int)(span / std::min(p.dx, p.dy)) + 3;
@@ -625,9 +630,8 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
   I.kln_tmax = P.kln_tmax; I.kln_dT = P.kln_dT; I.A = p.Aproj; I.B = p.Atarg;
 
   size_t smem2 = smc::grid_smem(P);
-  int dev_smem = 0;
-  cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
-  if ((int)smem2 > dev_smem) { smc_destroy(c); return SMC_ERR_CONFIG; }
+  cudaDeviceGetAttribute(&c->dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  if ((int)smem2 > c->dev_smem) { smc_destroy(c); return SMC_ERR_CONFIG; }
   // persistent grid sizes from the occupancy the kernels reach
   c->occ1 = std::max(1, (int)(227 * 1024 / (smc::sample_pair_smem() + 1024)));
   c->occ1 = std::min(c->occ1, 8);
@@ -651,6 +655,8 @@ void smc_destroy(void *ctx) {
   c->attempts.release(); c->wounded.release(); c->rho_ev.release(); c->corr_ev.release(); c->cm_ev.release();
   c->mix_sys.release(); c->mix_ev.release(); c->mix_order.release(); c->kln64.release(); c->kln32.release();
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
+  c->avg_frame.release(); c->avg_order.release(); c->avg_seg.release(); c->avg_count.release();
+  c->avg_edges.release(); c->avg_bins.release();
   c->adj_rho.release(); c->adj_lam.release(); c->adj_grho.release(); c->adj_geps.release(); c->adj_out.release();
   c->icdf_tab[0].release(); c->icdf_tab[1].release(); c->ntan.release(); c->inj_tp.release(); c->inj_tt.release();
   c->stan.release();
@@ -686,6 +692,8 @@ static smc_status set_thickness_flags(Ctx *c, const smc_outputs *out) {
   // sqrt(T_A T_B) scaling rho_A, rho_B
   P.n_planes = P.which_mc_model == 5 ? ((P.want_ta || P.want_tb) ? 3 : 1) : 2;
   if (P.ny > 512) return SMC_ERR_CONFIG;
+  // the CUDA-core splat's accumulator strip must fit (T_A, T_B on a wide grid may not)
+  if ((int)smc::grid_smem(P) > c->dev_smem) return SMC_ERR_CONFIG;
   c->occ2 = smc::grid_blocks_per_sm(P);
   return SMC_OK;
 }
@@ -995,6 +1003,90 @@ smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_
   for (size_t k = 0; k < g * norders; k++) mean[k] = h[k] / used * ff;
   if (rp)
     for (size_t k = 0; k < g * norders; k++) mean_rp[k] = h[g * norders + k] / used * ff;
+  return SMC_OK;
+}
+
+smc_status smc_average_binned(void *ctx, uint64_t first_event, int n, int order, int method, int nbins,
+                              const int *npart_edges, double *mean, int *counts) {
+  if (!ctx || !mean || !npart_edges || n < 0 || order < 1 || order > 9 || nbins < 1 || nbins > 64 ||
+      (method != 0 && method != 1))
+    return SMC_ERR_ARGUMENT;
+  for (int k = 0; k < nbins; k++)
+    if (npart_edges[k] > npart_edges[k + 1]) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  CK(cudaSetDevice(c->device));
+  smc_outputs none{};
+  smc_status s = set_thickness_flags(c, &none);
+  if (s) return s;
+  DevParams P = c->P;
+  P.no_moments = 1;
+  const size_t g = (size_t)P.nx * P.ny;
+  CK(c->avg_bins.ensure(g * nbins));
+  CK(c->avg_count.ensure(nbins));
+  CK(c->avg_seg.ensure(nbins + 1));
+  CK(c->avg_edges.ensure(nbins + 1));
+  CK(cudaMemsetAsync(c->avg_bins.p, 0, sizeof(float2) * g * nbins, c->st));
+  CK(cudaMemsetAsync(c->avg_count.p, 0, sizeof(int) * nbins, c->st));
+  CK(cudaMemcpyAsync(c->avg_edges.p, npart_edges, sizeof(int) * (nbins + 1), cudaMemcpyHostToDevice, c->st));
+  for (int off = 0; off < n; off += c->chunk) {
+    const int m = std::min(c->chunk, n - off);
+    CK(c->recs.ensure(m));
+    CK(c->srcs.ensure((size_t)m * P.max_src));
+    CK(c->status.ensure(m));
+    CK(c->avg_rho.ensure((size_t)m * g));
+    CK(c->ecc.ensure((size_t)m * smc::kEccLen));
+    CK(c->avg_frame.ensure(m));
+    CK(c->avg_order.ensure(m));
+    if (method == 0) CK(c->avg_state.ensure((size_t)m * P.max_src));
+    const int grid1 = std::max(1, std::min(m, c->sms * c->occ1));
+    const int grid3 = std::max(1, std::min(m, c->sms * 4));
+    auto splat = [&]() {
+      return timed(c, 1, [&] {
+        return launch_splat(c, P, m, c->recs.p, c->srcs.p, c->avg_rho.p, nullptr, nullptr, nullptr, c->ecc.p,
+                            c->status.p);
+      });
+    };
+    CK(timed(c, 0, [&] {
+      return smc::launch_sample_pair(P, first_event + off, m, nullptr, nullptr, nullptr, c->recs.p, c->srcs.p,
+                                     nullptr, nullptr, grid1, c->st);
+    }));
+    if (method == 0) CK(smc::launch_avg_init(P, m, c->recs.p, c->srcs.p, c->avg_state.p, grid3, c->st));
+    CK(splat());
+    // method 0: MCnucl::rotateGrid (src/MCnucl.cpp:1152-1174) and a second
+    // splat; method 1: the frame only, the density is resampled below
+    CK(smc::launch_avg_transform(P, m, c->recs.p, c->srcs.p, c->avg_state.p, c->avg_rho.p, order,
+                                 method == 0 ? 1 : 2, grid3, c->st, c->avg_frame.p));
+    if (method == 0) CK(splat());
+    CK(smc::launch_avg_bins(c->recs.p, m, c->avg_edges.p, nbins, c->avg_order.p, c->avg_seg.p, c->avg_count.p,
+                            c->st));
+    CK(timed(c, 1, [&] {
+      return smc::launch_avg_binned(P, c->avg_rho.p, method == 1 ? c->avg_frame.p : nullptr, c->avg_order.p,
+                                    c->avg_seg.p, nbins, c->avg_bins.p, c->st);
+    }));
+    c->stats.launches += method == 0 ? 3 : 2;
+    c->h_status.resize(m);
+    CK(cudaMemcpyAsync(c->h_status.data(), c->status.p, sizeof(int) * m, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    collect_timing(c);
+    c->stats.events += m;
+    int worst = 0;
+    for (int e = 0; e < m; e++) worst = std::max(worst, c->h_status[e]);
+    if (worst) return status_error(worst);
+  }
+  std::vector<float2> h(g * nbins);
+  std::vector<int> cnt(nbins);
+  CK(cudaMemcpyAsync(h.data(), c->avg_bins.p, sizeof(float2) * h.size(), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(cnt.data(), c->avg_count.p, sizeof(int) * nbins, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  // MakeDensity::setSd (src/MakeDensity.cpp:2514-2522): entropy = rho * finalFactor
+  const double ff = c->P.final_factor;
+  for (int b = 0; b < nbins; b++) {
+    if (counts) counts[b] = cnt[b];
+    for (size_t k = 0; k < g; k++) {
+      const float2 a = h[(size_t)b * g + k];
+      mean[(size_t)b * g + k] = cnt[b] ? ((double)a.x - (double)a.y) / cnt[b] * ff : 0.0;
+    }
+  }
   return SMC_OK;
 }
 

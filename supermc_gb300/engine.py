@@ -187,6 +187,20 @@ class Engine:
         self.last_average_events = used.value
         return mean, mean_rp
 
+    def average_binned(self, first_event: int, n: int, npart_edges, order: int = 2, method: int = 1):
+        """Npart-binned event averages of rho * finalFactor, each event
+        recentred and rotated to its order-n participant plane: method 0
+        moves and re-splats the sources (the reference's method), method 1
+        resamples the density bilinearly.  Returns (mean [nbins,nx,ny],
+        counts [nbins])."""
+        edges = np.ascontiguousarray(npart_edges, dtype=np.int32)
+        nb = len(edges) - 1
+        mean = np.zeros((nb, self.nx, self.ny))
+        counts = np.zeros(nb, dtype=np.int32)
+        _lib.check(self.lib.smc_average_binned(self.h, first_event, n, order, method, nb, _lib.ptr(edges),
+                                               _lib.ptr(mean), _lib.ptr(counts)), "smc_average_binned")
+        return mean, counts
+
     def adjoint(self, first_event: int, n: int, g_eps=None, g_rho=None, xy_proj=None, xy_targ=None, b=None,
                 tangent_proj=None, tangent_targ=None):
         """Gradients of L = sum_e g_eps[e,0] |eps_2| + g_eps[e,1] |eps_3| +

@@ -115,3 +115,19 @@ def test_tensor_core_generated_kln_vs_cuda_core():
     np.testing.assert_allclose(tc["ecc"], cc["ecc"], rtol=1e-5, atol=1e-5)
     eps25 = [5 * (n - 1) + c for n in range(2, 6) for c in range(4)]
     assert np.median(np.abs(tc["ecc"][:, eps25] - cc["ecc"][:, eps25]).max(axis=1)) < 1e-6
+
+
+@pytest.mark.parametrize("over", [dict(maxx=15, maxy=15),                            # 301 x 301
+                                  dict(maxx=12.5, maxy=12.5, dx=0.05, dy=0.05),      # 501 x 501
+                                  dict(maxx=13, maxy=11.3, dx=0.1, dy=0.1)])         # 261 x 227
+def test_grid_sizes_vs_oracle(oracle, over):
+    """Grid shapes whose shared-memory layouts differ from 261 x 261 (odd
+    word counts of the hot-spot mask), both splat paths against the oracle."""
+    vals = values(SYSTEMS["auau200"], **over)
+    pa, pb, bs, res = _oracle_events(oracle, vals, 4, 41)
+    tc, cc = _both_paths(vals, pa, pb, bs, ("ecc", "npart", "ncoll", "rho"))
+    for k, (np_, nc, rho, ecc) in enumerate(res):
+        for out in (tc, cc):
+            assert tuple(out["npart"][k]) == np_ and out["ncoll"][k] == nc
+            assert np.abs(out["rho"][k] - rho).max() <= GRID_RTOL * rho.max()
+            assert_ecc_close(out["ecc"][k], ecc)
