@@ -305,6 +305,91 @@ def mixed_batch(dev, stream, n: int) -> dict:
                        "MC-Glauber 261x261, one smc_generate_mixed call"}
 
 
+# differentiable Pb+Pb Glauber (radii by inverse CDF, so that positions move
+# with R and a): 4096 events at seed 7, w = 0.5 fm, alpha = 0.118
+DIFF_PARAMS = {
+    "which_mc_model": 5, "sub_model": 1, "aproj": 208, "atarg": 208, "proj_r": 6.62, "proj_a": 0.546,
+    "targ_r": 6.62, "targ_a": 0.546, "sigininn_override": 64.0, "ecm": 2760.0, "shape_of_nucleons": 4,
+    "gauss_nucl_width": 0.5, "collision_criterion": 1, "shape_of_entropy": 2, "quark_width": 0.3, "alpha": 0.118,
+    "bmin": 0.0, "bmax": 20.0, "npmin": 2, "npmax": 500, "maxx": 13.0, "maxy": 13.0, "dx": 0.1, "dy": 0.1,
+    "finalfactor": 40.0, "ecc_from_order": 2, "ecc_to_order": 3, "cc_fluctuation_model": 0, "ws_inverse_cdf": 1,
+}
+
+
+def differentiable_batch(stream, n: int = 4096) -> dict:
+    """Forward (smc_generate) and backward (smc_adjoint: forward recomputed,
+    then the adjoint kernel) of <|eps_2|> over n events; rates in events/s."""
+    import numpy as np
+    import torch
+    from supermc_gb300.engine import Engine
+    eng = Engine(dict(DIFF_PARAMS), seed=7)
+    eng.set_stream(stream.cuda_stream)
+    g = np.zeros((n, 2))
+    g[:, 0] = 1.0 / n
+    eng.generate(0, n, want=("ecc",))
+    eng.adjoint(0, n, g_eps=g)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.generate(0, n, want=("ecc",))
+    t1 = time.perf_counter()
+    eng.reset_stats()
+    eng.set_timing(True)
+    grad, _ = eng.adjoint(0, n, g_eps=g)
+    t2 = time.perf_counter()
+    st = eng.stats()
+    eng.close()
+    return {"forward": n / (t1 - t0), "forward_backward": n / (t2 - t1), "unit": "events/s", "events": n,
+            "adjoint_kernel_ms": st["post_ms"], "grad_mean_eps2": {"w": grad[0], "alpha": grad[1], "R": grad[2],
+                                                                   "a": grad[3]},
+            "workload": "Pb+Pb 2.76 TeV, sigma_NN=64 mb, radii by inverse CDF, w=0.5 fm, alpha=0.118, 261x261"}
+
+
+AVG_BASE = {
+    "which_mc_model": 5, "sub_model": 1, "shape_of_nucleons": 4, "gauss_nucl_width": 0.5, "collision_criterion": 1,
+    "shape_of_entropy": 2, "quark_width": 0.3, "alpha": 0.118, "bmin": 0.0, "bmax": 20.0, "npmin": 2,
+    "npmax": 500, "maxx": 12.5, "maxy": 12.5, "dx": 0.05, "dy": 0.05, "finalfactor": 40.0, "ecc_from_order": 2,
+    "ecc_to_order": 2, "cc_fluctuation_model": 0,
+}
+AVG_SYSTEMS = {
+    "Pb+Pb": ({"aproj": 208, "atarg": 208, "proj_r": 6.62, "proj_a": 0.546, "targ_r": 6.62, "targ_a": 0.546,
+               "sigininn_override": 64.0, "ecm": 2760.0}, [2, 20, 40, 60, 80, 100, 150, 200, 250, 300, 417]),
+    "O+O": ({"aproj": 16, "atarg": 16, "proj_r": 2.608, "proj_a": 0.513, "targ_r": 2.608, "targ_a": 0.513,
+             "sigininn_override": 68.0, "ecm": 7000.0}, [2, 4, 6, 8, 10, 12, 14, 16, 20, 25, 33]),
+}
+
+
+def binned_average(stream, n: int) -> dict:
+    """Npart-binned averages on the 501x501 grid (recentred, rotated to the
+    second-order plane by bilinear resampling): events/s per system and the
+    HBM roofline of the binned resampling kernel."""
+    import torch
+    from supermc_gb300.engine import Engine
+    hbm_peak, _, peak_kind = peaks()
+    out = {}
+    for name, (sysp, edges) in AVG_SYSTEMS.items():
+        eng = Engine(dict(AVG_BASE, **sysp), seed=3)
+        eng.set_stream(stream.cuda_stream)
+        eng.average_binned(0, min(n, 4096), edges, order=2, method=1)
+        torch.cuda.synchronize()
+        eng.reset_stats()
+        eng.set_timing(True)
+        t0 = time.perf_counter()
+        _, counts = eng.average_binned(4096, n, edges, order=2, method=1)
+        dt = time.perf_counter() - t0
+        st = eng.stats()
+        cells = eng.nx * eng.ny
+        bytes_ev = 4.0 * cells   # one FP32 density read per event (bin sums stay on chip per chunk)
+        achieved = bytes_ev * n / (st["post_ms"] / 1e3) / 1e9 if st["post_ms"] > 0 else None
+        out[name] = {"value": n / dt, "unit": "events/s", "events": n, "counts": counts.tolist(),
+                     "sample_ms": st["sample_ms"], "splat_ms": st["grid_ms"], "binned_ms": st["post_ms"],
+                     "binned_roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                                         "frac": achieved / hbm_peak if achieved else None,
+                                         "work": "4*Nx*Ny bytes per event (its density, read once)",
+                                         "peak_kind": peak_kind}}
+        eng.close()
+    return out
+
+
 # ------------------------------------------------------------------ GPU arm
 def run_gpu(args, vals) -> dict | None:
     import numpy as np
@@ -417,6 +502,8 @@ def run_gpu(args, vals) -> dict | None:
     # ---- mixed-system batch (p+Pb, d+Au, Cu+Cu, deformed U+U, Au+Au in the
     # proportions 1:2:2:2:3, MC-Glauber), one smc_generate_mixed call
     mixed = mixed_batch(dev, stream, args.mixed_events)
+    diff = differentiable_batch(stream) if args.side_workloads else None
+    binned = binned_average(stream, args.binned_events) if args.side_workloads else None
 
     # ---- plain per-event path, same workload (sample)
     m = args.plain_events
@@ -471,6 +558,8 @@ def run_gpu(args, vals) -> dict | None:
             "plain_gpu": {"value": plain, "unit": "events/s", "events": m,
                           "batched_over_plain": value / plain},
             "mixed_batch": mixed,
+            "differentiable": diff,
+            "binned_average_501": binned,
             "batched_cuda_core_splat": {"value": cuda_core, "unit": "events/s", "events": n,
                                         "note": "same batched path, FP32 CUDA-core splat (smc_set_grid_path 0)"},
             "eps_abs_err_vs_fp64_oracle": err, "init_s": t_init}
@@ -490,6 +579,8 @@ def main():
     ap.add_argument("--events", type=int, default=EVENTS_PER_STEP)
     ap.add_argument("--plain-events", type=int, default=200)
     ap.add_argument("--mixed-events", type=int, default=20000)
+    ap.add_argument("--binned-events", type=int, default=32768)
+    ap.add_argument("--side-workloads", type=int, default=1, help="differentiable and 501^2 binned workloads")
     ap.add_argument("--ref-events", type=int, default=1600, help="reference arm: events per step (all cores)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--seed", type=int, default=1)

@@ -256,6 +256,9 @@ typedef struct smc_stats {
   uint64_t launches;        /* kernels launched                             */
   uint64_t sample_launches, grid_launches;
   double sample_ms, grid_ms;/* summed kernel durations (timing enabled)     */
+  uint64_t post_launches;   /* kernels after the splat: the binned
+                               accumulation, the adjoint                    */
+  double post_ms;
 } smc_stats;
 smc_status smc_set_timing(void *ctx, int enabled);
 /* Splat implementation of the batched entry points (smc_generate,

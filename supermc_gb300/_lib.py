@@ -74,7 +74,8 @@ class SmcInfo(ctypes.Structure):
 class SmcStats(ctypes.Structure):
     _fields_ = [("events", ctypes.c_uint64), ("attempts", ctypes.c_uint64), ("launches", ctypes.c_uint64),
                 ("sample_launches", ctypes.c_uint64), ("grid_launches", ctypes.c_uint64),
-                ("sample_ms", ctypes.c_double), ("grid_ms", ctypes.c_double)]
+                ("sample_ms", ctypes.c_double), ("grid_ms", ctypes.c_double),
+                ("post_launches", ctypes.c_uint64), ("post_ms", ctypes.c_double)]
 
 
 class SmcOutputs(ctypes.Structure):

@@ -255,10 +255,14 @@ __global__ void k_avg_bins(const EventRec *recs, int n, const int *edges, int nb
 // under the recentring and rotation, R(-phi) (x', y') + (X, Y), by bilinear
 // interpolation (corners beyond the grid read zero); without, the cell's
 // value.  One thread per output cell, 16 x 16 cells per CTA, events in bin
-// order with one compensated sum in registers per bin.
-__global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const float *rho, const double4 *frame,
-                                                   const int *order, const int *seg, int nbins, float2 *acc) {
+// order with one compensated sum in registers per bin.  A CTA skips an
+// event whose density (zero outside its windows' bounding box) cannot reach
+// the tile: the preimage of the tile's corners lies beyond that box.
+__global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const EventRec *recs, const float *rho,
+                                                   const double4 *frame, const int *order, const int *seg,
+                                                   int nbins, float2 *acc) {
   const int i = blockIdx.y * 16 + (threadIdx.x >> 4), j = blockIdx.x * 16 + (threadIdx.x & 15);
+  const int ti0 = blockIdx.y * 16, tj0 = blockIdx.x * 16;   // the tile's first cell
   const int nx = P.nx, ny = P.ny;
   const bool in = i < nx && j < ny;
   const size_t g = (size_t)nx * ny;
@@ -270,11 +274,28 @@ __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const float *rh
     const int e0 = seg[b], e1 = seg[b + 1];
     for (int q = e0; q < e1; q++) {
       const int e = order[q];
+      const EventRec &r = recs[e];
       const float *G = rho + (size_t)e * g;
       float v = 0.f;
-      if (!in) continue;
       if (frame) {
         const double4 f = frame[e];
+        // preimage of the tile's corner cells, in grid units (uniform over the CTA)
+        {
+          const float c = (float)f.z, s = (float)f.w;
+          float lo_x = 1e30f, hi_x = -1e30f, lo_y = 1e30f, hi_y = -1e30f;
+#pragma unroll
+          for (int corner = 0; corner < 4; corner++) {
+            const float cx = (float)(P.xmin + (ti0 + (corner & 1) * 15) * P.dx);
+            const float cy = (float)(P.ymin + (tj0 + (corner >> 1) * 15) * P.dy);
+            const float qx = (c * cx + s * cy + (float)f.x - xmin) * inv_dx;
+            const float qy = (-s * cx + c * cy + (float)f.y - ymin) * inv_dy;
+            lo_x = fminf(lo_x, qx); hi_x = fmaxf(hi_x, qx);
+            lo_y = fminf(lo_y, qy); hi_y = fmaxf(hi_y, qy);
+          }
+          // bilinear corners floor(p), floor(p) + 1 against the box [imin, imax)
+          if (hi_x < r.imin - 1 || lo_x >= r.imax || hi_y < r.jmin - 1 || lo_y >= r.jmax) continue;
+        }
+        if (!in) continue;
         const float c = (float)f.z, s = (float)f.w;
         // preimage in grid units
         const float px = (c * xo + s * yo + (float)f.x - xmin) * inv_dx;
@@ -291,6 +312,8 @@ __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const float *rh
           v = (1.f - tx) * ((1.f - ty) * v00 + ty * v01) + tx * ((1.f - ty) * v10 + ty * v11);
         }
       } else {
+        if (ti0 >= r.imax || ti0 + 16 <= r.imin || tj0 >= r.jmax || tj0 + 16 <= r.jmin) continue;
+        if (!in) continue;
         v = G[(size_t)i * ny + j];
       }
       k.add(v);
@@ -312,10 +335,10 @@ cudaError_t launch_avg_bins(const EventRec *recs, int n, const int *edges, int n
   return cudaGetLastError();
 }
 
-cudaError_t launch_avg_binned(const DevParams &P, const float *rho, const double4 *frame, const int *order,
-                              const int *seg, int nbins, float2 *acc, cudaStream_t st) {
+cudaError_t launch_avg_binned(const DevParams &P, const EventRec *recs, const float *rho, const double4 *frame,
+                              const int *order, const int *seg, int nbins, float2 *acc, cudaStream_t st) {
   dim3 grid((P.ny + 15) / 16, (P.nx + 15) / 16);
-  k_avg_binned<<<grid, 256, 0, st>>>(P, rho, frame, order, seg, nbins, acc);
+  k_avg_binned<<<grid, 256, 0, st>>>(P, recs, rho, frame, order, seg, nbins, acc);
   return cudaGetLastError();
 }
 

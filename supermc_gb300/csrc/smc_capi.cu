@@ -262,7 +262,8 @@ cudaError_t timed(Ctx *c, int kind, F &&launch) {
   }
   c->stats.launches++;
   if (kind == 0) c->stats.sample_launches++;
-  else c->stats.grid_launches++;
+  else if (kind == 1) c->stats.grid_launches++;
+  else c->stats.post_launches++;
   return e;
 }
 
@@ -272,7 +273,8 @@ void collect_timing(Ctx *c) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
       if (p.first == 0) c->stats.sample_ms += ms;
-      else c->stats.grid_ms += ms;
+      else if (p.first == 1) c->stats.grid_ms += ms;
+      else c->stats.post_ms += ms;
     }
   }
   c->pending.clear();
@@ -883,7 +885,7 @@ smc_status smc_adjoint(void *ctx, uint64_t first_event, int n, const double *xy_
         grho = c->adj_grho.p;
       }
     }
-    CK(timed(c, 1, [&] {
+    CK(timed(c, 2, [&] {
       return smc::launch_adjoint(P, m, c->recs.p, c->srcs.p, tangents ? c->stan.p : nullptr, c->adj_rho.p, grho,
                                  geps, c->adj_lam.p, c->adj_out.p, grid, c->st);
     }));
@@ -1059,8 +1061,8 @@ smc_status smc_average_binned(void *ctx, uint64_t first_event, int n, int order,
     if (method == 0) CK(splat());
     CK(smc::launch_avg_bins(c->recs.p, m, c->avg_edges.p, nbins, c->avg_order.p, c->avg_seg.p, c->avg_count.p,
                             c->st));
-    CK(timed(c, 1, [&] {
-      return smc::launch_avg_binned(P, c->avg_rho.p, method == 1 ? c->avg_frame.p : nullptr, c->avg_order.p,
+    CK(timed(c, 2, [&] {
+      return smc::launch_avg_binned(P, c->recs.p, c->avg_rho.p, method == 1 ? c->avg_frame.p : nullptr, c->avg_order.p,
                                     c->avg_seg.p, nbins, c->avg_bins.p, c->st);
     }));
     c->stats.launches += method == 0 ? 3 : 2;

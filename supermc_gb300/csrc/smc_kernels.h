@@ -47,8 +47,8 @@ cudaError_t launch_avg_bins(const EventRec *recs, int n, const int *edges, int n
                             int *counts, cudaStream_t st);
 // per-bin compensated sums acc [nbins][nx][ny] of the chunk's densities,
 // bilinearly resampled in each event's frame (frame != NULL) or as they are
-cudaError_t launch_avg_binned(const DevParams &P, const float *rho, const double4 *frame, const int *order,
-                              const int *seg, int nbins, float2 *acc, cudaStream_t st);
+cudaError_t launch_avg_binned(const DevParams &P, const EventRec *recs, const float *rho, const double4 *frame,
+                              const int *order, const int *seg, int nbins, float2 *acc, cudaStream_t st);
 cudaError_t launch_avg_accum(const float *rho, int n, size_t cells, double *acc, cudaStream_t st);
 // Adjoint of a batch (k_adjoint, one CTA per event in turn): per-event
 // gradients dtheta [n][4] = (dL/dw, dL/dalpha, dL/dR, dL/da; the last two
