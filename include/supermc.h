@@ -84,6 +84,12 @@ typedef struct smc_params {
                                             rejection, so that positions are
                                             differentiable in R and a
                                             (smc_adjoint); spherical A > 2 */
+  int cc_fluctuation_model;              /* 0 none; 6: mean-one Gamma weight per
+                                            participant and binary collision
+                                            (MCnucl.cpp:1271-1301; the
+                                            reference's parameters.dat default);
+                                            1-5 (per-cell NBD) unsupported  */
+  double cc_fluctuation_gamma_theta;     /* Gamma scale (cc_fluctuation_Gamma_theta) */
 } smc_params;
 
 /* Derived constants (MCnucl::MCnucl, src/MCnucl.cpp:22-154). */

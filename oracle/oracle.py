@@ -67,6 +67,7 @@ class Params(ctypes.Structure):
         ("final_factor", ctypes.c_double),
         ("npmin", ctypes.c_int), ("npmax", ctypes.c_int),
         ("kln_table", _D), ("kln_tmax", ctypes.c_int), ("kln_dT", ctypes.c_double),
+        ("cc_fluctuation_model", ctypes.c_int), ("cc_fluctuation_gamma_theta", ctypes.c_double),
     ]
 
 
@@ -149,6 +150,9 @@ class Oracle:
         lib.smco_kln_dndy.argtypes = [ctypes.POINTER(KLN), ctypes.c_double, ctypes.c_double,
                                       ctypes.c_int, ctypes.c_int, ctypes.c_int]
         lib.smco_gauss_legendre01.argtypes = [ctypes.c_int, _D, _D]
+        lib.smco_gamma_philox.restype = ctypes.c_double
+        lib.smco_gamma_philox.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint32,
+                                          ctypes.c_double, ctypes.c_double]
         lib.smco_set_pair_stream.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
         lib.smco_run_ecc_table.restype = ctypes.c_long
         lib.smco_run_ecc_table.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(Nucleus),

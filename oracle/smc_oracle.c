@@ -55,7 +55,7 @@ void smco_uniform2(uint64_t seed, uint64_t event, uint32_t stream, uint32_t slot
 }
 
 /* stream ids (low byte of the stream word; the retry attempt is above) */
-enum { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4 };
+enum { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5 };
 static uint32_t stream_id(int attempt, int sid) { return ((uint32_t)attempt << 8) | (uint32_t)sid; }
 
 /* ================================================================== */
@@ -679,6 +679,38 @@ static int hit(const smco_event *e, const nucleon_t *p1, const nucleon_t *p2, do
 static uint64_t g_pair_seed, g_pair_event;
 static int g_pair_attempt, g_pair_philox;
 
+/* Gamma(k, theta) from the Philox stream of one source: the method of
+ * Marsaglia and Tsang ("A simple method for generating gamma variables",
+ * ACM TOMS 26 (2000) 363), with Gamma(k) = Gamma(k+1) U^(1/k) for k < 1 and
+ * Box-Muller normals.  Iteration t draws counters 32 slot + 2t, 2t + 1
+ * (t < 15), the k < 1 uniform counter 32 slot + 31.  The reference draws
+ * the same distribution from GSL (gsl_ran_gamma, MCnucl.cpp:1285,1298). */
+double smco_gamma_philox(uint64_t seed, uint64_t event, int attempt, uint32_t slot, double k, double theta) {
+  uint32_t sid = stream_id(attempt, ST_FLUCT);
+  double kk = k < 1 ? k + 1 : k;
+  double d = kk - 1.0 / 3.0, c = 1.0 / sqrt(9.0 * d);
+  double g = d; /* after 15 rejections (probability below 1e-19) */
+  for (int t = 0; t < 15; t++) {
+    double u[2], w[2];
+    smco_uniform2(seed, event, sid, 32 * slot + 2 * t, u);
+    smco_uniform2(seed, event, sid, 32 * slot + 2 * t + 1, w);
+    double x = sqrt(-2.0 * log(1.0 - u[0])) * cos(2.0 * M_PI * u[1]);
+    double v = 1.0 + c * x;
+    if (v <= 0) continue;
+    v = v * v * v;
+    if (log(1.0 - w[0]) < 0.5 * x * x + d - d * v + d * log(v)) {
+      g = d * v;
+      break;
+    }
+  }
+  if (k < 1) {
+    double u[2];
+    smco_uniform2(seed, event, sid, 32 * slot + 31, u);
+    g *= pow(1.0 - u[0], 1.0 / k);
+  }
+  return g * theta;
+}
+
 void smco_set_pair_stream(uint64_t seed, uint64_t event, int attempt, int philox) {
   g_pair_seed = seed;
   g_pair_event = event;
@@ -857,11 +889,31 @@ int smco_event_thickness(smco_event *e) {
   return 0;
 }
 
+/* MCnucl::sampleFluctuationFactorforParticipant / ...forBinaryCollision
+ * (MCnucl.cpp:1271-1301), cc_fluctuation_model 6: mean-one Gamma weights,
+ * k = (1 - alpha + eps)/(2 theta) per participant and (alpha + eps)/theta
+ * per binary collision.  Slots: participant i (sorted order) of nucleus w
+ * is w A + i; collision (i, j) is A + B + i B + j. */
+static double part_fluct(const smco_event *e, int w, int i) {
+  if (e->p.cc_fluctuation_model != 6) return 1.0;
+  const double eps = 1e-8, th = e->p.cc_fluctuation_gamma_theta;
+  const double k = (1 - e->p.alpha + eps) / 2. / th, theta = 2. / (1 - e->p.alpha + eps) * th;
+  return smco_gamma_philox(g_pair_seed, g_pair_event, g_pair_attempt, (uint32_t)(w ? e->n[0] + i : i), k, theta);
+}
+static double coll_fluct(const smco_event *e, int c) {
+  if (e->p.cc_fluctuation_model != 6) return 1.0;
+  const double eps = 1e-8, th = e->p.cc_fluctuation_gamma_theta;
+  const double k = (e->p.alpha + eps) / th, theta = th / (e->p.alpha + eps);
+  uint32_t slot = (uint32_t)(e->n[0] + e->n[1] + e->cpa[c] * e->n[1] + e->cpb[c]);
+  return smco_gamma_philox(g_pair_seed, g_pair_event, g_pair_attempt, slot, k, theta);
+}
+
 /* MCnucl::addDensity (MCnucl.cpp:822-866), shape_of_entropy 1 and 2 */
 static void add_density(smco_event *e, int w, double *dens) {
   double Xmin = -e->p.xmax, Ymin = -e->p.ymax, dx = e->p.dx, dy = e->p.dy;
   for (int k = 0; k < e->npart[w]; k++) {
     const nucleon_t *q = &e->nuc[w][e->part[w][k]];
+    const double f = part_fluct(e, w, e->part[w][k]);   /* Particle::getSmoothDensity's fluctfactor */
     double x = q->x, y = q->y;
     int xl = (int)((q->box.xl - Xmin) / dx), xr = (int)((q->box.xr - Xmin) / dx);
     int yl = (int)((q->box.yl - Ymin) / dy), yr = (int)((q->box.yr - Ymin) / dy);
@@ -876,9 +928,9 @@ static void add_density(smco_event *e, int w, double *dens) {
         double dc = (x - xg) * (x - xg) + (y - yg) * (y - yg);
         if (e->p.shape_of_entropy == 1) {
           if (dc > e->p.dsq) continue;
-          G(dens, ir, jr) += 10.0 / e->p.sigin * 1.0;
+          G(dens, ir, jr) += 10.0 / e->p.sigin * f;
         } else {
-          G(dens, ir, jr) += smooth_tn(e->p.width, x, y, xg, yg) * 1.0;
+          G(dens, ir, jr) += smooth_tn(e->p.width, x, y, xg, yg) * f;
         }
       }
     }
@@ -900,6 +952,7 @@ static double powi(double x, int m) {
 }
 
 static double peak_height(double w) { return 1 / (2 * M_PI * w * w); }
+
 
 int smco_event_density(smco_event *e) {
   size_t g = (size_t)e->p.nx * e->p.ny;
@@ -943,6 +996,7 @@ int smco_event_density(smco_event *e) {
       for (int c = 0; c < e->ncoll; c++) {
         double x = e->cx[c], y = e->cy[c];
         double fw = alpha + (1. - alpha) * e->caw[c];
+        double f = coll_fluct(e, c);   /* CollisionPair::getfluctfactor, MCnucl.cpp:730-731 */
         int xl, xr, yl, yr;
         window(e, x - d_max, x + d_max, Xmin, dx, e->p.nx, &xl, &xr);
         window(e, y - d_max, y + d_max, Ymin, dy, e->p.ny, &yl, &yr);
@@ -952,11 +1006,11 @@ int smco_event_density(smco_event *e) {
             double yg = Ymin + jr * dy;
             double dc = (x - xg) * (x - xg) + (y - yg) * (y - yg);
             if (e->p.shape_of_entropy == 1) {
-              if (dc <= e->p.dsq) tab[(size_t)ir * e->p.ny + jr] += 1.0 * (10.0 / e->p.sigin) * fw;
+              if (dc <= e->p.dsq) tab[(size_t)ir * e->p.ny + jr] += f * (10.0 / e->p.sigin) * fw;
             } else {
               if (dc <= dc_sq_max)
                 tab[(size_t)ir * e->p.ny + jr] +=
-                    1.0 * peak_height(w) * exp(-dc / (2 * w2)) * fw;
+                    f * peak_height(w) * exp(-dc / (2 * w2)) * fw;
             }
           }
         }
@@ -1011,6 +1065,7 @@ int smco_event_density_moved(smco_event *e, double w, double alpha, const double
     for (int nw = 0; nw < 2; nw++)
       for (int k = 0; k < e->npart[nw]; k++) {
         const nucleon_t *q = &e->nuc[nw][e->part[nw][k]];
+        const double f = part_fluct(e, nw, e->part[nw][k]);
         double x = q->x, y = q->y;
         double mx = x, my = y;
         if (disp[nw]) { mx += disp[nw][2 * q->id]; my += disp[nw][2 * q->id + 1]; }
@@ -1026,7 +1081,7 @@ int smco_event_density_moved(smco_event *e, double w, double alpha, const double
             double r = sqrt((xg - x) * (xg - x) + (yg - y) * (yg - y));
             if (r > 5 * w0) continue;
             double r2 = (xg - mx) * (xg - mx) + (yg - my) * (yg - my);
-            G(rho, ir, jr) += pre * peak_height(w) * exp(-r2 / (2 * w * w));
+            G(rho, ir, jr) += f * pre * peak_height(w) * exp(-r2 / (2 * w * w));
           }
       }
   } else if (e->p.sub_model != 2) {
@@ -1039,6 +1094,7 @@ int smco_event_density_moved(smco_event *e, double w, double alpha, const double
     if (dA) { mx += 0.5 * dA[2 * pa->id]; my += 0.5 * dA[2 * pa->id + 1]; }
     if (dB) { mx += 0.5 * dB[2 * pb->id]; my += 0.5 * dB[2 * pb->id + 1]; }
     double fw = alpha + (1. - alpha) * e->caw[c];
+    double f = coll_fluct(e, c);
     int xl, xr, yl, yr;
     window(e, x - d_max, x + d_max, Xmin, dx, e->p.nx, &xl, &xr);
     window(e, y - d_max, y + d_max, Ymin, dy, e->p.ny, &yl, &yr);
@@ -1048,7 +1104,7 @@ int smco_event_density_moved(smco_event *e, double w, double alpha, const double
         double dc = (x - xg) * (x - xg) + (y - yg) * (y - yg);
         if (dc > 25. * w0 * w0) continue;
         double dm = (mx - xg) * (mx - xg) + (my - yg) * (my - yg);
-        G(rho, ir, jr) += peak_height(w) * exp(-dm / (2 * w * w)) * fw;
+        G(rho, ir, jr) += f * peak_height(w) * exp(-dm / (2 * w * w)) * fw;
       }
   }
   return 0;

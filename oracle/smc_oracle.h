@@ -69,7 +69,15 @@ typedef struct {
   const double *kln_table;
   int kln_tmax;
   double kln_dT;
+  /* multiplicity fluctuations: 6 = Gamma-distributed weight per participant
+   * and binary collision (MCnucl.cpp:1271-1301), drawn from the Philox
+   * streams set by smco_set_pair_stream; 0 = none */
+  int cc_fluctuation_model;
+  double cc_fluctuation_gamma_theta;
 } smco_params;
+/* Gamma(k, theta) variate of one source (slot) of an event's fluctuation
+ * stream */
+double smco_gamma_philox(uint64_t seed, uint64_t event, int attempt, uint32_t slot, double k, double theta);
 
 typedef struct smco_event smco_event;
 smco_event *smco_event_new(const smco_params *p);

@@ -59,6 +59,7 @@ class SmcParams(ctypes.Structure):
         ("seed", ctypes.c_uint64),
         ("max_attempts", ctypes.c_int), ("max_collisions", ctypes.c_int),
         ("ws_inverse_cdf", ctypes.c_int),
+        ("cc_fluctuation_model", ctypes.c_int), ("cc_fluctuation_gamma_theta", ctypes.c_double),
     ]
 
 

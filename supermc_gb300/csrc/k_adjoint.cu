@@ -207,12 +207,13 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
         ly *= ex;
         lr = ex * lr + dx2 * l0;   // sum lambda e (dx^2 + dy^2)
         const float W = s.weight;
-        // W = peak (1-a)/2 for participants; peak (a + (1-a) aw) for binary
-        // collisions, aw in {0, 1, 2} (nonzero with sub_model 2 only)
-        float dWda = -0.5f * peak;
+        // W = f peak (1-a)/2 for participants, f peak (a + (1-a) aw) for
+        // binary collisions (aw in {0, 1, 2}, nonzero with sub_model 2; f the
+        // multiplicity weight, held fixed, 1 without fluctuations)
+        float dWda = alpha < 1.f ? -W / (1.f - alpha) : -0.5f * peak;
         if (kind == SRC_COLL) {
-          const float aw = alpha < 1.f ? rintf((W / peak - alpha) / (1.f - alpha)) : 0.f;
-          dWda = peak * (1.f - aw);
+          const float aw = (float)((s.kind >> SRC_AW_SHIFT) & 3);
+          dWda = W * (1.f - aw) / (alpha + (1.f - alpha) * aw);
         }
         dw += W * (lr / (float)(w * w * w) - 2.f * l0 / (float)w);
         da += dWda * l0;

@@ -428,6 +428,39 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
   __syncthreads();
 }
 
+// Gamma(k, theta) weight of one source (slot) from the event's fluctuation
+// stream: the method of Marsaglia and Tsang ("A simple method for
+// generating gamma variables", ACM TOMS 26 (2000) 363) with
+// Gamma(k) = Gamma(k+1) U^(1/k) for k < 1 and Box-Muller normals; iteration
+// t draws counters 32 slot + 2t, 2t + 1 (t < 15), the k < 1 uniform counter
+// 32 slot + 31.  The reference draws the same distribution from GSL
+// (gsl_ran_gamma, src/MCnucl.cpp:1271-1301).
+__device__ double gamma_weight(uint64_t seed, uint64_t ev, int attempt, uint32_t slot, double k, double theta) {
+  const uint32_t sid = stream_id(attempt, ST_FLUCT);
+  const double kk = k < 1 ? k + 1 : k;
+  const double d = kk - 1.0 / 3.0, c = 1.0 / sqrt(9.0 * d);
+  double g = d;   // after 15 rejections (probability below 1e-19)
+  for (int t = 0; t < 15; t++) {
+    double u0, u1, w0, w1;
+    uniform2(seed, ev, sid, 32 * slot + 2 * t, u0, u1);
+    uniform2(seed, ev, sid, 32 * slot + 2 * t + 1, w0, w1);
+    const double x = sqrt(-2.0 * log(1.0 - u0)) * cos(2.0 * M_PI * u1);
+    double v = 1.0 + c * x;
+    if (v <= 0) continue;
+    v = v * v * v;
+    if (log(1.0 - w0) < 0.5 * x * x + d - d * v + d * log(v)) {
+      g = d * v;
+      break;
+    }
+  }
+  if (k < 1) {
+    double u0, u1;
+    uniform2(seed, ev, sid, 32 * slot + 31, u0, u1);
+    g *= pow(1.0 - u0, 1.0 / k);
+  }
+  return g * theta;
+}
+
 // tangent of nucleon k (sorted order, projectile first) of event e
 __device__ __forceinline__ float4 nucleon_tangent(const double *ntan, int e, int AB, int k) {
   const double *t = ntan + ((size_t)e * AB + k) * 4;
@@ -781,6 +814,10 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
             s.plane = (model == 7 && w == 1) ? 1 : 0;
             s.weight = disk_e ? disk_val * (model == 5 ? (float)((1.0 - P.alpha) / 2.) : 1.f)
                               : peak * (model == 5 ? (float)((1.0 - P.alpha) / 2.) : 1.f);
+            // Particle::getSmoothDensity's multiplicity factor (MCnucl::selectFluctFactors)
+            if (P.fluct)
+              s.weight = (float)((double)s.weight *
+                                 gamma_weight(P.seed, ev, attempt, (uint32_t)k, P.fluct_k_part, P.fluct_th_part));
             // a Woods-Saxon nucleon is constructed at its nucleus-frame
             // position and then moved (Nucleus::populate,
             // src/Nucleus.cpp:274-309, Particle::setX/setY): its base box
@@ -843,11 +880,14 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
           set_window(s, s.x - d_max, s.x + d_max, P.xmin, P.dx, inv_dx, P.nx, true);
           set_window(s, s.y - d_max, s.y + d_max, P.ymin, P.dy, inv_dy, P.ny, false);
           s.mx0 = s.mx1 = s.my0 = s.my1 = 0;
-          s.kind = SRC_COLL | (disk_e ? 16 : 0);
           s.plane = 0;
           double aw = 0.;
           if (model == 5 && P.sub_model == 2) aw = (double)(1 / c) + (double)(1 / sm.hits[1][j]);
+          s.kind = SRC_COLL | (disk_e ? 16 : 0) | ((int)aw << SRC_AW_SHIFT);
           double fw = P.alpha + (1. - P.alpha) * aw;
+          // CollisionPair::getfluctfactor (src/MCnucl.cpp:730-731)
+          if (P.fluct)
+            fw *= gamma_weight(P.seed, ev, attempt, (uint32_t)(AB + tid * B + j), P.fluct_k_coll, P.fluct_th_coll);
           s.weight = (float)((disk_e ? 10.0 / P.sigin : P.peak) * fw);
           s.bx = s.by = 0.f;
           if (stan) {

@@ -297,6 +297,9 @@ smc_status validate(const smc_params &p) {
   if (!(p.dx > 0) || !(p.dy > 0) || !(p.maxx > 0) || !(p.maxy > 0)) return SMC_ERR_CONFIG;
   if (p.ecc_from_order < 1 || p.ecc_to_order > 9 || p.ecc_from_order > p.ecc_to_order) return SMC_ERR_CONFIG;
   if (p.bmax < p.bmin || p.bmin < 0) return SMC_ERR_CONFIG;
+  // multiplicity fluctuations: none, or the Gamma weights of model 6
+  if (p.cc_fluctuation_model != 0 && p.cc_fluctuation_model != 6) return SMC_ERR_CONFIG;
+  if (p.cc_fluctuation_model == 6 && !(p.cc_fluctuation_gamma_theta > 0)) return SMC_ERR_CONFIG;
   // inverse-CDF radii: spherical Woods-Saxon nuclei
   if (p.ws_inverse_cdf && (p.Aproj < 3 || p.Atarg < 3 || p.proj_deformed || p.targ_deformed)) return SMC_ERR_CONFIG;
   return SMC_OK;
@@ -591,6 +594,14 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
   P.sigin = sigin;
   P.sigma_gg = sigma_gg_from(sigin, width);
   P.alpha = p.alpha; P.final_factor = p.final_factor;
+  if (p.cc_fluctuation_model == 6) {   // MCnucl.cpp:1271-1301
+    const double eps = 1e-8, th = p.cc_fluctuation_gamma_theta;
+    P.fluct = 1;
+    P.fluct_k_part = (1 - p.alpha + eps) / 2. * (1. / th);
+    P.fluct_th_part = 2. / (1 - p.alpha + eps) * th;
+    P.fluct_k_coll = (p.alpha + eps) * (1. / th);
+    P.fluct_th_coll = 1. / (p.alpha + eps) * th;
+  }
   P.which_mc_model = p.which_mc_model; P.sub_model = p.sub_model;
   P.shape_of_nucleons = p.shape_of_nucleons; P.shape_of_entropy = p.shape_of_entropy;
   P.collision_criterion = p.collision_criterion;

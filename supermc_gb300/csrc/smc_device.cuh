@@ -15,6 +15,7 @@ enum SrcKind : int {
   SRC_COLL = 1,       // binary collision, +-d_max window, dc <= 25 w^2 (MCnucl::setDensity)
   SRC_THICK = 2,      // participant, +-d_max window, r <= 5w (MCnucl::setThickness)
   SRC_RAW_BASE = 32,  // flag: participant box built at (bx, by), then moved
+  SRC_AW_SHIFT = 6,   // bits 6-7: a binary collision's additional weight (sub_model 2)
 };
 
 // One source of the density/thickness splat.  Windows are grid index
@@ -88,6 +89,10 @@ struct DevParams {
   int splat_mw;             // widest splat window in columns (+ margin)
   int n_planes;             // accumulator planes of the splat (1..3)
   int no_moments;           // skip the eccentricity pass (averaged mode)
+  // multiplicity fluctuations (cc_fluctuation_model 6): Gamma(k, theta)
+  // weights per participant and per binary collision
+  int fluct;
+  double fluct_k_part, fluct_th_part, fluct_k_coll, fluct_th_coll;
 };
 
 // Per-event record written by the sampling/pairing stage.
@@ -131,7 +136,7 @@ __host__ __device__ __forceinline__ void uniform2(uint64_t seed, uint64_t event,
   u1 = u53(c[2], c[3]);
 }
 
-enum StreamId : uint32_t { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4 };
+enum StreamId : uint32_t { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5 };
 __host__ __device__ __forceinline__ uint32_t stream_id(int attempt, uint32_t sid) {
   return ((uint32_t)attempt << 8) | sid;
 }

@@ -145,6 +145,8 @@ extern "C" smc_status smc_inject_noalloc(const smc_params *params, int n, const 
   if (p.Aproj < 1 || p.Atarg < 1 || p.Aproj > smc::kMaxA || p.Atarg > smc::kMaxA) return SMC_ERR_CONFIG;
   if (!(p.dx > 0) || !(p.dy > 0) || !(p.maxx > 0) || !(p.maxy > 0)) return SMC_ERR_CONFIG;
   if (p.ecc_from_order < 1 || p.ecc_to_order > 9 || p.ecc_from_order > p.ecc_to_order) return SMC_ERR_CONFIG;
+  if (p.cc_fluctuation_model != 0 && p.cc_fluctuation_model != 6) return SMC_ERR_CONFIG;
+  if (p.cc_fluctuation_model == 6 && !(p.cc_fluctuation_gamma_theta > 0)) return SMC_ERR_CONFIG;
   if (n == 0) return SMC_OK;
 
   smc::DevParams P{};
@@ -162,6 +164,14 @@ extern "C" smc_status smc_inject_noalloc(const smc_params *params, int n, const 
   P.sigin = sigin;
   P.sigma_gg = na_sigma_gg(sigin, width);
   P.alpha = p.alpha; P.final_factor = p.final_factor;
+  if (p.cc_fluctuation_model == 6) {   // Gamma weights, MCnucl.cpp:1271-1301
+    const double eps = 1e-8, th = p.cc_fluctuation_gamma_theta;
+    P.fluct = 1;
+    P.fluct_k_part = (1 - p.alpha + eps) / 2. * (1. / th);
+    P.fluct_th_part = 2. / (1 - p.alpha + eps) * th;
+    P.fluct_k_coll = (p.alpha + eps) * (1. / th);
+    P.fluct_th_coll = 1. / (p.alpha + eps) * th;
+  }
   P.which_mc_model = p.which_mc_model; P.sub_model = p.sub_model;
   P.shape_of_nucleons = p.shape_of_nucleons; P.shape_of_entropy = p.shape_of_entropy;
   P.collision_criterion = p.collision_criterion;

@@ -44,6 +44,8 @@ def smc_params_from(vals: dict[str, float], seed: int = 1) -> _lib.SmcParams:
     p.max_attempts = int(v["max_attempts"])
     p.max_collisions = int(v["max_collisions"])
     p.ws_inverse_cdf = int(v["ws_inverse_cdf"])
+    p.cc_fluctuation_model = int(v["cc_fluctuation_model"])
+    p.cc_fluctuation_gamma_theta = v["cc_fluctuation_gamma_theta"]
     return p
 
 

@@ -31,7 +31,9 @@ def oracle_params(vals: dict, sigma_gg: float | None = None):
                   sub_model=int(vals["sub_model"]), shape_of_nucleons=int(vals["shape_of_nucleons"]),
                   shape_of_entropy=int(vals["shape_of_entropy"]),
                   collision_criterion=int(vals["collision_criterion"]), final_factor=vals["finalfactor"],
-                  npmin=int(vals["npmin"]), npmax=int(vals["npmax"]))
+                  npmin=int(vals["npmin"]), npmax=int(vals["npmax"]),
+                  cc_fluctuation_model=int(vals["cc_fluctuation_model"]),
+                  cc_fluctuation_gamma_theta=vals["cc_fluctuation_gamma_theta"])
 
 
 def fmt8(a):

@@ -240,3 +240,28 @@ def test_autograd_wrt_woods_saxon_parameters(icdf_events):
     g[:, 0] = 1.0 / n
     grad, _ = eng.adjoint(0, n, g_eps=g)
     np.testing.assert_allclose([float(w.grad), float(al.grad), float(R.grad), float(a.grad)], grad, rtol=1e-12)
+
+
+def test_adjoint_with_multiplicity_fluctuations(oracle):
+    """Gamma-weighted sources (cc_fluctuation_model 6, weights held fixed):
+    w and alpha gradients against the oracle's frozen density with the same
+    weights (its Philox stream of each injected event)."""
+    vals = values(PBPB2760, ecc_from_order=2, ecc_to_order=3, cc_fluctuation_model=6)
+    pa, pb, bs = _events(oracle, values(PBPB2760), 4, 19)
+    from supermc_gb300.engine import Engine
+    eng = Engine({k: v for k, v in vals.items()}, seed=7)
+    rng = np.random.default_rng(2)
+    g_eps = rng.uniform(-1, 1, (4, 2))
+    g_rho = rng.uniform(0, 1, (4, eng.nx, eng.ny)).astype(np.float32)
+    _, per = eng.adjoint(0, 4, g_eps=g_eps, g_rho=g_rho, xy_proj=pa, xy_targ=pb, b=bs)
+    ev = oracle.event(oracle_params(vals))
+    X, Y = grid_coords(vals, ev.nx, ev.ny)
+    try:
+        for k in range(4):
+            oracle.lib.smco_set_pair_stream(7, k, 0, 1)
+            ev.inject(pa[k], pb[k])
+            ev.pair()
+            fd = fd_gradient(ev, ev.hotspot_mask(), X, Y, vals["gauss_nucl_width"], vals["alpha"], g_eps[k], g_rho[k])
+            np.testing.assert_allclose(per[k, :2], fd, rtol=REL)
+    finally:
+        oracle.lib.smco_set_pair_stream(0, 0, 0, 0)

@@ -125,6 +125,10 @@ def test_injected_random_events_vs_oracle(oracle, name):
     dict(shape_of_nucleons=1, shape_of_entropy=1),       # disk nucleons
     dict(collision_criterion=2),                         # Gaussian collision profile
     dict(alpha=0.0),
+    dict(cc_fluctuation_model=6),                        # Gamma multiplicity weights
+    dict(cc_fluctuation_model=6, sub_model=2),
+    dict(cc_fluctuation_model=6, which_mc_model=7),
+    dict(cc_fluctuation_model=6, shape_of_entropy=1),
 ])
 def test_model_variants_vs_oracle(oracle, over):
     vals = values(SYSTEMS["auau200"], **over)

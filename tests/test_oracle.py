@@ -204,3 +204,16 @@ def test_average_sequence_matches_reference(oracle, golden, name):
         scale = np.abs(g[key + "values"]).max()
         np.testing.assert_allclose(grid[cells[:, 0], cells[:, 1]], g[key + "values"], rtol=0, atol=1e-10 * scale)
         np.testing.assert_allclose(grid.sum(axis=1), g[key + "rowsum"], rtol=0, atol=1e-9 * scale)
+
+
+@pytest.mark.parametrize("k,theta", [((1 - 0.118) / 2 / 0.75, 2 / (1 - 0.118) * 0.75),   # participant, default
+                                     (0.118 / 0.75, 0.75 / 0.118),                      # binary collision
+                                     (2.5, 0.4)])
+def test_gamma_weights_follow_the_gamma_distribution(oracle, k, theta):
+    """The multiplicity weights of cc_fluctuation_model 6 (the reference
+    draws them with gsl_ran_gamma, MCnucl.cpp:1285,1298): KS against
+    Gamma(k, theta), unit mean."""
+    from scipy import stats
+    x = np.array([oracle.lib.smco_gamma_philox(11, ev, 0, s, k, theta) for ev in range(4) for s in range(5000)])
+    assert stats.kstest(x, "gamma", args=(k, 0, theta)).pvalue > 1e-3
+    assert abs(x.mean() - k * theta) < 5 * np.sqrt(k * theta * theta / len(x))
