@@ -176,6 +176,15 @@ smc_status smc_inject(void *ctx, int n, const double *xy_proj, const double *xy_
 smc_status smc_generate_mixed(void *ctx, const smc_params *systems, int nsys, uint64_t first_event, int n,
                               const int *system_of_event, const smc_outputs *out);
 
+/* smc_generate as one CUDA graph: the launch sequence of the whole batch
+ * (every chunk's sampling, splat and eccentricity kernels, the per-event
+ * status reduced on the device, no host synchronisation in between) is
+ * captured on the first call for a given n, output set and launch
+ * configuration -- that call runs eagerly -- and replayed by later calls
+ * with new event ids (an on-device event-id base).  Device outputs only
+ * (out->device != 0); the results equal smc_generate's. */
+smc_status smc_generate_graph(void *ctx, uint64_t first_event, int n, const smc_outputs *out);
+
 /* Plain per-event path: the same results as smc_generate, one event per
  * kernel launch sequence (the unbatched baseline). */
 smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_outputs *out);
@@ -277,6 +286,19 @@ smc_status smc_set_timing(void *ctx, int enabled);
  * shape_of_entropy != 1).  0: the FP32 CUDA-core splat.  The plain path
  * (smc_generate_plain) always uses the CUDA-core splat. */
 smc_status smc_set_grid_path(void *ctx, int tensor_cores);
+/* Launch-configuration autotuner (no reference counterpart): times the
+ * context's own workload -- n_events events (0: 8192) of smc_generate with
+ * device outputs, event ids from 2^62 on -- for each splat path
+ * (tensor-core contraction, CUDA-core splat) and events per launch
+ * (2048, 4096, 8192), keeps the fastest for the context's later calls and
+ * reports the rates (events/s, tensor-core path first; 0 where a path does
+ * not apply).  Both paths give the same results within FP32 rounding. */
+typedef struct smc_tuning {
+  int tensor_cores;         /* chosen splat path                            */
+  int chunk;                /* chosen events per launch                     */
+  double events_per_s[6];   /* (tensor cores, CUDA cores) x (2048, 4096, 8192) */
+} smc_tuning;
+smc_status smc_autotune(void *ctx, int n_events, smc_tuning *out);
 smc_status smc_get_stats(void *ctx, smc_stats *stats);
 smc_status smc_reset_stats(void *ctx);
 

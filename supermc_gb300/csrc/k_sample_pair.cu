@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
                                                      const double *inj_b, EventRec *recs, Source *srcs,
                                                      double *out_pos, uint8_t *out_wounded,
                                                      const SystemDev *systems, const int *ev_sys,
-                                                     const int *order, TangentIO tio) {
+                                                     const int *order, TangentIO tio, const uint64_t *ev_base) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SampleSmem &sm = *reinterpret_cast<SampleSmem *>(smem_raw);
   __shared__ DevParams s_P;   // the context's parameters with the event's system
@@ -619,7 +619,7 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
     // with a hit radius well inside the box width every hit pair is swept, so
     // all pairs are tested; otherwise the sweep's tested set is reproduced.
     const bool swept = P.collision_criterion != 1 || sqrt(P.dsq) > 7.9 * fmax(P.width, P.quark_width);
-    const uint64_t ev = first_event + (uint64_t)e;
+    const uint64_t ev = (ev_base ? *ev_base : 0) + first_event + (uint64_t)e;
     int status = 0, attempt = 0, ncoll = 0, np1 = 0, np2 = 0;
     for (;; attempt++) {
       if (attempt >= P.max_attempts) { status = 3; break; }
@@ -950,7 +950,7 @@ cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, i
                                      const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
                                      double *out_pos, uint8_t *out_wounded, const SystemDev *systems,
                                      const int *ev_sys, const int *order, int grid, cudaStream_t st,
-                                     const TangentIO *tio) {
+                                     const TangentIO *tio, const uint64_t *ev_base) {
   size_t smem = sizeof(SampleSmem);
   static bool attr = false;
   if (!attr) {
@@ -959,7 +959,7 @@ cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, i
     attr = true;
   }
   k_sample_pair<<<grid, kNT, smem, st>>>(P, first_event, n_events, inj_proj, inj_targ, inj_b, recs, srcs, out_pos,
-                                         out_wounded, systems, ev_sys, order, tio ? *tio : TangentIO{});
+                                         out_wounded, systems, ev_sys, order, tio ? *tio : TangentIO{}, ev_base);
   return cudaGetLastError();
 }
 

@@ -2,6 +2,7 @@
 // derived constants (MCnucl::MCnucl, src/MCnucl.cpp:22-154), device buffers,
 // batching and the two-stage launch sequence.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -219,6 +220,17 @@ struct Ctx {
   DevBuf<float4> stan;
   smc::TangentIO tio{};
   std::vector<double> h_adj;
+  // captured batch (smc_generate_graph): the instantiated graph and what it
+  // was captured for, the device event-id base and worst status, and their
+  // pinned host copies
+  cudaGraphExec_t graph = nullptr;
+  int graph_n = 0, graph_chunk = 0, graph_launches = 0;
+  bool graph_tc = false;
+  smc_outputs graph_out{};
+  DevBuf<uint64_t> ev_base;
+  DevBuf<int> worst;
+  uint64_t *h_first = nullptr;
+  int *h_worst = nullptr;
   DevBuf<smc::AvgSrc> avg_state;
   // binned averages: event frames, bin order, bin segments and counts,
   // bin edges, per-bin compensated sums
@@ -371,6 +383,14 @@ __global__ void k_scalars(const EventRec *r, int n, int *npart, int *ncoll, doub
   if (ncoll) ncoll[e] = r[e].ncoll;
   if (b) b[e] = r[e].b;
   if (attempts) attempts[e] = r[e].attempts;
+}
+
+// worst per-event status of a chunk into *worst (atomic max)
+__global__ void k_status_max(const int *status, int n, int *worst) {
+  int v = 0;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) v = max(v, status[e]);
+  for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0 && v) atomicMax(worst, v);
 }
 
 // Batched splat of one chunk: the tensor-core contraction where the profile
@@ -673,6 +693,10 @@ void smc_destroy(void *ctx) {
   c->adj_rho.release(); c->adj_lam.release(); c->adj_grho.release(); c->adj_geps.release(); c->adj_out.release();
   c->icdf_tab[0].release(); c->icdf_tab[1].release(); c->ntan.release(); c->inj_tp.release(); c->inj_tt.release();
   c->stan.release();
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  c->ev_base.release(); c->worst.release();
+  if (c->h_first) cudaFreeHost(c->h_first);
+  if (c->h_worst) cudaFreeHost(c->h_worst);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -1101,6 +1125,155 @@ smc_status smc_average_binned(void *ctx, uint64_t first_event, int n, int order,
     }
   }
   return SMC_OK;
+}
+
+// The launch sequence of a whole batch with device outputs and no host
+// synchronisation: event ids from the device value ev_base, the worst
+// event status reduced on the device and copied to h_worst at the end.
+// Buffers must already have their sizes (no allocation: it is captured).
+smc_status enqueue_batch(Ctx *c, int n, const smc_outputs *out, int *launches) {
+  const DevParams &P = c->P;
+  const size_t g = (size_t)P.nx * P.ny;
+  const int AB = c->info.A + c->info.B;
+  int nl = 0;
+  CK(cudaMemcpyAsync(c->ev_base.p, c->h_first, sizeof(uint64_t), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(c->worst.p, 0, sizeof(int), c->st));
+  for (int off = 0; off < n; off += c->chunk) {
+    const int m = std::min(c->chunk, n - off);
+    double *ecc = out->ecc ? out->ecc + (size_t)off * smc::kEccLen : c->ecc.p;
+    float *rho = out->rho ? out->rho + (size_t)off * g : nullptr;
+    float *ta = out->ta ? out->ta + (size_t)off * g : nullptr;
+    float *tb = out->tb ? out->tb + (size_t)off * g : nullptr;
+    double *pos = out->positions ? out->positions + (size_t)off * 2 * AB : nullptr;
+    uint8_t *wnd = out->wounded ? out->wounded + (size_t)off * AB : nullptr;
+    smc::TangentIO tio{};
+    tio.ntan = out->tangents ? out->tangents + (size_t)off * 4 * AB : nullptr;
+    const int grid1 = std::max(1, std::min(m, c->sms * c->occ1));
+    CK(smc::launch_sample_pair_mixed(P, off, m, nullptr, nullptr, nullptr, c->recs.p, c->srcs.p, pos, wnd, nullptr,
+                                     nullptr, nullptr, grid1, c->st, &tio, c->ev_base.p));
+    CK(launch_splat(c, P, m, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p));
+    nl += 2 + ((c->use_tc && smc::grid_tc_supported(P) && !P.no_moments) ? 1 : 0);
+    int *np = out->npart ? out->npart + 2 * off : nullptr;
+    int *nc = out->ncoll ? out->ncoll + off : nullptr;
+    double *bb = out->b ? out->b + off : nullptr;
+    int *at = out->attempts ? out->attempts + off : nullptr;
+    if (np || nc || bb || at) {
+      k_scalars<<<(m + 255) / 256, 256, 0, c->st>>>(c->recs.p, m, np, nc, bb, at);
+      CK(cudaGetLastError());
+      nl++;
+    }
+    k_status_max<<<(m + 255) / 256, 256, 0, c->st>>>(c->status.p, m, c->worst.p);
+    CK(cudaGetLastError());
+    nl++;
+  }
+  CK(cudaMemcpyAsync(c->h_worst, c->worst.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  *launches = nl;
+  return SMC_OK;
+}
+
+smc_status smc_autotune(void *ctx, int n_events, smc_tuning *out) {
+  if (!ctx || n_events < 0) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  const int n = n_events > 0 ? n_events : 8192;
+  CK(cudaSetDevice(c->device));
+  smc_outputs none{};
+  smc_status s = set_thickness_flags(c, &none);
+  if (s) return s;
+  DevBuf<double> ecc;
+  CK(ecc.ensure((size_t)n * smc::kEccLen));
+  smc_outputs o{};
+  o.device = 1;
+  o.ecc = ecc.p;
+  const bool tc_ok = smc::grid_tc_supported(c->P);
+  static const int chunks[3] = {2048, 4096, 8192};
+  smc_tuning t{};
+  double best = -1;
+  const bool saved_timing = c->timing;
+  c->timing = false;
+  uint64_t first = (uint64_t)1 << 62;   // event ids of the trial batches
+  for (int path = 1; path >= 0; path--) {
+    for (int q = 0; q < 3; q++) {
+      const int k = (1 - path) * 3 + q;
+      t.events_per_s[k] = 0;
+      if (path == 1 && !tc_ok) continue;
+      c->use_tc = path == 1;
+      c->chunk = chunks[q];
+      s = run(c, first, std::min(n, chunks[q]), &o, nullptr, nullptr, nullptr, false);   // warm-up, buffers
+      if (s && s != SMC_ERR_ZERO_DNDY) { ecc.release(); c->timing = saved_timing; return s; }
+      first += n;
+      const auto t0 = std::chrono::steady_clock::now();
+      s = run(c, first, n, &o, nullptr, nullptr, nullptr, false);
+      const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      if (s && s != SMC_ERR_ZERO_DNDY) { ecc.release(); c->timing = saved_timing; return s; }
+      first += n;
+      t.events_per_s[k] = n / dt;
+      if (t.events_per_s[k] > best) {
+        best = t.events_per_s[k];
+        t.tensor_cores = path;
+        t.chunk = chunks[q];
+      }
+    }
+  }
+  c->timing = saved_timing;
+  c->use_tc = t.tensor_cores != 0;
+  c->chunk = t.chunk;
+  ecc.release();
+  c->stats = smc_stats{};
+  if (out) *out = t;
+  return SMC_OK;
+}
+
+smc_status smc_generate_graph(void *ctx, uint64_t first_event, int n, const smc_outputs *out) {
+  if (!ctx || !out || n < 0 || !out->device) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  if (n == 0) return SMC_OK;
+  CK(cudaSetDevice(c->device));
+  smc_status s = set_thickness_flags(c, out);
+  if (s) return s;
+  const bool same = c->graph && c->graph_n == n && c->graph_chunk == c->chunk && c->graph_tc == c->use_tc &&
+                    std::memcmp(&c->graph_out, out, sizeof(smc_outputs)) == 0;
+  if (!same) {
+    // this call runs eagerly (sizing every buffer), then the batch is captured
+    if (c->graph) {
+      cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+    }
+    s = run(c, first_event, n, out, nullptr, nullptr, nullptr, false);
+    if (s && s != SMC_ERR_ZERO_DNDY) return s;
+    CK(c->ev_base.ensure(1));
+    CK(c->worst.ensure(1));
+    if (!c->h_first) CK(cudaHostAlloc(&c->h_first, sizeof(uint64_t), cudaHostAllocDefault));
+    if (!c->h_worst) CK(cudaHostAlloc(&c->h_worst, sizeof(int), cudaHostAllocDefault));
+    CK(c->scratch.ensure((size_t)c->sms * c->occ2 * c->P.nx * c->P.ny));
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+    int launches = 0;
+    const bool timing = c->timing;
+    c->timing = false;
+    const smc_status se = enqueue_batch(c, n, out, &launches);
+    c->timing = timing;
+    const cudaError_t ee = cudaStreamEndCapture(c->st, &graph);
+    if (se) {
+      if (graph) cudaGraphDestroy(graph);
+      return se;
+    }
+    CK(ee);
+    const cudaError_t ei = cudaGraphInstantiate(&c->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ei);
+    c->graph_n = n;
+    c->graph_chunk = c->chunk;
+    c->graph_tc = c->use_tc;
+    c->graph_out = *out;
+    c->graph_launches = launches;
+    return s;
+  }
+  *c->h_first = first_event;
+  CK(cudaGraphLaunch(c->graph, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->stats.launches += c->graph_launches;
+  c->stats.events += n;
+  return status_error(*c->h_worst);
 }
 
 smc_status smc_set_grid_path(void *ctx, int tensor_cores) {

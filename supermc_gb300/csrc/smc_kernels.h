@@ -17,11 +17,13 @@ cudaError_t launch_sample_pair(const DevParams &P, uint64_t first_event, int n_e
                                double *out_pos, uint8_t *out_wounded, int grid, cudaStream_t st);
 // Mixed batch: event e takes the system parameters systems[ev_sys[e]]; the
 // CTAs take the events in the given order (NULL: 0, 1, ...).
+// event ids are first_event + e, plus *ev_base when ev_base is given (a
+// device value, so that a captured graph replays with new event ids)
 cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, int n_events, const double *inj_proj,
                                      const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
                                      double *out_pos, uint8_t *out_wounded, const SystemDev *systems,
                                      const int *ev_sys, const int *order, int grid, cudaStream_t st,
-                                     const TangentIO *tio = nullptr);
+                                     const TangentIO *tio = nullptr, const uint64_t *ev_base = nullptr);
 size_t grid_smem(const DevParams &P);
 int grid_blocks_per_sm(const DevParams &P);
 cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs, float *out_rho,

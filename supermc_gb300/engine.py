@@ -143,6 +143,12 @@ class Engine:
                    "smc_generate_mixed")
         return bufs
 
+    def generate_graph_into(self, first_event: int, n: int, device_bufs: dict) -> None:
+        """generate_into through smc_generate_graph: the batch's launches
+        captured once as a CUDA graph and replayed."""
+        o = self._outputs(device_bufs, True)
+        _lib.check(self.lib.smc_generate_graph(self.h, first_event, n, ctypes.byref(o)), "smc_generate_graph")
+
     def generate_into(self, first_event: int, n: int, device_bufs: dict, plain: bool = False) -> None:
         """Writes into caller-owned device tensors (keys of OUTPUT_NAMES)."""
         o = self._outputs(device_bufs, True)
@@ -236,6 +242,15 @@ class Engine:
         out = np.zeros((t, t))
         _lib.check(self.lib.smc_kln_table(self.h, _lib.ptr(out), t * t), "smc_kln_table")
         return out
+
+    def autotune(self, n_events: int = 8192) -> dict:
+        """Times the splat paths and events per launch on this context's
+        workload and keeps the fastest (smc_autotune)."""
+        t = _lib.SmcTuning()
+        _lib.check(self.lib.smc_autotune(self.h, n_events, ctypes.byref(t)), "smc_autotune")
+        names = [f"{p}_{c}" for p in ("tensor_cores", "cuda_cores") for c in (2048, 4096, 8192)]
+        return {"tensor_cores": bool(t.tensor_cores), "chunk": t.chunk,
+                "events_per_s": dict(zip(names, list(t.events_per_s)))}
 
     def set_grid_path(self, tensor_cores: bool) -> None:
         """Batched splat on the tcgen05 tensor cores (default) or the FP32 CUDA cores."""
