@@ -409,6 +409,9 @@ def run_gpu(args, vals) -> dict | None:
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
     dev = torch.device("cuda", local)
+    # launch configuration (splat path, events per launch) tuned on this
+    # workload before timing, like the context's construction
+    tuning = eng.autotune(n) if args.autotune else None
     bufs = {"ecc": torch.empty((n, 49), dtype=torch.float64, device=dev),
             "npart": torch.empty((n, 2), dtype=torch.int32, device=dev),
             "ncoll": torch.empty((n,), dtype=torch.int32, device=dev),
@@ -418,12 +421,13 @@ def run_gpu(args, vals) -> dict | None:
     def first_event(step):
         return (step * world + rank) * n
 
-    # ---- device-resident value
+    # ---- device-resident value: the batch as one CUDA graph (captured by the
+    # first warm-up step, replayed with new event ids)
+    gen = eng.generate_graph_into if args.graph else eng.generate_into
     for s in range(args.warmup):
-        eng.generate_into(first_event(s), n, bufs)
+        gen(first_event(s), n, bufs)
     torch.cuda.synchronize()
     eng.reset_stats()
-    eng.set_timing(True)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     clocks = ClockSampler(local)
@@ -434,13 +438,21 @@ def run_gpu(args, vals) -> dict | None:
     for s in range(args.steps):
         flush.fill_(float(s))            # evict L2 between timed steps (outside the events)
         starts[s].record(stream)
-        eng.generate_into(first_event(args.warmup + s), n, bufs)
+        gen(first_event(args.warmup + s), n, bufs)
         ends[s].record(stream)
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    launches = eng.stats()["launches"]
+    # per-kernel durations of the same batch, launched eagerly with CUDA
+    # events around every kernel (a graph replay records none)
+    eng.reset_stats()
+    eng.set_timing(True)
+    flush.fill_(0.5)
+    eng.generate_into(first_event(args.warmup + args.steps), n, bufs)
+    torch.cuda.synchronize()
     st = eng.stats()
     eng.set_timing(False)
     tot_ms = sum(step_ms)
@@ -486,18 +498,20 @@ def run_gpu(args, vals) -> dict | None:
             dist.destroy_process_group()
         return None
 
-    # ---- batched path with the CUDA-core splat instead of the tensor cores
-    eng.set_grid_path(False)
-    eng.generate_into(10 ** 8, n, bufs)
-    torch.cuda.synchronize()
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    eng.generate_into(10 ** 8 + n, n, bufs)
-    b.record(stream)
-    torch.cuda.synchronize()
-    cuda_core = n / (a.elapsed_time(b) / 1e3)
-    eng.set_grid_path(True)
+    # ---- the batched path with each splat (eager launches)
+    paths = {}
+    for tc in (True, False):
+        eng.set_grid_path(tc)
+        eng.generate_into(10 ** 8, n, bufs)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.generate_into(10 ** 8 + n, n, bufs)
+        b.record(stream)
+        torch.cuda.synchronize()
+        paths[tc] = n / (a.elapsed_time(b) / 1e3)
+    eng.set_grid_path(tuning["tensor_cores"] if tuning else True)
 
     # ---- mixed-system batch (p+Pb, d+Au, Cu+Cu, deformed U+U, Au+Au in the
     # proportions 1:2:2:2:3, MC-Glauber), one smc_generate_mixed call
@@ -525,11 +539,13 @@ def run_gpu(args, vals) -> dict | None:
     nsrc = float(npart.sum(axis=1).mean())     # MC-KLN: T_A, T_B sources are the participants
     flops_per_event = 2.0 * eng.nx * eng.ny * nsrc
     grid_launch_ms = st["grid_ms"] / max(1, st["grid_launches"])
-    events_per_launch = n * args.steps / max(1, st["grid_launches"])
+    events_per_launch = n / max(1, st["grid_launches"])
     achieved = flops_per_event * events_per_launch / (grid_launch_ms / 1e3) / 1e12
+    tc_used = tuning["tensor_cores"] if tuning else True
     roof = {"bound": "tensor", "achieved": achieved, "peak": tf_peak, "unit": "TFLOP/s",
             "frac": achieved / tf_peak, "traffic": None,
-            "kernel": "k_grid_tc (tcgen05 split-TF32 thickness contraction, KLN lookup, eps_n)",
+            "kernel": ("k_grid_tc (tcgen05 split-TF32 thickness contraction, KLN lookup, eps_n)" if tc_used else
+                       "k_grid (CUDA-core thickness splat, KLN lookup, eps_n)"),
             "work": "2*Nx*Ny*N_src FLOP per event (dense separable contraction), N_src = Npart",
             "peak_kind": f"bf16 dense, {peak_kind}",
             "sample_kernel_ms_per_launch": st["sample_ms"] / max(1, st["sample_launches"]),
@@ -537,7 +553,9 @@ def run_gpu(args, vals) -> dict | None:
     try:
         with open(os.path.join(HERE, "profiles", "traffic.json")) as f:
             tr = json.load(f)
-        roof["traffic"] = tr.get("k_grid_bytes_per_event", 0.0) * events_per_launch
+        key = "k_grid_tc_bytes_per_event" if tc_used else "k_grid_cc_bytes_per_event"
+        if key in tr:
+            roof["traffic"] = tr[key] * events_per_launch
     except Exception:
         pass
 
@@ -550,18 +568,21 @@ def run_gpu(args, vals) -> dict | None:
             "data": "synthetic (Monte-Carlo events from Philox streams)",
             "config": {"workload": WORKLOAD_NAME, "events_per_step": n, "grid": [eng.nx, eng.ny],
                        "parallelism": f"event data parallel, {world} GPU(s)",
-                       "l2": "256 MB buffer written between timed steps"},
+                       "l2": "256 MB buffer written between timed steps",
+                       "launch": ("one CUDA graph per step (smc_generate_graph)" if args.graph else
+                                  "eager launches (smc_generate)"),
+                       "tuning": tuning},
             "e2e": {"value": e2e, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
                     "note": "smc_generate with pinned host output buffers; per-step input is the event range"},
-            "gpu_launches": int(st["launches"]),
+            "gpu_launches": int(launches),
             "clocks": clk, "roofline": roof, "cpu_baseline": base,
             "plain_gpu": {"value": plain, "unit": "events/s", "events": m,
                           "batched_over_plain": value / plain},
             "mixed_batch": mixed,
             "differentiable": diff,
             "binned_average_501": binned,
-            "batched_cuda_core_splat": {"value": cuda_core, "unit": "events/s", "events": n,
-                                        "note": "same batched path, FP32 CUDA-core splat (smc_set_grid_path 0)"},
+            "batched_by_splat_path": {"tensor_cores": paths[True], "cuda_cores": paths[False], "unit": "events/s",
+                                      "events": n, "note": "eager smc_generate with each splat (smc_set_grid_path)"},
             "eps_abs_err_vs_fp64_oracle": err, "init_s": t_init}
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -581,6 +602,8 @@ def main():
     ap.add_argument("--mixed-events", type=int, default=20000)
     ap.add_argument("--binned-events", type=int, default=32768)
     ap.add_argument("--side-workloads", type=int, default=1, help="differentiable and 501^2 binned workloads")
+    ap.add_argument("--graph", type=int, default=1, help="time the batch as a CUDA graph (smc_generate_graph)")
+    ap.add_argument("--autotune", type=int, default=1, help="tune the launch configuration before timing")
     ap.add_argument("--ref-events", type=int, default=1600, help="reference arm: events per step (all cores)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--seed", type=int, default=1)

@@ -290,13 +290,13 @@ smc_status smc_set_grid_path(void *ctx, int tensor_cores);
  * context's own workload -- n_events events (0: 8192) of smc_generate with
  * device outputs, event ids from 2^62 on -- for each splat path
  * (tensor-core contraction, CUDA-core splat) and events per launch
- * (2048, 4096, 8192), keeps the fastest for the context's later calls and
+ * (2048, 4096, 8192, 16384), keeps the fastest for the context's later calls and
  * reports the rates (events/s, tensor-core path first; 0 where a path does
  * not apply).  Both paths give the same results within FP32 rounding. */
 typedef struct smc_tuning {
   int tensor_cores;         /* chosen splat path                            */
   int chunk;                /* chosen events per launch                     */
-  double events_per_s[6];   /* (tensor cores, CUDA cores) x (2048, 4096, 8192) */
+  double events_per_s[8];   /* (tensor cores, CUDA cores) x (2048 .. 16384)  */
 } smc_tuning;
 smc_status smc_autotune(void *ctx, int n_events, smc_tuning *out);
 smc_status smc_get_stats(void *ctx, smc_stats *stats);

@@ -90,7 +90,7 @@ class SmcOutputs(ctypes.Structure):
 
 
 class SmcTuning(ctypes.Structure):
-    _fields_ = [("tensor_cores", ctypes.c_int), ("chunk", ctypes.c_int), ("events_per_s", ctypes.c_double * 6)]
+    _fields_ = [("tensor_cores", ctypes.c_int), ("chunk", ctypes.c_int), ("events_per_s", ctypes.c_double * 8)]
 
 
 class SmcAdjointArgs(ctypes.Structure):

@@ -1185,15 +1185,15 @@ smc_status smc_autotune(void *ctx, int n_events, smc_tuning *out) {
   o.device = 1;
   o.ecc = ecc.p;
   const bool tc_ok = smc::grid_tc_supported(c->P);
-  static const int chunks[3] = {2048, 4096, 8192};
+  static const int chunks[4] = {2048, 4096, 8192, 16384};
   smc_tuning t{};
   double best = -1;
   const bool saved_timing = c->timing;
   c->timing = false;
   uint64_t first = (uint64_t)1 << 62;   // event ids of the trial batches
   for (int path = 1; path >= 0; path--) {
-    for (int q = 0; q < 3; q++) {
-      const int k = (1 - path) * 3 + q;
+    for (int q = 0; q < 4; q++) {
+      const int k = (1 - path) * 4 + q;
       t.events_per_s[k] = 0;
       if (path == 1 && !tc_ok) continue;
       c->use_tc = path == 1;

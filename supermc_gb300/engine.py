@@ -248,7 +248,7 @@ class Engine:
         workload and keeps the fastest (smc_autotune)."""
         t = _lib.SmcTuning()
         _lib.check(self.lib.smc_autotune(self.h, n_events, ctypes.byref(t)), "smc_autotune")
-        names = [f"{p}_{c}" for p in ("tensor_cores", "cuda_cores") for c in (2048, 4096, 8192)]
+        names = [f"{p}_{c}" for p in ("tensor_cores", "cuda_cores") for c in (2048, 4096, 8192, 16384)]
         return {"tensor_cores": bool(t.tensor_cores), "chunk": t.chunk,
                 "events_per_s": dict(zip(names, list(t.events_per_s)))}
 
