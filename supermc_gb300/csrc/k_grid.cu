@@ -69,7 +69,7 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
 template <int LO, int HI>
 __global__ void __launch_bounds__(kGT) k_grid(DevParams P, int n_events, const EventRec *recs, const Source *srcs,
                                               float *out_rho, float *out_ta, float *out_tb, float *scratch,
-                                              double *out_ecc, int *status) {
+                                              double *out_ecc, int *status, EventQueue q) {
   extern __shared__ __align__(16) unsigned char smem[];
   const GridLayout L = grid_layout(P.nx, P.ny, P.splat_mw, P.n_planes);
   float *acc = reinterpret_cast<float *>(smem + L.off_acc);
@@ -94,7 +94,9 @@ __global__ void __launch_bounds__(kGT) k_grid(DevParams P, int n_events, const E
   for (int i = tid; i < nx; i += kGT) xg[i] = (float)(P.xmin + i * P.dx);
   for (int j = tid; j < ny; j += kGT) yg[j] = (float)(P.ymin + j * P.dy);
 
-  for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
+  __shared__ int s_k;
+  for (int k = queue_first(q, &s_k); k < n_events; k = queue_next(q, k, &s_k)) {
+    const int e = queue_event(q, k);
     const EventRec rec = recs[e];
     const Source *S = srcs + (size_t)e * P.max_src;
     float *rho = out_rho ? out_rho + (size_t)e * nx * ny : scratch + (size_t)blockIdx.x * nx * ny;
@@ -271,13 +273,18 @@ int grid_blocks_per_sm(const DevParams &P) {
 
 cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs, float *out_rho,
                         float *out_ta, float *out_tb, float *scratch, double *out_ecc, int *status, int grid,
-                        cudaStream_t st) {
+                        cudaStream_t st, const int *order, int *ticket) {
   size_t smem = grid_smem(P);
   const bool narrow = P.ecc_from >= 2 && P.ecc_to <= 5;
   auto kern = narrow ? k_grid<2, 5> : k_grid<1, 9>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  kern<<<grid, kGT, smem, st>>>(P, n_events, recs, srcs, out_rho, out_ta, out_tb, scratch, out_ecc, status);
+  if (ticket) {
+    e = cudaMemsetAsync(ticket, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+  }
+  kern<<<grid, kGT, smem, st>>>(P, n_events, recs, srcs, out_rho, out_ta, out_tb, scratch, out_ecc, status,
+                                EventQueue{order, ticket});
   return cudaGetLastError();
 }
 

@@ -139,7 +139,7 @@ __device__ __forceinline__ bool splat_source(const Source &s) {
 __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, const EventRec *recs,
                                                     const Source *srcs, float *out_rho, float *out_ta,
                                                     float *out_tb, float *rho_ev, int *corr_scratch,
-                                                    double *cm_ev, int *status) {
+                                                    double *cm_ev, int *status, EventQueue q) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int np = P.n_planes;
   const TcLayout L = tc_layout(P.nx, P.ny, np);
@@ -186,7 +186,9 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
   const uint32_t tmem = s_tmem;
   uint32_t phase[2] = {0u, 0u};
 
-  for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
+  __shared__ int s_k;
+  for (int k = queue_first(q, &s_k); k < n_events; k = queue_next(q, k, &s_k)) {
+    const int e = queue_event(q, k);
     const EventRec rec = recs[e];
     const Source *S = srcs + (size_t)e * P.max_src;
     float *rho = (out_rho ? out_rho : rho_ev) + (size_t)e * nx * ny;
@@ -509,7 +511,7 @@ __host__ __device__ inline size_t moments_red_offset(int nx, int ny) {
 template <int LO, int HI>
 __global__ void __launch_bounds__(kCT) k_moments(DevParams P, int n_events, const EventRec *recs,
                                                  const Source *srcs, const float *rho_ev, const double *cm_ev,
-                                                 double *out_ecc) {
+                                                 double *out_ecc, EventQueue q) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nx = P.nx, ny = P.ny;
   uint32_t *mask = reinterpret_cast<uint32_t *>(smem);
@@ -517,7 +519,9 @@ __global__ void __launch_bounds__(kCT) k_moments(DevParams P, int n_events, cons
   float *yo = xo + nx;
   float2 *red = reinterpret_cast<float2 *>(smem + moments_red_offset(nx, ny));
   const int tid = threadIdx.x;
-  for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
+  __shared__ int s_k;
+  for (int k = queue_first(q, &s_k); k < n_events; k = queue_next(q, k, &s_k)) {
+    const int e = queue_event(q, k);
     const EventRec rec = recs[e];
     const double tot0 = cm_ev[3 * (size_t)e], xc = cm_ev[3 * (size_t)e + 1], yc = cm_ev[3 * (size_t)e + 2];
     for (int i = tid; i < nx; i += kCT) xo[i] = (float)((P.xmin + i * P.dx) - xc);
@@ -551,15 +555,21 @@ static int blocks_per_sm(K kern, int threads, size_t smem) {
 
 cudaError_t launch_grid_tc(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs,
                            float *out_rho, float *out_ta, float *out_tb, float *rho_ev, int *corr_scratch,
-                           double *cm_ev, double *out_ecc, int *status, int sms, cudaStream_t st) {
+                           double *cm_ev, double *out_ecc, int *status, int sms, cudaStream_t st,
+                           const int *order, int *tickets) {
   if (n_events <= 0) return cudaSuccess;
+  if (tickets) {
+    cudaError_t e = cudaMemsetAsync(tickets, 0, 2 * sizeof(int), st);
+    if (e != cudaSuccess) return e;
+  }
   // contraction, post-op, centre of mass
   {
     const size_t smem = grid_tc_smem(P);
     cudaError_t e = cudaFuncSetAttribute(k_grid_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_grid_tc<<<std::max(1, std::min(n_events, sms)), kTT, smem, st>>>(P, n_events, recs, srcs, out_rho, out_ta,
-                                                                       out_tb, rho_ev, corr_scratch, cm_ev, status);
+    k_grid_tc<<<std::max(1, std::min(n_events, sms)), kTT, smem, st>>>(
+        P, n_events, recs, srcs, out_rho, out_ta, out_tb, rho_ev, corr_scratch, cm_ev, status,
+        EventQueue{order, tickets});
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -568,8 +578,9 @@ cudaError_t launch_grid_tc(const DevParams &P, int n_events, const EventRec *rec
   const bool narrow = P.ecc_from >= 2 && P.ecc_to <= 5;
   auto kern = narrow ? k_moments<2, 5> : k_moments<1, 9>;
   const int nb = blocks_per_sm(kern, kCT, smem);
-  kern<<<std::max(1, std::min(n_events, sms * nb)), kCT, smem, st>>>(P, n_events, recs, srcs,
-                                                                    out_rho ? out_rho : rho_ev, cm_ev, out_ecc);
+  kern<<<std::max(1, std::min(n_events, sms * nb)), kCT, smem, st>>>(
+      P, n_events, recs, srcs, out_rho ? out_rho : rho_ev, cm_ev, out_ecc,
+      EventQueue{order, tickets ? tickets + 1 : nullptr});
   return cudaGetLastError();
 }
 

@@ -584,7 +584,8 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
                                                      const double *inj_b, EventRec *recs, Source *srcs,
                                                      double *out_pos, uint8_t *out_wounded,
                                                      const SystemDev *systems, const int *ev_sys,
-                                                     const int *order, TangentIO tio, const uint64_t *ev_base) {
+                                                     const int *order, TangentIO tio, const uint64_t *ev_base,
+                                                     int *ticket) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SampleSmem &sm = *reinterpret_cast<SampleSmem *>(smem_raw);
   __shared__ DevParams s_P;   // the context's parameters with the event's system
@@ -593,8 +594,11 @@ __global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t
   const bool inject = inj_proj != nullptr;
   const float inv_dx = (float)(1.0 / P_in.dx), inv_dy = (float)(1.0 / P_in.dy);
 
-  for (int k_ev = blockIdx.x; k_ev < n_events; k_ev += gridDim.x) {
-    const int e = order ? order[k_ev] : k_ev;
+  // events by ticket (retries make their costs uneven), in `order` when given
+  const EventQueue q{order, ticket};
+  __shared__ int s_k;
+  for (int k_ev = queue_first(q, &s_k); k_ev < n_events; k_ev = queue_next(q, k_ev, &s_k)) {
+    const int e = queue_event(q, k_ev);
     __syncthreads();   // s_P of the previous event is no longer read
     if (tid == 0) {
       s_P = P_in;
@@ -950,7 +954,7 @@ cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, i
                                      const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
                                      double *out_pos, uint8_t *out_wounded, const SystemDev *systems,
                                      const int *ev_sys, const int *order, int grid, cudaStream_t st,
-                                     const TangentIO *tio, const uint64_t *ev_base) {
+                                     const TangentIO *tio, const uint64_t *ev_base, int *ticket) {
   size_t smem = sizeof(SampleSmem);
   static bool attr = false;
   if (!attr) {
@@ -958,8 +962,13 @@ cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, i
     if (e != cudaSuccess) return e;
     attr = true;
   }
+  if (ticket) {
+    cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+  }
   k_sample_pair<<<grid, kNT, smem, st>>>(P, first_event, n_events, inj_proj, inj_targ, inj_b, recs, srcs, out_pos,
-                                         out_wounded, systems, ev_sys, order, tio ? *tio : TangentIO{}, ev_base);
+                                         out_wounded, systems, ev_sys, order, tio ? *tio : TangentIO{}, ev_base,
+                                         ticket);
   return cudaGetLastError();
 }
 

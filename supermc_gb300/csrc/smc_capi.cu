@@ -200,6 +200,9 @@ struct Ctx {
   // buffers of the tensor-core splat: per-event densities (when not an
   // output), per-CTA corner corrections, per-event centre-of-mass sums
   DevBuf<float> rho_ev;
+  // event queues of the batched kernels: per-chunk order (most sources
+  // first) and the tickets of the splat, moments and sampler launches
+  DevBuf<int> ev_order, tickets;
   DevBuf<int> corr_ev;
   DevBuf<double> cm_ev;
   // mixed batches: system table, per-event system of the chunk, event order
@@ -385,6 +388,27 @@ __global__ void k_scalars(const EventRec *r, int n, int *npart, int *ncoll, doub
   if (attempts) attempts[e] = r[e].attempts;
 }
 
+// The events of a chunk by decreasing source count (counting sort on
+// nsrc / 8; the order within a bin does not matter: events are independent).
+__global__ void k_order_events(const EventRec *recs, int n, int *order) {
+  __shared__ int hist[1024];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < 1024; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (int e = tid; e < n; e += blockDim.x) atomicAdd(&hist[1023 - min(recs[e].nsrc >> 3, 1023)], 1);
+  __syncthreads();
+  if (tid == 0) {
+    int acc = 0;
+    for (int b = 0; b < 1024; b++) {
+      const int c = hist[b];
+      hist[b] = acc;
+      acc += c;
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < n; e += blockDim.x) order[atomicAdd(&hist[1023 - min(recs[e].nsrc >> 3, 1023)], 1)] = e;
+}
+
 // worst per-event status of a chunk into *worst (atomic max)
 __global__ void k_status_max(const int *status, int n, int *worst) {
   int v = 0;
@@ -397,6 +421,13 @@ __global__ void k_status_max(const int *status, int n, int *worst) {
 // allows it, else the CUDA-core splat.
 cudaError_t launch_splat(Ctx *c, const DevParams &P, int n, const EventRec *recs, const Source *srcs, float *rho,
                          float *ta, float *tb, float *scratch, double *ecc, int *status) {
+  // the heaviest events first, each CTA taking the next event when it is free
+  cudaError_t eo = c->ev_order.ensure(n);
+  if (eo != cudaSuccess) return eo;
+  k_order_events<<<1, 1024, 0, c->st>>>(recs, n, c->ev_order.p);
+  eo = cudaGetLastError();
+  if (eo != cudaSuccess) return eo;
+  c->stats.launches++;
   if (c->use_tc && smc::grid_tc_supported(P)) {
     const size_t g = (size_t)P.nx * P.ny;
     cudaError_t e = c->corr_ev.ensure((size_t)c->sms * P.n_planes * g);
@@ -405,10 +436,11 @@ cudaError_t launch_splat(Ctx *c, const DevParams &P, int n, const EventRec *recs
     if (e != cudaSuccess) return e;
     c->stats.launches += P.no_moments ? 0 : 1;   // k_moments besides the timed launch
     return smc::launch_grid_tc(P, n, recs, srcs, rho, ta, tb, c->rho_ev.p, c->corr_ev.p, c->cm_ev.p, ecc, status,
-                               c->sms, c->st);
+                               c->sms, c->st, c->ev_order.p, c->tickets.p);
   }
   const int grid = std::max(1, std::min(n, c->sms * c->occ2));
-  return smc::launch_grid(P, n, recs, srcs, rho, ta, tb, scratch, ecc, status, grid, c->st);
+  return smc::launch_grid(P, n, recs, srcs, rho, ta, tb, scratch, ecc, status, grid, c->st, c->ev_order.p,
+                          c->tickets.p);
 }
 
 // One chunk of events through both stages.  Device outputs land directly in
@@ -466,7 +498,7 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
       return smc::launch_sample_pair_mixed(P, first_event, n, inj_p, inj_t, inj_b, c->recs.p, c->srcs.p, pos, wnd,
                                            c->mix_sys.p && c->mixing ? c->mix_sys.p : nullptr,
                                            c->mixing ? c->mix_ev.p : nullptr, c->mixing ? c->mix_order.p : nullptr,
-                                           grid1, c->st, &tio);
+                                           grid1, c->st, &tio, nullptr, c->tickets.p + 2);
     }));
     CK(timed(c, 1, [&] {
       return launch_splat(c, P, n, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p);
@@ -662,6 +694,7 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
   I.nx = P.nx; I.ny = P.ny; I.sigin = sigin; I.dsq = P.dsq; I.width = width; I.sigma_gg = P.sigma_gg;
   I.kln_tmax = P.kln_tmax; I.kln_dT = P.kln_dT; I.A = p.Aproj; I.B = p.Atarg;
 
+  if (c->tickets.ensure(4) != cudaSuccess) { smc_destroy(c); return SMC_ERR_CUDA; }
   size_t smem2 = smc::grid_smem(P);
   cudaDeviceGetAttribute(&c->dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
   if ((int)smem2 > c->dev_smem) { smc_destroy(c); return SMC_ERR_CONFIG; }
@@ -690,6 +723,7 @@ void smc_destroy(void *ctx) {
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
   c->avg_frame.release(); c->avg_order.release(); c->avg_seg.release(); c->avg_count.release();
   c->avg_edges.release(); c->avg_bins.release();
+  c->ev_order.release(); c->tickets.release();
   c->adj_rho.release(); c->adj_lam.release(); c->adj_grho.release(); c->adj_geps.release(); c->adj_out.release();
   c->icdf_tab[0].release(); c->icdf_tab[1].release(); c->ntan.release(); c->inj_tp.release(); c->inj_tt.release();
   c->stan.release();
@@ -1150,9 +1184,9 @@ smc_status enqueue_batch(Ctx *c, int n, const smc_outputs *out, int *launches) {
     tio.ntan = out->tangents ? out->tangents + (size_t)off * 4 * AB : nullptr;
     const int grid1 = std::max(1, std::min(m, c->sms * c->occ1));
     CK(smc::launch_sample_pair_mixed(P, off, m, nullptr, nullptr, nullptr, c->recs.p, c->srcs.p, pos, wnd, nullptr,
-                                     nullptr, nullptr, grid1, c->st, &tio, c->ev_base.p));
+                                     nullptr, nullptr, grid1, c->st, &tio, c->ev_base.p, c->tickets.p + 2));
     CK(launch_splat(c, P, m, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p));
-    nl += 2 + ((c->use_tc && smc::grid_tc_supported(P) && !P.no_moments) ? 1 : 0);
+    nl += 3 + ((c->use_tc && smc::grid_tc_supported(P) && !P.no_moments) ? 1 : 0);
     int *np = out->npart ? out->npart + 2 * off : nullptr;
     int *nc = out->ncoll ? out->ncoll + off : nullptr;
     double *bb = out->b ? out->b + off : nullptr;

@@ -95,6 +95,27 @@ struct DevParams {
   double fluct_k_part, fluct_th_part, fluct_k_coll, fluct_th_coll;
 };
 
+// Which events a persistent CTA takes.  Static: blockIdx.x, + gridDim.x, ...
+// Dynamic (next != NULL): a ticket from the counter *next (zeroed before the
+// launch) per event, so that CTAs that finish early take more; with order,
+// ticket k is event order[k] (the heaviest first).  Every event's result is
+// independent of which CTA computes it.
+struct EventQueue {
+  const int *order;
+  int *next;
+};
+__device__ __forceinline__ int queue_first(const EventQueue &q, int *s_k) {
+  if (!q.next) return blockIdx.x;
+  __syncthreads();   // every thread has read the previous ticket
+  if (threadIdx.x == 0) *s_k = atomicAdd(q.next, 1);
+  __syncthreads();
+  return *s_k;
+}
+__device__ __forceinline__ int queue_next(const EventQueue &q, int k, int *s_k) {
+  return q.next ? queue_first(q, s_k) : k + (int)gridDim.x;
+}
+__device__ __forceinline__ int queue_event(const EventQueue &q, int k) { return q.order ? q.order[k] : k; }
+
 // Per-event record written by the sampling/pairing stage.
 struct EventRec {
   double b;

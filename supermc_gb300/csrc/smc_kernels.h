@@ -23,12 +23,15 @@ cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, i
                                      const double *inj_targ, const double *inj_b, EventRec *recs, Source *srcs,
                                      double *out_pos, uint8_t *out_wounded, const SystemDev *systems,
                                      const int *ev_sys, const int *order, int grid, cudaStream_t st,
-                                     const TangentIO *tio = nullptr, const uint64_t *ev_base = nullptr);
+                                     const TangentIO *tio = nullptr, const uint64_t *ev_base = nullptr,
+                                     int *ticket = nullptr);
 size_t grid_smem(const DevParams &P);
 int grid_blocks_per_sm(const DevParams &P);
+// the grid kernels take their events from a queue (EventQueue): with ticket
+// (a device counter the launcher zeroes) dynamically, in `order` when given
 cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs, float *out_rho,
                         float *out_ta, float *out_tb, float *scratch, double *out_ecc, int *status, int grid,
-                        cudaStream_t st);
+                        cudaStream_t st, const int *order = nullptr, int *ticket = nullptr);
 size_t grid_tc_smem(const DevParams &P);
 bool grid_tc_supported(const DevParams &P);
 // Tensor-core splat of a batch: contraction, corner corrections and post-op
@@ -38,7 +41,8 @@ bool grid_tc_supported(const DevParams &P);
 // corner corrections), cm_ev [n][3] doubles (centre-of-mass sums).
 cudaError_t launch_grid_tc(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs,
                            float *out_rho, float *out_ta, float *out_tb, float *rho_ev, int *corr_scratch,
-                           double *cm_ev, double *out_ecc, int *status, int sms, cudaStream_t st);
+                           double *cm_ev, double *out_ecc, int *status, int sms, cudaStream_t st,
+                           const int *order = nullptr, int *tickets = nullptr);
 cudaError_t launch_avg_init(const DevParams &P, int n, const EventRec *recs, const Source *srcs, AvgSrc *state,
                             int grid, cudaStream_t st);
 cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Source *srcs, AvgSrc *state,
