@@ -412,6 +412,9 @@ def run_gpu(args, vals) -> dict | None:
     # launch configuration (splat path, events per launch) tuned on this
     # workload before timing, like the context's construction
     tuning = eng.autotune(n) if args.autotune else None
+    if not args.autotune and args.grid_path != "auto":
+        eng.set_grid_path(args.grid_path == "tc")
+        tuning = {"tensor_cores": args.grid_path == "tc", "chunk": 4096, "events_per_s": None}
     bufs = {"ecc": torch.empty((n, 49), dtype=torch.float64, device=dev),
             "npart": torch.empty((n, 2), dtype=torch.int32, device=dev),
             "ncoll": torch.empty((n,), dtype=torch.int32, device=dev),
@@ -604,6 +607,8 @@ def main():
     ap.add_argument("--side-workloads", type=int, default=1, help="differentiable and 501^2 binned workloads")
     ap.add_argument("--graph", type=int, default=1, help="time the batch as a CUDA graph (smc_generate_graph)")
     ap.add_argument("--autotune", type=int, default=1, help="tune the launch configuration before timing")
+    ap.add_argument("--grid-path", default="auto", choices=["auto", "tc", "cc"],
+                    help="with --autotune 0: the splat (tensor-core or CUDA-core)")
     ap.add_argument("--ref-events", type=int, default=1600, help="reference arm: events per step (all cores)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--seed", type=int, default=1)
