@@ -53,6 +53,10 @@ EXTENSION_KEYS: dict[str, float] = {
 }
 
 
+# other spellings accepted for extension keys (lower case)
+ALIASES: dict[str, str] = {"siginnn_override": "sigininn_override"}
+
+
 class ParameterError(ValueError):
     """Raised where the reference calls exit() on a bad parameter file."""
 
@@ -65,6 +69,7 @@ def _parse_line(line: str, out: dict[str, float], strict: bool) -> None:
         raise ParameterError(f'"=" symbol not found in equation assignment {line!r}')
     lhs, rhs = body.split("=", 1)
     name = lhs.strip().lower()
+    name = ALIASES.get(name, name)
     try:
         value = float(rhs.strip())
     except ValueError as exc:
