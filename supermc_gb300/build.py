@@ -16,6 +16,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libsupermc_gb300.so")
+HOST = os.path.join(HERE, "host")
+HOST_SOURCES = ["ParameterReader.cpp", "MakeDensity.cpp", "main.cpp"]
+EXE = os.path.join(OUT_DIR, "superMC")
 SOURCES = ["smc_capi.cu", "k_sample_pair.cu", "k_grid.cu", "k_kln.cu", "k_average.cu", "smc_noalloc.cu", "k_grid_tc.cu", "k_adjoint.cu", "smc_output.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -60,7 +63,25 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if r.returncode:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
         os.replace(tmp, LIB)
+    build_host(force)
     return LIB
+
+
+def build_host(force: bool = False) -> str:
+    """The C++ drop-in driver ``_build/superMC`` (ParameterReader,
+    MakeDensity, main over the C ABI), linked to the library."""
+    srcs = [os.path.join(HOST, f) for f in HOST_SOURCES]
+    deps = srcs + [os.path.join(HOST, h) for h in os.listdir(HOST) if h.endswith(".h")] + [LIB]
+    if not force and not _stale(EXE, deps):
+        return EXE
+    cxx = shutil.which("g++") or "g++"
+    tmp = EXE + ".tmp"
+    r = subprocess.run([cxx, "-O2", "-std=c++17", "-Wall", "-o", tmp, *srcs, "-L" + OUT_DIR, "-lsupermc_gb300",
+                        "-Wl,-rpath,$ORIGIN"], capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("host build failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp, EXE)
+    return EXE
 
 
 if __name__ == "__main__":

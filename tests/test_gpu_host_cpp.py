@@ -1,0 +1,67 @@
+"""The C++ drop-in driver (supermc_gb300/_build/superMC, the reference's
+main over the C ABI) writes the same files as the Python host over the same
+calls: operations 9, 1 and 3."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from systems import SYSTEMS, values
+
+pytestmark = pytest.mark.gpu
+
+PARAMS = {"which_mc_model": 5, "sub_model": 1, "Aproj": 197, "Atarg": 197, "ecm": 200, "shape_of_nucleons": 4,
+          "gauss_nucl_width": 0.5, "collision_criterion": 1, "shape_of_entropy": 2, "alpha": 0.118,
+          "maxx": 13, "maxy": 13, "dx": 0.1, "dy": 0.1, "cc_fluctuation_model": 6, "randomSeed": 5,
+          "ecc_from_order": 2, "ecc_to_order": 5, "use_sd": 1, "use_ed": 0, "use_block": 1, "use_4col": 1,
+          "average_from_order": 2, "average_to_order": 2, "generate_reaction_plane_avg_profile": 1}
+
+
+def _run(tmp_path, **over):
+    from supermc_gb300 import build
+    p = dict(PARAMS, **over)
+    (tmp_path / "parameters.dat").write_text("".join(f"{k} = {v}\n" for k, v in p.items()))
+    r = subprocess.run([build.EXE], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return p
+
+
+def _engine(p):
+    from supermc_gb300.engine import Engine
+    q = {k: v for k, v in p.items() if k not in ("randomSeed", "operation", "nev")}
+    return Engine(q, seed=p["randomSeed"])
+
+
+def test_operation_9_eccentricity_files(tmp_path):
+    from supermc_gb300.output import write_ecc
+    p = _run(tmp_path, operation=9, nev=300)
+    ref = tmp_path / "ref"
+    ref.mkdir()
+    out = _engine(p).generate(0, 300, want=("ecc",))
+    write_ecc(out["ecc"], 2, 5, str(ref / "sn_ecc_eccp_%d.dat"))
+    for order in (2, 3, 4, 5, 10):
+        name = f"sn_ecc_eccp_{order}.dat"
+        assert (tmp_path / "data" / name).read_text() == (ref / name).read_text(), name
+
+
+def test_operation_1_profiles(tmp_path):
+    from supermc_gb300.output import write_density_block
+    p = _run(tmp_path, operation=1, nev=3)
+    out = _engine(p).generate(0, 3, want=("rho", "npart"))
+    for e in range(3):
+        sd = out["rho"][e].astype(np.float64) * 40.0
+        write_density_block(sd, str(tmp_path / "ref_block.dat"))
+        assert (tmp_path / "data" / f"sd_event_{e + 1}_block.dat").read_text() == \
+            (tmp_path / "ref_block.dat").read_text()
+        head = (tmp_path / "data" / f"sd_event_{e + 1}_4col.dat").read_text().split("\n", 1)[0]
+        assert head == "# <npart>= %g xmax= %d ymax= %d" % (out["npart"][e].sum(), 261, 261)
+
+
+def test_operation_3_averages(tmp_path):
+    p = _run(tmp_path, operation=3, nev=16)
+    mean, mean_rp = _engine(p).average(0, 16, 2, 2, True)
+    got = np.loadtxt(tmp_path / "data" / "sdAvg_order_2_block.dat")
+    np.testing.assert_allclose(got, mean[0], rtol=1e-11, atol=1e-300)
+    got_rp = np.loadtxt(tmp_path / "data" / "sdAvg_RP_order_2_block.dat")
+    np.testing.assert_allclose(got_rp, mean_rp[0], rtol=1e-11, atol=1e-300)
