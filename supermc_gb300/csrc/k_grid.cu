@@ -27,7 +27,7 @@ namespace smc {
 
 constexpr int kGT = 512;            // threads per CTA
 constexpr int kWarps = kGT / 32;
-constexpr int kRW = 2;              // rows per warp
+constexpr int kRW = 1;              // rows per warp (16-row strips: half the shared memory)
 constexpr int kR = kWarps * kRW;    // rows per strip
 constexpr int kGS = 64;             // sources per group
 
@@ -67,7 +67,8 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
 }
 
 template <int LO, int HI>
-__global__ void __launch_bounds__(kGT) k_grid(DevParams P, int n_events, const EventRec *recs, const Source *srcs,
+// two CTAs per SM (64 registers per thread, shared memory for two 16-row strips)
+__global__ void __launch_bounds__(kGT, 2) k_grid(DevParams P, int n_events, const EventRec *recs, const Source *srcs,
                                               float *out_rho, float *out_ta, float *out_tb, float *scratch,
                                               double *out_ecc, int *status, EventQueue q) {
   extern __shared__ __align__(16) unsigned char smem[];
