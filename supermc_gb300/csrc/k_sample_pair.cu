@@ -40,6 +40,7 @@ struct alignas(16) SampleSmem {
   float2 red2[kNT / 32 * 2];
   int ired[kNT / 32 * 4];
   double red4[kNT / 32];
+  double bmean[2];   // block means broadcast by block_mean2_f
   long long lred[32];
   double b;
 };
@@ -137,27 +138,28 @@ __device__ void icdf_tangent(const NucleusDev &n, double r, double &sR, double &
 }
 
 // One Woods-Saxon candidate from four uniforms (Nucleus::getDeformRandomWS)
-__device__ __forceinline__ bool ws_candidate(const NucleusDev &n, float ctr, float phir, double u0, double u1,
-                                             double u2, double u3, float &x, float &y, float &z) {
+// (u0..u3 rounded to float; u0d the FP64 u0, read only by inverse-CDF radii)
+__device__ __forceinline__ bool ws_candidate(const NucleusDev &n, float ctr, float phir, double u0d, float u0,
+                                             float u1, float u2, float u3, float &x, float &y, float &z) {
   float R = (float)n.R, a = (float)n.a;
-  float r = (float)n.rmax_cut * powf((float)u0, 1.0f / 3.0f);
+  float r = (float)n.rmax_cut * powf(u0, 1.0f / 3.0f);
   if (n.deformed) {
-    float cx = 1.0f - 2.0f * (float)u1;
+    float cx = 1.0f - 2.0f * u1;
     float rad1 = R * (1.0f + (float)n.beta2 * sph2(cx) + (float)n.beta4 * sph4(cx));
     float rw1 = 1.0f / (1.0f + expf(-rad1 / a));
-    if ((float)u2 * rw1 > 1.0f / (1.0f + expf((r - rad1) / a))) return false;
+    if (u2 * rw1 > 1.0f / (1.0f + expf((r - rad1) / a))) return false;
     float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
     float sp, cp;
-    sincospif(2.0f * (float)u3, &sp, &cp);
+    sincospif(2.0f * u3, &sp, &cp);
     x = r * sx * cp; y = r * sx * sp; z = r * cx;
     rotate3f(x, y, z, ctr, phir);
   } else {
-    if (n.icdf) r = (float)icdf_radius(n, u0);   // every candidate passes the radial step
-    else if ((float)u1 * (float)n.rw_max > 1.0f / (1.0f + expf((r - R) / a))) return false;
-    float cx = 1.0f - 2.0f * (float)u2;
+    if (n.icdf) r = (float)icdf_radius(n, u0d);   // every candidate passes the radial step
+    else if (u1 * (float)n.rw_max > 1.0f / (1.0f + expf((r - R) / a))) return false;
+    float cx = 1.0f - 2.0f * u2;
     float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
     float sp, cp;
-    sincospif(2.0f * (float)u3, &sp, &cp);
+    sincospif(2.0f * u3, &sp, &cp);
     x = r * sx * cp; y = r * sx * sp; z = r * cx;
   }
   return true;
@@ -186,23 +188,39 @@ __device__ double hulthen_inv(double y) {
   return XX2;
 }
 
-// Sum over the block of FP32 values, exact to double precision for the
-// sums that occur here (double-float pairs; no FP64 arithmetic).
-__device__ __forceinline__ double block_sum_f(float v, float2 *red, int slot) {
-  float hi = v, lo = 0.f;
-  for (int o = 16; o; o >>= 1) {
-    float bh = __shfl_xor_sync(0xffffffffu, hi, o), bl = __shfl_xor_sync(0xffffffffu, lo, o);
-    float s2 = hi + bh, bb = s2 - hi;
-    float e = (hi - (s2 - bb)) + (bh - bb) + (lo + bl);
-    hi = s2 + e;
-    lo = e - (hi - s2);
+// Means over the block of two FP32 values per thread, (sum v0) / n and
+// (sum v1) / n, exact to double precision for the sums that occur here:
+// double-float warp sums, then the FP64 additions and divisions by one
+// thread (FP64 throughput is a small fraction of FP32 here), broadcast
+// through shared memory.
+__device__ __forceinline__ void block_mean2_f(float v0, float v1, int n, float2 *red, double *out, double &m0,
+                                              double &m1) {
+  float hi[2] = {v0, v1}, lo[2] = {0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 2; k++)
+    for (int o = 16; o; o >>= 1) {
+      float bh = __shfl_xor_sync(0xffffffffu, hi[k], o), bl = __shfl_xor_sync(0xffffffffu, lo[k], o);
+      float s2 = hi[k] + bh, bb = s2 - hi[k];
+      float e = (hi[k] - (s2 - bb)) + (bh - bb) + (lo[k] + bl);
+      hi[k] = s2 + e;
+      lo[k] = e - (hi[k] - s2);
+    }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    red[w] = make_float2(hi[0], lo[0]);
+    red[kNT / 32 + w] = make_float2(hi[1], lo[1]);
   }
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) red[slot * (kNT / 32) + w] = make_float2(hi, lo);
   __syncthreads();
-  double s = 0;
-  for (int i = 0; i < kNT / 32; i++) s += (double)red[slot * (kNT / 32) + i].x + (double)red[slot * (kNT / 32) + i].y;
-  return s;
+  if (threadIdx.x == 0) {
+    double s0 = 0, s1 = 0;
+    for (int i = 0; i < kNT / 32; i++) s0 += (double)red[i].x + (double)red[i].y;
+    for (int i = 0; i < kNT / 32; i++) s1 += (double)red[kNT / 32 + i].x + (double)red[kNT / 32 + i].y;
+    out[0] = s0 / n;
+    out[1] = s1 / n;
+  }
+  __syncthreads();
+  m0 = out[0];
+  m1 = out[1];
 }
 
 __device__ __forceinline__ int block_sum_i(int v, int *red, int slot) {
@@ -230,11 +248,13 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
   for (uint32_t base = 0; n_acc < A; base += kNT) {
     if (base > (1u << 20)) return false;
     uint32_t c = base + tid;
-    double u0, u1, u2, u3;
-    uniform2(seed, ev, sid, 2 * c, u0, u1);
-    uniform2(seed, ev, sid, 2 * c + 1, u2, u3);
+    float u0, u1, u2, u3;
+    uniform2f(seed, ev, sid, 2 * c, u0, u1);
+    uniform2f(seed, ev, sid, 2 * c + 1, u2, u3);
+    double u0d = 0, unused;
+    if (n.icdf) uniform2(seed, ev, sid, 2 * c, u0d, unused);
     float x = 0, y = 0, z = 0;
-    const bool ws = ws_candidate(n, ctr, phir, u0, u1, u2, u3, x, y, z);
+    const bool ws = ws_candidate(n, ctr, phir, u0d, u0, u1, u2, u3, x, y, z);
     // the radially accepted candidates, compacted in candidate order: the
     // hard-core tests below then run on full warps
     const int lane = tid & 31, wid = tid >> 5;
@@ -373,24 +393,24 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
     }
     float v[4] = {(float)(sR * x), (float)(sR * y), (float)(sa * x), (float)(sa * y)};
     for (int c = 0; c < 4; c += 2) {
-      const double m0 = block_sum_f(tid < A ? v[c] : 0.f, sm.red2, 0);
-      const double m1 = block_sum_f(tid < A ? v[c + 1] : 0.f, sm.red2, 1);
+      double m0, m1;
+      block_mean2_f(tid < A ? v[c] : 0.f, tid < A ? v[c + 1] : 0.f, A, sm.red2, sm.bmean, m0, m1);
       __syncthreads();
-      tg[c] = (float)(v[c] - m0 / A);
-      tg[c + 1] = (float)(v[c + 1] - m1 / A);
+      tg[c] = (float)(v[c] - m0);
+      tg[c + 1] = (float)(v[c + 1] - m1);
     }
   }
   if (inj_xy) {
     if (tid < A) { px = inj_xy[2 * tid]; py = inj_xy[2 * tid + 1]; }
   } else {
-    double mx = block_sum_f(tid < A ? sm.ax[w][tid] : 0.f, sm.red2, 0);
-    double my = block_sum_f(tid < A ? sm.ay[w][tid] : 0.f, sm.red2, 1);
+    double mxa, mya;   // centre of mass
+    block_mean2_f(tid < A ? sm.ax[w][tid] : 0.f, tid < A ? sm.ay[w][tid] : 0.f, A, sm.red2, sm.bmean, mxa, mya);
     __syncthreads();
     if (tid < A) {
       rx = sm.ax[w][tid];
       ry = sm.ay[w][tid];
-      px = (double)rx - mx / A + xc;
-      py = (double)ry - my / A;
+      px = (double)rx - mxa + xc;
+      py = (double)ry - mya;
     }
   }
   // stash unsorted, then rank-sort by x: FP32 keys order the FP64 values

@@ -147,6 +147,41 @@ __host__ __device__ __forceinline__ double u53(uint32_t lo, uint32_t hi) {
   return ((double)(v >> 11) + 0.5) * (1.0 / 9007199254740992.0);
 }
 
+// (float)u53(lo, hi) with integer operations only: the value (m + 1/2) 2^-53,
+// m the top 53 bits of (hi, lo), rounded to double and then to float (each
+// to nearest, ties to even), as the FP64 expression (float)u53 rounds it.
+__host__ __device__ __forceinline__ float u53f(uint32_t lo, uint32_t hi) {
+  const uint64_t m = (((uint64_t)hi << 32) | lo) >> 11;
+  uint64_t x = 2 * m + 1;   // the value is x 2^e
+  int e = -54;
+  if (x >> 53) {            // 54 significant bits: the double drops the last one (a tie) to even
+    const uint64_t h = x >> 1;
+    x = h + (h & 1);
+    e = -53;
+  }
+#ifdef __CUDA_ARCH__
+  const int msb = 63 - __clzll((long long)x);
+#else
+  const int msb = 63 - __builtin_clzll(x);
+#endif
+  if (msb > 23) {           // to 24 significant bits
+    const int sh = msb - 23;
+    uint64_t q = x >> sh;
+    const uint64_t rem = x & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (q & 1))) q++;
+    x = q;
+    e += sh;
+  }
+  const uint32_t bits = (uint32_t)(e + 127) << 23;   // 2^e, a normal float (e >= -54)
+  float scale;
+#ifdef __CUDA_ARCH__
+  scale = __int_as_float((int)bits);
+#else
+  __builtin_memcpy(&scale, &bits, sizeof(scale));
+#endif
+  return (float)(uint32_t)x * scale;   // x <= 2^24: exact
+}
+
 // Two uniforms in (0,1): counter {slot, stream, event_lo, event_hi},
 // key {seed_lo, seed_hi}.
 __host__ __device__ __forceinline__ void uniform2(uint64_t seed, uint64_t event, uint32_t stream,
@@ -155,6 +190,15 @@ __host__ __device__ __forceinline__ void uniform2(uint64_t seed, uint64_t event,
   philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
   u0 = u53(c[0], c[1]);
   u1 = u53(c[2], c[3]);
+}
+
+// uniform2 rounded to float, without FP64 arithmetic
+__host__ __device__ __forceinline__ void uniform2f(uint64_t seed, uint64_t event, uint32_t stream, uint32_t slot,
+                                                   float &u0, float &u1) {
+  uint32_t c[4] = {slot, stream, (uint32_t)event, (uint32_t)(event >> 32)};
+  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  u0 = u53f(c[0], c[1]);
+  u1 = u53f(c[2], c[3]);
 }
 
 enum StreamId : uint32_t { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5 };
