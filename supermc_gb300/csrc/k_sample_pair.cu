@@ -599,7 +599,9 @@ __device__ __forceinline__ void set_window(Source &s, double lo, double hi, doub
 // systems / ev_sys (mixed batches, else NULL): the system parameters of
 // event e are systems[ev_sys[e]]; order (else NULL): the order in which the
 // CTAs take the events (heavy systems first).
-__global__ void __launch_bounds__(kNT, 3) k_sample_pair(DevParams P_in, uint64_t first_event, int n_events,
+// six CTAs per SM (shared memory allows six; more resident warps beat the spills
+// this register budget costs)
+__global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t first_event, int n_events,
                                                      const double *inj_proj, const double *inj_targ,
                                                      const double *inj_b, EventRec *recs, Source *srcs,
                                                      double *out_pos, uint8_t *out_wounded,
