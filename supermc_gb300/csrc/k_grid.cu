@@ -61,14 +61,23 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
   L.off_xg = o; o += sizeof(float) * 2 * nx;   // grid x, then x - x_cm
   L.off_yg = o; o += sizeof(float) * 2 * L.nyp;
   o = (o + 15) / 16 * 16;
-  L.off_red = o; o += sizeof(float2) * kWarps * 64;
+  // the reduction slots are used after the strips (centre of mass, moments):
+  // inside the accumulator region after the mask when they fit there
+  const size_t red_bytes = sizeof(float2) * kWarps * 64, acc_bytes = sizeof(float) * np * kR * L.nyp;
+  const size_t red_in = (mask_bytes + 15) / 16 * 16;
+  if (red_in + red_bytes <= acc_bytes) {
+    L.off_red = L.off_acc + red_in;
+  } else {
+    L.off_red = o;
+    o += red_bytes;
+  }
   L.total = o;
   return L;
 }
 
 template <int LO, int HI>
-// two CTAs per SM (64 registers per thread, shared memory for two 16-row strips)
-__global__ void __launch_bounds__(kGT, 2) k_grid(DevParams P, int n_events, const EventRec *recs, const Source *srcs,
+// three CTAs per SM (42 registers per thread, shared memory for three 16-row strips)
+__global__ void __launch_bounds__(kGT, 3) k_grid(DevParams P, int n_events, const EventRec *recs, const Source *srcs,
                                               float *out_rho, float *out_ta, float *out_tb, float *scratch,
                                               double *out_ecc, int *status, EventQueue q) {
   extern __shared__ __align__(16) unsigned char smem[];
