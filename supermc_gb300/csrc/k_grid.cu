@@ -25,9 +25,9 @@
 
 namespace smc {
 
-constexpr int kGT = 512;            // threads per CTA
+constexpr int kGT = 256;            // threads per CTA
 constexpr int kWarps = kGT / 32;
-constexpr int kRW = 1;              // rows per warp (16-row strips: half the shared memory)
+constexpr int kRW = 1;              // rows per warp: 8-row strips, small enough for five CTAs per SM
 constexpr int kR = kWarps * kRW;    // rows per strip
 constexpr int kGS = 64;             // sources per group
 
@@ -76,8 +76,9 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
 }
 
 template <int LO, int HI>
-// three CTAs per SM (42 registers per thread, shared memory for three 16-row strips)
-__global__ void __launch_bounds__(kGT, 3) k_grid(DevParams P, int n_events, const EventRec *recs, const Source *srcs,
+// five CTAs per SM (51 registers per thread, shared memory for five 8-row strips):
+// latency-bound work wants resident warps more than registers
+__global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, const EventRec *recs, const Source *srcs,
                                               float *out_rho, float *out_ta, float *out_tb, float *scratch,
                                               double *out_ecc, int *status, EventQueue q) {
   extern __shared__ __align__(16) unsigned char smem[];
