@@ -283,6 +283,7 @@ def mixed_batch(dev, stream, n: int) -> dict:
     from supermc_gb300.engine import Engine
     eng = Engine(dict(MIXED_BASE, **MIXED_SYSTEMS[-1][1]), seed=2)
     eng.set_stream(stream.cuda_stream)
+    tuning = eng.autotune(4096)   # on the Au+Au system, before timing
     shares = np.array([s for s, _ in MIXED_SYSTEMS], dtype=float)
     counts = np.floor(n * shares / shares.sum()).astype(int)
     counts[-1] += n - counts.sum()
@@ -302,7 +303,8 @@ def mixed_batch(dev, stream, n: int) -> dict:
     eng.close()
     return {"value": rate, "unit": "events/s", "events": n,
             "systems": "p+Pb 5.02 TeV, d+Au, Cu+Cu, deformed U+U, Au+Au (200 GeV) in shares 1:2:2:2:3, "
-                       "MC-Glauber 261x261, one smc_generate_mixed call"}
+                       "MC-Glauber 261x261, one smc_generate_mixed call",
+            "splat": "tensor cores" if tuning["tensor_cores"] else "CUDA cores", "chunk": tuning["chunk"]}
 
 
 # differentiable Pb+Pb Glauber (radii by inverse CDF, so that positions move
@@ -324,6 +326,7 @@ def differentiable_batch(stream, n: int = 4096) -> dict:
     from supermc_gb300.engine import Engine
     eng = Engine(dict(DIFF_PARAMS), seed=7)
     eng.set_stream(stream.cuda_stream)
+    tuning = eng.autotune(n)
     g = np.zeros((n, 2))
     g[:, 0] = 1.0 / n
     eng.generate(0, n, want=("ecc",))
@@ -341,7 +344,8 @@ def differentiable_batch(stream, n: int = 4096) -> dict:
     return {"forward": n / (t1 - t0), "forward_backward": n / (t2 - t1), "unit": "events/s", "events": n,
             "adjoint_kernel_ms": st["post_ms"], "grad_mean_eps2": {"w": grad[0], "alpha": grad[1], "R": grad[2],
                                                                    "a": grad[3]},
-            "workload": "Pb+Pb 2.76 TeV, sigma_NN=64 mb, radii by inverse CDF, w=0.5 fm, alpha=0.118, 261x261"}
+            "workload": "Pb+Pb 2.76 TeV, sigma_NN=64 mb, radii by inverse CDF, w=0.5 fm, alpha=0.118, 261x261",
+            "splat": "tensor cores" if tuning["tensor_cores"] else "CUDA cores", "chunk": tuning["chunk"]}
 
 
 AVG_BASE = {
@@ -369,6 +373,7 @@ def binned_average(stream, n: int) -> dict:
     for name, (sysp, edges) in AVG_SYSTEMS.items():
         eng = Engine(dict(AVG_BASE, **sysp), seed=3)
         eng.set_stream(stream.cuda_stream)
+        tuning = eng.autotune(4096)
         eng.average_binned(0, min(n, 4096), edges, order=2, method=1)
         torch.cuda.synchronize()
         eng.reset_stats()
@@ -381,6 +386,7 @@ def binned_average(stream, n: int) -> dict:
         bytes_ev = 4.0 * cells   # one FP32 density read per event (bin sums stay on chip per chunk)
         achieved = bytes_ev * n / (st["post_ms"] / 1e3) / 1e9 if st["post_ms"] > 0 else None
         out[name] = {"value": n / dt, "unit": "events/s", "events": n, "counts": counts.tolist(),
+                     "splat": "tensor cores" if tuning["tensor_cores"] else "CUDA cores", "chunk": tuning["chunk"],
                      "sample_ms": st["sample_ms"], "splat_ms": st["grid_ms"], "binned_ms": st["post_ms"],
                      "binned_roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                                          "frac": achieved / hbm_peak if achieved else None,

@@ -255,13 +255,38 @@ __global__ void k_avg_bins(const EventRec *recs, int n, const int *edges, int nb
 // under the recentring and rotation, R(-phi) (x', y') + (X, Y), by bilinear
 // interpolation (corners beyond the grid read zero); without, the cell's
 // value.  One thread per output cell, 16 x 16 cells per CTA, events in bin
-// order with one compensated sum in registers per bin.  A CTA skips an
-// event whose density (zero outside its windows' bounding box) cannot reach
-// the tile: the preimage of the tile's corners lies beyond that box.
+// order with one compensated sum in registers.  The CTA stages the events
+// 256 at a time: each thread tests one event against the tile (the
+// preimage of the tile's corners against the event's window box, outside
+// which its density is zero) and the events that can reach the tile are
+// compacted in order into shared memory with their frames; the cells then
+// read four events' values at a time and add them in order.
+__device__ __forceinline__ float binned_value(const float *G, int nx, int ny, float4 f, float xo, float yo,
+                                              float inv_dx, float inv_dy, bool resample, int i, int j) {
+  if (!resample) return G[(size_t)i * ny + j];
+  // preimage in grid units (f: cos, sin, X - xmin, Y - ymin)
+  const float px = (f.x * xo + f.y * yo + f.z) * inv_dx;
+  const float py = (-f.y * xo + f.x * yo + f.w) * inv_dy;
+  const float fx = floorf(px), fy = floorf(py);
+  const int i0 = (int)fx, j0 = (int)fy;
+  const float tx = px - fx, ty = py - fy;
+  if (!(i0 >= -1 && i0 < nx && j0 >= -1 && j0 < ny)) return 0.f;
+  const bool xa = i0 >= 0, xb = i0 + 1 < nx, ya = j0 >= 0, yb = j0 + 1 < ny;
+  const float v00 = xa && ya ? G[(size_t)i0 * ny + j0] : 0.f;
+  const float v01 = xa && yb ? G[(size_t)i0 * ny + j0 + 1] : 0.f;
+  const float v10 = xb && ya ? G[(size_t)(i0 + 1) * ny + j0] : 0.f;
+  const float v11 = xb && yb ? G[(size_t)(i0 + 1) * ny + j0 + 1] : 0.f;
+  return (1.f - tx) * ((1.f - ty) * v00 + ty * v01) + tx * ((1.f - ty) * v10 + ty * v11);
+}
+
 __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const EventRec *recs, const float *rho,
                                                    const double4 *frame, const int *order, const int *seg,
                                                    int nbins, float2 *acc) {
-  const int i = blockIdx.y * 16 + (threadIdx.x >> 4), j = blockIdx.x * 16 + (threadIdx.x & 15);
+  __shared__ float4 s_fr[256];
+  __shared__ int s_ev[256];
+  __shared__ int s_wc[8];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int i = blockIdx.y * 16 + (tid >> 4), j = blockIdx.x * 16 + (tid & 15);
   const int ti0 = blockIdx.y * 16, tj0 = blockIdx.x * 16;   // the tile's first cell
   const int nx = P.nx, ny = P.ny;
   const bool in = i < nx && j < ny;
@@ -269,54 +294,69 @@ __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const EventRec 
   const float xo = (float)(P.xmin + i * P.dx), yo = (float)(P.ymin + j * P.dy);
   const float inv_dx = (float)(1.0 / P.dx), inv_dy = (float)(1.0 / P.dy);
   const float xmin = (float)P.xmin, ymin = (float)P.ymin;
+  const bool resample = frame != nullptr;
   for (int b = 0; b < nbins; b++) {
     Kahan k;
     const int e0 = seg[b], e1 = seg[b + 1];
-    for (int q = e0; q < e1; q++) {
-      const int e = order[q];
-      const EventRec &r = recs[e];
-      const float *G = rho + (size_t)e * g;
-      float v = 0.f;
-      if (frame) {
-        const double4 f = frame[e];
-        // preimage of the tile's corner cells, in grid units (uniform over the CTA)
-        {
-          const float c = (float)f.z, s = (float)f.w;
+    for (int q0 = e0; q0 < e1; q0 += 256) {
+      // ---- stage: which of the next 256 events can reach this tile
+      bool hit = false;
+      float4 fr = make_float4(1.f, 0.f, 0.f, 0.f);
+      int e = 0;
+      if (q0 + tid < e1) {
+        e = order[q0 + tid];
+        const EventRec r = recs[e];
+        if (resample) {
+          const double4 f = frame[e];
+          fr = make_float4((float)f.z, (float)f.w, (float)f.x - xmin, (float)f.y - ymin);
           float lo_x = 1e30f, hi_x = -1e30f, lo_y = 1e30f, hi_y = -1e30f;
 #pragma unroll
           for (int corner = 0; corner < 4; corner++) {
             const float cx = (float)(P.xmin + (ti0 + (corner & 1) * 15) * P.dx);
             const float cy = (float)(P.ymin + (tj0 + (corner >> 1) * 15) * P.dy);
-            const float qx = (c * cx + s * cy + (float)f.x - xmin) * inv_dx;
-            const float qy = (-s * cx + c * cy + (float)f.y - ymin) * inv_dy;
+            const float qx = (fr.x * cx + fr.y * cy + fr.z) * inv_dx;
+            const float qy = (-fr.y * cx + fr.x * cy + fr.w) * inv_dy;
             lo_x = fminf(lo_x, qx); hi_x = fmaxf(hi_x, qx);
             lo_y = fminf(lo_y, qy); hi_y = fmaxf(hi_y, qy);
           }
           // bilinear corners floor(p), floor(p) + 1 against the box [imin, imax)
-          if (hi_x < r.imin - 1 || lo_x >= r.imax || hi_y < r.jmin - 1 || lo_y >= r.jmax) continue;
+          hit = !(hi_x < r.imin - 1 || lo_x >= r.imax || hi_y < r.jmin - 1 || lo_y >= r.jmax);
+        } else {
+          hit = !(ti0 >= r.imax || ti0 + 16 <= r.imin || tj0 >= r.jmax || tj0 + 16 <= r.jmin);
         }
-        if (!in) continue;
-        const float c = (float)f.z, s = (float)f.w;
-        // preimage in grid units
-        const float px = (c * xo + s * yo + (float)f.x - xmin) * inv_dx;
-        const float py = (-s * xo + c * yo + (float)f.y - ymin) * inv_dy;
-        const float fx = floorf(px), fy = floorf(py);
-        const int i0 = (int)fx, j0 = (int)fy;
-        const float tx = px - fx, ty = py - fy;
-        if (i0 >= -1 && i0 < nx && j0 >= -1 && j0 < ny) {
-          const bool xa = i0 >= 0, xb = i0 + 1 < nx, ya = j0 >= 0, yb = j0 + 1 < ny;
-          const float v00 = xa && ya ? G[(size_t)i0 * ny + j0] : 0.f;
-          const float v01 = xa && yb ? G[(size_t)i0 * ny + j0 + 1] : 0.f;
-          const float v10 = xb && ya ? G[(size_t)(i0 + 1) * ny + j0] : 0.f;
-          const float v11 = xb && yb ? G[(size_t)(i0 + 1) * ny + j0 + 1] : 0.f;
-          v = (1.f - tx) * ((1.f - ty) * v00 + ty * v01) + tx * ((1.f - ty) * v10 + ty * v11);
-        }
-      } else {
-        if (ti0 >= r.imax || ti0 + 16 <= r.imin || tj0 >= r.jmax || tj0 + 16 <= r.jmin) continue;
-        if (!in) continue;
-        v = G[(size_t)i * ny + j];
       }
-      k.add(v);
+      const unsigned bal = __ballot_sync(0xffffffffu, hit);
+      if (lane == 0) s_wc[wid] = __popc(bal);
+      __syncthreads();
+      int off = 0, tot = 0;
+#pragma unroll
+      for (int w = 0; w < 8; w++) {
+        const int c = s_wc[w];
+        off += w < wid ? c : 0;
+        tot += c;
+      }
+      if (hit) {
+        const int p = off + __popc(bal & ((1u << lane) - 1u));
+        s_ev[p] = e;
+        s_fr[p] = fr;
+      }
+      __syncthreads();
+      // ---- accumulate in event order, four loads in flight
+      if (in) {
+        int m = 0;
+        for (; m + 4 <= tot; m += 4) {
+          float v[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            v[u] = binned_value(rho + (size_t)s_ev[m + u] * g, nx, ny, s_fr[m + u], xo, yo, inv_dx, inv_dy,
+                                resample, i, j);
+#pragma unroll
+          for (int u = 0; u < 4; u++) k.add(v[u]);
+        }
+        for (; m < tot; m++)
+          k.add(binned_value(rho + (size_t)s_ev[m] * g, nx, ny, s_fr[m], xo, yo, inv_dx, inv_dy, resample, i, j));
+      }
+      __syncthreads();   // the staged events are read before the next stage
     }
     if (in && e1 > e0) {
       // merge the chunk's compensated sum into the accumulator's
