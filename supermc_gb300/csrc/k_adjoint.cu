@@ -61,7 +61,7 @@ __host__ __device__ inline size_t red_offset(int nx, int ny) {
 
 __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, const EventRec *recs, const Source *srcs,
                                                  const float4 *src_tan, const float *rho_ev, const float *g_grid, const double *g_eps,
-                                                 float *lam_scratch, double *dtheta) {
+                                                 float *lam_scratch, double *dtheta, EventQueue q) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nx = P.nx, ny = P.ny, nw = (ny + 31) / 32;
   uint32_t *mask = reinterpret_cast<uint32_t *>(smem);
@@ -80,7 +80,9 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
   for (int j = tid; j < ny; j += kAT) yg[j] = (float)(P.ymin + j * P.dy);
   float *lam = lam_scratch + (size_t)blockIdx.x * nx * ny;
 
-  for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
+  __shared__ int s_k;
+  for (int kq = queue_first(q, &s_k); kq < n_events; kq = queue_next(q, kq, &s_k)) {
+    const int e = queue_event(q, kq);
     const EventRec rec = recs[e];
     const Source *S = srcs + (size_t)e * P.max_src;
     const float *rho = rho_ev + (size_t)e * nx * ny;
@@ -247,11 +249,17 @@ int adjoint_blocks_per_sm(const DevParams &P) {
 
 cudaError_t launch_adjoint(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs,
                            const float4 *src_tan, const float *rho_ev, const float *g_grid, const double *g_eps,
-                           float *lam_scratch, double *dtheta, int grid, cudaStream_t st) {
+                           float *lam_scratch, double *dtheta, int grid, cudaStream_t st, const int *order,
+                           int *ticket) {
   const size_t smem = adjoint_smem(P);
   cudaError_t e = cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_adjoint<<<grid, kAT, smem, st>>>(P, n_events, recs, srcs, src_tan, rho_ev, g_grid, g_eps, lam_scratch, dtheta);
+  if (ticket) {
+    e = cudaMemsetAsync(ticket, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+  }
+  k_adjoint<<<grid, kAT, smem, st>>>(P, n_events, recs, srcs, src_tan, rho_ev, g_grid, g_eps, lam_scratch, dtheta,
+                                     EventQueue{order, ticket});
   return cudaGetLastError();
 }
 

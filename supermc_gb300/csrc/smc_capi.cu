@@ -955,8 +955,9 @@ smc_status smc_adjoint(void *ctx, uint64_t first_event, int n, const double *xy_
       }
     }
     CK(timed(c, 2, [&] {
+      // the splat's heaviest-first order of the chunk, one ticket per event
       return smc::launch_adjoint(P, m, c->recs.p, c->srcs.p, tangents ? c->stan.p : nullptr, c->adj_rho.p, grho,
-                                 geps, c->adj_lam.p, c->adj_out.p, grid, c->st);
+                                 geps, c->adj_lam.p, c->adj_out.p, grid, c->st, c->ev_order.p, c->tickets.p + 3);
     }));
     c->h_adj.resize((size_t)m * 4);
     CK(cudaMemcpyAsync(c->h_adj.data(), c->adj_out.p, sizeof(double) * m * 4, cudaMemcpyDeviceToHost, c->st));

@@ -67,7 +67,8 @@ size_t adjoint_smem(const DevParams &P);
 int adjoint_blocks_per_sm(const DevParams &P);
 cudaError_t launch_adjoint(const DevParams &P, int n_events, const EventRec *recs, const Source *srcs,
                            const float4 *src_tan, const float *rho_ev, const float *g_grid, const double *g_eps,
-                           float *lam_scratch, double *dtheta, int grid, cudaStream_t st);
+                           float *lam_scratch, double *dtheta, int grid, cudaStream_t st, const int *order = nullptr,
+                           int *ticket = nullptr);
 cudaError_t launch_kln_table(const KlnDev &K, int tmax, double dT, double *table64, float *table32,
                              cudaStream_t st);
 
