@@ -207,6 +207,33 @@ smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_
                        const double *xy_targ, const double *b, int from_order, int to_order,
                        int reaction_plane, double *mean, double *mean_rp, int *n_used);
 
+/* All averaged profiles of MakeDensity::generate_profile_average
+ * (src/MakeDensity.cpp:1240-1577) for the integrated-p_T entropy density:
+ * for every order from_order..to_order and both frames -- the
+ * participant plane (rotateGrid) and the reaction plane (recenterGrid, the
+ * *_rp grids) -- the event means, after each frame's transform, of
+ *   sd          rho * finalFactor           (sdAvg[_RP]_order_<n>)
+ *   ta_tb       T_A T_B                     (TATB_fromSd[_RP]_order_<n>, :1342-1349)
+ *   ta, tb      T_A, T_B                    (nuclear_thickness_T{A,B}_fromSd[_RP]_order_<n>, :1362-1370)
+ *   rho_binary  unit Gaussians at the binary collisions
+ *               (MCnucl::calculate_rho_binary, src/MCnucl.cpp:481-531)
+ *   spectator_a/_b  unit Gaussians at the projectile / target spectators
+ *               (MCnucl::calculate_spectator_density, :534-614)
+ * Each pointer is host memory [to-from+1][nx][ny] or NULL (not produced;
+ * the reaction-plane frame runs when any *_rp pointer is set).  Events and
+ * moves as for smc_average; T_A T_B and the thickness means need
+ * which_mc_model 5 or 1. */
+typedef struct smc_average_outputs {
+  double *sd, *sd_rp;
+  double *ta_tb, *ta_tb_rp;
+  double *ta, *tb, *ta_rp, *tb_rp;
+  double *rho_binary, *rho_binary_rp;
+  double *spectator_a, *spectator_b, *spectator_a_rp, *spectator_b_rp;
+} smc_average_outputs;
+smc_status smc_average_profiles(void *ctx, uint64_t first_event, int n, const double *xy_proj,
+                                const double *xy_targ, const double *b, int from_order, int to_order,
+                                const smc_average_outputs *out, int *n_used);
+
 /* Centrality-binned averaged profiles (the per-order mean of
  * MakeDensity::generate_profile_average, src/MakeDensity.cpp:1331-1340,
  * split into Npart classes).  Every event of [first_event, first_event + n)

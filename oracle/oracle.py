@@ -127,6 +127,7 @@ class Oracle:
         lib.smco_event_rho_binary.argtypes = [ctypes.c_void_p]
         lib.smco_event_eccentricities.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                   ctypes.c_double, _D]
+        lib.smco_event_spectator_density.argtypes = [ctypes.c_void_p, _D, _D]
         lib.smco_event_hotspot_mask.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         lib.smco_event_density_frozen.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _D]
         lib.smco_event_density_moved.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
@@ -254,6 +255,11 @@ class OracleEvent:
         out = np.zeros(49)
         self.lib.smco_event_eccentricities(self.h, from_order, to_order, b, _ptr(out))
         return out
+
+    def spectator_density(self):
+        a, b = np.zeros((self.nx, self.ny)), np.zeros((self.nx, self.ny))
+        self.lib.smco_event_spectator_density(self.h, _ptr(a), _ptr(b))
+        return a, b
 
     def hotspot_mask(self):
         m = np.zeros((self.nx, self.ny), dtype=np.uint8)

@@ -1357,6 +1357,57 @@ void smco_event_cm_angle(const smco_event *e, int n, double *xcm, double *ycm, d
   *angle = -atan2(-ni, -nr) / n;
 }
 
+/* The spectators (nucleons without a collision, MCnucl::getSpectators,
+ * MCnucl.cpp:1223-1248) follow recenterGrid's shift (:1145-1149) and, with
+ * rotate, rotateGrid's rotation (:1172-1173; a Spectator's z is never set,
+ * and the rotation about z does not mix it into x, y). */
+static void move_spectators(smco_event *e, double X, double Y, int rotate, double ang) {
+  for (int w = 0; w < 2; w++)
+    for (int i = 0; i < e->n[w]; i++) {
+      nucleon_t *q = &e->nuc[w][i];
+      if (q->nhits) continue;
+      q->x = q->x - X;
+      q->y = q->y - Y;
+      if (rotate) {
+        double z = 0;
+        rotate3(&q->x, &q->y, &z, cos(0.0), ang);
+      }
+    }
+}
+
+/* MCnucl::calculate_spectator_density (MCnucl.cpp:534-614): projectile
+ * spectators into A, target spectators into B */
+void smco_event_spectator_density(const smco_event *e, double *A, double *B) {
+  double Xmin = -e->p.xmax, Ymin = -e->p.ymax, dx = e->p.dx, dy = e->p.dy;
+  double w = e->p.width, w2 = w * w;
+  double d_max = e->p.shape_of_nucleons == 1 ? 2. * sqrt(e->p.dsq) : 5. * w;
+  memset(A, 0, sizeof(double) * e->p.nx * e->p.ny);
+  memset(B, 0, sizeof(double) * e->p.nx * e->p.ny);
+  for (int nw = 0; nw < 2; nw++)
+    for (int i = 0; i < e->n[nw]; i++) {
+      const nucleon_t *q = &e->nuc[nw][i];
+      if (q->nhits) continue;
+      double *out = nw == 0 ? A : B;
+      double x = q->x, y = q->y;
+      int xl, xr, yl, yr;
+      window(e, x - d_max, x + d_max, Xmin, dx, e->p.nx, &xl, &xr);
+      window(e, y - d_max, y + d_max, Ymin, dy, e->p.ny, &yl, &yr);
+      for (int ir = xl; ir < xr; ir++) {
+        double xg = Xmin + ir * dx;
+        for (int jr = yl; jr < yr; jr++) {
+          double yg = Ymin + jr * dy;
+          double dc = (x - xg) * (x - xg) + (y - yg) * (y - yg);
+          if (e->p.shape_of_nucleons == 1) {
+            if (dc <= e->p.dsq) G(out, ir, jr) += (10.0 / e->p.sigin);
+          } else {
+            if (dc > 25. * w2) continue;
+            G(out, ir, jr) += peak_height(w) * exp(-dc / (2 * w2));
+          }
+        }
+      }
+    }
+}
+
 /* MCnucl::recenterGrid (MCnucl.cpp:1119-1150): shifts every source by the
  * density's centre of mass (the boxes move with Box2D::setCenter), then
  * calculateThickness and setDensity -- the reaction-plane-frame step of
@@ -1376,6 +1427,7 @@ int smco_event_recenter_resplat(smco_event *e, int order) {
     e->cy[c] = e->cy[c] - Y;
     box_set_center_xy(&e->cbox[c], e->cbox[c].xc, e->cy[c]);
   }
+  move_spectators(e, X, Y, 0, 0.0);
   int rc = smco_event_thickness(e);
   if (rc) return rc;
   return smco_event_density(e);
@@ -1410,6 +1462,7 @@ int smco_event_rotate_resplat(smco_event *e, int order) {
     double z = 0;
     rotate3(&e->cx[c], &e->cy[c], &z, cos(0.0), ang);
   }
+  move_spectators(e, X, Y, 1, ang);
   int rc = smco_event_thickness(e);
   if (rc) return rc;
   return smco_event_density(e);

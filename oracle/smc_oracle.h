@@ -144,6 +144,8 @@ void smco_event_icdf_tangents(const smco_event *e, const smco_nucleus *nA, const
                               double *tB);
 /* pre-sort index (injection / acceptance order) of each nucleon in sorted order */
 int smco_event_nucleon_ids(const smco_event *e, int which, int *ids, int maxn);
+/* MCnucl::calculate_spectator_density (MCnucl.cpp:534-614) into A, B [nx][ny] */
+void smco_event_spectator_density(const smco_event *e, double *A, double *B);
 /* GlueDensity::calcCMAngle (GlueDensity.cpp:87-144) on rho */
 void smco_event_cm_angle(const smco_event *e, int n, double *xcm, double *ycm, double *angle);
 /* MCnucl::rotateGrid (MCnucl.cpp:1152-1174) + calculateThickness +

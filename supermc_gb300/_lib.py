@@ -27,7 +27,7 @@ EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "sm
            "smc_set_timing",
            "smc_set_grid_path", "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_write_ecc",
            "smc_write_density_block", "smc_write_density_4col", "smc_inject_noalloc", "smc_average",
-           "smc_average_binned", "smc_adjoint", "smc_autotune", "smc_generate_graph"]
+           "smc_average_binned", "smc_adjoint", "smc_autotune", "smc_generate_graph", "smc_average_profiles"]
 
 
 class SmcError(RuntimeError):
@@ -89,6 +89,14 @@ class SmcOutputs(ctypes.Structure):
     ]
 
 
+AVERAGE_FIELDS = ("sd", "sd_rp", "ta_tb", "ta_tb_rp", "ta", "tb", "ta_rp", "tb_rp", "rho_binary", "rho_binary_rp",
+                  "spectator_a", "spectator_b", "spectator_a_rp", "spectator_b_rp")
+
+
+class SmcAverageOutputs(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in AVERAGE_FIELDS]
+
+
 class SmcTuning(ctypes.Structure):
     _fields_ = [("tensor_cores", ctypes.c_int), ("chunk", ctypes.c_int), ("events_per_s", ctypes.c_double * 8)]
 
@@ -138,6 +146,8 @@ def load() -> ctypes.CDLL:
     lib.smc_inject_noalloc.argtypes = [ctypes.POINTER(SmcParams), ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]
     lib.smc_average_binned.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        vp, vp, vp]
+    lib.smc_average_profiles.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(SmcAverageOutputs), ctypes.POINTER(ctypes.c_int)]
     lib.smc_generate_graph.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(SmcOutputs)]
     lib.smc_autotune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(SmcTuning)]
     lib.smc_adjoint.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.POINTER(SmcAdjointArgs), vp]

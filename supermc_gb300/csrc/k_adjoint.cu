@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
         const int k = q / hmax;
         const Source &s = S[k];
         const int kind = s.kind & 15;
-        if (kind == 3 || kind == SRC_THICK || s.xr <= s.xl || s.yr <= s.yl) continue;
+        if (kind >= 3 || kind == SRC_THICK || s.xr <= s.xl || s.yr <= s.yl) continue;
         const int i = s.xl + (q - k * hmax);
         if (i >= s.xr) continue;
         const float xf = (float)s.x, yf = (float)s.y;

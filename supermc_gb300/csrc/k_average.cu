@@ -221,6 +221,60 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
   }
 }
 
+// Sources of a derived grid of the averaged mode, written to `out`:
+//   mode 0, rho_binary (MCnucl::calculate_rho_binary, src/MCnucl.cpp:481-531):
+//     the binary collisions with unit weight 1/(2 pi w^2) (10/sigma_in for
+//     disk nucleons), plane 0;
+//   mode 1, spectator densities (MCnucl::calculate_spectator_density,
+//     src/MCnucl.cpp:534-614): the spectators, projectile into plane 1,
+//     target into plane 2.
+// Both cut at dc <= 25 w^2 (dc <= dsq for disks), the SRC_COLL rule; every
+// other record becomes a mask-only record with an empty window.
+__global__ void k_avg_view(DevParams P, int n_events, const EventRec *recs, const Source *in, Source *out, int mode) {
+  const bool disk = P.shape_of_nucleons == 1;
+  const float w_unit = disk ? (float)(10.0 / P.sigin) : (float)P.peak;
+  for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
+    const int ns = recs[e].nsrc;
+    for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+      Source s = in[(size_t)e * P.max_src + k];
+      const int kind = s.kind & 15;
+      if (mode == 0 && (kind == SRC_COLL || kind == SRC_BINARY)) {
+        s.kind = SRC_COLL | (disk ? 16 : 0);
+        s.plane = 0;
+        s.weight = w_unit;
+      } else if (mode == 1 && kind == SRC_SPECT) {
+        s.kind = SRC_COLL | (s.kind & 16);
+        s.plane = 1 + s.plane;
+      } else {
+        s.kind = 3;
+        s.xl = s.xr = s.yl = s.yr = 0;
+      }
+      out[(size_t)e * P.max_src + k] = s;
+    }
+  }
+}
+
+// acc[cell] += sum over the chunk's events of a_e[cell] * b_e[cell] (T_A T_B)
+__global__ void k_avg_accum_prod(const float *a, const float *b, int n_events, size_t cells, double *acc) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (size_t)gridDim.x * blockDim.x) {
+    Kahan k;
+    for (int e = 0; e < n_events; e++) k.add(a[(size_t)e * cells + c] * b[(size_t)e * cells + c]);
+    acc[c] += (double)k.s - (double)k.c;
+  }
+}
+
+cudaError_t launch_avg_view(const DevParams &P, int n, const EventRec *recs, const Source *in, Source *out, int mode,
+                            int grid, cudaStream_t st) {
+  k_avg_view<<<grid, kAT, 0, st>>>(P, n, recs, in, out, mode);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_avg_accum_prod(const float *a, const float *b, int n, size_t cells, double *acc, cudaStream_t st) {
+  int blocks = (int)std::min<size_t>((cells + 255) / 256, 4096);
+  k_avg_accum_prod<<<blocks, 256, 0, st>>>(a, b, n, cells, acc);
+  return cudaGetLastError();
+}
+
 // acc[cell] += sum over the chunk's events of rho_e[cell] (Kahan in FP32 over
 // the chunk, then one FP64 add per cell)
 __global__ void k_avg_accum(const float *rho, int n_events, size_t cells, double *acc) {

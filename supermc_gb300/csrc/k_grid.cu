@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
           bool hit = false;
           if (k < rec.nsrc) {
             const Source &s = S[k];
-            hit = s.xl < r0 + rows && s.xr > r0 && s.yr > s.yl && (s.kind & 15) != 3;
+            hit = s.xl < r0 + rows && s.xr > r0 && s.yr > s.yl && (s.kind & 15) < 3;   // kinds >= 3: no splat
           }
           unsigned bal = __ballot_sync(0xffffffffu, hit);
           __syncthreads();

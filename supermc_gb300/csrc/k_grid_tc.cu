@@ -133,7 +133,7 @@ __device__ __forceinline__ void compact_append(bool hit, int v, int16_t *list, i
 }
 
 __device__ __forceinline__ bool splat_source(const Source &s) {
-  return (s.kind & 15) != 3 && s.xr > s.xl && s.yr > s.yl;
+  return (s.kind & 15) < 3 && s.xr > s.xl && s.yr > s.yl;   // kinds >= 3: no splat
 }
 
 __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, const EventRec *recs,

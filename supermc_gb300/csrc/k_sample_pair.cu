@@ -743,6 +743,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
     const int model = P.which_mc_model;
     const bool box_src = (model == 5 && P.sub_model == 1) || model == 7;
     const bool coll_src = model == 5 && P.alpha > 1e-8;
+    const bool coll_rec = coll_src || P.want_binary;   // density sources, or records for rho_binary
     const bool thick_src = model == 1 || P.want_ta || P.want_tb;
     const bool disk_n = P.shape_of_nucleons == 1, disk_e = P.shape_of_entropy == 1;
     const float peak = (float)P.peak;
@@ -878,7 +879,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
     }
     // collision sources, ordered by (projectile, target) index
     int ncs = 0;
-    if (coll_src && ncoll > 0) {
+    if (coll_rec && ncoll > 0) {
       // exclusive scan of per-projectile hit counts
       int c = tid < A ? sm.hits[0][tid] : 0;
       int v = c;
@@ -909,7 +910,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
           s.plane = 0;
           double aw = 0.;
           if (model == 5 && P.sub_model == 2) aw = (double)(1 / c) + (double)(1 / sm.hits[1][j]);
-          s.kind = SRC_COLL | (disk_e ? 16 : 0) | ((int)aw << SRC_AW_SHIFT);
+          s.kind = coll_src ? (SRC_COLL | (disk_e ? 16 : 0) | ((int)aw << SRC_AW_SHIFT)) : SRC_BINARY;
           double fw = P.alpha + (1. - P.alpha) * aw;
           // CollisionPair::getfluctfactor (src/MCnucl.cpp:730-731)
           if (P.fluct)
@@ -928,6 +929,38 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
     }
     __syncthreads();
     nsrc += ncs;
+    // spectators (MCnucl::getSpectators, src/MCnucl.cpp:1223-1248): the
+    // nucleons without a collision, projectile then target, nucleon order
+    if (P.want_spect) {
+      for (int k0 = 0; k0 < AB; k0 += kNT) {
+        const int k = k0 + tid, w = k < A ? 0 : 1, i = k < A ? k : k - A;
+        const bool flag = k < AB && sm.hits[w][i] == 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, flag);
+        __syncthreads();
+        if ((tid & 31) == 0) sm.ired[tid >> 5] = __popc(bal);
+        __syncthreads();
+        int woff = 0, tot = 0;
+        for (int q = 0; q < kNT / 32; q++) {
+          woff += q < (tid >> 5) ? sm.ired[q] : 0;
+          tot += sm.ired[q];
+        }
+        if (flag) {
+          Source s;
+          s.x = sm.X[w][i];
+          s.y = sm.Y[w][i];
+          set_window(s, s.x - d_max, s.x + d_max, P.xmin, P.dx, inv_dx, P.nx, true);
+          set_window(s, s.y - d_max, s.y + d_max, P.ymin, P.dy, inv_dy, P.ny, false);
+          s.mx0 = s.mx1 = s.my0 = s.my1 = 0;
+          s.kind = SRC_SPECT | (disk_n ? 16 : 0);
+          s.plane = w;
+          s.weight = disk_n ? disk_val : peak;
+          s.bx = s.by = 0.f;
+          S[nsrc + woff + __popc(bal & ((1u << (tid & 31)) - 1u))] = s;
+        }
+        nsrc += tot;
+      }
+      __syncthreads();
+    }
     // bounding box of all windows
     for (int k = tid; k < nsrc; k += kNT) {
       Source s = S[k];

@@ -240,7 +240,9 @@ struct Ctx {
   DevBuf<double4> avg_frame;
   DevBuf<int> avg_order, avg_seg, avg_count, avg_edges;
   DevBuf<float2> avg_bins;
-  DevBuf<float> avg_rho;
+  DevBuf<float> avg_rho, avg_ta, avg_tb, avg_aux;
+  DevBuf<Source> avg_view;
+  DevBuf<int> avg_status;
   DevBuf<double> avg_acc;
   std::vector<int> h_status;
   std::vector<EventRec> h_recs;
@@ -721,6 +723,7 @@ void smc_destroy(void *ctx) {
   c->attempts.release(); c->wounded.release(); c->rho_ev.release(); c->corr_ev.release(); c->cm_ev.release();
   c->mix_sys.release(); c->mix_ev.release(); c->mix_order.release(); c->kln64.release(); c->kln32.release();
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
+  c->avg_ta.release(); c->avg_tb.release(); c->avg_aux.release(); c->avg_view.release(); c->avg_status.release();
   c->avg_frame.release(); c->avg_order.release(); c->avg_seg.release(); c->avg_count.release();
   c->avg_edges.release(); c->avg_bins.release();
   c->ev_order.release(); c->tickets.release();
@@ -972,26 +975,44 @@ smc_status smc_adjoint(void *ctx, uint64_t first_event, int n, const double *xy_
   return worst;
 }
 
-smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_proj, const double *xy_targ,
-                       const double *b, int from_order, int to_order, int reaction_plane, double *mean,
-                       double *mean_rp, int *n_used) {
-  if (!ctx || !mean || n < 0 || from_order < 1 || to_order < from_order || (xy_proj && !xy_targ))
+smc_status smc_average_profiles(void *ctx, uint64_t first_event, int n, const double *xy_proj,
+                                const double *xy_targ, const double *b, int from_order, int to_order,
+                                const smc_average_outputs *o, int *n_used) {
+  if (!ctx || !o || n < 0 || from_order < 1 || to_order < from_order || (xy_proj && !xy_targ))
     return SMC_ERR_ARGUMENT;
   Ctx *c = static_cast<Ctx *>(ctx);
   if (n_used) *n_used = 0;
   if (n == 0) return SMC_OK;
   CK(cudaSetDevice(c->device));
-  smc_outputs none{};
-  smc_status s = set_thickness_flags(c, &none);
+  // what to produce: [kind][frame] host grids, frame 0 = participant plane, 1 = reaction plane
+  enum { K_SD, K_TA, K_TB, K_TATB, K_RHOB, K_SPA, K_SPB, K_N };
+  double *const want[K_N][2] = {{o->sd, o->sd_rp},           {o->ta, o->ta_rp},
+                                {o->tb, o->tb_rp},           {o->ta_tb, o->ta_tb_rp},
+                                {o->rho_binary, o->rho_binary_rp}, {o->spectator_a, o->spectator_a_rp},
+                                {o->spectator_b, o->spectator_b_rp}};
+  bool frame_on[2] = {false, false}, kind_on[K_N] = {};
+  for (int k = 0; k < K_N; k++)
+    for (int f = 0; f < 2; f++)
+      if (want[k][f]) { frame_on[f] = true; kind_on[k] = true; }
+  if (!frame_on[0] && !frame_on[1]) return SMC_ERR_ARGUMENT;
+  const bool thick = kind_on[K_TA] || kind_on[K_TB] || kind_on[K_TATB];
+  if (thick && c->P.which_mc_model == 7) return SMC_ERR_CONFIG;
+  // T_A, T_B from the thickness records splatted beside the density
+  smc_outputs req{};
+  float dummy = 0.f;
+  if (thick) req.ta = req.tb = &dummy;
+  smc_status s = set_thickness_flags(c, &req);
   if (s) return s;
   DevParams P = c->P;
   P.no_moments = 1;
+  P.want_spect = kind_on[K_SPA] || kind_on[K_SPB];
+  P.want_binary = kind_on[K_RHOB];
   const size_t g = (size_t)P.nx * P.ny;
   const int norders = to_order - from_order + 1;
-  const bool rp = reaction_plane != 0 && mean_rp;
-  CK(c->avg_acc.ensure(g * norders * 2));
-  CK(cudaMemsetAsync(c->avg_acc.p, 0, sizeof(double) * g * norders * 2, c->st));
-  double *acc = c->avg_acc.p, *acc_rp = c->avg_acc.p + g * norders;
+  const size_t slab = g * norders;   // one kind and frame
+  CK(c->avg_acc.ensure(slab * K_N * 2));
+  CK(cudaMemsetAsync(c->avg_acc.p, 0, sizeof(double) * slab * K_N * 2, c->st));
+  auto acc_of = [&](int k, int f, int q) { return c->avg_acc.p + ((size_t)(k * 2 + f) * norders + q) * g; };
   int used = 0;
   for (int off = 0; off < n; off += c->chunk) {
     const int m = std::min(c->chunk, n - off);
@@ -1001,30 +1022,53 @@ smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_
     CK(c->avg_state.ensure((size_t)m * P.max_src));
     CK(c->avg_rho.ensure((size_t)m * g));
     CK(c->ecc.ensure((size_t)m * smc::kEccLen));
-    const double *ip = nullptr, *it = nullptr, *ib = nullptr;
-    if (xy_proj) {
-      size_t np = (size_t)m * 2 * c->info.A, nt = (size_t)m * 2 * c->info.B;
-      CK(c->inj_p.ensure(np));
-      CK(c->inj_t.ensure(nt));
-      CK(cudaMemcpyAsync(c->inj_p.p, xy_proj + (size_t)off * 2 * c->info.A, sizeof(double) * np,
-                         cudaMemcpyHostToDevice, c->st));
-      CK(cudaMemcpyAsync(c->inj_t.p, xy_targ + (size_t)off * 2 * c->info.B, sizeof(double) * nt,
-                         cudaMemcpyHostToDevice, c->st));
-      ip = c->inj_p.p;
-      it = c->inj_t.p;
-      if (b) {
-        CK(c->inj_b.ensure(m));
-        CK(cudaMemcpyAsync(c->inj_b.p, b + off, sizeof(double) * m, cudaMemcpyHostToDevice, c->st));
-        ib = c->inj_b.p;
-      }
+    if (thick) { CK(c->avg_ta.ensure((size_t)m * g)); CK(c->avg_tb.ensure((size_t)m * g)); }
+    if (P.want_spect || P.want_binary) {
+      CK(c->avg_view.ensure((size_t)m * P.max_src));
+      CK(c->avg_status.ensure(m));
+      CK(c->avg_aux.ensure((size_t)m * g * 2));
+      CK(c->scratch.ensure((size_t)c->sms * c->occ2 * g));
     }
+    const double *ip, *it, *ib;
+    s = stage_injection(c, off, m, xy_proj, xy_targ, b, false, &ip, &it, &ib);
+    if (s) return s;
     const int grid1 = std::max(1, std::min(m, c->sms * c->occ1));
     const int grid3 = std::max(1, std::min(m, c->sms * 4));
     auto splat = [&]() {
       return timed(c, 1, [&] {
-        return launch_splat(c, P, m, c->recs.p, c->srcs.p, c->avg_rho.p, nullptr, nullptr, nullptr, c->ecc.p,
-                            c->status.p);
+        return launch_splat(c, P, m, c->recs.p, c->srcs.p, c->avg_rho.p, thick ? c->avg_ta.p : nullptr,
+                            thick ? c->avg_tb.p : nullptr, nullptr, c->ecc.p, c->status.p);
       });
+    };
+    // the grids of one frame after its transform and splat
+    auto accumulate = [&](int f, int q) -> smc_status {
+      if (want[K_SD][f]) CK(smc::launch_avg_accum(c->avg_rho.p, m, g, acc_of(K_SD, f, q), c->st));
+      if (want[K_TA][f]) CK(smc::launch_avg_accum(c->avg_ta.p, m, g, acc_of(K_TA, f, q), c->st));
+      if (want[K_TB][f]) CK(smc::launch_avg_accum(c->avg_tb.p, m, g, acc_of(K_TB, f, q), c->st));
+      if (want[K_TATB][f])
+        CK(smc::launch_avg_accum_prod(c->avg_ta.p, c->avg_tb.p, m, g, acc_of(K_TATB, f, q), c->st));
+      if (want[K_RHOB][f]) {   // MCnucl::calculate_rho_binary on the moved collisions
+        DevParams Pv = P;
+        Pv.n_planes = 1;
+        Pv.want_ta = Pv.want_tb = 0;
+        CK(smc::launch_avg_view(Pv, m, c->recs.p, c->srcs.p, c->avg_view.p, 0, grid3, c->st));
+        CK(launch_splat(c, Pv, m, c->recs.p, c->avg_view.p, c->avg_aux.p, nullptr, nullptr, c->scratch.p, c->ecc.p,
+                        c->avg_status.p));   // (a view's own status, e.g. zero density, is not the event's)
+        CK(smc::launch_avg_accum(c->avg_aux.p, m, g, acc_of(K_RHOB, f, q), c->st));
+      }
+      if (want[K_SPA][f] || want[K_SPB][f]) {   // MCnucl::calculate_spectator_density
+        DevParams Pv = P;
+        Pv.which_mc_model = 5;   // planes 1, 2 are written out as they are
+        Pv.n_planes = 3;
+        Pv.want_ta = Pv.want_tb = 1;
+        CK(smc::launch_avg_view(Pv, m, c->recs.p, c->srcs.p, c->avg_view.p, 1, grid3, c->st));
+        CK(launch_splat(c, Pv, m, c->recs.p, c->avg_view.p, nullptr, c->avg_aux.p, c->avg_aux.p + (size_t)m * g,
+                        c->scratch.p, c->ecc.p, c->avg_status.p));
+        if (want[K_SPA][f]) CK(smc::launch_avg_accum(c->avg_aux.p, m, g, acc_of(K_SPA, f, q), c->st));
+        if (want[K_SPB][f])
+          CK(smc::launch_avg_accum(c->avg_aux.p + (size_t)m * g, m, g, acc_of(K_SPB, f, q), c->st));
+      }
+      return SMC_OK;
     };
     CK(timed(c, 0, [&] {
       return smc::launch_sample_pair(P, xy_proj ? 0 : first_event + off, m, ip, it, ib, c->recs.p, c->srcs.p,
@@ -1034,18 +1078,21 @@ smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_
     CK(splat());   // MakeDensity.cpp:1275
     for (int q = 0; q < norders; q++) {
       const int order = from_order + q;
-      if (rp) {    // MakeDensity.cpp:1289-1300
+      if (frame_on[1]) {    // MakeDensity.cpp:1289-1330
         CK(smc::launch_avg_transform(P, m, c->recs.p, c->srcs.p, c->avg_state.p, c->avg_rho.p, order, 0, grid3,
                                      c->st));
         CK(splat());
-        CK(smc::launch_avg_accum(c->avg_rho.p, m, g, acc_rp + q * g, c->st));
+        s = accumulate(1, q);
+        if (s) return s;
       }
-      // MakeDensity.cpp:1331-1340
+      // MakeDensity.cpp:1331-1386
       CK(smc::launch_avg_transform(P, m, c->recs.p, c->srcs.p, c->avg_state.p, c->avg_rho.p, order, 1, grid3,
                                    c->st));
       CK(splat());
-      CK(smc::launch_avg_accum(c->avg_rho.p, m, g, acc + q * g, c->st));
-      c->stats.launches += rp ? 4 : 2;
+      if (frame_on[0]) {
+        s = accumulate(0, q);
+        if (s) return s;
+      }
     }
     c->stats.launches += 1;
     c->h_status.resize(m);
@@ -1066,16 +1113,29 @@ smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_
     if (worst) return status_error(worst);
   }
   if (n_used) *n_used = used;
-  if (used == 0) return SMC_OK;
-  std::vector<double> h(g * norders * (rp ? 2 : 1));
+  std::vector<double> h(slab * K_N * 2);
   CK(cudaMemcpyAsync(h.data(), c->avg_acc.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
-  // MakeDensity::setSd (src/MakeDensity.cpp:2514-2522): entropy = rho * finalFactor
-  const double ff = c->P.final_factor;
-  for (size_t k = 0; k < g * norders; k++) mean[k] = h[k] / used * ff;
-  if (rp)
-    for (size_t k = 0; k < g * norders; k++) mean_rp[k] = h[g * norders + k] / used * ff;
+  // means over the events with a collision; the entropy density is
+  // getRho * finalFactor (MakeDensity::setSd, src/MakeDensity.cpp:2514-2522)
+  for (int k = 0; k < K_N; k++)
+    for (int f = 0; f < 2; f++) {
+      if (!want[k][f]) continue;
+      const double scale = used ? (k == K_SD ? c->P.final_factor : 1.0) / used : 0.0;
+      const double *src = h.data() + (size_t)(k * 2 + f) * slab;
+      for (size_t i = 0; i < slab; i++) want[k][f][i] = src[i] * scale;
+    }
   return SMC_OK;
+}
+
+smc_status smc_average(void *ctx, uint64_t first_event, int n, const double *xy_proj, const double *xy_targ,
+                       const double *b, int from_order, int to_order, int reaction_plane, double *mean,
+                       double *mean_rp, int *n_used) {
+  if (!mean) return SMC_ERR_ARGUMENT;
+  smc_average_outputs o{};
+  o.sd = mean;
+  o.sd_rp = reaction_plane ? mean_rp : nullptr;
+  return smc_average_profiles(ctx, first_event, n, xy_proj, xy_targ, b, from_order, to_order, &o, n_used);
 }
 
 smc_status smc_average_binned(void *ctx, uint64_t first_event, int n, int order, int method, int nbins,

@@ -14,6 +14,12 @@ enum SrcKind : int {
   SRC_PART_BOX = 0,   // participant, bounding-box window, r <= 5w cut (MCnucl::addDensity)
   SRC_COLL = 1,       // binary collision, +-d_max window, dc <= 25 w^2 (MCnucl::setDensity)
   SRC_THICK = 2,      // participant, +-d_max window, r <= 5w (MCnucl::setThickness)
+  // 3: a participant's record for the eccentricity mask only (no splat)
+  SRC_SPECT = 4,      // spectator (non-participant), +-d_max window; splatted only
+                      // through the averaged mode's spectator view (MCnucl::getSpectators)
+  SRC_BINARY = 5,     // binary collision kept only for the averaged mode's rho_binary
+                      // view (no density source: MC-KLN, alpha = 0); kinds >= 3 are
+                      // never splatted directly
   SRC_RAW_BASE = 32,  // flag: participant box built at (bx, by), then moved
   SRC_AW_SHIFT = 6,   // bits 6-7: a binary collision's additional weight (sub_model 2)
 };
@@ -89,6 +95,8 @@ struct DevParams {
   int splat_mw;             // widest splat window in columns (+ margin)
   int n_planes;             // accumulator planes of the splat (1..3)
   int no_moments;           // skip the eccentricity pass (averaged mode)
+  int want_spect;           // spectator records (averaged mode's spectator densities)
+  int want_binary;          // binary-collision records whatever the model (rho_binary)
   // multiplicity fluctuations (cc_fluctuation_model 6): Gamma(k, theta)
   // weights per participant and per binary collision
   int fluct;

@@ -195,6 +195,29 @@ class Engine:
         self.last_average_events = used.value
         return mean, mean_rp
 
+    def average_profiles(self, first_event: int, n: int, from_order: int = 2, to_order: int = 3,
+                         want=("sd", "sd_rp"), xy_proj=None, xy_targ=None, b=None) -> dict:
+        """Averaged-mode means (smc_average_profiles): any of sd, ta_tb, ta,
+        tb, rho_binary, spectator_a, spectator_b and their _rp (reaction
+        plane) versions, each [orders, nx, ny]; the events used are left in
+        last_average_events."""
+        no = to_order - from_order + 1
+        outs = {k: np.zeros((no, self.nx, self.ny)) for k in want}
+        o = _lib.SmcAverageOutputs(*[_lib.ptr(outs.get(k)) for k in _lib.AVERAGE_FIELDS])
+        xp = xt = bb = None
+        if xy_proj is not None:
+            xp = np.ascontiguousarray(xy_proj, dtype=np.float64)
+            xt = np.ascontiguousarray(xy_targ, dtype=np.float64)
+            n = xp.shape[0]
+            if b is not None:
+                bb = np.ascontiguousarray(np.broadcast_to(b, (n,)), dtype=np.float64)
+        used = ctypes.c_int(0)
+        _lib.check(self.lib.smc_average_profiles(self.h, first_event, n, _lib.ptr(xp), _lib.ptr(xt), _lib.ptr(bb),
+                                                 from_order, to_order, ctypes.byref(o), ctypes.byref(used)),
+                   "smc_average_profiles")
+        self.last_average_events = used.value
+        return outs
+
     def average_binned(self, first_event: int, n: int, npart_edges, order: int = 2, method: int = 1):
         """Npart-binned event averages of rho * finalFactor, each event
         recentred and rotated to its order-n participant plane: method 0

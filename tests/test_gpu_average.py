@@ -123,3 +123,61 @@ def test_average_kln_vs_oracle(oracle, golden):
     want, used = oracle_average(oracle, vals, fill, len(bs), params=p)
     assert used == len(bs)
     assert_means_close(mean, mean_rp, want, tol=1e-4)
+
+
+def _oracle_profiles(oracle, vals, pa, pb, orders=(2, 3), params=None):
+    """The averaged-mode grids of the oracle after each frame's transform:
+    sd, T_A, T_B, T_A T_B, rho_binary, spectators A and B."""
+    from systems import oracle_params as op
+    ev = oracle.event(params if params is not None else op(vals))
+    acc, used = {}, 0
+    for k in range(len(pa)):
+        ev.inject(pa[k], pb[k])
+        if ev.pair() == 0:
+            continue
+        used += 1
+        assert ev.thickness() == 0 and ev.density() == 0
+        for o in orders:
+            for frame, step in (("rp", ev.recenter_resplat), ("rot", ev.rotate_resplat)):
+                assert step(o) == 0
+                ta, tb = ev.grid(0), ev.grid(1)
+                spa, spb = ev.spectator_density()
+                grids = {"sd": ev.grid(2) * vals["finalfactor"], "ta": ta, "tb": tb, "ta_tb": ta * tb,
+                         "rho_binary": ev.rho_binary(), "spectator_a": spa, "spectator_b": spb}
+                for name, gr in grids.items():
+                    key = (name + ("_rp" if frame == "rp" else ""), o)
+                    acc[key] = acc.get(key, 0.0) + gr
+    return {k: v / used for k, v in acc.items()}, used
+
+
+ALL = ("sd", "sd_rp", "ta_tb", "ta_tb_rp", "ta", "tb", "ta_rp", "tb_rp", "rho_binary", "rho_binary_rp",
+       "spectator_a", "spectator_b", "spectator_a_rp", "spectator_b_rp")
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_average_profiles_all_grids_vs_oracle(oracle, golden, name):
+    """T_A T_B, T_A, T_B, rho_binary and spectator means of the averaged mode
+    (MakeDensity.cpp:1342-1386, both frames) against the oracle."""
+    g = golden("glauber_inject.npz")
+    vals = values(SYSTEMS[name])
+    pa, pb, bs = g[name + "_pos_a"], g[name + "_pos_b"], g[name + "_b"]
+    eng = engine(vals)
+    out = eng.average_profiles(0, 0, 2, 3, want=ALL, xy_proj=pa, xy_targ=pb, b=bs)
+    want, used = _oracle_profiles(oracle, vals, pa, pb)
+    assert eng.last_average_events == used
+    for key in ALL:
+        for q, o in enumerate((2, 3)):
+            ref = want[(key, o)]
+            err = np.abs(out[key][q] - ref).max()
+            assert err <= GRID_TOL * max(ref.max(), 1e-30), f"{key} order {o}: {err:.3g} of {ref.max():.4g}"
+
+
+def test_average_profiles_sd_equals_smc_average(golden):
+    g = golden("glauber_inject.npz")
+    vals = values(SYSTEMS["auau200"])
+    pa, pb, bs = g["auau200_pos_a"], g["auau200_pos_b"], g["auau200_b"]
+    eng = engine(vals)
+    mean, mean_rp = eng.average(0, 0, 2, 3, True, xy_proj=pa, xy_targ=pb, b=bs)
+    out = eng.average_profiles(0, 0, 2, 3, want=("sd", "sd_rp", "ta_tb"), xy_proj=pa, xy_targ=pb, b=bs)
+    np.testing.assert_allclose(out["sd"], mean, rtol=0, atol=1e-6 * mean.max())
+    np.testing.assert_allclose(out["sd_rp"], mean_rp, rtol=0, atol=1e-6 * mean_rp.max())
