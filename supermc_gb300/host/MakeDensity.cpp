@@ -27,6 +27,7 @@ const Default kDefaults[] = {
     {"ecc_from_order", 1}, {"ecc_to_order", 9}, {"use_sd", 1}, {"use_ed", 1}, {"use_4col", 0}, {"use_block", 1},
     {"maxx", 15.0}, {"maxy", 15.0}, {"dx", 0.1}, {"dy", 0.1}, {"cc_fluctuation_model", 6},
     {"cc_fluctuation_Gamma_theta", 0.75}, {"generate_reaction_plane_avg_profile", 1}, {"cutdSdy", 0},
+    {"output_TATB", 1}, {"output_rho_binary", 1}, {"output_TA", 1}, {"output_spectator_density", 1},
     // extensions (0: the reference's hard-coded value)
     {"proj_R", 0}, {"proj_a", 0}, {"targ_R", 0}, {"targ_a", 0}, {"proj_d_min", 0}, {"targ_d_min", 0},
     {"siginNN_override", 0}, {"kln_npt", 48}, {"kln_nkt", 64}, {"kln_nphi", 32}, {"max_attempts", 0},
@@ -173,28 +174,51 @@ void MakeDensity::generate_profile_average(int nevent) {
   const bool sd = val(*reader_, "use_sd") != 0, block = val(*reader_, "use_block") != 0,
              four = val(*reader_, "use_4col") != 0;
   const bool rp = val(*reader_, "generate_reaction_plane_avg_profile") == 1;
+  const bool tatb = val(*reader_, "output_TATB") != 0, rhob = val(*reader_, "output_rho_binary") != 0,
+             ta = val(*reader_, "output_TA") != 0, spect = val(*reader_, "output_spectator_density") != 0;
+  const bool thick_ok = params_.which_mc_model != 7;   // sqrt(T_A T_B) has no thickness planes here
+  if ((tatb || ta) && !thick_ok)
+    std::fprintf(stderr, "supermc_gb300: output_TATB / output_TA: not produced for which_mc_model 7\n");
   const size_t g = (size_t)info_.nx * info_.ny;
   const int no = to - from + 1;
-  std::vector<double> mean(g * no), mean_rp(g * no);
+  // grids, in the order of smc_average_outputs
+  std::vector<double> grid[14];
+  smc_average_outputs o{};
+  double **slot[14] = {&o.sd, &o.sd_rp, &o.ta_tb, &o.ta_tb_rp, &o.ta, &o.tb, &o.ta_rp, &o.tb_rp,
+                       &o.rho_binary, &o.rho_binary_rp, &o.spectator_a, &o.spectator_b, &o.spectator_a_rp,
+                       &o.spectator_b_rp};
+  const bool on[14] = {true, rp, tatb && thick_ok, tatb && thick_ok && rp, ta && thick_ok, ta && thick_ok,
+                       ta && thick_ok && rp, ta && thick_ok && rp, rhob, rhob && rp, spect, spect, false, false};
+  // file stems (MakeDensity.cpp:741-1180; the reference writes no spectator
+  // means in the reaction-plane frame)
+  const char *stem[14] = {"sdAvg_order", "sdAvg_RP_order", "TATB_fromSd_order", "TATB_fromSd_RP_order",
+                          "nuclear_thickness_TA_fromSd_order", "nuclear_thickness_TB_fromSd_order",
+                          "nuclear_thickness_TA_fromSd_RP_order", "nuclear_thickness_TB_fromSd_RP_order",
+                          "rho_binary_fromSd_order", "rho_binary_fromSd_RP_order",
+                          "spectator_density_A_fromSd_order", "spectator_density_B_fromSd_order", "", ""};
+  for (int k = 0; k < 14; k++)
+    if (on[k]) {
+      grid[k].assign(g * no, 0.0);
+      *slot[k] = grid[k].data();
+    }
   int used = 0;
-  check(smc_average(ctx_, 0, nevent, nullptr, nullptr, nullptr, from, to, rp ? 1 : 0, mean.data(),
-                    rp ? mean_rp.data() : nullptr, &used),
-        "smc_average");
+  check(smc_average_profiles(ctx_, 0, nevent, nullptr, nullptr, nullptr, from, to, &o, &used),
+        "smc_average_profiles");
   if (!sd) return;
   char name[256];
-  for (int q = 0; q < no; q++) {
-    const int order = from + q;
-    for (int pass = 0; pass < (rp ? 2 : 1); pass++) {
-      const double *m = (pass ? mean_rp.data() : mean.data()) + (size_t)q * g;
-      const char *tag = pass ? "sdAvg_RP" : "sdAvg";
+  for (int k = 0; k < 14; k++) {
+    if (!on[k]) continue;
+    for (int q = 0; q < no; q++) {
+      const double *m = grid[k].data() + (size_t)q * g;
+      const int order = from + q;
       if (four) {
-        std::snprintf(name, sizeof(name), "data/%s_order_%d_4col.dat", tag, order);
+        std::snprintf(name, sizeof(name), "data/%s_%d_4col.dat", stem[k], order);
         check(smc_write_density_4col(m, info_.nx, info_.ny, -params_.maxx, -params_.maxy, params_.dx, params_.dy,
                                      0.0, 0.0, name),
               "smc_write_density_4col");
       }
       if (block) {
-        std::snprintf(name, sizeof(name), "data/%s_order_%d_block.dat", tag, order);
+        std::snprintf(name, sizeof(name), "data/%s_%d_block.dat", stem[k], order);
         check(smc_write_density_block(m, info_.nx, info_.ny, name), "smc_write_density_block");
       }
     }

@@ -3,7 +3,8 @@
 // (src/main.cpp:42-61) write the same files under data/.
 //   generateEccTable          operation 9: data/sn_ecc_eccp_<order>.dat
 //   generate_profile_ebe      operation 1: data/sd_event_<n>_block.dat / _4col.dat
-//   generate_profile_average  operation 3: data/sdAvg[_RP]_order_<n>_block.dat / _4col.dat
+//   generate_profile_average  operation 3: data/sdAvg[_RP]_order_<n>_block.dat / _4col.dat and
+//                             the TATB, rho_binary, nuclear_thickness, spectator_density means
 // Parameters are the reference's parameters.dat keys; a key the file does not
 // set takes the value the reference ships in its parameters.dat.  Failures
 // throw smc::Error (the reference exits).

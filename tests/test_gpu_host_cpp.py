@@ -60,8 +60,15 @@ def test_operation_1_profiles(tmp_path):
 
 def test_operation_3_averages(tmp_path):
     p = _run(tmp_path, operation=3, nev=16)
-    mean, mean_rp = _engine(p).average(0, 16, 2, 2, True)
-    got = np.loadtxt(tmp_path / "data" / "sdAvg_order_2_block.dat")
-    np.testing.assert_allclose(got, mean[0], rtol=1e-11, atol=1e-300)
-    got_rp = np.loadtxt(tmp_path / "data" / "sdAvg_RP_order_2_block.dat")
-    np.testing.assert_allclose(got_rp, mean_rp[0], rtol=1e-11, atol=1e-300)
+    # the means the reference writes by default (use_sd, output_TATB,
+    # output_rho_binary, output_TA, output_spectator_density), requested
+    # together as the driver requests them
+    prof = _engine(p).average_profiles(0, 16, 2, 2, want=(
+        "sd", "sd_rp", "ta_tb", "ta_tb_rp", "ta", "tb", "ta_rp", "tb_rp", "rho_binary", "rho_binary_rp",
+        "spectator_a", "spectator_b"))
+    for fname, key in (("sdAvg_order_2", "sd"), ("sdAvg_RP_order_2", "sd_rp"),
+                       ("TATB_fromSd_order_2", "ta_tb"), ("TATB_fromSd_RP_order_2", "ta_tb_rp"),
+                       ("nuclear_thickness_TA_fromSd_order_2", "ta"), ("nuclear_thickness_TB_fromSd_RP_order_2", "tb_rp"),
+                       ("rho_binary_fromSd_order_2", "rho_binary"), ("spectator_density_B_fromSd_order_2", "spectator_b")):
+        got = np.loadtxt(tmp_path / "data" / f"{fname}_block.dat")
+        np.testing.assert_allclose(got, prof[key][0], rtol=1e-11, atol=1e-300, err_msg=fname)
