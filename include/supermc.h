@@ -102,6 +102,8 @@ typedef struct smc_info {
   int kln_tmax;             /* subdivided table size                        */
   double kln_dT;            /* table thickness step [fm^-2]                 */
   int A, B;                 /* nucleons per nucleus                         */
+  int max_collisions;       /* per-event collision capacity (rows of
+                               smc_outputs.collisions)                      */
 } smc_info;
 
 /* Per-event results.  Every pointer may be NULL (not produced).  When
@@ -126,6 +128,10 @@ typedef struct smc_outputs {
   double *tangents;     /* [n][A+B][4] d(x,y)/dR, d(x,y)/da of each nucleon
                            (same order as positions; both nuclei's R, a
                            move together; zero unless ws_inverse_cdf)        */
+  double *collisions;   /* [n][max_collisions][2] binary-collision positions
+                           (pair midpoints) in the reference's order
+                           (MCnucl::createBinaryCollisions, src/MCnucl.cpp:
+                           326-352); the first ncoll rows of each event     */
 } smc_outputs;
 
 /* MCnucl::MCnucl + MakeDensity::MakeDensity: validates the configuration,
@@ -349,6 +355,20 @@ smc_status smc_write_ecc(const double *ecc, int n, int from_order, int to_order,
 smc_status smc_write_density_block(const double *grid, int nx, int ny, const char *filename);
 smc_status smc_write_density_4col(const double *grid, int nx, int ny, double xmin, double ymin, double dx, double dy,
                                   double rapidity, double npart, const char *filename);
+/* MCnucl::dumpBinaryTable (src/MCnucl.cpp:1175-1189): appends one line per
+ * binary collision, x and y (%10.3g each), of xy[ncoll][2]. */
+smc_status smc_write_binary_table(const double *xy, int ncoll, const char *filename);
+/* Nucleus::dumpParticipants / dumpNucleons (src/Nucleus.cpp:753-778) as
+ * dumpBinaryTable writes them (src/MCnucl.cpp:1193-1207) for one event:
+ * `participants` (wounded.data, overwritten): the wounded nucleons of the
+ * projectile then the target, x, y and the nucleus id 1 or 2 (each
+ * nucleus in nucleon order; the reference lists a target's participants
+ * in the order they were first hit); `proj`,
+ * `targ` (nucl1.data, nucl2.data, overwritten): every nucleon, x and y.
+ * xy [A+B][2] and wounded [A+B] as smc_outputs.positions / .wounded; any
+ * file name may be NULL. */
+smc_status smc_write_nucleon_tables(const double *xy, const uint8_t *wounded, int A, int B, const char *participants,
+                                    const char *proj, const char *targ);
 
 /* smc_inject without any device allocation.  No counterpart in the
  * reference (which allocates host arrays freely); it exists for callers that

@@ -27,7 +27,8 @@ EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "sm
            "smc_set_timing",
            "smc_set_grid_path", "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_write_ecc",
            "smc_write_density_block", "smc_write_density_4col", "smc_inject_noalloc", "smc_average",
-           "smc_average_binned", "smc_adjoint", "smc_autotune", "smc_generate_graph", "smc_average_profiles"]
+           "smc_average_binned", "smc_adjoint", "smc_autotune", "smc_generate_graph", "smc_average_profiles",
+           "smc_write_binary_table", "smc_write_nucleon_tables"]
 
 
 class SmcError(RuntimeError):
@@ -68,7 +69,7 @@ class SmcInfo(ctypes.Structure):
         ("nx", ctypes.c_int), ("ny", ctypes.c_int),
         ("sigin", ctypes.c_double), ("dsq", ctypes.c_double), ("width", ctypes.c_double),
         ("sigma_gg", ctypes.c_double), ("kln_tmax", ctypes.c_int), ("kln_dT", ctypes.c_double),
-        ("A", ctypes.c_int), ("B", ctypes.c_int),
+        ("A", ctypes.c_int), ("B", ctypes.c_int), ("max_collisions", ctypes.c_int),
     ]
 
 
@@ -85,7 +86,7 @@ class SmcOutputs(ctypes.Structure):
         ("ecc", ctypes.c_void_p), ("rho", ctypes.c_void_p), ("ta", ctypes.c_void_p), ("tb", ctypes.c_void_p),
         ("npart", ctypes.c_void_p), ("ncoll", ctypes.c_void_p), ("b", ctypes.c_void_p),
         ("attempts", ctypes.c_void_p), ("positions", ctypes.c_void_p), ("wounded", ctypes.c_void_p),
-        ("tangents", ctypes.c_void_p),
+        ("tangents", ctypes.c_void_p), ("collisions", ctypes.c_void_p),
     ]
 
 
@@ -140,6 +141,9 @@ def load() -> ctypes.CDLL:
     lib.smc_write_density_block.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
     lib.smc_write_density_4col.argtypes = [vp, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6 + [ctypes.c_char_p]
     lib.smc_get_stats.argtypes = [vp, ctypes.POINTER(SmcStats)]
+    lib.smc_write_binary_table.argtypes = [vp, ctypes.c_int, ctypes.c_char_p]
+    lib.smc_write_nucleon_tables.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p,
+                                             ctypes.c_char_p]
     lib.smc_reset_stats.argtypes = [vp]
     lib.smc_average.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_int, vp, vp, ctypes.POINTER(ctypes.c_int)]

@@ -194,7 +194,7 @@ struct Ctx {
   int chunk = 4096;
   DevBuf<EventRec> recs;
   DevBuf<Source> srcs;
-  DevBuf<double> ecc, pos, bvec, inj_p, inj_t, inj_b;
+  DevBuf<double> ecc, pos, bvec, inj_p, inj_t, inj_b, coll;
   DevBuf<float> rho, ta, tb, scratch;
   DevBuf<int> status, npart, ncoll, attempts;
   // buffers of the tensor-core splat: per-event densities (when not an
@@ -375,6 +375,7 @@ smc_status ensure_buffers(Ctx *c, int n, const smc_outputs *out) {
     if (out->positions) CK(c->pos.ensure((size_t)n * 2 * (c->info.A + c->info.B)));
     if (out->wounded) CK(c->wounded.ensure((size_t)n * (c->info.A + c->info.B)));
     if (out->tangents) CK(c->ntan.ensure((size_t)n * 4 * (c->info.A + c->info.B)));
+    if (out->collisions) CK(c->coll.ensure((size_t)n * 2 * P.max_coll));
   }
   if (!out->ecc || out->device == 0) CK(c->ecc.ensure((size_t)n * smc::kEccLen));
   return SMC_OK;
@@ -409,6 +410,34 @@ __global__ void k_order_events(const EventRec *recs, int n, int *order) {
   }
   __syncthreads();
   for (int e = tid; e < n; e += blockDim.x) order[atomicAdd(&hist[1023 - min(recs[e].nsrc >> 3, 1023)], 1)] = e;
+}
+
+// Binary-collision positions of each event, in source order (the
+// reference's order), one warp per event: out [n][max_coll][2].
+__global__ void k_collisions(const EventRec *recs, const Source *srcs, int n, int max_src, int max_coll,
+                             double *out) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int e = warp; e < n; e += nwarps) {
+    const Source *S = srcs + (size_t)e * max_src;
+    const int ns = recs[e].nsrc;
+    double *o = out + (size_t)e * max_coll * 2;
+    int pos = 0;
+    for (int k0 = 0; k0 < ns; k0 += 32) {
+      const int k = k0 + lane;
+      const int kind = k < ns ? (S[k].kind & 15) : -1;
+      const bool is = kind == smc::SRC_COLL || kind == smc::SRC_BINARY;
+      const unsigned bal = __ballot_sync(0xffffffffu, is);
+      if (is) {
+        const int p = pos + __popc(bal & ((1u << lane) - 1u));
+        if (p < max_coll) {
+          o[2 * p] = S[k].x;
+          o[2 * p + 1] = S[k].y;
+        }
+      }
+      pos += __popc(bal);
+    }
+  }
 }
 
 // worst per-event status of a chunk into *worst (atomic max)
@@ -506,6 +535,12 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
       return launch_splat(c, P, n, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p);
     }));
   }
+  double *coll = out->collisions ? (dev ? out->collisions + (size_t)off * 2 * P.max_coll : c->coll.p) : nullptr;
+  if (coll) {
+    k_collisions<<<(n + 7) / 8, 256, 0, c->st>>>(c->recs.p, c->srcs.p, n, P.max_src, P.max_coll, coll);
+    CK(cudaGetLastError());
+    c->stats.launches++;
+  }
   int *np = out->npart ? (dev ? out->npart + 2 * off : nullptr) : nullptr;
   int *nc = out->ncoll ? (dev ? out->ncoll + off : nullptr) : nullptr;
   double *bb = out->b ? (dev ? out->b + off : nullptr) : nullptr;
@@ -532,6 +567,9 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
       CK(cudaMemcpyAsync(out->wounded + (size_t)off * AB, wnd, (size_t)n * AB, cudaMemcpyDeviceToHost, c->st));
     if (out->tangents)
       CK(cudaMemcpyAsync(out->tangents + (size_t)off * 4 * AB, tg, sizeof(double) * n * 4 * AB,
+                         cudaMemcpyDeviceToHost, c->st));
+    if (out->collisions)
+      CK(cudaMemcpyAsync(out->collisions + (size_t)off * 2 * P.max_coll, coll, sizeof(double) * n * 2 * P.max_coll,
                          cudaMemcpyDeviceToHost, c->st));
     if (out->npart || out->ncoll || out->b || out->attempts) {
       c->h_recs.resize(n);
@@ -694,7 +732,7 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
   }
   smc_info &I = c->info;
   I.nx = P.nx; I.ny = P.ny; I.sigin = sigin; I.dsq = P.dsq; I.width = width; I.sigma_gg = P.sigma_gg;
-  I.kln_tmax = P.kln_tmax; I.kln_dT = P.kln_dT; I.A = p.Aproj; I.B = p.Atarg;
+  I.kln_tmax = P.kln_tmax; I.kln_dT = P.kln_dT; I.A = p.Aproj; I.B = p.Atarg; I.max_collisions = P.max_coll;
 
   if (c->tickets.ensure(4) != cudaSuccess) { smc_destroy(c); return SMC_ERR_CUDA; }
   size_t smem2 = smc::grid_smem(P);
@@ -717,7 +755,7 @@ void smc_destroy(void *ctx) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->st) cudaStreamSynchronize(c->st);
-  c->recs.release(); c->srcs.release(); c->ecc.release(); c->pos.release(); c->bvec.release();
+  c->recs.release(); c->srcs.release(); c->ecc.release(); c->pos.release(); c->bvec.release(); c->coll.release();
   c->inj_p.release(); c->inj_t.release(); c->inj_b.release(); c->rho.release(); c->ta.release();
   c->tb.release(); c->scratch.release(); c->status.release(); c->npart.release(); c->ncoll.release();
   c->attempts.release(); c->wounded.release(); c->rho_ev.release(); c->corr_ev.release(); c->cm_ev.release();
@@ -761,6 +799,7 @@ static smc_status set_thickness_flags(Ctx *c, const smc_outputs *out) {
   DevParams &P = c->P;
   P.want_ta = out->ta != nullptr;
   P.want_tb = out->tb != nullptr;
+  P.want_binary = out->collisions != nullptr;   // collision records whatever the model
   if ((out->ta || out->tb) && P.which_mc_model == 7) return SMC_ERR_CONFIG;
   // splat planes: Glauber rho (+ T_A, T_B on request); MC-KLN T_A, T_B;
   // sqrt(T_A T_B) scaling rho_A, rho_B
@@ -1254,6 +1293,12 @@ smc_status enqueue_batch(Ctx *c, int n, const smc_outputs *out, int *launches) {
     int *at = out->attempts ? out->attempts + off : nullptr;
     if (np || nc || bb || at) {
       k_scalars<<<(m + 255) / 256, 256, 0, c->st>>>(c->recs.p, m, np, nc, bb, at);
+      CK(cudaGetLastError());
+      nl++;
+    }
+    if (out->collisions) {
+      k_collisions<<<(m + 7) / 8, 256, 0, c->st>>>(c->recs.p, c->srcs.p, m, P.max_src, P.max_coll,
+                                                   out->collisions + (size_t)off * 2 * P.max_coll);
       CK(cudaGetLastError());
       nl++;
     }

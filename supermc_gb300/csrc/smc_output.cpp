@@ -76,4 +76,35 @@ smc_status smc_write_density_4col(const double *grid, int nx, int ny, double xmi
   return SMC_OK;
 }
 
+smc_status smc_write_binary_table(const double *xy, int ncoll, const char *filename) {
+  if (!filename || ncoll < 0 || (ncoll > 0 && !xy)) return SMC_ERR_ARGUMENT;
+  FILE *f = std::fopen(filename, "a");
+  if (!f) return SMC_ERR_ARGUMENT;
+  for (int c = 0; c < ncoll; c++) std::fprintf(f, "%10.3g%10.3g\n", xy[2 * c], xy[2 * c + 1]);
+  std::fclose(f);
+  return SMC_OK;
+}
+
+smc_status smc_write_nucleon_tables(const double *xy, const uint8_t *wounded, int A, int B, const char *participants,
+                                    const char *proj, const char *targ) {
+  if (!xy || A < 0 || B < 0 || (participants && !wounded)) return SMC_ERR_ARGUMENT;
+  if (participants) {
+    FILE *f = std::fopen(participants, "w");
+    if (!f) return SMC_ERR_ARGUMENT;
+    for (int k = 0; k < A + B; k++)
+      if (wounded[k]) std::fprintf(f, "%10.3g   %10.3g   %d\n", xy[2 * k], xy[2 * k + 1], k < A ? 1 : 2);
+    std::fclose(f);
+  }
+  const char *names[2] = {proj, targ};
+  for (int w = 0; w < 2; w++) {
+    if (!names[w]) continue;
+    FILE *f = std::fopen(names[w], "w");
+    if (!f) return SMC_ERR_ARGUMENT;
+    const int k0 = w ? A : 0, k1 = w ? A + B : A;
+    for (int k = k0; k < k1; k++) std::fprintf(f, "%10.3g%10.3g\n", xy[2 * k], xy[2 * k + 1]);
+    std::fclose(f);
+  }
+  return SMC_OK;
+}
+
 }  // extern "C"

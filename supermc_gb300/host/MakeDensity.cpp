@@ -136,19 +136,39 @@ void MakeDensity::generate_profile_ebe(int nevent) {
              four = val(*reader_, "use_4col") != 0;
   const double ff = params_.final_factor;
   const size_t g = (size_t)info_.nx * info_.ny;
+  const int AB = info_.A + info_.B, mc = info_.max_collisions;
   const int batch = std::max(1, std::min(batch_, 1024));   // host grids of one call
   std::vector<float> rho;
-  std::vector<int> npart;
-  std::vector<double> grid(g);
+  std::vector<int> npart, ncoll;
+  std::vector<double> grid(g), pos, coll;
+  std::vector<uint8_t> wounded;
   char name[256];
   for (int done = 0; done < nevent; done += batch) {
     const int n = std::min(batch, nevent - done);
     rho.resize((size_t)n * g);
     npart.resize((size_t)n * 2);
+    ncoll.resize(n);
+    pos.resize((size_t)n * AB * 2);
+    wounded.resize((size_t)n * AB);
+    coll.resize((size_t)n * mc * 2);
     smc_outputs out{};
     out.rho = rho.data();
     out.npart = npart.data();
+    out.ncoll = ncoll.data();
+    out.positions = pos.data();
+    out.wounded = wounded.data();
+    out.collisions = coll.data();
     check(smc_generate(ctx_, (uint64_t)done, n, &out), "smc_generate");
+    // MCnucl::dumpBinaryTable("data/binary.dat") after each event's pairing
+    // (src/MakeDensity.cpp:598; src/MCnucl.cpp:1175-1207)
+    for (int e = 0; e < n; e++) {
+      check(smc_write_binary_table(coll.data() + (size_t)e * mc * 2, std::min(ncoll[e], mc), "data/binary.dat"),
+            "smc_write_binary_table");
+      if (done + e + 1 == nevent)
+        check(smc_write_nucleon_tables(pos.data() + (size_t)e * AB * 2, wounded.data() + (size_t)e * AB, info_.A,
+                                       info_.B, "data/wounded.data", "data/nucl1.data", "data/nucl2.data"),
+              "smc_write_nucleon_tables");
+    }
     if (!sd) continue;
     for (int e = 0; e < n; e++) {
       // MakeDensity::setSd (src/MakeDensity.cpp:2514-2522)

@@ -2,7 +2,8 @@
 // GPU library's C ABI (include/supermc.h): the operations main() runs
 // (src/main.cpp:42-61) write the same files under data/.
 //   generateEccTable          operation 9: data/sn_ecc_eccp_<order>.dat
-//   generate_profile_ebe      operation 1: data/sd_event_<n>_block.dat / _4col.dat
+//   generate_profile_ebe      operation 1: data/sd_event_<n>_block.dat / _4col.dat,
+//                             data/binary.dat, wounded.data, nucl1.data, nucl2.data
 //   generate_profile_average  operation 3: data/sdAvg[_RP]_order_<n>_block.dat / _4col.dat and
 //                             the TATB, rho_binary, nuclear_thickness, spectator_density means
 // Parameters are the reference's parameters.dat keys; a key the file does not

@@ -48,7 +48,14 @@ def test_operation_9_eccentricity_files(tmp_path):
 def test_operation_1_profiles(tmp_path):
     from supermc_gb300.output import write_density_block
     p = _run(tmp_path, operation=1, nev=3)
-    out = _engine(p).generate(0, 3, want=("rho", "npart"))
+    out = _engine(p).generate(0, 3, want=("rho", "npart", "ncoll", "collisions", "positions", "wounded"))
+    # binary.dat: every event's collisions appended, %10.3g columns
+    lines = [f"{x:10.3g}{y:10.3g}" for e in range(3) for x, y in out["collisions"][e][:out["ncoll"][e]]]
+    assert (tmp_path / "data" / "binary.dat").read_text() == "".join(l + "\n" for l in lines)
+    A = 197
+    pos, wnd = out["positions"][2], out["wounded"][2].astype(bool)
+    want = "".join(f"{x:10.3g}   {y:10.3g}   {1 if k < A else 2}\n" for k, (x, y) in enumerate(pos) if wnd[k])
+    assert (tmp_path / "data" / "wounded.data").read_text() == want
     for e in range(3):
         sd = out["rho"][e].astype(np.float64) * 40.0
         write_density_block(sd, str(tmp_path / "ref_block.dat"))

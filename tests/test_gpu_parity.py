@@ -58,7 +58,7 @@ def test_injected_fixture_events(golden, name):
     vals = values(SYSTEMS[name])
     eng = engine(vals)
     out = eng.inject(g[name + "_pos_a"], g[name + "_pos_b"], g[name + "_b"],
-                     want=("ecc", "npart", "ncoll", "rho", "ta", "tb", "positions", "wounded"))
+                     want=("ecc", "npart", "ncoll", "rho", "ta", "tb", "positions", "wounded", "collisions"))
     np.testing.assert_array_equal(out["npart"][:, 0], g[name + "_npart1"])
     np.testing.assert_array_equal(out["npart"][:, 1], g[name + "_npart2"])
     np.testing.assert_array_equal(out["ncoll"], g[name + "_ncoll"])
@@ -70,6 +70,9 @@ def test_injected_fixture_events(golden, name):
             got = pos[sl][wnd[sl]]
             ref = g[name + f"_ev{k}_{key}"]
             np.testing.assert_array_equal(got[np.lexsort(got.T)], ref[np.lexsort(ref.T)])
+        # binary-collision positions of the reference's own run, in its order
+        ref_coll = g[f"{name}_ev{k}_coll"]
+        np.testing.assert_array_equal(out["collisions"][k][:out["ncoll"][k]], ref_coll.reshape(-1, 2))
         if k in (1, 3):
             for gname in ("ta", "tb", "rho"):
                 _digest(out[gname][k], g, f"{name}_ev{k}_{gname}")
