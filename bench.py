@@ -427,8 +427,10 @@ def run_gpu(args, vals) -> dict | None:
             "b": torch.empty((n,), dtype=torch.float64, device=dev)}
     flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device=dev)   # > L2 (129 MB)
 
-    def first_event(step):
-        return (step * world + rank) * n
+    from supermc_gb300.distributed import step_events
+
+    def first_event(step):   # disjoint event-id blocks per rank (no collective on the data path)
+        return step_events(step, rank, world, n)
 
     # ---- device-resident value: the batch as one CUDA graph (captured by the
     # first warm-up step, replayed with new event ids)
