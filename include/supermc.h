@@ -88,8 +88,13 @@ typedef struct smc_params {
                                             participant and binary collision
                                             (MCnucl.cpp:1271-1301; the
                                             reference's parameters.dat default);
-                                            1-5 (per-cell NBD) unsupported  */
+                                            1, 2: per-cell negative-binomial
+                                            density (MCnucl::fluctuateCurrent-
+                                            Density, :869-905) with k =
+                                            cc_fluctuation_k (1) or from
+                                            min(T_A, T_B) (2); 3-5 rejected */
   double cc_fluctuation_gamma_theta;     /* Gamma scale (cc_fluctuation_Gamma_theta) */
+  double cc_fluctuation_k;               /* NBD shape of model 1 (cc_fluctuation_k)  */
 } smc_params;
 
 /* Derived constants (MCnucl::MCnucl, src/MCnucl.cpp:22-154). */

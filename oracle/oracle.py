@@ -68,6 +68,7 @@ class Params(ctypes.Structure):
         ("npmin", ctypes.c_int), ("npmax", ctypes.c_int),
         ("kln_table", _D), ("kln_tmax", ctypes.c_int), ("kln_dT", ctypes.c_double),
         ("cc_fluctuation_model", ctypes.c_int), ("cc_fluctuation_gamma_theta", ctypes.c_double),
+        ("cc_fluctuation_k", ctypes.c_double),
     ]
 
 
@@ -151,6 +152,9 @@ class Oracle:
         lib.smco_kln_dndy.argtypes = [ctypes.POINTER(KLN), ctypes.c_double, ctypes.c_double,
                                       ctypes.c_int, ctypes.c_int, ctypes.c_int]
         lib.smco_gauss_legendre01.argtypes = [ctypes.c_int, _D, _D]
+        lib.smco_nbd_draw.restype = ctypes.c_double
+        lib.smco_nbd_draw.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_double,
+                                      ctypes.c_double]
         lib.smco_gamma_philox.restype = ctypes.c_double
         lib.smco_gamma_philox.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint32,
                                           ctypes.c_double, ctypes.c_double]

@@ -55,7 +55,7 @@ void smco_uniform2(uint64_t seed, uint64_t event, uint32_t stream, uint32_t slot
 }
 
 /* stream ids (low byte of the stream word; the retry attempt is above) */
-enum { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5 };
+enum { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5, ST_NBD = 6 };
 static uint32_t stream_id(int attempt, int sid) { return ((uint32_t)attempt << 8) | (uint32_t)sid; }
 
 /* ================================================================== */
@@ -685,15 +685,20 @@ static int g_pair_attempt, g_pair_philox;
  * Box-Muller normals.  Iteration t draws counters 32 slot + 2t, 2t + 1
  * (t < 15), the k < 1 uniform counter 32 slot + 31.  The reference draws
  * the same distribution from GSL (gsl_ran_gamma, MCnucl.cpp:1285,1298). */
+static double gamma_stream(uint64_t seed, uint64_t event, uint32_t sid, uint32_t base, double k, double theta);
 double smco_gamma_philox(uint64_t seed, uint64_t event, int attempt, uint32_t slot, double k, double theta) {
-  uint32_t sid = stream_id(attempt, ST_FLUCT);
+  return gamma_stream(seed, event, stream_id(attempt, ST_FLUCT), 32 * slot, k, theta);
+}
+
+/* Gamma(k, theta) from counters base + 2t, base + 2t + 1 and base + 31 */
+static double gamma_stream(uint64_t seed, uint64_t event, uint32_t sid, uint32_t base, double k, double theta) {
   double kk = k < 1 ? k + 1 : k;
   double d = kk - 1.0 / 3.0, c = 1.0 / sqrt(9.0 * d);
   double g = d; /* after 15 rejections (probability below 1e-19) */
   for (int t = 0; t < 15; t++) {
     double u[2], w[2];
-    smco_uniform2(seed, event, sid, 32 * slot + 2 * t, u);
-    smco_uniform2(seed, event, sid, 32 * slot + 2 * t + 1, w);
+    smco_uniform2(seed, event, sid, base + 2 * t, u);
+    smco_uniform2(seed, event, sid, base + 2 * t + 1, w);
     double x = sqrt(-2.0 * log(1.0 - u[0])) * cos(2.0 * M_PI * u[1]);
     double v = 1.0 + c * x;
     if (v <= 0) continue;
@@ -705,7 +710,7 @@ double smco_gamma_philox(uint64_t seed, uint64_t event, int attempt, uint32_t sl
   }
   if (k < 1) {
     double u[2];
-    smco_uniform2(seed, event, sid, 32 * slot + 31, u);
+    smco_uniform2(seed, event, sid, base + 31, u);
     g *= pow(1.0 - u[0], 1.0 / k);
   }
   return g * theta;
@@ -954,6 +959,68 @@ static double powi(double x, int m) {
 static double peak_height(double w) { return 1 / (2 * M_PI * w * w); }
 
 
+/* Poisson(lambda) from counters base.. (inversion below 10, else the
+ * transformed rejection of Hoermann, Insurance: Mathematics and Economics
+ * 12 (1993) 39) */
+static double poisson_stream(uint64_t seed, uint64_t event, uint32_t sid, uint32_t base, double lam) {
+  if (!(lam > 0)) return 0;
+  if (lam < 10) {
+    double u[2];
+    smco_uniform2(seed, event, sid, base, u);
+    double p = exp(-lam), s = p;
+    int n = 0;
+    while (u[0] > s && n < 1000) {
+      n++;
+      p *= lam / n;
+      s += p;
+    }
+    return n;
+  }
+  double slam = sqrt(lam), loglam = log(lam);
+  double b = 0.931 + 2.53 * slam, a = -0.059 + 0.02483 * b;
+  double invalpha = 1.1239 + 1.1328 / (b - 3.4), vr = 0.9277 - 3.6224 / (b - 2);
+  for (int t = 0; t < 32; t++) {
+    double uv[2];
+    smco_uniform2(seed, event, sid, base + t, uv);
+    double U = uv[0] - 0.5, V = uv[1];
+    double us = 0.5 - fabs(U);
+    double kf = floor((2 * a / us + b) * U + lam + 0.43);
+    if (us >= 0.07 && V <= vr) return kf;
+    if (kf < 0 || (us < 0.013 && V > us)) continue;
+    if (log(V) + log(invalpha) - log(a / (us * us) + b) <= -lam + kf * loglam - lgamma(kf + 1)) return kf;
+  }
+  return floor(lam + 0.5);
+}
+
+/* MCnucl::fluctuateCurrentDensity (MCnucl.cpp:869-905): every cell's density
+ * becomes n/(dx dy), n negative-binomial with mean nb = rho dx dy and shape
+ * k (constant, model 1; kpp min(T_A, T_B) sigma/10, model 2), drawn as
+ * Poisson(Gamma(k, nb/k)) from the cell's Philox stream (the event's stream
+ * set by smco_set_pair_stream; counters 64 cell + ...) */
+static void fluctuate_density(smco_event *e) {
+  const int model = e->p.cc_fluctuation_model;
+  const double area = e->p.dx * e->p.dy;
+  const double kpp = 1.0 / M_PI * area * 1.0 * (0.25 * 0.25 / 0.197327053 / 0.197327053);
+  const uint32_t sid = stream_id(0, ST_NBD);
+  size_t g = (size_t)e->p.nx * e->p.ny;
+  for (size_t c = 0; c < g; c++) {
+    double nb = e->rho[c] * area, k = e->p.cc_fluctuation_k;
+    if (model == 2) {
+      k = kpp * fmin(e->TA[c], e->TB[c]) * e->p.sigin / 10;
+      if (nb < 1e-10) continue;
+    }
+    if (!(nb > 0) || !(k > 0)) { e->rho[c] = 0; continue; }
+    double lam = gamma_stream(g_pair_seed, g_pair_event, sid, (uint32_t)(64 * c), k, nb / k);
+    e->rho[c] = poisson_stream(g_pair_seed, g_pair_event, sid, (uint32_t)(64 * c + 32), lam) / area;
+  }
+}
+
+double smco_nbd_draw(uint64_t seed, uint64_t event, uint32_t cell, double nb, double k) {
+  const uint32_t sid = stream_id(0, ST_NBD);
+  double lam = gamma_stream(seed, event, sid, 64 * cell, k, nb / k);
+  return poisson_stream(seed, event, sid, 64 * cell + 32, lam);
+}
+
 int smco_event_density(smco_event *e) {
   size_t g = (size_t)e->p.nx * e->p.ny;
   double Xmin = -e->p.xmax, Ymin = -e->p.ymax, dx = e->p.dx, dy = e->p.dy;
@@ -1038,6 +1105,7 @@ int smco_event_density(smco_event *e) {
     return 5;
   }
   if (e->dndy < 1e-15) return 3;
+  if (e->p.cc_fluctuation_model == 1 || e->p.cc_fluctuation_model == 2) fluctuate_density(e);
   return 0;
 }
 

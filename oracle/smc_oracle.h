@@ -74,7 +74,11 @@ typedef struct {
    * streams set by smco_set_pair_stream; 0 = none */
   int cc_fluctuation_model;
   double cc_fluctuation_gamma_theta;
+  double cc_fluctuation_k;   /* NBD shape of model 1 */
 } smco_params;
+/* negative-binomial count (mean nb, shape k) of one cell's stream, as
+ * fluctuateCurrentDensity draws it */
+double smco_nbd_draw(uint64_t seed, uint64_t event, uint32_t cell, double nb, double k);
 /* Gamma(k, theta) variate of one source (slot) of an event's fluctuation
  * stream */
 double smco_gamma_philox(uint64_t seed, uint64_t event, int attempt, uint32_t slot, double k, double theta);

@@ -61,6 +61,7 @@ class SmcParams(ctypes.Structure):
         ("max_attempts", ctypes.c_int), ("max_collisions", ctypes.c_int),
         ("ws_inverse_cdf", ctypes.c_int),
         ("cc_fluctuation_model", ctypes.c_int), ("cc_fluctuation_gamma_theta", ctypes.c_double),
+        ("cc_fluctuation_k", ctypes.c_double),
     ]
 
 

@@ -333,16 +333,20 @@ __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, co
     const double ff = P.final_factor, eps = 1e-15;
     double *out = ecc_out;
     const double dn = tot0;
+    // an all-zero density (possible after NBD fluctuations) has no centre of
+    // mass: the reference's sums are then NaN (0 * NaN), as here
+    const bool empty = !(dn > 0);
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
     for (int n = 1; n < 10; n++) {
       double *o = out + 5 * (n - 1);
       o[0] = o[1] = o[2] = o[3] = 0.0;
-      o[4] = (tot[n - 1] * ff) / (dn * ff);
+      o[4] = empty ? nan : (tot[n - 1] * ff) / (dn * ff);
       if (n >= LO && n <= HI && n >= from && n <= to) {
         int q = n - LO;
-        o[0] = -(tot[10 + 5 * q] * ff) / (tot[9] * ff + eps);
-        o[1] = -(tot[11 + 5 * q] * ff) / (tot[9] * ff + eps);
-        o[2] = -(tot[12 + 5 * q] * ff) / (tot[14 + 5 * q] * ff + eps);
-        o[3] = -(tot[13 + 5 * q] * ff) / (tot[14 + 5 * q] * ff + eps);
+        o[0] = empty ? nan : -(tot[10 + 5 * q] * ff) / (tot[9] * ff + eps);
+        o[1] = empty ? nan : -(tot[11 + 5 * q] * ff) / (tot[9] * ff + eps);
+        o[2] = empty ? nan : -(tot[12 + 5 * q] * ff) / (tot[14 + 5 * q] * ff + eps);
+        o[3] = empty ? nan : -(tot[13 + 5 * q] * ff) / (tot[14 + 5 * q] * ff + eps);
       }
     }
     out[45] = (double)(rec.npart1 + rec.npart2);

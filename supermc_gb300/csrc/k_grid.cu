@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
     float *ta = out_ta ? out_ta + (size_t)e * nx * ny : nullptr;
     float *tb = out_tb ? out_tb + (size_t)e * nx * ny : nullptr;
     if (tid == 0) s_status = rec.status;
-    KSum cm0, cm1, cm2;
+    KSum cm0, cm1, cm2, pre;   // pre: the density before NBD fluctuations (the zero-dN/dy test)
     const bool full = out_rho || ta || tb;
     __syncthreads();
 
@@ -221,6 +221,10 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
               const float a1 = np > 1 ? acc[(kR + rr) * nyp + j] : 0.f;
               const float a2 = np > 2 ? acc[(2 * kR + rr) * nyp + j] : 0.f;
               if (!post_cell(P, np, a0, a1, a2, v, t1, t2)) s_status = 4;
+              if (P.nbd) {
+                pre.add(v);
+                v = nbd_cell(P, rec.ev, (uint32_t)(i * ny + j), v, t1, t2);
+              }
             }
             rho[(size_t)i * ny + j] = v;
             if (ta) ta[(size_t)i * ny + j] = t1;
@@ -237,22 +241,25 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
     }
     // ---- centre of mass
     {
-      DF a = df_warp_sum(cm0.df()), b = df_warp_sum(cm1.df()), c = df_warp_sum(cm2.df());
+      DF a = df_warp_sum(cm0.df()), b = df_warp_sum(cm1.df()), c = df_warp_sum(cm2.df()), d = df_warp_sum(pre.df());
       if (lane == 0) {
         red[wid * 64] = make_float2(a.hi, a.lo);
         red[wid * 64 + 1] = make_float2(b.hi, b.lo);
         red[wid * 64 + 2] = make_float2(c.hi, c.lo);
+        red[wid * 64 + 3] = make_float2(d.hi, d.lo);
       }
       __syncthreads();
       if (tid == 0) {
-        double sa = 0, sb = 0, sc = 0;
+        double sa = 0, sb = 0, sc = 0, sd = 0;
         for (int w = 0; w < kWarps; w++) {
           sa += (double)red[w * 64].x + (double)red[w * 64].y;
           sb += (double)red[w * 64 + 1].x + (double)red[w * 64 + 1].y;
           sc += (double)red[w * 64 + 2].x + (double)red[w * 64 + 2].y;
+          sd += (double)red[w * 64 + 3].x + (double)red[w * 64 + 3].y;
         }
         s_cm[0] = sa; s_cm[1] = sb / sa; s_cm[2] = sc / sa;
-        if (!(sa * P.dx * P.dy >= 1e-15) && s_status == 0) s_status = 5;   // MCnucl.cpp:812-816
+        // MCnucl.cpp:812-816, on the density before the NBD fluctuations (:819)
+        if (!((P.nbd ? sd : sa) * P.dx * P.dy >= 1e-15) && s_status == 0) s_status = 5;
       }
       __syncthreads();
     }

@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
     int *corr = corr_scratch + (size_t)blockIdx.x * np * nx * ny;   // [plane][i][j], this CTA's
     const bool full = out_rho || ta || tb;
     if (tid == 0) s_status = rec.status;
-    KSum cm0, cm1, cm2;
+    KSum cm0, cm1, cm2, pre;   // pre: the density before NBD fluctuations (the zero-dN/dy test)
     const bool any = rec.imax > rec.imin && rec.jmax > rec.jmin;
     const int ti0 = rec.imin, tj0 = rec.jmin;
     const int nmt = any ? (rec.imax - rec.imin + kTM - 1) / kTM : 0;
@@ -448,6 +448,10 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
             const float a2 = 0.f;
             float v, t1, t2;
             if (!post_cell(P, np, a0, a1, a2, v, t1, t2)) s_status = 4;
+            if (P.nbd) {
+              pre.add(v);
+              v = nbd_cell(P, rec.ev, (uint32_t)g, v, t1, t2);
+            }
             rho[g] = v;
             if (ta) ta[g] = t1;
             if (tb) tb[g] = t2;
@@ -463,22 +467,25 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
     }
     // ---- centre of mass
     {
-      DF a = df_warp_sum(cm0.df()), b = df_warp_sum(cm1.df()), c = df_warp_sum(cm2.df());
+      DF a = df_warp_sum(cm0.df()), b = df_warp_sum(cm1.df()), c = df_warp_sum(cm2.df()), d = df_warp_sum(pre.df());
       if (lane == 0) {
         red[wid * 64] = make_float2(a.hi, a.lo);
         red[wid * 64 + 1] = make_float2(b.hi, b.lo);
         red[wid * 64 + 2] = make_float2(c.hi, c.lo);
+        red[wid * 64 + 3] = make_float2(d.hi, d.lo);
       }
       __syncthreads();
       if (tid == 0) {
-        double sa = 0, sb = 0, sc = 0;
+        double sa = 0, sb = 0, sc = 0, sd = 0;
         for (int w = 0; w < kTW; w++) {
           sa += (double)red[w * 64].x + (double)red[w * 64].y;
           sb += (double)red[w * 64 + 1].x + (double)red[w * 64 + 1].y;
           sc += (double)red[w * 64 + 2].x + (double)red[w * 64 + 2].y;
+          sd += (double)red[w * 64 + 3].x + (double)red[w * 64 + 3].y;
         }
         s_cm[0] = sa; s_cm[1] = sb / sa; s_cm[2] = sc / sa;
-        if (!(sa * P.dx * P.dy >= 1e-15) && s_status == 0) s_status = 5;   // MCnucl.cpp:812-816
+        // MCnucl.cpp:812-816, on the density before the NBD fluctuations (:819)
+        if (!((P.nbd ? sd : sa) * P.dx * P.dy >= 1e-15) && s_status == 0) s_status = 5;
       }
       __syncthreads();
     }

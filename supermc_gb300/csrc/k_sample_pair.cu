@@ -456,29 +456,7 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
 // 32 slot + 31.  The reference draws the same distribution from GSL
 // (gsl_ran_gamma, src/MCnucl.cpp:1271-1301).
 __device__ double gamma_weight(uint64_t seed, uint64_t ev, int attempt, uint32_t slot, double k, double theta) {
-  const uint32_t sid = stream_id(attempt, ST_FLUCT);
-  const double kk = k < 1 ? k + 1 : k;
-  const double d = kk - 1.0 / 3.0, c = 1.0 / sqrt(9.0 * d);
-  double g = d;   // after 15 rejections (probability below 1e-19)
-  for (int t = 0; t < 15; t++) {
-    double u0, u1, w0, w1;
-    uniform2(seed, ev, sid, 32 * slot + 2 * t, u0, u1);
-    uniform2(seed, ev, sid, 32 * slot + 2 * t + 1, w0, w1);
-    const double x = sqrt(-2.0 * log(1.0 - u0)) * cos(2.0 * M_PI * u1);
-    double v = 1.0 + c * x;
-    if (v <= 0) continue;
-    v = v * v * v;
-    if (log(1.0 - w0) < 0.5 * x * x + d - d * v + d * log(v)) {
-      g = d * v;
-      break;
-    }
-  }
-  if (k < 1) {
-    double u0, u1;
-    uniform2(seed, ev, sid, 32 * slot + 31, u0, u1);
-    g *= pow(1.0 - u0, 1.0 / k);
-  }
-  return g * theta;
+  return gamma_philox(seed, ev, stream_id(attempt, ST_FLUCT), 32 * slot, k, theta);
 }
 
 // tangent of nucleon k (sorted order, projectile first) of event e
@@ -990,6 +968,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
       r.npart1 = np1; r.npart2 = np2; r.ncoll = ncoll; r.nsrc = nsrc;
       r.attempts = attempt + 1; r.status = status;
       r.imin = imin; r.imax = imax; r.jmin = jmin; r.jmax = jmax;
+      r.ev = ev;
       recs[e] = r;
     }
     __syncthreads();

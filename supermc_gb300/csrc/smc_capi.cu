@@ -315,8 +315,10 @@ smc_status validate(const smc_params &p) {
   if (p.ecc_from_order < 1 || p.ecc_to_order > 9 || p.ecc_from_order > p.ecc_to_order) return SMC_ERR_CONFIG;
   if (p.bmax < p.bmin || p.bmin < 0) return SMC_ERR_CONFIG;
   // multiplicity fluctuations: none, or the Gamma weights of model 6
-  if (p.cc_fluctuation_model != 0 && p.cc_fluctuation_model != 6) return SMC_ERR_CONFIG;
+  if (p.cc_fluctuation_model < 0 || (p.cc_fluctuation_model > 2 && p.cc_fluctuation_model != 6)) return SMC_ERR_CONFIG;
   if (p.cc_fluctuation_model == 6 && !(p.cc_fluctuation_gamma_theta > 0)) return SMC_ERR_CONFIG;
+  if (p.cc_fluctuation_model == 1 && !(p.cc_fluctuation_k > 0)) return SMC_ERR_CONFIG;
+  if (p.cc_fluctuation_model == 2 && p.which_mc_model == 7) return SMC_ERR_CONFIG;   // no T_A, T_B planes
   // inverse-CDF radii: spherical Woods-Saxon nuclei
   if (p.ws_inverse_cdf && (p.Aproj < 3 || p.Atarg < 3 || p.proj_deformed || p.targ_deformed)) return SMC_ERR_CONFIG;
   return SMC_OK;
@@ -686,6 +688,12 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
   P.sigin = sigin;
   P.sigma_gg = sigma_gg_from(sigin, width);
   P.alpha = p.alpha; P.final_factor = p.final_factor;
+  if (p.cc_fluctuation_model == 1 || p.cc_fluctuation_model == 2) {   // MCnucl.cpp:869-905
+    const double hbarc = 0.197327053;
+    P.nbd = p.cc_fluctuation_model;
+    P.nbd_k = p.cc_fluctuation_k;
+    P.nbd_kpp = 1.0 / M_PI * p.dx * p.dy * 1.0 * (0.25 * 0.25 / hbarc / hbarc);
+  }
   if (p.cc_fluctuation_model == 6) {   // MCnucl.cpp:1271-1301
     const double eps = 1e-8, th = p.cc_fluctuation_gamma_theta;
     P.fluct = 1;
@@ -797,8 +805,10 @@ smc_status smc_synchronize(void *ctx) {
 
 static smc_status set_thickness_flags(Ctx *c, const smc_outputs *out) {
   DevParams &P = c->P;
-  P.want_ta = out->ta != nullptr;
-  P.want_tb = out->tb != nullptr;
+  // model-2 NBD fluctuations of the Glauber density need T_A, T_B per cell
+  const bool nbd_thick = P.nbd == 2 && P.which_mc_model == 5;
+  P.want_ta = out->ta != nullptr || nbd_thick;
+  P.want_tb = out->tb != nullptr || nbd_thick;
   P.want_binary = out->collisions != nullptr;   // collision records whatever the model
   if ((out->ta || out->tb) && P.which_mc_model == 7) return SMC_ERR_CONFIG;
   // splat planes: Glauber rho (+ T_A, T_B on request); MC-KLN T_A, T_B;

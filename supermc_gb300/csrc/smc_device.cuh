@@ -101,6 +101,10 @@ struct DevParams {
   // weights per participant and per binary collision
   int fluct;
   double fluct_k_part, fluct_th_part, fluct_k_coll, fluct_th_coll;
+  // per-cell negative-binomial fluctuations (cc_fluctuation_model 1, 2):
+  // k = nbd_k (model 1) or nbd_kpp min(T_A, T_B) sigma_in / 10 (model 2)
+  int nbd;
+  double nbd_k, nbd_kpp;
 };
 
 // Which events a persistent CTA takes.  Static: blockIdx.x, + gridDim.x, ...
@@ -130,6 +134,7 @@ struct EventRec {
   int npart1, npart2, ncoll, nsrc;
   int attempts, status;
   int imin, imax, jmin, jmax;   // bounding box of all splat windows (grid idx)
+  unsigned long long ev;        // global event id (keys the per-cell fluctuation streams)
 };
 
 // ---------------------------------------------------------------- Philox
@@ -209,10 +214,94 @@ __host__ __device__ __forceinline__ void uniform2f(uint64_t seed, uint64_t event
   u1 = u53f(c[2], c[3]);
 }
 
-enum StreamId : uint32_t { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5 };
+enum StreamId : uint32_t { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5, ST_NBD = 6 };
 __host__ __device__ __forceinline__ uint32_t stream_id(int attempt, uint32_t sid) {
   return ((uint32_t)attempt << 8) | sid;
 }
+
+#ifdef __CUDACC__
+// Gamma(k, theta) from counters base + 2t, base + 2t + 1 (t < 15) and, for
+// k < 1, base + 31 of a Philox stream: the method of Marsaglia and Tsang
+// ("A simple method for generating gamma variables", ACM TOMS 26 (2000)
+// 363) with Gamma(k) = Gamma(k+1) U^(1/k) for k < 1 and Box-Muller normals.
+static __device__ inline double gamma_philox(uint64_t seed, uint64_t ev, uint32_t sid, uint32_t base, double k,
+                                      double theta) {
+  const double kk = k < 1 ? k + 1 : k;
+  const double d = kk - 1.0 / 3.0, c = 1.0 / sqrt(9.0 * d);
+  double g = d;   // after 15 rejections (probability below 1e-19)
+  for (int t = 0; t < 15; t++) {
+    double u0, u1, w0, w1;
+    uniform2(seed, ev, sid, base + 2 * t, u0, u1);
+    uniform2(seed, ev, sid, base + 2 * t + 1, w0, w1);
+    const double x = sqrt(-2.0 * log(1.0 - u0)) * cos(2.0 * M_PI * u1);
+    double v = 1.0 + c * x;
+    if (v <= 0) continue;
+    v = v * v * v;
+    if (log(1.0 - w0) < 0.5 * x * x + d - d * v + d * log(v)) {
+      g = d * v;
+      break;
+    }
+  }
+  if (k < 1) {
+    double u0, u1;
+    uniform2(seed, ev, sid, base + 31, u0, u1);
+    g *= pow(1.0 - u0, 1.0 / k);
+  }
+  return g * theta;
+}
+
+// Poisson(lambda) from counters base, base + 1, ... (< 32): inversion below
+// lambda = 10, else the transformed rejection with squeeze of Hoermann
+// ("The transformed rejection method for generating Poisson random
+// variables", Insurance: Mathematics and Economics 12 (1993) 39).
+static __device__ inline double poisson_philox(uint64_t seed, uint64_t ev, uint32_t sid, uint32_t base, double lam) {
+  if (!(lam > 0)) return 0;
+  if (lam < 10) {
+    double u, unused;
+    uniform2(seed, ev, sid, base, u, unused);
+    double p = exp(-lam), s = p;
+    int n = 0;
+    while (u > s && n < 1000) {
+      n++;
+      p *= lam / n;
+      s += p;
+    }
+    return n;
+  }
+  const double slam = sqrt(lam), loglam = log(lam);
+  const double b = 0.931 + 2.53 * slam, a = -0.059 + 0.02483 * b;
+  const double invalpha = 1.1239 + 1.1328 / (b - 3.4), vr = 0.9277 - 3.6224 / (b - 2);
+  for (int t = 0; t < 32; t++) {
+    double U, V;
+    uniform2(seed, ev, sid, base + t, U, V);
+    U -= 0.5;
+    const double us = 0.5 - fabs(U);
+    const double kf = floor((2 * a / us + b) * U + lam + 0.43);
+    if (us >= 0.07 && V <= vr) return kf;
+    if (kf < 0 || (us < 0.013 && V > us)) continue;
+    if (log(V) + log(invalpha) - log(a / (us * us) + b) <= -lam + kf * loglam - lgamma(kf + 1)) return kf;
+  }
+  return floor(lam + 0.5);   // after 32 rejections (probability below 1e-30)
+}
+
+// MCnucl::fluctuateCurrentDensity (src/MCnucl.cpp:869-905): the cell's
+// density v becomes n/(dx dy), n negative-binomial with mean nb = v dx dy
+// and shape k (NBD::rand(nb/(nb+k), k)), drawn as Poisson(Gamma(k, nb/k))
+// from the cell's stream (stream 6, counters 64 cell + ...).  t1, t2: T_A,
+// T_B of the cell (model 2).
+static __device__ __noinline__ float nbd_cell(const DevParams &P, uint64_t ev, uint32_t cell, float v, float t1, float t2) {
+  const double area = P.dx * P.dy, nb = (double)v * area;
+  double k = P.nbd_k;
+  if (P.nbd == 2) {
+    k = P.nbd_kpp * fmin((double)t1, (double)t2) * P.sigin / 10;
+    if (nb < 1e-10) return v;   // left as it is (MCnucl.cpp:893-895)
+  }
+  if (!(nb > 0) || !(k > 0)) return 0.f;   // NBD::rand is 0 for p = 0 or p = 1
+  const uint32_t sid = stream_id(0, ST_NBD);
+  const double lam = gamma_philox(P.seed, ev, sid, 64 * cell, k, nb / k);
+  return (float)(poisson_philox(P.seed, ev, sid, 64 * cell + 32, lam) / area);
+}
+#endif
 
 // ------------------------------------------------------- exact helpers
 // (int)((v - mn)/d) as the reference computes it in FP64 (C++ truncation

@@ -145,7 +145,7 @@ extern "C" smc_status smc_inject_noalloc(const smc_params *params, int n, const 
   if (p.Aproj < 1 || p.Atarg < 1 || p.Aproj > smc::kMaxA || p.Atarg > smc::kMaxA) return SMC_ERR_CONFIG;
   if (!(p.dx > 0) || !(p.dy > 0) || !(p.maxx > 0) || !(p.maxy > 0)) return SMC_ERR_CONFIG;
   if (p.ecc_from_order < 1 || p.ecc_to_order > 9 || p.ecc_from_order > p.ecc_to_order) return SMC_ERR_CONFIG;
-  if (p.cc_fluctuation_model != 0 && p.cc_fluctuation_model != 6) return SMC_ERR_CONFIG;
+  if (p.cc_fluctuation_model != 0 && p.cc_fluctuation_model != 6) return SMC_ERR_CONFIG;   // no per-cell NBD here
   if (p.cc_fluctuation_model == 6 && !(p.cc_fluctuation_gamma_theta > 0)) return SMC_ERR_CONFIG;
   if (n == 0) return SMC_OK;
 

@@ -46,6 +46,7 @@ def smc_params_from(vals: dict[str, float], seed: int = 1) -> _lib.SmcParams:
     p.ws_inverse_cdf = int(v["ws_inverse_cdf"])
     p.cc_fluctuation_model = int(v["cc_fluctuation_model"])
     p.cc_fluctuation_gamma_theta = v["cc_fluctuation_gamma_theta"]
+    p.cc_fluctuation_k = v["cc_fluctuation_k"]
     return p
 
 

@@ -26,7 +26,7 @@ const Default kDefaults[] = {
     {"randomSeed", -1}, {"finalFactor", 40.0}, {"average_from_order", 2}, {"average_to_order", 3},
     {"ecc_from_order", 1}, {"ecc_to_order", 9}, {"use_sd", 1}, {"use_ed", 1}, {"use_4col", 0}, {"use_block", 1},
     {"maxx", 15.0}, {"maxy", 15.0}, {"dx", 0.1}, {"dy", 0.1}, {"cc_fluctuation_model", 6},
-    {"cc_fluctuation_Gamma_theta", 0.75}, {"generate_reaction_plane_avg_profile", 1}, {"cutdSdy", 0},
+    {"cc_fluctuation_Gamma_theta", 0.75}, {"cc_fluctuation_k", 0.75}, {"generate_reaction_plane_avg_profile", 1}, {"cutdSdy", 0},
     {"output_TATB", 1}, {"output_rho_binary", 1}, {"output_TA", 1}, {"output_spectator_density", 1},
     // extensions (0: the reference's hard-coded value)
     {"proj_R", 0}, {"proj_a", 0}, {"targ_R", 0}, {"targ_a", 0}, {"proj_d_min", 0}, {"targ_d_min", 0},
@@ -96,6 +96,7 @@ smc_params params_from(const ParameterReader &p) {
   s.ws_inverse_cdf = (int)val(p, "ws_inverse_cdf");
   s.cc_fluctuation_model = (int)val(p, "cc_fluctuation_model");
   s.cc_fluctuation_gamma_theta = val(p, "cc_fluctuation_Gamma_theta");
+  s.cc_fluctuation_k = val(p, "cc_fluctuation_k");
   return s;
 }
 

@@ -33,7 +33,8 @@ def oracle_params(vals: dict, sigma_gg: float | None = None):
                   collision_criterion=int(vals["collision_criterion"]), final_factor=vals["finalfactor"],
                   npmin=int(vals["npmin"]), npmax=int(vals["npmax"]),
                   cc_fluctuation_model=int(vals["cc_fluctuation_model"]),
-                  cc_fluctuation_gamma_theta=vals["cc_fluctuation_gamma_theta"])
+                  cc_fluctuation_gamma_theta=vals["cc_fluctuation_gamma_theta"],
+                  cc_fluctuation_k=vals["cc_fluctuation_k"])
 
 
 def fmt8(a):

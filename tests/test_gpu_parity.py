@@ -287,3 +287,49 @@ def test_kln_events_vs_oracle(oracle):
             ref = ev.grid(w)
             assert np.abs(out[key][k] - ref).max() <= 1e-4 * ref.max()
         np.testing.assert_allclose(out["ecc"][k], ev.eccentricities(1, 9, bs[k]), rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("model,over", [
+    (1, dict()),                                                         # Glauber, constant k
+    (2, dict()),                                                         # Glauber, k from min(T_A, T_B)
+    (2, dict(which_mc_model=1, sub_model=7, **{"lambda": 0.288})),       # MC-KLN
+])
+def test_nbd_fluctuations_vs_oracle(oracle, model, over):
+    """Per-cell negative-binomial densities (cc_fluctuation_model 1, 2): the
+    GPU draws each cell's count from the same Philox stream as the oracle.
+    A cell whose FP32 mean sits within rounding of a count boundary can
+    draw the neighbouring count, so nearly all events match everywhere."""
+    from oracle.oracle import _ptr
+    vals = values(SYSTEMS["auau200"], cc_fluctuation_model=model, cc_fluctuation_k=0.75, **over)
+    pa, pb, bs, _ = _oracle_events(oracle, values(SYSTEMS["auau200"]), 8, 5)
+    eng = engine(vals, seed=0)
+    out = eng.inject(pa, pb, bs, want=("ecc", "npart", "ncoll", "rho"))
+    p = oracle_params(vals)
+    if int(vals["which_mc_model"]) == 1:
+        table = np.ascontiguousarray(eng.kln_table())
+        p.kln_table = _ptr(table)
+        p.kln_tmax = eng.info.kln_tmax
+        p.kln_dT = eng.info.kln_dT
+    ev = oracle.event(p)
+    area = vals["dx"] * vals["dy"]
+    exact = 0
+    try:
+        for k in range(len(bs)):
+            oracle.lib.smco_set_pair_stream(0, k, 0, 1)
+            ev.inject(pa[k], pb[k])
+            ev.pair()
+            assert ev.thickness() == 0
+            if ev.density() != 0:
+                continue
+            rho = ev.grid(2)
+            # counts per cell: integers on both sides
+            n_gpu, n_ref = out["rho"][k] * area, rho * area
+            assert np.abs(n_gpu - np.round(n_gpu)).max() < 1e-3
+            bad = np.abs(n_gpu - n_ref) > 0.5
+            assert bad.sum() <= max(2, 1e-3 * (n_ref > 0).sum())
+            if not bad.any():
+                exact += 1
+                assert_ecc_close(out["ecc"][k], ev.eccentricities(1, 9, bs[k]))
+    finally:
+        oracle.lib.smco_set_pair_stream(0, 0, 0, 0)
+    assert exact >= len(bs) - 2

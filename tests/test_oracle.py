@@ -217,3 +217,25 @@ def test_gamma_weights_follow_the_gamma_distribution(oracle, k, theta):
     x = np.array([oracle.lib.smco_gamma_philox(11, ev, 0, s, k, theta) for ev in range(4) for s in range(5000)])
     assert stats.kstest(x, "gamma", args=(k, 0, theta)).pvalue > 1e-3
     assert abs(x.mean() - k * theta) < 5 * np.sqrt(k * theta * theta / len(x))
+
+
+@pytest.mark.parametrize("nb,k", [(0.3, 0.75), (4.0, 0.75), (25.0, 2.0), (60.0, 0.5)])
+def test_nbd_counts_follow_the_negative_binomial(oracle, nb, k):
+    """The per-cell counts of cc_fluctuation_model 1/2 (NBD::rand(nb/(nb+k), k)
+    in MCnucl::fluctuateCurrentDensity, MCnucl.cpp:869-905): mean nb,
+    variance nb (1 + nb/k), the negative-binomial pmf (chi-square)."""
+    from scipy import stats
+    x = np.array([oracle.lib.smco_nbd_draw(5, ev, c, nb, k) for ev in range(4) for c in range(5000)])
+    assert np.all(x == np.floor(x)) and x.min() >= 0
+    n = len(x)
+    assert abs(x.mean() - nb) < 5 * np.sqrt(nb * (1 + nb / k) / n)
+    p = k / (k + nb)   # scipy's success probability
+    var = nb * (1 + nb / k)
+    assert abs(x.var() / var - 1) < 0.1
+    hi = int(stats.nbinom.ppf(0.999, k, p))
+    obs = np.bincount(np.minimum(x.astype(int), hi), minlength=hi + 1)
+    exp_ = stats.nbinom.pmf(np.arange(hi + 1), k, p) * n
+    exp_[-1] += stats.nbinom.sf(hi, k, p) * n
+    keep = exp_ > 5
+    chi2 = (((obs - exp_) ** 2 / exp_)[keep]).sum()
+    assert stats.chi2.sf(chi2, keep.sum() - 1) > 1e-4
