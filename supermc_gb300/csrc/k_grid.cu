@@ -75,7 +75,9 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
   return L;
 }
 
-template <int LO, int HI>
+// NBD: the per-cell negative-binomial fluctuations (a separate instance, so
+// that the common case carries none of their registers)
+template <int LO, int HI, bool NBD>
 // five CTAs per SM (51 registers per thread, shared memory for five 8-row strips):
 // latency-bound work wants resident warps more than registers
 __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, const EventRec *recs, const Source *srcs,
@@ -221,7 +223,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
               const float a1 = np > 1 ? acc[(kR + rr) * nyp + j] : 0.f;
               const float a2 = np > 2 ? acc[(2 * kR + rr) * nyp + j] : 0.f;
               if (!post_cell(P, np, a0, a1, a2, v, t1, t2)) s_status = 4;
-              if (P.nbd) {
+              if (NBD) {
                 pre.add(v);
                 v = nbd_cell(P, rec.ev, (uint32_t)(i * ny + j), v, t1, t2);
               }
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
         }
         s_cm[0] = sa; s_cm[1] = sb / sa; s_cm[2] = sc / sa;
         // MCnucl.cpp:812-816, on the density before the NBD fluctuations (:819)
-        if (!((P.nbd ? sd : sa) * P.dx * P.dy >= 1e-15) && s_status == 0) s_status = 5;
+        if (!((NBD ? sd : sa) * P.dx * P.dy >= 1e-15) && s_status == 0) s_status = 5;
       }
       __syncthreads();
     }
@@ -281,7 +283,8 @@ size_t grid_smem(const DevParams &P) { return grid_layout(P.nx, P.ny, P.splat_mw
 
 int grid_blocks_per_sm(const DevParams &P) {
   const bool narrow = P.ecc_from >= 2 && P.ecc_to <= 5;
-  const void *k = narrow ? (const void *)k_grid<2, 5> : (const void *)k_grid<1, 9>;
+  const void *k = P.nbd ? (narrow ? (const void *)k_grid<2, 5, true> : (const void *)k_grid<1, 9, true>)
+                        : (narrow ? (const void *)k_grid<2, 5, false> : (const void *)k_grid<1, 9, false>);
   size_t smem = grid_smem(P);
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 1;
   int nb = 1;
@@ -294,7 +297,8 @@ cudaError_t launch_grid(const DevParams &P, int n_events, const EventRec *recs, 
                         cudaStream_t st, const int *order, int *ticket) {
   size_t smem = grid_smem(P);
   const bool narrow = P.ecc_from >= 2 && P.ecc_to <= 5;
-  auto kern = narrow ? k_grid<2, 5> : k_grid<1, 9>;
+  auto kern = P.nbd ? (narrow ? k_grid<2, 5, true> : k_grid<1, 9, true>)
+                    : (narrow ? k_grid<2, 5, false> : k_grid<1, 9, false>);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if (ticket) {
