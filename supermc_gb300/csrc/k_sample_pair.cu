@@ -92,7 +92,10 @@ __device__ __forceinline__ double hermite(double t, double h, double y0, double 
 __device__ double icdf_radius(const NucleusDev &n, double u) {
   const double *N = n.icdf;
   const double T = u * n.icdf_ntot;
-  int lo = 0, hi = n.icdf_m - 1;   // N[lo] <= T < N[hi]
+  // N[lo] <= T < N[hi], starting from the bucket of u
+  const double *start = N + 3 * (size_t)n.icdf_m;
+  const int b = min((int)(u * n.icdf_nb), n.icdf_nb - 1);
+  int lo = (int)start[b], hi = min((int)start[b + 1] + 1, n.icdf_m - 1);
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
     if (N[mid] <= T) lo = mid;
@@ -104,7 +107,7 @@ __device__ double icdf_radius(const NucleusDev &n, double u) {
   ws_weights(n, r0 + h, f1, g0, g1);
   const double y0 = N[lo], y1 = N[lo + 1];
   double t = y1 > y0 ? (T - y0) / (y1 - y0) : 0.0;
-  for (int it = 0; it < 8; it++) {
+  for (int it = 0; it < 6; it++) {   // quadratic convergence from the linear guess
     const double t2 = t * t;
     const double p = hermite(t, h, y0, y1, f0, f1) - T;
     const double dp =

@@ -156,6 +156,15 @@ void icdf_table(smc::NucleusDev &n, std::vector<double> &tab) {
   }
   double f, fR, fa;
   integrand(rmax, f, fR, fa);
+  // search starts: the largest node below each of nb + 1 evenly spaced fractions
+  const int nb = 512;
+  tab.resize((size_t)3 * m + nb + 1);
+  for (int b = 0, k = 0; b <= nb; b++) {
+    const double target = (double)b / nb * tab[m - 1];
+    while (k + 1 < m && tab[k + 1] <= target) k++;
+    tab[(size_t)3 * m + b] = k;
+  }
+  n.icdf_nb = nb;
   n.icdf_m = m;
   n.icdf_h = h;
   n.icdf_ntot = tab[m - 1];

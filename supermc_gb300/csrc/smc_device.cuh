@@ -50,8 +50,10 @@ struct NucleusDev {
   // cumulative integrals N, dN/dR, dN/da of r^2 rho(r) at r_k = k icdf_h,
   // k < icdf_m (three rows of icdf_m); icdf_ntot = N(rmax) and its
   // derivatives, the moving end point rmax = R + 2.5 included.
+  // A fourth row of icdf_nb + 1 entries holds, for u = b / icdf_nb, the
+  // largest node k with N[k] <= u N(rmax) (where the search starts).
   const double *icdf;
-  int icdf_m;
+  int icdf_m, icdf_nb;
   double icdf_h, icdf_ntot, icdf_dntot_R, icdf_dntot_a;
 };
 
