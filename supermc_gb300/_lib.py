@@ -21,7 +21,7 @@ STATUS_NAMES = {
 }
 ECC_LEN = 49
 
-# exported symbols, in the order include/supermc.h declares them
+# the entry points include/supermc.h declares (tests/test_capi.py checks the set)
 EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "smc_set_stream",
            "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_mixed", "smc_generate_plain",
            "smc_set_timing",

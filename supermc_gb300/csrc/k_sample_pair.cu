@@ -993,12 +993,9 @@ cudaError_t launch_sample_pair_mixed(const DevParams &P, uint64_t first_event, i
                                      const int *ev_sys, const int *order, int grid, cudaStream_t st,
                                      const TangentIO *tio, const uint64_t *ev_base, int *ticket) {
   size_t smem = sizeof(SampleSmem);
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_sample_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  // per launch: the attribute belongs to the current device's context
+  cudaError_t ea = cudaFuncSetAttribute(k_sample_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (ea != cudaSuccess) return ea;
   if (ticket) {
     cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
