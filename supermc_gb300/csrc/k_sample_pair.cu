@@ -22,11 +22,9 @@ static_assert(kMaxA % 4 == 0, "float4 rows");
 
 struct alignas(16) SampleSmem {
   float cx[kNT], cy[kNT], cz[kNT];          // candidate batch (nucleus frame)
-  uint8_t valid[kNT];
-  uint32_t keep[kNT / 32], conf[kNT / 32];   // batch resolution state: kept, conflicted
+  uint32_t vb[2][kNT / 32];                  // hard-core survivors, per half of the accepted list
+  uint32_t keep[kNT / 32], conf[kNT / 32];   // batch resolution state: kept, undecided
   uint32_t cmask[kNT][kNT / 32];             // earlier batch candidates each one conflicts with
-  int order[kNT];
-  int n_new;
   // read four at a time (float4): 16-byte aligned rows of kMaxA (a multiple of 4)
   alignas(16) float ax[2][kMaxA];
   alignas(16) float ay[2][kMaxA];
@@ -43,6 +41,7 @@ struct alignas(16) SampleSmem {
   double bmean[2];   // block means broadcast by block_mean2_f
   long long lred[32];
   double b;
+  float ori[2][2];   // nucleus orientations (cos theta, phi) of the attempt
 };
 
 // ---------------------------------------------------------------- helpers
@@ -144,11 +143,11 @@ __device__ void icdf_tangent(const NucleusDev &n, double r, double &sR, double &
 // (u0..u3 rounded to float; u0d the FP64 u0, read only by inverse-CDF radii)
 __device__ __forceinline__ bool ws_candidate(const NucleusDev &n, float ctr, float phir, double u0d, float u0,
                                              float u1, float u2, float u3, float &x, float &y, float &z) {
-  float R = (float)n.R, a = (float)n.a;
-  float r = (float)n.rmax_cut * powf(u0, 1.0f / 3.0f);
+  const float R = n.R_f, a = n.a_f;
+  float r = n.rmax_f * powf(u0, 1.0f / 3.0f);
   if (n.deformed) {
     float cx = 1.0f - 2.0f * u1;
-    float rad1 = R * (1.0f + (float)n.beta2 * sph2(cx) + (float)n.beta4 * sph4(cx));
+    float rad1 = R * (1.0f + n.beta2_f * sph2(cx) + n.beta4_f * sph4(cx));
     float rw1 = 1.0f / (1.0f + expf(-rad1 / a));
     if (u2 * rw1 > 1.0f / (1.0f + expf((r - rad1) / a))) return false;
     float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
@@ -158,7 +157,7 @@ __device__ __forceinline__ bool ws_candidate(const NucleusDev &n, float ctr, flo
     rotate3f(x, y, z, ctr, phir);
   } else {
     if (n.icdf) r = (float)icdf_radius(n, u0d);   // every candidate passes the radial step
-    else if (u1 * (float)n.rw_max > 1.0f / (1.0f + expf((r - R) / a))) return false;
+    else if (u1 * n.rw_max_f > 1.0f / (1.0f + expf((r - R) / a))) return false;
     float cx = 1.0f - 2.0f * u2;
     float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
     float sp, cp;
@@ -241,11 +240,21 @@ __device__ __forceinline__ int block_sum_i(int v, int *red, int slot) {
 // iff it passes the radial test and lies at least d_min from every nucleon
 // kept before it -- the sequential rule of Nucleus::populate, evaluated a
 // batch of kNT candidates at a time.  Returns false if the candidate cap is hit.
+//
+// Per batch: the radially accepted candidates are compacted (nv of them);
+// each is tested against the nucleons accepted so far (two threads per
+// candidate, one per half of the accepted list, when nv <= kNT/2), then
+// against the earlier valid candidates of the batch in 32x32 blocks spread
+// over the warps, giving a bit row per candidate.  Candidates without
+// conflicts are kept; the conflicted ones are decided by warp 0 in rounds:
+// a candidate is dropped once an earlier conflicting candidate is kept and
+// kept once all of them are dropped (the earliest undecided one is decided
+// every round, so the rounds end).  This reproduces the sequential rule.
 __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t seed, uint64_t ev, int attempt,
                           float ctr, float phir) {
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int A = n.A;
-  const float dmin2 = (float)(n.d_min * n.d_min);
+  const float dmin2 = n.dmin2_f;
   const uint32_t sid = stream_id(attempt, w == 0 ? ST_PROJ : ST_TARG);
   int n_acc = 0;
   for (uint32_t base = 0; n_acc < A; base += kNT) {
@@ -260,7 +269,6 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
     const bool ws = ws_candidate(n, ctr, phir, u0d, u0, u1, u2, u3, x, y, z);
     // the radially accepted candidates, compacted in candidate order: the
     // hard-core tests below then run on full warps
-    const int lane = tid & 31, wid = tid >> 5;
     const unsigned bal = __ballot_sync(0xffffffffu, ws);
     if (lane == 0) sm.ired[wid] = __popc(bal);
     __syncthreads();
@@ -276,95 +284,118 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
       sm.cx[v] = x; sm.cy[v] = y; sm.cz[v] = z;
     }
     __syncthreads();
-    // candidate tid (< nv): hard core against the nucleons accepted so far
-    bool ok = tid < nv;
-    if (ok) {
-      x = sm.cx[tid]; y = sm.cy[tid]; z = sm.cz[tid];
-      // four accepted nucleons per step (the arrays are 16-byte aligned;
-      // entries past n_acc are never compared)
-      int k = 0;
-      for (; k + 4 <= n_acc && ok; k += 4) {
-        const float4 ax = *reinterpret_cast<const float4 *>(&sm.ax[w][k]);
-        const float4 ay = *reinterpret_cast<const float4 *>(&sm.ay[w][k]);
-        const float4 az = *reinterpret_cast<const float4 *>(&sm.az[w][k]);
-        const float d0 = (x - ax.x) * (x - ax.x) + (y - ay.x) * (y - ay.x) + (z - az.x) * (z - az.x);
-        const float d1 = (x - ax.y) * (x - ax.y) + (y - ay.y) * (y - ay.y) + (z - az.y) * (z - az.y);
-        const float d2 = (x - ax.z) * (x - ax.z) + (y - ay.z) * (y - ay.z) + (z - az.z) * (z - az.z);
-        const float d3 = (x - ax.w) * (x - ax.w) + (y - ay.w) * (y - ay.w) + (z - az.w) * (z - az.w);
-        if (fminf(fminf(d0, d1), fminf(d2, d3)) < dmin2) ok = false;
+    // hard core against the nucleons accepted so far: candidate cv, accepted
+    // nucleons [k0, k1) (both halves of the list when split)
+    {
+      const bool split = nv <= kNT / 2;
+      const int cv = split ? (tid & (kNT / 2 - 1)) : tid, h = split ? (tid >> 7) : 0;
+      const int mid = split ? min(n_acc, ((n_acc >> 1) + 3) & ~3) : n_acc;
+      const int k0 = h ? mid : 0, k1 = h ? n_acc : mid;
+      bool ok = cv < nv;
+      if (ok) {
+        x = sm.cx[cv]; y = sm.cy[cv]; z = sm.cz[cv];
+        // four accepted nucleons per step (16-byte aligned rows, k0 a
+        // multiple of 4; entries past n_acc are never compared)
+        int k = k0;
+        for (; k + 4 <= k1 && ok; k += 4) {
+          const float4 ax = *reinterpret_cast<const float4 *>(&sm.ax[w][k]);
+          const float4 ay = *reinterpret_cast<const float4 *>(&sm.ay[w][k]);
+          const float4 az = *reinterpret_cast<const float4 *>(&sm.az[w][k]);
+          const float d0 = (x - ax.x) * (x - ax.x) + (y - ay.x) * (y - ay.x) + (z - az.x) * (z - az.x);
+          const float d1 = (x - ax.y) * (x - ax.y) + (y - ay.y) * (y - ay.y) + (z - az.y) * (z - az.y);
+          const float d2 = (x - ax.z) * (x - ax.z) + (y - ay.z) * (y - ay.z) + (z - az.z) * (z - az.z);
+          const float d3 = (x - ax.w) * (x - ax.w) + (y - ay.w) * (y - ay.w) + (z - az.w) * (z - az.w);
+          if (fminf(fminf(d0, d1), fminf(d2, d3)) < dmin2) ok = false;
+        }
+        for (; k < k1 && ok; k++) {
+          float dx = x - sm.ax[w][k], dy = y - sm.ay[w][k], dz = z - sm.az[w][k];
+          if (dx * dx + dy * dy + dz * dz < dmin2) ok = false;
+        }
       }
-      for (; k < n_acc && ok; k++) {
-        float dx = x - sm.ax[w][k], dy = y - sm.ay[w][k], dz = z - sm.az[w][k];
-        if (dx * dx + dy * dy + dz * dz < dmin2) ok = false;
+      // valid word of candidates 32 (cv >> 5) ..: the AND of both halves
+      const unsigned vb = __ballot_sync(0xffffffffu, ok);
+      if (lane == 0) {
+        sm.vb[h][cv >> 5] = vb;
+        if (!split) sm.vb[1][cv >> 5] = ~0u;
+        sm.conf[cv >> 5] = 0u;
       }
     }
-    sm.valid[tid] = ok;
     __syncthreads();
-    // conflicts with earlier candidates of the batch, one 32-bit word per warp
-    bool conflicted = false;
-#pragma unroll
-    for (int q = 0; q < kNT / 32; q++) {
+    // conflicts with earlier valid candidates of the batch: block (q, r)
+    // holds later candidates q*32+lane against earlier ones r*32+kk
+    const int Q = (nv + 31) >> 5;
+    for (int blk = wid; blk < Q * (Q + 1) / 2; blk += kNT / 32) {
+      int q = 0, s0 = 0;
+      while (s0 + q + 1 <= blk) { s0 += q + 1; q++; }
+      const int r = blk - s0, cq = q * 32 + lane;
       uint32_t bits = 0;
-      if (ok && q * 32 < tid) {
-        const int kmax = min(32, tid - q * 32);
-        for (int kk = 0; kk < kmax; kk++) {
-          const int k = q * 32 + kk;
-          if (!sm.valid[k]) continue;
-          float dx = x - sm.cx[k], dy = y - sm.cy[k], dz = z - sm.cz[k];
+      if (((sm.vb[0][q] & sm.vb[1][q]) >> lane) & 1u) {
+        const float cxq = sm.cx[cq], cyq = sm.cy[cq], czq = sm.cz[cq];
+        uint32_t m = sm.vb[0][r] & sm.vb[1][r];
+        if (r == q) m &= (1u << lane) - 1u;
+        while (m) {
+          const int kk = __ffs(m) - 1;
+          m &= m - 1u;
+          const int k = r * 32 + kk;
+          const float dx = cxq - sm.cx[k], dy = cyq - sm.cy[k], dz = czq - sm.cz[k];
           if (dx * dx + dy * dy + dz * dz < dmin2) bits |= 1u << kk;
         }
       }
-      sm.cmask[tid][q] = bits;
-      conflicted |= bits != 0;
-    }
-    // Sequential rule "keep candidate c iff it conflicts with no earlier kept
-    // candidate": a valid candidate without such conflicts is kept; the few
-    // with conflicts (a 0.9 fm hard core in a nucleus) are then decided one
-    // by one in candidate order.
-    {
-      const unsigned kb = __ballot_sync(0xffffffffu, ok && !conflicted);
-      const unsigned cb = __ballot_sync(0xffffffffu, ok && conflicted);
-      if ((tid & 31) == 0) {
-        sm.keep[tid >> 5] = kb;
-        sm.conf[tid >> 5] = cb;
-      }
+      sm.cmask[cq][r] = bits;
+      const unsigned cf = __ballot_sync(0xffffffffu, bits != 0u);
+      if (lane == 0 && cf) atomicOr(&sm.conf[q], cf);
     }
     __syncthreads();
-    if (tid == 0) {
-      for (int q = 0; q < kNT / 32; q++) {
-        uint32_t pend = sm.conf[q];
-        while (pend) {
-          const int c = q * 32 + __ffs(pend) - 1;
-          pend &= pend - 1;
-          bool kept = true;
-          for (int r = 0; r <= q; r++)
-            if (sm.cmask[c][r] & sm.keep[r]) kept = false;
-          if (kept) sm.keep[q] |= 1u << (c & 31);
+    if (wid == 0) {
+      // kept / undecided words (lane q < 8 owns word q)
+      if (lane < kNT / 32) {
+        const uint32_t v = lane < Q ? (sm.vb[0][lane] & sm.vb[1][lane]) : 0u, u = lane < Q ? sm.conf[lane] : 0u;
+        sm.keep[lane] = v & ~u;
+        sm.conf[lane] = u;
+      }
+      __syncwarp();
+      for (int round = 0; round < kNT; round++) {
+        uint32_t kw = lane < kNT / 32 ? sm.keep[lane] : 0u, uw = lane < kNT / 32 ? sm.conf[lane] : 0u;
+        if (!__any_sync(0xffffffffu, uw != 0u)) break;
+        for (int q = 0; q < Q; q++) {
+          bool kept = false, decided = false;
+          if ((sm.conf[q] >> lane) & 1u) {
+            bool hit = false, pend = false;
+            for (int r = 0; r <= q; r++) {
+              const uint32_t m = sm.cmask[q * 32 + lane][r];
+              hit |= (m & sm.keep[r]) != 0u;
+              pend |= (m & sm.conf[r]) != 0u;
+            }
+            decided = hit || !pend;
+            kept = !hit && !pend;
+          }
+          const unsigned kb = __ballot_sync(0xffffffffu, kept), db = __ballot_sync(0xffffffffu, decided);
+          if (lane == q) { kw |= kb; uw &= ~db; }
         }
+        __syncwarp();
+        if (lane < kNT / 32) { sm.keep[lane] = kw; sm.conf[lane] = uw; }
+        __syncwarp();
       }
     }
     __syncthreads();
     // kept candidates in candidate order, up to the nucleons still missing
     {
-      uint32_t kw = sm.keep[tid >> 5];
-      int before = 0;
-      for (int q = 0; q < (tid >> 5); q++) before += __popc(sm.keep[q]);
-      before += __popc(kw & ((1u << (tid & 31)) - 1u));
-      bool kept = (kw >> (tid & 31)) & 1u;
-      if (kept && n_acc + before < A) sm.order[before] = tid;
-      int total = 0;
-      for (int q = 0; q < kNT / 32; q++) total += __popc(sm.keep[q]);
-      if (tid == 0) sm.n_new = min(total, A - n_acc);
+      const uint32_t kw = sm.keep[wid];
+      int before = 0, total = 0;
+#pragma unroll
+      for (int q = 0; q < kNT / 32; q++) {
+        const int pq = __popc(sm.keep[q]);
+        before += q < wid ? pq : 0;
+        total += pq;
+      }
+      before += __popc(kw & ((1u << lane) - 1u));
+      if (((kw >> lane) & 1u) && n_acc + before < A) {
+        sm.ax[w][n_acc + before] = sm.cx[tid];
+        sm.ay[w][n_acc + before] = sm.cy[tid];
+        sm.az[w][n_acc + before] = sm.cz[tid];
+      }
+      n_acc += min(total, A - n_acc);
     }
-    __syncthreads();
-    int k = sm.n_new;
-    if (tid < k) {
-      int cc = sm.order[tid];
-      sm.ax[w][n_acc + tid] = sm.cx[cc];
-      sm.ay[w][n_acc + tid] = sm.cy[cc];
-      sm.az[w][n_acc + tid] = sm.cz[cc];
-    }
-    n_acc += k;
     __syncthreads();
   }
   return true;
@@ -617,6 +648,16 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
         s_P.npmin = sd.npmin;
         s_P.npmax = sd.npmax;
       }
+      for (int w = 0; w < 2; w++) {
+        NucleusDev &nu = s_P.nuc[w];
+        nu.R_f = (float)nu.R;
+        nu.a_f = (float)nu.a;
+        nu.rmax_f = (float)nu.rmax_cut;
+        nu.rw_max_f = (float)nu.rw_max;
+        nu.beta2_f = (float)nu.beta2;
+        nu.beta4_f = (float)nu.beta4;
+        nu.dmin2_f = (float)(nu.d_min * nu.d_min);
+      }
     }
     __syncthreads();
     const int A = P.nuc[0].A, B = P.nuc[1].A;
@@ -637,6 +678,13 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
           double u, unused;
           uniform2(P.seed, ev, stream_id(attempt, ST_EVENT), 0, u, unused);
           sm.b = sqrt((P.bmax * P.bmax - P.bmin * P.bmin) * u + P.bmin * P.bmin);
+          // nucleus orientations (cos theta, phi), rounded to float
+          for (int w = 0; w < 2; w++) {
+            double o0, o1;
+            uniform2(P.seed, ev, stream_id(attempt, ST_EVENT), 1 + w, o0, o1);
+            sm.ori[w][0] = (float)(1.0 - 2.0 * o0);
+            sm.ori[w][1] = (float)(2 * M_PI * o1);
+          }
         }
       }
       __syncthreads();
@@ -652,9 +700,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
                        itan ? itan + (size_t)e * 4 * nu.A : nullptr, ntan);
           continue;
         }
-        double o0, o1;
-        uniform2(P.seed, ev, stream_id(attempt, ST_EVENT), 1 + w, o0, o1);
-        float ctr = (float)(1.0 - 2.0 * o0), phir = (float)(2 * M_PI * o1);
+        const float ctr = sm.ori[w][0], phir = sm.ori[w][1];
         if (nu.A == 1) {
           if (tid == 0) { sm.ax[w][0] = 0.f; sm.ay[w][0] = 0.f; sm.az[w][0] = 0.f; }
           __syncthreads();
