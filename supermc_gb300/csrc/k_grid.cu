@@ -15,9 +15,11 @@
 // the cells the reference includes (window and r <= 5w / dc <= 25w^2 /
 // dc <= dsq cut): FP32 away from the cut, FP64 rounded as the reference
 // rounds for the one cell per side that can sit within the FP32 error of
-// it.  Column factors exp(-dy^2/2w^2) are computed once per (source,
-// column).  Each warp then owns kRW rows of the strip and adds its
-// sources' rows with plain shared-memory read-modify-writes (no atomics).
+// it.  Each lane then owns one column of the strip (a warp 32 adjacent
+// columns), holds the strip's kR rows of one plane in registers and adds
+// the group's sources in order: its column factor exp(-dy^2/2w^2) once per
+// source, then one predicated FMA per row inside that row's interval.  No
+// atomics: every cell has one owner, so the sums are deterministic.
 // All reductions run in FP32 pairs (double-float): FP64 arithmetic is rare
 // on this part and used only for the per-event totals.
 #include "grid_common.cuh"
@@ -27,19 +29,16 @@ namespace smc {
 
 constexpr int kGT = 256;            // threads per CTA
 constexpr int kWarps = kGT / 32;
-constexpr int kRW = 1;              // rows per warp: 8-row strips, small enough for five CTAs per SM
-constexpr int kR = kWarps * kRW;    // rows per strip
+constexpr int kR = 8;               // rows per strip (held in registers by the accumulating lanes)
 constexpr int kGS = 64;             // sources per group
+static_assert(kR % 4 == 0, "rows are read four at a time");
 
-
-struct PairDat {      // one (source, row) pair of a strip
-  float exw;          // weight * exp(-dx^2 / 2w^2)
-  int16_t ja, jb;     // included columns [ja, jb)
-};
-
+// (source, row) pairs of a strip, structure of arrays [kGS][kR]: the row
+// factor weight * exp(-dx^2 / 2w^2), the first included column and the
+// number of included columns (0: the source misses the row)
 struct GridLayout {
   int nyp, mw, np;
-  size_t off_acc, off_list, off_grp, off_pair, off_ey, off_xg, off_yg, off_red, total;
+  size_t off_acc, off_list, off_grp, off_exw, off_ja, off_len, off_xg, off_yg, off_red, total;
 };
 
 __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np) {
@@ -55,9 +54,10 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
   L.off_list = o; o += sizeof(int) * kGT;
   o = (o + 15) / 16 * 16;
   L.off_grp = o; o += sizeof(GroupSrc) * kGS;
-  L.off_pair = o; o += sizeof(PairDat) * kGS * kR;
-  L.off_ey = o; o += sizeof(float) * kGS * mw;
   o = (o + 15) / 16 * 16;
+  L.off_exw = o; o += sizeof(float) * kGS * kR;
+  L.off_ja = o; o += sizeof(int) * kGS * kR;
+  L.off_len = o; o += sizeof(int) * kGS * kR;
   L.off_xg = o; o += sizeof(float) * 2 * nx;   // grid x, then x - x_cm
   L.off_yg = o; o += sizeof(float) * 2 * L.nyp;
   o = (o + 15) / 16 * 16;
@@ -88,8 +88,9 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
   float *acc = reinterpret_cast<float *>(smem + L.off_acc);
   int *list = reinterpret_cast<int *>(smem + L.off_list);
   GroupSrc *grp = reinterpret_cast<GroupSrc *>(smem + L.off_grp);
-  PairDat *pairs = reinterpret_cast<PairDat *>(smem + L.off_pair);
-  float *eyb = reinterpret_cast<float *>(smem + L.off_ey);
+  float *p_exw = reinterpret_cast<float *>(smem + L.off_exw);
+  int *p_ja = reinterpret_cast<int *>(smem + L.off_ja);
+  int *p_len = reinterpret_cast<int *>(smem + L.off_len);
   float *xg = reinterpret_cast<float *>(smem + L.off_xg);
   float *yg = reinterpret_cast<float *>(smem + L.off_yg);
   float2 *red = reinterpret_cast<float2 *>(smem + L.off_red);
@@ -97,7 +98,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
   __shared__ double s_cm[3];
 
   const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
-  const int nx = P.nx, ny = P.ny, nyp = L.nyp, mw = L.mw, np = L.np;
+  const int nx = P.nx, ny = P.ny, nyp = L.nyp, np = L.np;
   const float inv2w2 = (float)(1.0 / (2.0 * P.w2));
   const float lim = (float)(25.0 * P.w2), lim_lo = lim * (1.f - 1e-4f), lim_hi = lim * (1.f + 1e-4f);
   const float dsq = (float)P.dsq, dsq_lo = dsq * (1.f - 1e-4f), dsq_hi = dsq * (1.f + 1e-4f);
@@ -105,7 +106,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
   const int model = P.which_mc_model;
 
   for (int i = tid; i < nx; i += kGT) xg[i] = (float)(P.xmin + i * P.dx);
-  for (int j = tid; j < ny; j += kGT) yg[j] = (float)(P.ymin + j * P.dy);
+  for (int j = tid; j < nyp; j += kGT) yg[j] = j < ny ? (float)(P.ymin + j * P.dy) : 0.f;
 
   __shared__ int s_k;
   for (int k = queue_first(q, &s_k); k < n_events; k = queue_next(q, k, &s_k)) {
@@ -152,57 +153,60 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
               const Source &s = S[list[g0 + t]];
               GroupSrc g;
               g.x = s.x; g.y = s.y; g.xf = (float)s.x; g.yf = (float)s.y; g.weight = s.weight;
-              // the column table holds mw columns per source: a window never reaches past it
-              g.xl = s.xl; g.xr = s.xr; g.yl = s.yl; g.yr = (int16_t)min((int)s.yr, (int)s.yl + mw);
+              g.xl = s.xl; g.xr = s.xr; g.yl = s.yl; g.yr = s.yr;
               g.kind = s.kind; g.plane = s.plane;
               grp[t] = g;
             }
             __syncthreads();
-            // column factors, one per (source, column)
-            for (int t = tid; t < gn * mw; t += kGT) {
-              int q = t / mw, c = t - q * mw;
-              const GroupSrc &g = grp[q];
-              int j = g.yl + c;
-              float v = 0.f;
-              if (j < g.yr) {
-                float dy = yg[j] - g.yf;
-                v = (g.kind & 16) ? 1.f : __expf(-dy * dy * inv2w2);
-              }
-              eyb[t] = v;
-            }
             // row factors and included column intervals, one per (source, row)
             for (int t = tid; t < gn * kR; t += kGT) {
-              int q = t / kR, r = t - q * kR;
+              const int q = t / kR, r = t - q * kR;
               const GroupSrc &g = grp[q];
               const int i = r0 + r;
-              PairDat pd;
-              pd.exw = 0.f;
-              pd.ja = pd.jb = 0;
+              float exw = 0.f;
+              int ja = 0, len = 0;
               if (r < rows && i >= g.xl && i < g.xr) {
                 const bool disk = g.kind & 16;
                 const float dx = xg[i] - g.xf, dx2 = dx * dx;
-                pd.exw = disk ? g.weight : g.weight * __expf(-dx2 * inv2w2);
-                int ja, jb;
+                exw = disk ? g.weight : g.weight * __expf(-dx2 * inv2w2);
+                int jb;
                 row_interval(P, g, i, dx2, disk ? dsq_lo : lim_lo, disk ? dsq_hi : lim_hi, yg, inv_dy, ymin_f, ja,
                              jb);
-                pd.ja = (int16_t)ja;
-                pd.jb = (int16_t)jb;
+                len = max(jb - ja, 0);
               }
-              pairs[t] = pd;
+              p_exw[t] = exw;
+              p_ja[t] = ja;
+              p_len[t] = len;
             }
             __syncthreads();
-            // accumulation: warp wid owns rows wid*kRW .. wid*kRW+kRW-1 of the strip
+            // accumulation: lane owns column j of the strip, warp wid the
+            // 32-column blocks wid, wid + kWarps, ..
+            for (int j0 = wid * 32; j0 < nyp; j0 += kGT) {
+              const int j = j0 + lane;
+              const float yj = yg[j];
+              for (int pl = 0; pl < np; pl++) {
+                float *ab = acc + (size_t)pl * kR * nyp + j;
+                float a[kR];
 #pragma unroll
-            for (int rr = 0; rr < kRW; rr++) {
-              const int r = wid * kRW + rr;
-              if (r >= rows) continue;
-              for (int q = 0; q < gn; q++) {
-                const PairDat pd = pairs[q * kR + r];
-                if (pd.ja >= pd.jb) continue;
-                const int yl = grp[q].yl, pl = grp[q].plane;
-                float *arow = acc + ((size_t)pl * kR + r) * nyp;
-                const float *ey = eyb + q * mw - yl;
-                for (int j = pd.ja + lane; j < pd.jb; j += 32) arow[j] += pd.exw * ey[j];
+                for (int r = 0; r < kR; r++) a[r] = ab[r * nyp];
+                for (int q = 0; q < gn; q++) {
+                  const GroupSrc &g = grp[q];
+                  if (g.plane != pl || g.yr <= j0 || g.yl >= j0 + 32) continue;
+                  const float dy = yj - g.yf;
+                  const float ey = (g.kind & 16) ? 1.f : __expf(-dy * dy * inv2w2);
+#pragma unroll
+                  for (int r4 = 0; r4 < kR; r4 += 4) {
+                    const float4 w4 = *reinterpret_cast<const float4 *>(p_exw + q * kR + r4);
+                    const int4 a4 = *reinterpret_cast<const int4 *>(p_ja + q * kR + r4);
+                    const int4 l4 = *reinterpret_cast<const int4 *>(p_len + q * kR + r4);
+                    if ((unsigned)(j - a4.x) < (unsigned)l4.x) a[r4] += w4.x * ey;
+                    if ((unsigned)(j - a4.y) < (unsigned)l4.y) a[r4 + 1] += w4.y * ey;
+                    if ((unsigned)(j - a4.z) < (unsigned)l4.z) a[r4 + 2] += w4.z * ey;
+                    if ((unsigned)(j - a4.w) < (unsigned)l4.w) a[r4 + 3] += w4.w * ey;
+                  }
+                }
+#pragma unroll
+                for (int r = 0; r < kR; r++) ab[r * nyp] = a[r];
               }
             }
             __syncthreads();
