@@ -217,20 +217,53 @@ __device__ __forceinline__ void hotspot_mask(const DevParams &P, const EventRec 
   const int nw = (ny + 31) / 32;
   for (int k = tid; k < nx * nw; k += NT) mask[k] = 0;
   __syncthreads();
-  for (int s = tid; s < rec.nsrc; s += NT) {
-    const Source &src = S[s];
-    int kd = src.kind & 15;
-    if (kd != SRC_PART_BOX && kd != 3) continue;
-    int r0 = max(0, (int)src.mx0), r1 = min(nx, (int)src.mx1);
-    int c0 = max(0, (int)src.my0), c1 = min(ny, (int)src.my1);
-    if (r1 <= r0 || c1 <= c0) continue;
-    int w0 = c0 >> 5, w1 = (c1 - 1) >> 5;
-    for (int row = r0; row < r1; row++)
-      for (int wd = w0; wd <= w1; wd++) {
-        int lo = max(c0, wd * 32), hi = min(c1, wd * 32 + 32);
-        uint32_t bits = (hi - lo >= 32) ? 0xffffffffu : (((1u << (hi - lo)) - 1u) << (lo - wd * 32));
-        atomicOr(&mask[row * nw + wd], bits);
+  // sources in chunks of 32 per warp; the lanes then take the (source, row)
+  // pairs of the chunk's boxes, so that all lanes set bits
+  const int lane = tid & 31;
+  for (int s0 = (tid >> 5) * 32; s0 < rec.nsrc; s0 += NT) {
+    int r0 = 0, r1 = 0, c0 = 0, c1 = 0;
+    if (s0 + lane < rec.nsrc) {
+      const Source &src = S[s0 + lane];
+      const int kd = src.kind & 15;
+      if (kd == SRC_PART_BOX || kd == 3) {
+        r0 = max(0, (int)src.mx0); r1 = min(nx, (int)src.mx1);
+        c0 = max(0, (int)src.my0); c1 = min(ny, (int)src.my1);
+        if (r1 <= r0 || c1 <= c0) r1 = r0;
+      } else {
+        r1 = r0;
       }
+    }
+    // exclusive prefix of the row counts over the chunk
+    const int nr = r1 - r0;
+    int pre = nr;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, pre, o);
+      if (lane >= o) pre += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, pre, 31);
+    pre -= nr;
+    for (int t0 = 0; t0 < total; t0 += 32) {
+      const int t = t0 + lane;
+      // the box of pair t: the last lane whose prefix is <= t
+      int src_lane = 0;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        const int cand = src_lane + o;
+        const int pc = __shfl_sync(0xffffffffu, pre, cand);
+        if (pc <= t) src_lane = cand;
+      }
+      const int br0 = __shfl_sync(0xffffffffu, r0, src_lane), bpre = __shfl_sync(0xffffffffu, pre, src_lane);
+      const int bc0 = __shfl_sync(0xffffffffu, c0, src_lane), bc1 = __shfl_sync(0xffffffffu, c1, src_lane);
+      if (t < total) {
+        const int row = br0 + (t - bpre);
+        for (int wd = bc0 >> 5; wd <= (bc1 - 1) >> 5; wd++) {
+          const int lo = max(bc0, wd * 32), hi = min(bc1, wd * 32 + 32);
+          const uint32_t bits = (hi - lo >= 32) ? 0xffffffffu : (((1u << (hi - lo)) - 1u) << (lo - wd * 32));
+          atomicOr(&mask[row * nw + wd], bits);
+        }
+      }
+    }
   }
   __syncthreads();
 }
@@ -256,11 +289,20 @@ __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, co
   // warps take (row, 32-column block) items of the bounding box, lanes the columns
   const int nbj = rec.jmax > rec.jmin ? (rec.jmax - rec.jmin + 31) >> 5 : 0;
   const int nitem = rec.imax > rec.imin ? (rec.imax - rec.imin) * nbj : 0;
-  for (int c = wid; c < nitem; c += NT / 32) {
+  // the next item's density is loaded before the current one is processed
+  auto fetch = [&](int c, int &i, int &j) -> float {
+    if (c >= nitem) return 0.f;
     const int ib = c / nbj;
-    const int i = rec.imin + ib, j = rec.jmin + ((c - ib * nbj) << 5) + lane;
-    if (j >= rec.jmax) continue;
-    float d = rho[(size_t)i * ny + j];
+    i = rec.imin + ib;
+    j = rec.jmin + ((c - ib * nbj) << 5) + lane;
+    return j < rec.jmax ? rho[(size_t)i * ny + j] : 0.f;
+  };
+  int i_next = 0, j_next = 0;
+  float d_next = fetch(wid, i_next, j_next);
+  for (int c = wid; c < nitem; c += NT / 32) {
+    const int i = i_next, j = j_next;
+    const float d = d_next;
+    d_next = fetch(c + NT / 32, i_next, j_next);
     if (d == 0.f) continue;
     float x = xo[i], y = yo[j];
     float r2 = x * x + y * y;
@@ -328,31 +370,36 @@ __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, co
     s_tot[tid] = t;
   }
   __syncthreads();
-  if (tid == 0) {
+  // output k of the event's row (one division per thread):
+  // 5 (n - 1) + c, c < 4: the eps_n components, c = 4: <r^n>; 45..48 the totals
+  if (tid < kEccLen) {
     const double *tot = s_tot;
     const double ff = P.final_factor, eps = 1e-15;
-    double *out = ecc_out;
     const double dn = tot0;
     // an all-zero density (possible after NBD fluctuations) has no centre of
     // mass: the reference's sums are then NaN (0 * NaN), as here
     const bool empty = !(dn > 0);
     const double nan = __longlong_as_double(0x7ff8000000000000ll);
-    for (int n = 1; n < 10; n++) {
-      double *o = out + 5 * (n - 1);
-      o[0] = o[1] = o[2] = o[3] = 0.0;
-      o[4] = empty ? nan : (tot[n - 1] * ff) / (dn * ff);
-      if (n >= LO && n <= HI && n >= from && n <= to) {
-        int q = n - LO;
-        o[0] = empty ? nan : -(tot[10 + 5 * q] * ff) / (tot[9] * ff + eps);
-        o[1] = empty ? nan : -(tot[11 + 5 * q] * ff) / (tot[9] * ff + eps);
-        o[2] = empty ? nan : -(tot[12 + 5 * q] * ff) / (tot[14 + 5 * q] * ff + eps);
-        o[3] = empty ? nan : -(tot[13 + 5 * q] * ff) / (tot[14 + 5 * q] * ff + eps);
+    double v = 0.0;
+    if (tid < 45) {
+      const int n = tid / 5 + 1, c = tid - 5 * (n - 1);
+      if (c == 4) {
+        v = empty ? nan : (tot[n - 1] * ff) / (dn * ff);
+      } else if (n >= LO && n <= HI && n >= from && n <= to) {
+        const int q = n - LO;
+        const double den = c < 2 ? tot[9] * ff + eps : tot[14 + 5 * q] * ff + eps;
+        v = empty ? nan : -(tot[10 + 5 * q + c] * ff) / den;
       }
+    } else if (tid == 45) {
+      v = (double)(rec.npart1 + rec.npart2);
+    } else if (tid == 46) {
+      v = (double)rec.ncoll;
+    } else if (tid == 47) {
+      v = tot0 * ff * P.dx * P.dy;
+    } else {
+      v = rec.b;
     }
-    out[45] = (double)(rec.npart1 + rec.npart2);
-    out[46] = (double)rec.ncoll;
-    out[47] = tot0 * ff * P.dx * P.dy;
-    out[48] = rec.b;
+    ecc_out[tid] = v;
   }
   __syncthreads();
 }

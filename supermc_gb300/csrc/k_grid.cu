@@ -17,7 +17,8 @@
 // rounds for the one cell per side that can sit within the FP32 error of
 // it.  Each lane then owns one column of the strip (a warp 32 adjacent
 // columns), holds the strip's kR rows of one plane in registers and adds
-// the group's sources in order: its column factor exp(-dy^2/2w^2) once per
+// the group's sources that reach its columns (a bit mask per 32-column
+// block and plane) in order: the column factor exp(-dy^2/2w^2) once per
 // source, then one predicated FMA per row inside that row's interval.  No
 // atomics: every cell has one owner, so the sums are deterministic.
 // All reductions run in FP32 pairs (double-float): FP64 arithmetic is rare
@@ -30,15 +31,17 @@ namespace smc {
 constexpr int kGT = 256;            // threads per CTA
 constexpr int kWarps = kGT / 32;
 constexpr int kR = 8;               // rows per strip (held in registers by the accumulating lanes)
-constexpr int kGS = 64;             // sources per group
-static_assert(kR % 4 == 0, "rows are read four at a time");
+constexpr int kGS = 64;             // sources per group (two 32-bit words of a source mask)
+constexpr int kSplit = 1;           // work units per 32-column block (row slices of the strip)
+constexpr int kRU = kR / kSplit;    // rows of a work unit
+static_assert(kRU % 4 == 0, "units are read four rows at a time");
 
 // (source, row) pairs of a strip, structure of arrays [kGS][kR]: the row
 // factor weight * exp(-dx^2 / 2w^2), the first included column and the
 // number of included columns (0: the source misses the row)
 struct GridLayout {
   int nyp, mw, np;
-  size_t off_acc, off_list, off_grp, off_exw, off_ja, off_len, off_xg, off_yg, off_red, total;
+  size_t off_acc, off_list, off_grp, off_exw, off_ja, off_len, off_cmask, off_xg, off_yg, off_red, total;
 };
 
 __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np) {
@@ -58,6 +61,8 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
   L.off_exw = o; o += sizeof(float) * kGS * kR;
   L.off_ja = o; o += sizeof(int) * kGS * kR;
   L.off_len = o; o += sizeof(int) * kGS * kR;
+  L.off_cmask = o; o += sizeof(uint32_t) * 2 * np * (L.nyp / 32);
+  o = (o + 15) / 16 * 16;
   L.off_xg = o; o += sizeof(float) * 2 * nx;   // grid x, then x - x_cm
   L.off_yg = o; o += sizeof(float) * 2 * L.nyp;
   o = (o + 15) / 16 * 16;
@@ -91,6 +96,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
   float *p_exw = reinterpret_cast<float *>(smem + L.off_exw);
   int *p_ja = reinterpret_cast<int *>(smem + L.off_ja);
   int *p_len = reinterpret_cast<int *>(smem + L.off_len);
+  uint32_t *cmask = reinterpret_cast<uint32_t *>(smem + L.off_cmask);   // [block][plane][2]: sources reaching it
   float *xg = reinterpret_cast<float *>(smem + L.off_xg);
   float *yg = reinterpret_cast<float *>(smem + L.off_yg);
   float2 *red = reinterpret_cast<float2 *>(smem + L.off_red);
@@ -103,7 +109,6 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
   const float lim = (float)(25.0 * P.w2), lim_lo = lim * (1.f - 1e-4f), lim_hi = lim * (1.f + 1e-4f);
   const float dsq = (float)P.dsq, dsq_lo = dsq * (1.f - 1e-4f), dsq_hi = dsq * (1.f + 1e-4f);
   const float inv_dy = (float)(1.0 / P.dy), ymin_f = (float)P.ymin;
-  const int model = P.which_mc_model;
 
   for (int i = tid; i < nx; i += kGT) xg[i] = (float)(P.xmin + i * P.dx);
   for (int j = tid; j < nyp; j += kGT) yg[j] = j < ny ? (float)(P.ymin + j * P.dy) : 0.f;
@@ -158,6 +163,21 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
               grp[t] = g;
             }
             __syncthreads();
+            // per (32-column block, plane): the group's sources whose window reaches it
+            for (int it = wid; it < (nyp / 32) * np; it += kWarps) {
+              const int jb0 = (it / np) * 32, pl = it - (it / np) * np;
+#pragma unroll
+              for (int h = 0; h < 2; h++) {
+                const int q = h * 32 + lane;
+                bool in = false;
+                if (q < gn) {
+                  const GroupSrc &g = grp[q];
+                  in = g.plane == pl && g.yr > jb0 && g.yl < jb0 + 32 && g.yr > g.yl;
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, in);
+                if (lane == 0) cmask[it * 2 + h] = b;
+              }
+            }
             // row factors and included column intervals, one per (source, row)
             for (int t = tid; t < gn * kR; t += kGT) {
               const int q = t / kR, r = t - q * kR;
@@ -179,34 +199,42 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
               p_len[t] = len;
             }
             __syncthreads();
-            // accumulation: lane owns column j of the strip, warp wid the
-            // 32-column blocks wid, wid + kWarps, ..
-            for (int j0 = wid * 32; j0 < nyp; j0 += kGT) {
-              const int j = j0 + lane;
+            // accumulation: lane owns column j of the strip; the work units are
+            // (32-column block, slice of kRU rows), dealt to the warps round
+            // robin so that the busy central blocks spread over them; each
+            // unit visits only the sources that reach its block, in order
+            for (int u = wid; u < (nyp / 32) * kSplit; u += kWarps) {
+              const int jb = u / kSplit, j = jb * 32 + lane, rh = (u - jb * kSplit) * kRU;
               const float yj = yg[j];
               for (int pl = 0; pl < np; pl++) {
-                float *ab = acc + (size_t)pl * kR * nyp + j;
-                float a[kR];
+                float *ab = acc + ((size_t)pl * kR + rh) * nyp + j;
+                float a[kRU];
 #pragma unroll
-                for (int r = 0; r < kR; r++) a[r] = ab[r * nyp];
-                for (int q = 0; q < gn; q++) {
-                  const GroupSrc &g = grp[q];
-                  if (g.plane != pl || g.yr <= j0 || g.yl >= j0 + 32) continue;
-                  const float dy = yj - g.yf;
-                  const float ey = (g.kind & 16) ? 1.f : __expf(-dy * dy * inv2w2);
+                for (int r = 0; r < kRU; r++) a[r] = ab[r * nyp];
 #pragma unroll
-                  for (int r4 = 0; r4 < kR; r4 += 4) {
-                    const float4 w4 = *reinterpret_cast<const float4 *>(p_exw + q * kR + r4);
-                    const int4 a4 = *reinterpret_cast<const int4 *>(p_ja + q * kR + r4);
-                    const int4 l4 = *reinterpret_cast<const int4 *>(p_len + q * kR + r4);
-                    if ((unsigned)(j - a4.x) < (unsigned)l4.x) a[r4] += w4.x * ey;
-                    if ((unsigned)(j - a4.y) < (unsigned)l4.y) a[r4 + 1] += w4.y * ey;
-                    if ((unsigned)(j - a4.z) < (unsigned)l4.z) a[r4 + 2] += w4.z * ey;
-                    if ((unsigned)(j - a4.w) < (unsigned)l4.w) a[r4 + 3] += w4.w * ey;
+                for (int h = 0; h < 2; h++) {
+                  uint32_t m = cmask[(jb * np + pl) * 2 + h];
+                  while (m) {
+                    const int q = h * 32 + __ffs(m) - 1;
+                    m &= m - 1u;
+                    const GroupSrc &g = grp[q];
+                    const float dy = yj - g.yf;
+                    const float ey = (g.kind & 16) ? 1.f : __expf(-dy * dy * inv2w2);
+#pragma unroll
+                    for (int r4 = 0; r4 < kRU; r4 += 4) {
+                      const int o = q * kR + rh + r4;
+                      const float4 w4 = *reinterpret_cast<const float4 *>(p_exw + o);
+                      const int4 a4 = *reinterpret_cast<const int4 *>(p_ja + o);
+                      const int4 l4 = *reinterpret_cast<const int4 *>(p_len + o);
+                      if ((unsigned)(j - a4.x) < (unsigned)l4.x) a[r4] += w4.x * ey;
+                      if ((unsigned)(j - a4.y) < (unsigned)l4.y) a[r4 + 1] += w4.y * ey;
+                      if ((unsigned)(j - a4.z) < (unsigned)l4.z) a[r4 + 2] += w4.z * ey;
+                      if ((unsigned)(j - a4.w) < (unsigned)l4.w) a[r4 + 3] += w4.w * ey;
+                    }
                   }
                 }
 #pragma unroll
-                for (int r = 0; r < kR; r++) ab[r * nyp] = a[r];
+                for (int r = 0; r < kRU; r++) ab[r * nyp] = a[r];
               }
             }
             __syncthreads();
