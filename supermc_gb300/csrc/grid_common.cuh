@@ -107,7 +107,7 @@ __device__ __forceinline__ bool post_cell(const DevParams &P, int np, float a0, 
 // Column interval [ja, jb) of row i that the reference includes for source
 // g.  dc(j) is convex in j, so the included cells form one interval around
 // the column nearest the source.
-static __device__ __noinline__ void row_interval(const DevParams &P, const GroupSrc &g, int i, float dx2, float lo,
+static __device__ __forceinline__ void row_interval(const DevParams &P, const GroupSrc &g, int i, float dx2, float lo,
                                              float hi, const float *yg, float inv_dy, float ymin_f, int &ja,
                                              int &jb) {
   const int wl = g.yl, wr = g.yr;

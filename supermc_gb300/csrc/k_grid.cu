@@ -31,7 +31,9 @@ namespace smc {
 constexpr int kGT = 256;            // threads per CTA
 constexpr int kWarps = kGT / 32;
 constexpr int kR = 8;               // rows per strip (held in registers by the accumulating lanes)
-constexpr int kGS = 64;             // sources per group (two 32-bit words of a source mask)
+constexpr int kGS = 64;             // sources per group
+constexpr int kGW = kGS / 32;       // 32-bit words of a group's source mask
+static_assert(kGS % 32 == 0, "source masks are whole words");
 constexpr int kSplit = 1;           // work units per 32-column block (row slices of the strip)
 constexpr int kRU = kR / kSplit;    // rows of a work unit
 static_assert(kRU % 4 == 0, "units are read four rows at a time");
@@ -61,7 +63,7 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
   L.off_exw = o; o += sizeof(float) * kGS * kR;
   L.off_ja = o; o += sizeof(int) * kGS * kR;
   L.off_len = o; o += sizeof(int) * kGS * kR;
-  L.off_cmask = o; o += sizeof(uint32_t) * 2 * np * (L.nyp / 32);
+  L.off_cmask = o; o += sizeof(uint32_t) * kGW * np * (L.nyp / 32);
   o = (o + 15) / 16 * 16;
   L.off_xg = o; o += sizeof(float) * 2 * nx;   // grid x, then x - x_cm
   L.off_yg = o; o += sizeof(float) * 2 * L.nyp;
@@ -96,7 +98,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
   float *p_exw = reinterpret_cast<float *>(smem + L.off_exw);
   int *p_ja = reinterpret_cast<int *>(smem + L.off_ja);
   int *p_len = reinterpret_cast<int *>(smem + L.off_len);
-  uint32_t *cmask = reinterpret_cast<uint32_t *>(smem + L.off_cmask);   // [block][plane][2]: sources reaching it
+  uint32_t *cmask = reinterpret_cast<uint32_t *>(smem + L.off_cmask);   // [block][plane][kGW]: sources reaching it
   float *xg = reinterpret_cast<float *>(smem + L.off_xg);
   float *yg = reinterpret_cast<float *>(smem + L.off_yg);
   float2 *red = reinterpret_cast<float2 *>(smem + L.off_red);
@@ -167,7 +169,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
             for (int it = wid; it < (nyp / 32) * np; it += kWarps) {
               const int jb0 = (it / np) * 32, pl = it - (it / np) * np;
 #pragma unroll
-              for (int h = 0; h < 2; h++) {
+              for (int h = 0; h < kGW; h++) {
                 const int q = h * 32 + lane;
                 bool in = false;
                 if (q < gn) {
@@ -175,7 +177,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
                   in = g.plane == pl && g.yr > jb0 && g.yl < jb0 + 32 && g.yr > g.yl;
                 }
                 const unsigned b = __ballot_sync(0xffffffffu, in);
-                if (lane == 0) cmask[it * 2 + h] = b;
+                if (lane == 0) cmask[it * kGW + h] = b;
               }
             }
             // row factors and included column intervals, one per (source, row)
@@ -212,8 +214,8 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
 #pragma unroll
                 for (int r = 0; r < kRU; r++) a[r] = ab[r * nyp];
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
-                  uint32_t m = cmask[(jb * np + pl) * 2 + h];
+                for (int h = 0; h < kGW; h++) {
+                  uint32_t m = cmask[(jb * np + pl) * kGW + h];
                   while (m) {
                     const int q = h * 32 + __ffs(m) - 1;
                     m &= m - 1u;

@@ -18,13 +18,22 @@
 namespace smc {
 
 constexpr int kNT = 256;   // threads per CTA; also the candidate batch size
+constexpr int kSlab = 32;  // z slabs of the hard-core search, at most
 static_assert(kMaxA % 4 == 0, "float4 rows");
 
 struct alignas(16) SampleSmem {
-  float cx[kNT], cy[kNT], cz[kNT];          // candidate batch (nucleus frame)
-  uint32_t vb[2][kNT / 32];                  // hard-core survivors, per half of the accepted list
+  // candidate batch (nucleus frame): x, y, z; before the direction is drawn
+  // (r, candidate index bits, 0, 0)
+  float4 cpos[kNT];
+  union {
+    uint32_t cmask[kNT][kNT / 32];           // earlier batch candidates each one conflicts with
+    float4 spos[kMaxA];                      // accepted nucleons ordered by z slab
+  } u;
+  uint32_t smask[kSlab][kNT / 32];           // hard-core survivors of the batch per z slab
+  int slab_cnt[kSlab], slab_cur[kSlab], slab_start[kSlab + 1];
+  uint8_t cslab[kNT];                        // z slab of each batch candidate
+  uint32_t vb[kNT / 32];                     // hard-core survivors
   uint32_t keep[kNT / 32], conf[kNT / 32];   // batch resolution state: kept, undecided
-  uint32_t cmask[kNT][kNT / 32];             // earlier batch candidates each one conflicts with
   // read four at a time (float4): 16-byte aligned rows of kMaxA (a multiple of 4)
   alignas(16) float ax[2][kMaxA];
   alignas(16) float ay[2][kMaxA];
@@ -33,7 +42,7 @@ struct alignas(16) SampleSmem {
   alignas(16) float Xf[2][kMaxA];
   float Yf[2][kMaxA];
   int hits[2][kMaxA];
-  int scan[kNT];
+  int scan[32];
   double red[kNT / 32 * 3];
   float2 red2[kNT / 32 * 2];
   int ired[kNT / 32 * 4];
@@ -140,30 +149,40 @@ __device__ void icdf_tangent(const NucleusDev &n, double r, double &sR, double &
 }
 
 // One Woods-Saxon candidate from four uniforms (Nucleus::getDeformRandomWS)
-// (u0..u3 rounded to float; u0d the FP64 u0, read only by inverse-CDF radii)
-__device__ __forceinline__ bool ws_candidate(const NucleusDev &n, float ctr, float phir, double u0d, float u0,
-                                             float u1, float u2, float u3, float &x, float &y, float &z) {
-  const float R = n.R_f, a = n.a_f;
-  float r = n.rmax_f * powf(u0, 1.0f / 3.0f);
-  if (n.deformed) {
-    float cx = 1.0f - 2.0f * u1;
-    float rad1 = R * (1.0f + n.beta2_f * sph2(cx) + n.beta4_f * sph4(cx));
-    float rw1 = 1.0f / (1.0f + expf(-rad1 / a));
-    if (u2 * rw1 > 1.0f / (1.0f + expf((r - rad1) / a))) return false;
-    float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
-    float sp, cp;
-    sincospif(2.0f * u3, &sp, &cp);
-    x = r * sx * cp; y = r * sx * sp; z = r * cx;
-    rotate3f(x, y, z, ctr, phir);
-  } else {
-    if (n.icdf) r = (float)icdf_radius(n, u0d);   // every candidate passes the radial step
-    else if (u1 * n.rw_max_f > 1.0f / (1.0f + expf((r - R) / a))) return false;
-    float cx = 1.0f - 2.0f * u2;
-    float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
-    float sp, cp;
-    sincospif(2.0f * u3, &sp, &cp);
-    x = r * sx * cp; y = r * sx * sp; z = r * cx;
+// (u0..u3 rounded to float; u0d the FP64 u0, read only by inverse-CDF radii).
+// Spherical nuclei: the radius and its acceptance come from u0, u1 alone
+// (ws_radius), the direction from u2, u3 (ws_direction); deformed nuclei
+// need all four for the acceptance (ws_candidate_deformed).
+__device__ __forceinline__ bool ws_radius(const NucleusDev &n, double u0d, float u0, float u1, float &r) {
+  if (n.icdf) {   // every candidate passes the radial step
+    r = (float)icdf_radius(n, u0d);
+    return true;
   }
+  r = n.rmax_f * powf(u0, 1.0f / 3.0f);
+  return !(u1 * n.rw_max_f > 1.0f / (1.0f + expf((r - n.R_f) / n.a_f)));
+}
+
+__device__ __forceinline__ void ws_direction(float r, float u2, float u3, float &x, float &y, float &z) {
+  float cx = 1.0f - 2.0f * u2;
+  float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
+  float sp, cp;
+  sincospif(2.0f * u3, &sp, &cp);
+  x = r * sx * cp; y = r * sx * sp; z = r * cx;
+}
+
+__device__ __forceinline__ bool ws_candidate_deformed(const NucleusDev &n, float ctr, float phir, float u0, float u1,
+                                                      float u2, float u3, float &x, float &y, float &z) {
+  const float R = n.R_f, a = n.a_f;
+  const float r = n.rmax_f * powf(u0, 1.0f / 3.0f);
+  float cx = 1.0f - 2.0f * u1;
+  float rad1 = R * (1.0f + n.beta2_f * sph2(cx) + n.beta4_f * sph4(cx));
+  float rw1 = 1.0f / (1.0f + expf(-rad1 / a));
+  if (u2 * rw1 > 1.0f / (1.0f + expf((r - rad1) / a))) return false;
+  float sx = sqrtf(fmaxf(0.f, 1.0f - cx * cx));
+  float sp, cp;
+  sincospif(2.0f * u3, &sp, &cp);
+  x = r * sx * cp; y = r * sx * sp; z = r * cx;
+  rotate3f(x, y, z, ctr, phir);
   return true;
 }
 
@@ -241,9 +260,12 @@ __device__ __forceinline__ int block_sum_i(int v, int *red, int slot) {
 // kept before it -- the sequential rule of Nucleus::populate, evaluated a
 // batch of kNT candidates at a time.  Returns false if the candidate cap is hit.
 //
-// Per batch: the radially accepted candidates are compacted (nv of them);
-// each is tested against the nucleons accepted so far (two threads per
-// candidate, one per half of the accepted list, when nv <= kNT/2), then
+// Per batch: the radially accepted candidates are compacted (nv of them)
+// and, for spherical nuclei, only these draw their direction.  Distances
+// are tested only between neighbouring z slabs: the slabs are at least
+// 1.01 d_min thick, so points two or more slabs apart are farther than
+// d_min apart even after rounding.  Each candidate is tested against the
+// nucleons accepted so far (held ordered by slab, rebuilt every batch), then
 // against the earlier valid candidates of the batch in 32x32 blocks spread
 // over the warps, giving a bit row per candidate.  Candidates without
 // conflicts are kept; the conflicted ones are decided by warp 0 in rounds:
@@ -256,22 +278,38 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
   const int A = n.A;
   const float dmin2 = n.dmin2_f;
   const uint32_t sid = stream_id(attempt, w == 0 ? ST_PROJ : ST_TARG);
+  // z slabs over [-rmax, rmax]: nslab of them, each at least 1.01 d_min thick
+  const float rmax = n.rmax_f;
+  const int nslab = n.d_min > 0 ? max(1, min(kSlab, (int)floorf(2.f * rmax / (1.01f * (float)n.d_min)))) : 1;
+  const float inv_w = (float)nslab / (2.f * rmax);
+  auto slab_of = [&](float z) { return min(nslab - 1, max(0, (int)floorf((z + rmax) * inv_w))); };
+  if (tid < kSlab) { sm.slab_cnt[tid] = 0; sm.slab_cur[tid] = 0; }
+  __syncthreads();
   int n_acc = 0;
   for (uint32_t base = 0; n_acc < A; base += kNT) {
     if (base > (1u << 20)) return false;
-    uint32_t c = base + tid;
-    float u0, u1, u2, u3;
+    const uint32_t c = base + tid;
+    float u0, u1;
     uniform2f(seed, ev, sid, 2 * c, u0, u1);
-    uniform2f(seed, ev, sid, 2 * c + 1, u2, u3);
-    double u0d = 0, unused;
-    if (n.icdf) uniform2(seed, ev, sid, 2 * c, u0d, unused);
-    float x = 0, y = 0, z = 0;
-    const bool ws = ws_candidate(n, ctr, phir, u0d, u0, u1, u2, u3, x, y, z);
-    // the radially accepted candidates, compacted in candidate order: the
-    // hard-core tests below then run on full warps
+    float x = 0.f, y = 0.f, z = 0.f, r = 0.f;
+    bool ws;
+    if (n.deformed) {
+      float u2, u3;
+      uniform2f(seed, ev, sid, 2 * c + 1, u2, u3);
+      ws = ws_candidate_deformed(n, ctr, phir, u0, u1, u2, u3, x, y, z);
+    } else {
+      double u0d = 0, unused;
+      if (n.icdf) uniform2(seed, ev, sid, 2 * c, u0d, unused);
+      ws = ws_radius(n, u0d, u0, u1, r);
+    }
     const unsigned bal = __ballot_sync(0xffffffffu, ws);
     if (lane == 0) sm.ired[wid] = __popc(bal);
+    // accepted nucleons per slab
+    if (tid < n_acc) atomicAdd(&sm.slab_cnt[slab_of(sm.az[w][tid])], 1);
+    sm.smask[tid >> 3][tid & 7] = 0u;   // kSlab * kNT / 32 == kNT words
     __syncthreads();
+    // the radially accepted candidates, compacted in candidate order; the
+    // accepted nucleons ordered by slab
     int off = 0, nv = 0;
 #pragma unroll
     for (int q = 0; q < kNT / 32; q++) {
@@ -281,67 +319,76 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
     }
     if (ws) {
       const int v = off + __popc(bal & ((1u << lane) - 1u));
-      sm.cx[v] = x; sm.cy[v] = y; sm.cz[v] = z;
+      sm.cpos[v] = n.deformed ? make_float4(x, y, z, 0.f) : make_float4(r, __uint_as_float(c), 0.f, 0.f);
+    }
+    if (tid <= nslab) {
+      int st = 0;
+      for (int t = 0; t < tid; t++) st += sm.slab_cnt[t];
+      sm.slab_start[tid] = st;
+    }
+    if (tid < n_acc) {
+      const float ax = sm.ax[w][tid], ay = sm.ay[w][tid], az = sm.az[w][tid];
+      const int sl = slab_of(az);
+      int st = 0;
+      for (int t = 0; t < sl; t++) st += sm.slab_cnt[t];
+      sm.u.spos[st + atomicAdd(&sm.slab_cur[sl], 1)] = make_float4(ax, ay, az, 0.f);
     }
     __syncthreads();
-    // hard core against the nucleons accepted so far: candidate cv, accepted
-    // nucleons [k0, k1) (both halves of the list when split)
-    {
-      const bool split = nv <= kNT / 2;
-      const int cv = split ? (tid & (kNT / 2 - 1)) : tid, h = split ? (tid >> 7) : 0;
-      const int mid = split ? min(n_acc, ((n_acc >> 1) + 3) & ~3) : n_acc;
-      const int k0 = h ? mid : 0, k1 = h ? n_acc : mid;
-      bool ok = cv < nv;
-      if (ok) {
-        x = sm.cx[cv]; y = sm.cy[cv]; z = sm.cz[cv];
-        // four accepted nucleons per step (16-byte aligned rows, k0 a
-        // multiple of 4; entries past n_acc are never compared)
-        int k = k0;
-        for (; k + 4 <= k1 && ok; k += 4) {
-          const float4 ax = *reinterpret_cast<const float4 *>(&sm.ax[w][k]);
-          const float4 ay = *reinterpret_cast<const float4 *>(&sm.ay[w][k]);
-          const float4 az = *reinterpret_cast<const float4 *>(&sm.az[w][k]);
-          const float d0 = (x - ax.x) * (x - ax.x) + (y - ay.x) * (y - ay.x) + (z - az.x) * (z - az.x);
-          const float d1 = (x - ax.y) * (x - ax.y) + (y - ay.y) * (y - ay.y) + (z - az.y) * (z - az.y);
-          const float d2 = (x - ax.z) * (x - ax.z) + (y - ay.z) * (y - ay.z) + (z - az.z) * (z - az.z);
-          const float d3 = (x - ax.w) * (x - ax.w) + (y - ay.w) * (y - ay.w) + (z - az.w) * (z - az.w);
-          if (fminf(fminf(d0, d1), fminf(d2, d3)) < dmin2) ok = false;
-        }
-        for (; k < k1 && ok; k++) {
-          float dx = x - sm.ax[w][k], dy = y - sm.ay[w][k], dz = z - sm.az[w][k];
-          if (dx * dx + dy * dy + dz * dz < dmin2) ok = false;
-        }
+    // candidate tid (< nv): its direction, then the hard core against the
+    // accepted nucleons of the neighbouring slabs
+    bool ok = tid < nv;
+    int sl = 0;
+    if (ok) {
+      const float4 p = sm.cpos[tid];
+      if (n.deformed) {
+        x = p.x; y = p.y; z = p.z;
+      } else {
+        float u2, u3;
+        uniform2f(seed, ev, sid, 2 * __float_as_uint(p.y) + 1, u2, u3);
+        ws_direction(p.x, u2, u3, x, y, z);
+        sm.cpos[tid] = make_float4(x, y, z, 0.f);
       }
-      // valid word of candidates 32 (cv >> 5) ..: the AND of both halves
-      const unsigned vb = __ballot_sync(0xffffffffu, ok);
-      if (lane == 0) {
-        sm.vb[h][cv >> 5] = vb;
-        if (!split) sm.vb[1][cv >> 5] = ~0u;
-        sm.conf[cv >> 5] = 0u;
+      sl = slab_of(z);
+      const int k1 = sm.slab_start[min(nslab, sl + 2)];
+      for (int k = sm.slab_start[max(0, sl - 1)]; k < k1; k++) {
+        const float4 a = sm.u.spos[k];
+        const float dx = x - a.x, dy = y - a.y, dz = z - a.z;
+        if (dx * dx + dy * dy + dz * dz < dmin2) { ok = false; break; }
       }
+      sm.cslab[tid] = (uint8_t)sl;
     }
+    const unsigned vb = __ballot_sync(0xffffffffu, ok);
+    if (lane == 0) {
+      sm.vb[wid] = vb;
+      sm.conf[wid] = 0u;
+    }
+    if (ok) atomicOr(&sm.smask[sl][wid], 1u << lane);
     __syncthreads();
-    // conflicts with earlier valid candidates of the batch: block (q, r)
-    // holds later candidates q*32+lane against earlier ones r*32+kk
+    // conflicts with earlier valid candidates of the batch (neighbouring
+    // slabs): block (q, r) holds later candidates q*32+lane against earlier
+    // ones r*32+kk
     const int Q = (nv + 31) >> 5;
     for (int blk = wid; blk < Q * (Q + 1) / 2; blk += kNT / 32) {
       int q = 0, s0 = 0;
       while (s0 + q + 1 <= blk) { s0 += q + 1; q++; }
       const int r = blk - s0, cq = q * 32 + lane;
       uint32_t bits = 0;
-      if (((sm.vb[0][q] & sm.vb[1][q]) >> lane) & 1u) {
-        const float cxq = sm.cx[cq], cyq = sm.cy[cq], czq = sm.cz[cq];
-        uint32_t m = sm.vb[0][r] & sm.vb[1][r];
+      if ((sm.vb[q] >> lane) & 1u) {
+        const float4 pc = sm.cpos[cq];
+        const int sc = sm.cslab[cq];
+        uint32_t m = sm.smask[sc][r];
+        if (sc > 0) m |= sm.smask[sc - 1][r];
+        if (sc + 1 < nslab) m |= sm.smask[sc + 1][r];
         if (r == q) m &= (1u << lane) - 1u;
         while (m) {
           const int kk = __ffs(m) - 1;
           m &= m - 1u;
-          const int k = r * 32 + kk;
-          const float dx = cxq - sm.cx[k], dy = cyq - sm.cy[k], dz = czq - sm.cz[k];
+          const float4 pk = sm.cpos[r * 32 + kk];
+          const float dx = pc.x - pk.x, dy = pc.y - pk.y, dz = pc.z - pk.z;
           if (dx * dx + dy * dy + dz * dz < dmin2) bits |= 1u << kk;
         }
       }
-      sm.cmask[cq][r] = bits;
+      sm.u.cmask[cq][r] = bits;
       const unsigned cf = __ballot_sync(0xffffffffu, bits != 0u);
       if (lane == 0 && cf) atomicOr(&sm.conf[q], cf);
     }
@@ -349,7 +396,7 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
     if (wid == 0) {
       // kept / undecided words (lane q < 8 owns word q)
       if (lane < kNT / 32) {
-        const uint32_t v = lane < Q ? (sm.vb[0][lane] & sm.vb[1][lane]) : 0u, u = lane < Q ? sm.conf[lane] : 0u;
+        const uint32_t v = lane < Q ? sm.vb[lane] : 0u, u = lane < Q ? sm.conf[lane] : 0u;
         sm.keep[lane] = v & ~u;
         sm.conf[lane] = u;
       }
@@ -362,7 +409,7 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
           if ((sm.conf[q] >> lane) & 1u) {
             bool hit = false, pend = false;
             for (int r = 0; r <= q; r++) {
-              const uint32_t m = sm.cmask[q * 32 + lane][r];
+              const uint32_t m = sm.u.cmask[q * 32 + lane][r];
               hit |= (m & sm.keep[r]) != 0u;
               pend |= (m & sm.conf[r]) != 0u;
             }
@@ -390,11 +437,13 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
       }
       before += __popc(kw & ((1u << lane) - 1u));
       if (((kw >> lane) & 1u) && n_acc + before < A) {
-        sm.ax[w][n_acc + before] = sm.cx[tid];
-        sm.ay[w][n_acc + before] = sm.cy[tid];
-        sm.az[w][n_acc + before] = sm.cz[tid];
+        const float4 p = sm.cpos[tid];
+        sm.ax[w][n_acc + before] = p.x;
+        sm.ay[w][n_acc + before] = p.y;
+        sm.az[w][n_acc + before] = p.z;
       }
       n_acc += min(total, A - n_acc);
+      if (tid < kSlab) { sm.slab_cnt[tid] = 0; sm.slab_cur[tid] = 0; }
     }
     __syncthreads();
   }
