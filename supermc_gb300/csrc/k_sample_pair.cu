@@ -21,6 +21,21 @@ constexpr int kNT = 256;   // threads per CTA; also the candidate batch size
 constexpr int kSlab = 32;  // z slabs of the hard-core search, at most
 static_assert(kMaxA % 4 == 0, "float4 rows");
 
+// Per-event constants, derived once by thread 0 from the event's parameters
+// (FP64 work is costly here: the other threads read the results)
+struct SampleConsts {
+  double cbox, d_max, disk_val_d;   // participant box half width 4 max(w, w_q), splat radius, 10 / sigma_in
+  float cbox_f, d_max_f, xmin_f, ymin_f;
+  float dsq_lo, dsq_hi, hit_rad;    // FP32 disk-test thresholds, with margins
+  float peak, disk_val, wn;         // FP32 peak, 10 / sigma_in, (1 - alpha) / 2
+  float box_lim, w2, sigma_gg;      // FP32 copies for the pair tests
+  int swept;
+  // eccentricity region of the event
+  double rxl, ryl;
+  float rxl_f, ryl_f;
+  int nXp, nYp, ioff, joff;
+};
+
 struct alignas(16) SampleSmem {
   // candidate batch (nucleus frame): x, y, z; before the direction is drawn
   // (r, candidate index bits, 0, 0)
@@ -51,6 +66,7 @@ struct alignas(16) SampleSmem {
   long long lred[32];
   double b;
   float ori[2][2];   // nucleus orientations (cos theta, phi) of the attempt
+  SampleConsts sc;
 };
 
 // ---------------------------------------------------------------- helpers
@@ -211,8 +227,8 @@ __device__ double hulthen_inv(double y) {
 
 // Means over the block of two FP32 values per thread, (sum v0) / n and
 // (sum v1) / n, exact to double precision for the sums that occur here:
-// double-float warp sums, then the FP64 additions and divisions by one
-// thread (FP64 throughput is a small fraction of FP32 here), broadcast
+// double-float warp sums, then the FP64 additions and division of each sum
+// by one lane (FP64 throughput is a small fraction of FP32 here), broadcast
 // through shared memory.
 __device__ __forceinline__ void block_mean2_f(float v0, float v1, int n, float2 *red, double *out, double &m0,
                                               double &m1) {
@@ -232,12 +248,11 @@ __device__ __forceinline__ void block_mean2_f(float v0, float v1, int n, float2 
     red[kNT / 32 + w] = make_float2(hi[1], lo[1]);
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double s0 = 0, s1 = 0;
-    for (int i = 0; i < kNT / 32; i++) s0 += (double)red[i].x + (double)red[i].y;
-    for (int i = 0; i < kNT / 32; i++) s1 += (double)red[kNT / 32 + i].x + (double)red[kNT / 32 + i].y;
-    out[0] = s0 / n;
-    out[1] = s1 / n;
+  if (threadIdx.x < 2) {   // lane k: sum k
+    const float2 *rk = red + threadIdx.x * (kNT / 32);
+    double sk = 0;
+    for (int i = 0; i < kNT / 32; i++) sk += (double)rk[i].x + (double)rk[i].y;
+    out[threadIdx.x] = sk / n;
   }
   __syncthreads();
   m0 = out[0];
@@ -279,9 +294,8 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
   const float dmin2 = n.dmin2_f;
   const uint32_t sid = stream_id(attempt, w == 0 ? ST_PROJ : ST_TARG);
   // z slabs over [-rmax, rmax]: nslab of them, each at least 1.01 d_min thick
-  const float rmax = n.rmax_f;
-  const int nslab = n.d_min > 0 ? max(1, min(kSlab, (int)floorf(2.f * rmax / (1.01f * (float)n.d_min)))) : 1;
-  const float inv_w = (float)nslab / (2.f * rmax);
+  const float rmax = n.rmax_f, inv_w = n.slab_inv_w;
+  const int nslab = n.nslab;
   auto slab_of = [&](float z) { return min(nslab - 1, max(0, (int)floorf((z + rmax) * inv_w))); };
   if (tid < kSlab) { sm.slab_cnt[tid] = 0; sm.slab_cur[tid] = 0; }
   __syncthreads();
@@ -500,27 +514,31 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
   // exactly except between equal keys, where the FP64 values decide
   const float pxf = (float)px;
   if (tid < A) { sm.X[w][tid] = px; sm.Y[w][tid] = py; sm.Xf[w][tid] = pxf; }
-  __syncthreads();
-  // keys past A read as +inf (never below a key)
-  if (tid >= A && tid < ((A + 3) & ~3)) sm.Xf[w][tid] = INFINITY;
+  else if (tid < ((A + 3) & ~3)) sm.Xf[w][tid] = INFINITY;   // keys past A: never below a key
+  if (tid < kMaxA) sm.hits[w][tid] = 0;   // nucleons per rank (the pairing rewrites hits)
   __syncthreads();
   int rank = 0;
   if (tid < A) {
-    int eq = 0;
     for (int j = 0; j < A; j += 4) {
       const float4 k4 = *reinterpret_cast<const float4 *>(&sm.Xf[w][j]);
       rank += (k4.x < pxf) + (k4.y < pxf) + (k4.z < pxf) + (k4.w < pxf);
-      eq += (k4.x == pxf) + (k4.y == pxf) + (k4.z == pxf) + (k4.w == pxf);
     }
-    if (eq > 1) {   // equal FP32 keys (rare): the FP64 values, then the index, decide
+    atomicAdd(&sm.hits[w][rank], 1);
+  }
+  __syncthreads();
+  // nucleons with equal FP32 keys, and only those, share a rank (rare): the
+  // FP64 values, then the index, decide between them
+  const bool tie = tid < A && sm.hits[w][rank] > 1;
+  if (__syncthreads_or(tie)) {
+    if (tie) {
       for (int j = 0; j < A; j++) {
         if (sm.Xf[w][j] != pxf || j == tid) continue;
         const double xj = sm.X[w][j];
         rank += (xj < px) || (xj == px && j < tid);
       }
     }
+    __syncthreads();
   }
-  __syncthreads();
   if (tid < A) {
     sm.X[w][rank] = px; sm.Y[w][rank] = py;
     sm.Xf[w][rank] = (float)px; sm.Yf[w][rank] = (float)py;
@@ -621,7 +639,7 @@ __device__ __forceinline__ bool pair_hit(const SampleSmem &sm, const DevParams &
   float d2 = dx * dx + dy * dy;
   if (swept) {
     // y-overlap of the bounding boxes (src/MCnucl.cpp:272-274)
-    float ady = fabsf(dy), lim = 4.f * (float)(fmax(P.width, P.quark_width)) * 2.f;
+    float ady = fabsf(dy), lim = sm.sc.box_lim;
     if (ady > lim * (1.f + 1e-5f)) return false;
     if (ady > lim * (1.f - 1e-5f)) {
       double yi = sm.Y[0][i], yj = sm.Y[1][j];
@@ -635,21 +653,42 @@ __device__ __forceinline__ bool pair_hit(const SampleSmem &sm, const DevParams &
     return __dmul_rn(b, b) <= P.dsq;
   }
   // Gaussian profile: P = 1 - exp(-sigma_gg exp(-b^2/4w^2)/(4 pi w^2))
-  if (d2 > 576.f * (float)P.w2) return false;  // P < 1e-60 beyond 24 w
+  const float w2 = sm.sc.w2;
+  if (d2 > 576.f * w2) return false;  // P < 1e-60 beyond 24 w
+  float uf, unusedf;   // (float) of the FP64 uniform, without FP64 arithmetic
+  uniform2f(P.seed, ev, stream_id(attempt, ST_COLL), (uint32_t)(i * B + j), uf, unusedf);
+  float pf = 1.f - expf(-sm.sc.sigma_gg * expf(-d2 / (4.f * w2)) / (4.f * 3.14159265f * w2));
+  if (uf < pf - 1e-5f) return true;
+  if (uf > pf + 1e-5f) return false;
   double u, unused;
   uniform2(P.seed, ev, stream_id(attempt, ST_COLL), (uint32_t)(i * B + j), u, unused);
-  float w2 = (float)P.w2;
-  float pf = 1.f - expf(-(float)P.sigma_gg * expf(-d2 / (4.f * w2)) / (4.f * 3.14159265f * w2));
-  if ((float)u < pf - 1e-5f) return true;
-  if ((float)u > pf + 1e-5f) return false;
   double b = __dsqrt_rn(sq_dist_rn(sm.X[0][i], sm.Y[0][i], sm.X[1][j], sm.Y[1][j]));
   double w = P.width;
   return u < 1. - exp(-P.sigma_gg * exp(-b * b / (4. * w * w)) / (4. * M_PI * w * w));
 }
 
-__device__ __forceinline__ void set_window(Source &s, double lo, double hi, double mn, double d, float inv_d,
-                                           int nmax, bool is_x) {
-  int l = trunc_index(lo, mn, d, inv_d), r = trunc_index(hi, mn, d, inv_d);
+// trunc_index(a + b, mn, d) with a + b rounded in FP64 as the reference
+// rounds the edge, decided from the FP32 copies af, bf, mnf when they
+// settle it: the FP32 value of t = (a + b - mn) / d is off by at most
+// 3 2^-24 (|a| + |b| + |mn|) / d + 2^-23 |t| < 6e-4 while
+// (|a| + |b| + |mn|) / d < 2000, so a fractional part 1e-3 away from an
+// integer truncates as the exact value does.
+__device__ __forceinline__ int edge_index(double a, double b, float af, float bf, double mn, float mnf, double d,
+                                          float inv_d) {
+  const float t = ((af + bf) - mnf) * inv_d;
+  const float f = floorf(t), fr = t - f;
+  if ((fabsf(af) + fabsf(bf) + fabsf(mnf)) * inv_d < 2000.f && fr > 1e-3f && fr < 1.f - 1e-3f) {
+    const int i = (int)f;
+    return (t < 0.f) ? i + 1 : i;   // truncation toward zero
+  }
+  return trunc_index(a + b, mn, d, inv_d);
+}
+
+// window [x - h, x + h) of a source at x (FP32 copy xf) on the grid axis
+// starting at mn: the columns (rows) the reference's truncations give
+__device__ __forceinline__ void set_window_c(Source &s, double x, float xf, double h, float hf, double mn,
+                                             float mnf, double d, float inv_d, int nmax, bool is_x) {
+  int l = edge_index(x, -h, xf, -hf, mn, mnf, d, inv_d), r = edge_index(x, h, xf, hf, mn, mnf, d, inv_d);
   l = max(0, l);
   r = min(nmax, r);
   if (is_x) { s.xl = (int16_t)l; s.xr = (int16_t)r; }
@@ -706,16 +745,35 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
         nu.beta2_f = (float)nu.beta2;
         nu.beta4_f = (float)nu.beta4;
         nu.dmin2_f = (float)(nu.d_min * nu.d_min);
+        nu.nslab = nu.d_min > 0 ? max(1, min(kSlab, (int)floorf(2.f * nu.rmax_f / (1.01f * (float)nu.d_min)))) : 1;
+        nu.slab_inv_w = (float)nu.nslab / (2.f * nu.rmax_f);
       }
+      SampleConsts &c = sm.sc;
+      c.cbox = 4 * fmax(s_P.width, s_P.quark_width);
+      c.d_max = s_P.shape_of_nucleons == 1 ? 2. * sqrt(s_P.dsq) : 5. * s_P.width;
+      c.disk_val_d = 10.0 / s_P.sigin;
+      c.cbox_f = (float)c.cbox;
+      c.d_max_f = (float)c.d_max;
+      c.xmin_f = (float)s_P.xmin;
+      c.ymin_f = (float)s_P.ymin;
+      c.dsq_lo = (float)s_P.dsq * (1.f - 1e-4f);
+      c.dsq_hi = (float)s_P.dsq * (1.f + 1e-4f);
+      c.hit_rad = sqrtf(c.dsq_hi) * (1.f + 1e-4f);   // |dx| beyond it: no disk hit
+      c.peak = (float)s_P.peak;
+      c.disk_val = (float)c.disk_val_d;
+      c.wn = (float)((1.0 - s_P.alpha) / 2.);
+      c.box_lim = 4.f * (float)(fmax(s_P.width, s_P.quark_width)) * 2.f;
+      c.w2 = (float)s_P.w2;
+      c.sigma_gg = (float)s_P.sigma_gg;
+      // The reference only tests pairs its box sweep reaches.  For the disk test
+      // with a hit radius well inside the box width every hit pair is swept, so
+      // all pairs are tested; otherwise the sweep's tested set is reproduced.
+      c.swept = s_P.collision_criterion != 1 || sqrt(s_P.dsq) > 7.9 * fmax(s_P.width, s_P.quark_width);
     }
     __syncthreads();
     const int A = P.nuc[0].A, B = P.nuc[1].A;
-    const float dsq_lo = (float)P.dsq * (1.f - 1e-4f), dsq_hi = (float)P.dsq * (1.f + 1e-4f);
-    const float hit_rad = sqrtf(dsq_hi) * (1.f + 1e-4f);   // |dx| beyond it: no disk hit
-    // The reference only tests pairs its box sweep reaches.  For the disk test
-    // with a hit radius well inside the box width every hit pair is swept, so
-    // all pairs are tested; otherwise the sweep's tested set is reproduced.
-    const bool swept = P.collision_criterion != 1 || sqrt(P.dsq) > 7.9 * fmax(P.width, P.quark_width);
+    const float dsq_lo = sm.sc.dsq_lo, dsq_hi = sm.sc.dsq_hi, hit_rad = sm.sc.hit_rad;
+    const bool swept = sm.sc.swept;
     const uint64_t ev = (ev_base ? *ev_base : 0) + first_event + (uint64_t)e;
     int status = 0, attempt = 0, ncoll = 0, np1 = 0, np2 = 0;
     for (;; attempt++) {
@@ -815,23 +873,24 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
     // ---- splat sources (with their position tangents when requested)
     Source *S = srcs + (size_t)e * P.max_src;
     float4 *stan = tio.stan ? tio.stan + (size_t)e * P.max_src : nullptr;
-    const double d_max = P.shape_of_nucleons == 1 ? 2. * sqrt(P.dsq) : 5. * P.width;
+    const double d_max = sm.sc.d_max;
+    const float d_max_f = sm.sc.d_max_f, xmin_f = sm.sc.xmin_f, ymin_f = sm.sc.ymin_f;
     const int model = P.which_mc_model;
     const bool box_src = (model == 5 && P.sub_model == 1) || model == 7;
     const bool coll_src = model == 5 && P.alpha > 1e-8;
     const bool coll_rec = coll_src || P.want_binary;   // density sources, or records for rho_binary
     const bool thick_src = model == 1 || P.want_ta || P.want_tb;
     const bool disk_n = P.shape_of_nucleons == 1, disk_e = P.shape_of_entropy == 1;
-    const float peak = (float)P.peak;
-    const float disk_val = (float)(10.0 / P.sigin);
+    const float peak = sm.sc.peak;
+    const float disk_val = sm.sc.disk_val;
 
     // region of the eccentricity mask: union of participant boxes and the
     // (unset, all-zero) collision boxes.  Box edges are x -+ c with
     // c = 4 max(w, quark_width), monotone in x, so the region follows from
     // the extreme participant coordinates, found with integer order keys
-    // of the FP64 values (no FP64 arithmetic).
-    const double cbox = 4 * fmax(P.width, P.quark_width);
-    double rxl, rxr, ryl, ryr;
+    // of the FP64 values; thread 0 then derives the region (FP64).
+    const double cbox = sm.sc.cbox;
+    const float cbox_f = sm.sc.cbox_f;
     {
       long long kx0 = LLONG_MAX, kx1 = LLONG_MIN, ky0 = LLONG_MAX, ky1 = LLONG_MIN;
       for (int k = tid; k < AB; k += kNT) {
@@ -852,23 +911,32 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
         sm.lred[w] = kx0; sm.lred[8 + w] = kx1; sm.lred[16 + w] = ky0; sm.lred[24 + w] = ky1;
       }
       __syncthreads();
-      for (int q = 0; q < kNT / 32; q++) {
-        kx0 = min(kx0, sm.lred[q]); kx1 = max(kx1, sm.lred[8 + q]);
-        ky0 = min(ky0, sm.lred[16 + q]); ky1 = max(ky1, sm.lred[24 + q]);
+      if (tid == 0) {
+        for (int q = 0; q < kNT / 32; q++) {
+          kx0 = min(kx0, sm.lred[q]); kx1 = max(kx1, sm.lred[8 + q]);
+          ky0 = min(ky0, sm.lred[16 + q]); ky1 = max(ky1, sm.lred[24 + q]);
+        }
+        double rxl, rxr, ryl, ryr;
+        if (np1 + np2 == 0) {
+          rxl = rxr = ryl = ryr = 0.0;
+        } else {
+          rxl = from_order_key(kx0) - cbox; rxr = from_order_key(kx1) + cbox;
+          ryl = from_order_key(ky0) - cbox; ryr = from_order_key(ky1) + cbox;
+          if (ncoll > 0) {
+            rxl = fmin(rxl, 0.0); rxr = fmax(rxr, 0.0); ryl = fmin(ryl, 0.0); ryr = fmax(ryr, 0.0);
+          }
+        }
+        SampleConsts &c = sm.sc;
+        c.rxl = rxl; c.ryl = ryl;
+        c.rxl_f = (float)rxl; c.ryl_f = (float)ryl;
+        c.nXp = (int)((rxr - rxl) / P.dx); c.nYp = (int)((ryr - ryl) / P.dy);
+        c.ioff = (int)((rxl - P.xmin) / P.dx); c.joff = (int)((ryl - P.ymin) / P.dy);
       }
       __syncthreads();
-      if (np1 + np2 == 0) {
-        rxl = rxr = ryl = ryr = 0.0;
-      } else {
-        rxl = from_order_key(kx0) - cbox; rxr = from_order_key(kx1) + cbox;
-        ryl = from_order_key(ky0) - cbox; ryr = from_order_key(ky1) + cbox;
-        if (ncoll > 0) {
-          rxl = fmin(rxl, 0.0); rxr = fmax(rxr, 0.0); ryl = fmin(ryl, 0.0); ryr = fmax(ryr, 0.0);
-        }
-      }
     }
-    const int nXp = (int)((rxr - rxl) / P.dx), nYp = (int)((ryr - ryl) / P.dy);
-    const int ioff = (int)((rxl - P.xmin) / P.dx), joff = (int)((ryl - P.ymin) / P.dy);
+    const double rxl = sm.sc.rxl, ryl = sm.sc.ryl;
+    const float rxl_f = sm.sc.rxl_f, ryl_f = sm.sc.ryl_f;
+    const int nXp = sm.sc.nXp, nYp = sm.sc.nYp, ioff = sm.sc.ioff, joff = sm.sc.joff;
 
     // participant sources in nucleon order (projectile then target)
     int nsrc = 0;
@@ -897,26 +965,27 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
         }
         int pos = nsrc + (woff + v - flag) * per_part;
         if (flag) {
-          double x = sm.X[w][i], y = sm.Y[w][i];
+          const double x = sm.X[w][i], y = sm.Y[w][i];
+          const float xf = sm.Xf[w][i], yf = sm.Yf[w][i];
           {
             Source s;
             s.x = x; s.y = y;
-            const double bxl = x - cbox, bxr = x + cbox, byl = y - cbox, byr = y + cbox;
             if (box_src) {
-              set_window(s, bxl, bxr, P.xmin, P.dx, inv_dx, P.nx, true);
-              set_window(s, byl, byr, P.ymin, P.dy, inv_dy, P.ny, false);
+              set_window_c(s, x, xf, cbox, cbox_f, P.xmin, xmin_f, P.dx, inv_dx, P.nx, true);
+              set_window_c(s, y, yf, cbox, cbox_f, P.ymin, ymin_f, P.dy, inv_dy, P.ny, false);
             } else {
               s.xl = s.xr = s.yl = s.yr = 0;   // eccentricity mask only
             }
             // mask lattice of MakeDensity.cpp:2356-2358 (its y upper bound divides by dx)
-            int x0 = trunc_index(bxl, rxl, P.dx, inv_dx), x1 = trunc_index(bxr, rxl, P.dx, inv_dx);
-            int y0 = trunc_index(byl, ryl, P.dy, inv_dy), y1 = trunc_index(byr, ryl, P.dx, inv_dx);
+            int x0 = edge_index(x, -cbox, xf, -cbox_f, rxl, rxl_f, P.dx, inv_dx);
+            int x1 = edge_index(x, cbox, xf, cbox_f, rxl, rxl_f, P.dx, inv_dx);
+            int y0 = edge_index(y, -cbox, yf, -cbox_f, ryl, ryl_f, P.dy, inv_dy);
+            int y1 = edge_index(y, cbox, yf, cbox_f, ryl, ryl_f, P.dx, inv_dx);
             s.mx0 = (int16_t)(max(0, x0) + ioff); s.mx1 = (int16_t)(min(nXp, x1) + ioff);
             s.my0 = (int16_t)(max(0, y0) + joff); s.my1 = (int16_t)(min(nYp, y1) + joff);
             s.kind = box_src ? (SRC_PART_BOX | (disk_e ? 16 : 0)) : 3;
             s.plane = (model == 7 && w == 1) ? 1 : 0;
-            s.weight = disk_e ? disk_val * (model == 5 ? (float)((1.0 - P.alpha) / 2.) : 1.f)
-                              : peak * (model == 5 ? (float)((1.0 - P.alpha) / 2.) : 1.f);
+            s.weight = disk_e ? disk_val * (model == 5 ? sm.sc.wn : 1.f) : peak * (model == 5 ? sm.sc.wn : 1.f);
             // Particle::getSmoothDensity's multiplicity factor (MCnucl::selectFluctFactors)
             if (P.fluct)
               s.weight = (float)((double)s.weight *
@@ -938,8 +1007,8 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
           if (thick_src) {
             Source s;
             s.x = x; s.y = y;
-            set_window(s, x - d_max, x + d_max, P.xmin, P.dx, inv_dx, P.nx, true);
-            set_window(s, y - d_max, y + d_max, P.ymin, P.dy, inv_dy, P.ny, false);
+            set_window_c(s, x, xf, d_max, d_max_f, P.xmin, xmin_f, P.dx, inv_dx, P.nx, true);
+            set_window_c(s, y, yf, d_max, d_max_f, P.ymin, ymin_f, P.dy, inv_dy, P.ny, false);
             s.mx0 = s.mx1 = s.my0 = s.my1 = 0;
             s.kind = SRC_THICK | (disk_n ? 16 : 0);
             s.plane = model == 1 ? w : 1 + w;   // MC-KLN splats T_A, T_B only
@@ -980,8 +1049,8 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
           Source s;
           s.x = (sm.X[0][tid] + sm.X[1][j]) / 2.0;
           s.y = (sm.Y[0][tid] + sm.Y[1][j]) / 2.0;
-          set_window(s, s.x - d_max, s.x + d_max, P.xmin, P.dx, inv_dx, P.nx, true);
-          set_window(s, s.y - d_max, s.y + d_max, P.ymin, P.dy, inv_dy, P.ny, false);
+          set_window_c(s, s.x, (float)s.x, d_max, d_max_f, P.xmin, xmin_f, P.dx, inv_dx, P.nx, true);
+          set_window_c(s, s.y, (float)s.y, d_max, d_max_f, P.ymin, ymin_f, P.dy, inv_dy, P.ny, false);
           s.mx0 = s.mx1 = s.my0 = s.my1 = 0;
           s.plane = 0;
           double aw = 0.;
@@ -991,7 +1060,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
           // CollisionPair::getfluctfactor (src/MCnucl.cpp:730-731)
           if (P.fluct)
             fw *= gamma_weight(P.seed, ev, attempt, (uint32_t)(AB + tid * B + j), P.fluct_k_coll, P.fluct_th_coll);
-          s.weight = (float)((disk_e ? 10.0 / P.sigin : P.peak) * fw);
+          s.weight = (float)((disk_e ? sm.sc.disk_val_d : P.peak) * fw);
           s.bx = s.by = 0.f;
           if (stan) {
             const float4 ta = nucleon_tangent(tio.ntan, e, AB, tid), tb = nucleon_tangent(tio.ntan, e, AB, A + j);
@@ -1024,8 +1093,8 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
           Source s;
           s.x = sm.X[w][i];
           s.y = sm.Y[w][i];
-          set_window(s, s.x - d_max, s.x + d_max, P.xmin, P.dx, inv_dx, P.nx, true);
-          set_window(s, s.y - d_max, s.y + d_max, P.ymin, P.dy, inv_dy, P.ny, false);
+          set_window_c(s, s.x, sm.Xf[w][i], d_max, d_max_f, P.xmin, xmin_f, P.dx, inv_dx, P.nx, true);
+          set_window_c(s, s.y, sm.Yf[w][i], d_max, d_max_f, P.ymin, ymin_f, P.dy, inv_dy, P.ny, false);
           s.mx0 = s.mx1 = s.my0 = s.my1 = 0;
           s.kind = SRC_SPECT | (disk_n ? 16 : 0);
           s.plane = w;

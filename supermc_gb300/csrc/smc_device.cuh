@@ -47,8 +47,11 @@ struct NucleusDev {
   int A, deformed;
   double R, a, beta2, beta4, d_min, rmax_cut, rw_max;
   // FP32 roundings of the above (set by the sampler): R, a, rmax_cut, rw_max,
-  // beta2, beta4 and d_min^2 (rounded after the FP64 square)
+  // beta2, beta4 and d_min^2 (rounded after the FP64 square); the sampler's
+  // z slabs (count, inverse thickness) of the hard-core search
   float R_f, a_f, rmax_f, rw_max_f, beta2_f, beta4_f, dmin2_f;
+  int nslab;
+  float slab_inv_w;
   // inverse-CDF radii (NULL table: rejection sampling).  icdf holds the
   // cumulative integrals N, dN/dR, dN/da of r^2 rho(r) at r_k = k icdf_h,
   // k < icdf_m (three rows of icdf_m); icdf_ntot = N(rmax) and its
