@@ -230,11 +230,17 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
 //     target into plane 2.
 // Both cut at dc <= 25 w^2 (dc <= dsq for disks), the SRC_COLL rule; every
 // other record becomes a mask-only record with an empty window.
-__global__ void k_avg_view(DevParams P, int n_events, const EventRec *recs, const Source *in, Source *out, int mode) {
+__global__ void k_avg_view(DevParams P, int n_events, const EventRec *recs, const Source *in, Source *out, int mode,
+                           EventRec *vrecs) {
   const bool disk = P.shape_of_nucleons == 1;
   const float w_unit = disk ? (float)(10.0 / P.sigin) : (float)P.peak;
   for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
     const int ns = recs[e].nsrc;
+    if (threadIdx.x == 0) {   // the view's splat sources may lie anywhere in the records
+      EventRec r = recs[e];
+      r.nsplat = ns;
+      vrecs[e] = r;
+    }
     for (int k = threadIdx.x; k < ns; k += blockDim.x) {
       Source s = in[(size_t)e * P.max_src + k];
       const int kind = s.kind & 15;
@@ -264,8 +270,8 @@ __global__ void k_avg_accum_prod(const float *a, const float *b, int n_events, s
 }
 
 cudaError_t launch_avg_view(const DevParams &P, int n, const EventRec *recs, const Source *in, Source *out, int mode,
-                            int grid, cudaStream_t st) {
-  k_avg_view<<<grid, kAT, 0, st>>>(P, n, recs, in, out, mode);
+                            EventRec *vrecs, int grid, cudaStream_t st) {
+  k_avg_view<<<grid, kAT, 0, st>>>(P, n, recs, in, out, mode, vrecs);
   return cudaGetLastError();
 }
 

@@ -133,11 +133,11 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
       const bool active = r0 + rows > rec.imin && r0 < rec.imax;
       if (active) {
         for (int k = tid; k < np * kR * nyp; k += kGT) acc[k] = 0.f;
-        for (int c0 = 0; c0 < rec.nsrc; c0 += kGT) {
+        for (int c0 = 0; c0 < rec.nsplat; c0 += kGT) {   // the splat sources lead the records
           // compact the sources of this chunk that reach the strip
           int k = c0 + tid;
           bool hit = false;
-          if (k < rec.nsrc) {
+          if (k < rec.nsplat) {
             const Source &s = S[k];
             hit = s.xl < r0 + rows && s.xr > r0 && s.yr > s.yl && (s.kind & 15) < 3;   // kinds >= 3: no splat
           }

@@ -202,9 +202,10 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
     const int ti0 = rec.imin, tj0 = rec.jmin;
     const int nmt = any ? (rec.imax - rec.imin + kTM - 1) / kTM : 0;
     const int nnt = any ? (rec.jmax - rec.jmin + kTN - 1) / kTN : 0;
-    // the sources are taken in windows of kCap entries of the source array;
-    // one window (loaded once per event) for all but the largest events
-    const int nwin = (rec.nsrc + kCap - 1) / kCap;
+    // the splat sources (the leading nsplat records) are taken in windows of
+    // kCap entries of the source array; one window (loaded once per event)
+    // for all but the largest events
+    const int nwin = (rec.nsplat + kCap - 1) / kCap;
     __syncthreads();
     // output grids: cells outside the tiles are zero (the tiles cover every window)
     if (full) {
@@ -222,7 +223,7 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
     // the splat sources of source-array window w, into the cache
     auto load_window = [&](int w) {
       int count = 0;
-      const int lo = w * kCap, hi = min(rec.nsrc, lo + kCap);
+      const int lo = w * kCap, hi = min(rec.nsplat, lo + kCap);
       for (int b = lo; b < hi; b += kTT) {
         const int k = b + tid;
         const bool hit = k < hi && splat_source(S[k]);

@@ -938,13 +938,22 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
     const float rxl_f = sm.sc.rxl_f, ryl_f = sm.sc.ryl_f;
     const int nXp = sm.sc.nXp, nYp = sm.sc.nYp, ioff = sm.sc.ioff, joff = sm.sc.joff;
 
-    // participant sources in nucleon order (projectile then target)
-    int nsrc = 0;
+    // Records of the event: [participant boxes, when they splat][thickness
+    // records][collisions][participant boxes, mask-only][spectators].  The
+    // splat sources lead (nsplat of them); each kind is in the reference's
+    // order (participants: nucleon order, projectile then target).
+    const int Np = np1 + np2;
+    const int ncs = (coll_rec && ncoll > 0) ? min(ncoll, P.max_coll) : 0;
+    const int thick_base = box_src ? Np : 0;
+    const int coll_base = thick_base + (thick_src ? Np : 0);
+    const int mask_base = coll_base + ncs;
+    const int nsplat = coll_base + (coll_src ? ncs : 0);
+    int nsrc = mask_base + (box_src ? 0 : Np);
     int imin = P.nx, imax = 0, jmin = P.ny, jmax = 0;
     {
       // one box record per participant (a splat source, or mask-only when the
       // model does not splat boxes) plus a thickness record when T_A/T_B are made
-      int per_part = 1 + (thick_src ? 1 : 0);
+      int pdone = 0;   // participants placed
       // prefix over wounded flags
       int flag = 0;
       for (int k = tid; k < ((AB + kNT - 1) / kNT) * kNT; k += kNT) {
@@ -963,7 +972,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
           if (q < (tid >> 5)) woff += sm.ired[q];
           tot += sm.ired[q];
         }
-        int pos = nsrc + (woff + v - flag) * per_part;
+        const int p = pdone + woff + v - flag;   // participant index
         if (flag) {
           const double x = sm.X[w][i], y = sm.Y[w][i];
           const float xf = sm.Xf[w][i], yf = sm.Yf[w][i];
@@ -1001,8 +1010,9 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
             } else {
               s.bx = s.by = 0.f;
             }
+            const int pos = box_src ? p : mask_base + p;
             if (stan) stan[pos] = nucleon_tangent(tio.ntan, e, AB, k);
-            S[pos++] = s;
+            S[pos] = s;
           }
           if (thick_src) {
             Source s;
@@ -1014,16 +1024,15 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
             s.plane = model == 1 ? w : 1 + w;   // MC-KLN splats T_A, T_B only
             s.weight = disk_n ? disk_val : peak;
             s.bx = s.by = 0.f;
-            if (stan) stan[pos] = nucleon_tangent(tio.ntan, e, AB, k);
-            S[pos++] = s;
+            if (stan) stan[thick_base + p] = nucleon_tangent(tio.ntan, e, AB, k);
+            S[thick_base + p] = s;
           }
         }
-        nsrc += tot * per_part;
+        pdone += tot;
         __syncthreads();
       }
     }
     // collision sources, ordered by (projectile, target) index
-    int ncs = 0;
     if (coll_rec && ncoll > 0) {
       // exclusive scan of per-projectile hit counts
       int c = tid < A ? sm.hits[0][tid] : 0;
@@ -1038,7 +1047,6 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
       for (int q = 0; q < (tid >> 5); q++) woff += sm.ired[q];
       __syncthreads();
       int pos = woff + v - c;
-      ncs = min(ncoll, P.max_coll);
       if (ncoll > P.max_coll) status = 6;
       if (tid < A && c > 0) {
         int jlo = 0, jhi = B - 1;
@@ -1064,16 +1072,15 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
           s.bx = s.by = 0.f;
           if (stan) {
             const float4 ta = nucleon_tangent(tio.ntan, e, AB, tid), tb = nucleon_tangent(tio.ntan, e, AB, A + j);
-            stan[nsrc + pos] = make_float4(0.5f * (ta.x + tb.x), 0.5f * (ta.y + tb.y), 0.5f * (ta.z + tb.z),
+            stan[coll_base + pos] = make_float4(0.5f * (ta.x + tb.x), 0.5f * (ta.y + tb.y), 0.5f * (ta.z + tb.z),
                                            0.5f * (ta.w + tb.w));
           }
-          S[nsrc + pos] = s;
+          S[coll_base + pos] = s;
           pos++;
         }
       }
     }
     __syncthreads();
-    nsrc += ncs;
     // spectators (MCnucl::getSpectators, src/MCnucl.cpp:1223-1248): the
     // nucleons without a collision, projectile then target, nucleon order
     if (P.want_spect) {
@@ -1132,7 +1139,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
       }
       EventRec r;
       r.b = sm.b;
-      r.npart1 = np1; r.npart2 = np2; r.ncoll = ncoll; r.nsrc = nsrc;
+      r.npart1 = np1; r.npart2 = np2; r.ncoll = ncoll; r.nsrc = nsrc; r.nsplat = nsplat;
       r.attempts = attempt + 1; r.status = status;
       r.imin = imin; r.imax = imax; r.jmin = jmin; r.jmax = jmax;
       r.ev = ev;

@@ -251,6 +251,7 @@ struct Ctx {
   DevBuf<float2> avg_bins;
   DevBuf<float> avg_rho, avg_ta, avg_tb, avg_aux;
   DevBuf<Source> avg_view;
+  DevBuf<EventRec> avg_vrecs;   // the view's records (every record may splat)
   DevBuf<int> avg_status;
   DevBuf<double> avg_acc;
   std::vector<int> h_status;
@@ -778,7 +779,7 @@ void smc_destroy(void *ctx) {
   c->attempts.release(); c->wounded.release(); c->rho_ev.release(); c->corr_ev.release(); c->cm_ev.release();
   c->mix_sys.release(); c->mix_ev.release(); c->mix_order.release(); c->kln64.release(); c->kln32.release();
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
-  c->avg_ta.release(); c->avg_tb.release(); c->avg_aux.release(); c->avg_view.release(); c->avg_status.release();
+  c->avg_ta.release(); c->avg_tb.release(); c->avg_aux.release(); c->avg_view.release(); c->avg_vrecs.release(); c->avg_status.release();
   c->avg_frame.release(); c->avg_order.release(); c->avg_seg.release(); c->avg_count.release();
   c->avg_edges.release(); c->avg_bins.release();
   c->ev_order.release(); c->tickets.release();
@@ -1083,6 +1084,7 @@ smc_status smc_average_profiles(void *ctx, uint64_t first_event, int n, const do
     if (thick) { CK(c->avg_ta.ensure((size_t)m * g)); CK(c->avg_tb.ensure((size_t)m * g)); }
     if (P.want_spect || P.want_binary) {
       CK(c->avg_view.ensure((size_t)m * P.max_src));
+      CK(c->avg_vrecs.ensure(m));
       CK(c->avg_status.ensure(m));
       CK(c->avg_aux.ensure((size_t)m * g * 2));
       CK(c->scratch.ensure((size_t)c->sms * c->occ2 * g));
@@ -1109,8 +1111,8 @@ smc_status smc_average_profiles(void *ctx, uint64_t first_event, int n, const do
         DevParams Pv = P;
         Pv.n_planes = 1;
         Pv.want_ta = Pv.want_tb = 0;
-        CK(smc::launch_avg_view(Pv, m, c->recs.p, c->srcs.p, c->avg_view.p, 0, grid3, c->st));
-        CK(launch_splat(c, Pv, m, c->recs.p, c->avg_view.p, c->avg_aux.p, nullptr, nullptr, c->scratch.p, c->ecc.p,
+        CK(smc::launch_avg_view(Pv, m, c->recs.p, c->srcs.p, c->avg_view.p, 0, c->avg_vrecs.p, grid3, c->st));
+        CK(launch_splat(c, Pv, m, c->avg_vrecs.p, c->avg_view.p, c->avg_aux.p, nullptr, nullptr, c->scratch.p, c->ecc.p,
                         c->avg_status.p));   // (a view's own status, e.g. zero density, is not the event's)
         CK(smc::launch_avg_accum(c->avg_aux.p, m, g, acc_of(K_RHOB, f, q), c->st));
       }
@@ -1119,8 +1121,8 @@ smc_status smc_average_profiles(void *ctx, uint64_t first_event, int n, const do
         Pv.which_mc_model = 5;   // planes 1, 2 are written out as they are
         Pv.n_planes = 3;
         Pv.want_ta = Pv.want_tb = 1;
-        CK(smc::launch_avg_view(Pv, m, c->recs.p, c->srcs.p, c->avg_view.p, 1, grid3, c->st));
-        CK(launch_splat(c, Pv, m, c->recs.p, c->avg_view.p, nullptr, c->avg_aux.p, c->avg_aux.p + (size_t)m * g,
+        CK(smc::launch_avg_view(Pv, m, c->recs.p, c->srcs.p, c->avg_view.p, 1, c->avg_vrecs.p, grid3, c->st));
+        CK(launch_splat(c, Pv, m, c->avg_vrecs.p, c->avg_view.p, nullptr, c->avg_aux.p, c->avg_aux.p + (size_t)m * g,
                         c->scratch.p, c->ecc.p, c->avg_status.p));
         if (want[K_SPA][f]) CK(smc::launch_avg_accum(c->avg_aux.p, m, g, acc_of(K_SPA, f, q), c->st));
         if (want[K_SPB][f])

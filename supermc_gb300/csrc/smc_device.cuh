@@ -142,6 +142,7 @@ struct EventRec {
   int npart1, npart2, ncoll, nsrc;
   int attempts, status;
   int imin, imax, jmin, jmax;   // bounding box of all splat windows (grid idx)
+  int nsplat;                   // records [0, nsplat) hold every splat source
   unsigned long long ev;        // global event id (keys the per-cell fluctuation streams)
 };
 

@@ -59,7 +59,7 @@ cudaError_t launch_avg_accum(const float *rho, int n, size_t cells, double *acc,
 // averaged mode's derived grids: source views (0: rho_binary, 1: spectators)
 // and the T_A T_B product accumulation
 cudaError_t launch_avg_view(const DevParams &P, int n, const EventRec *recs, const Source *in, Source *out, int mode,
-                            int grid, cudaStream_t st);
+                            EventRec *vrecs, int grid, cudaStream_t st);
 cudaError_t launch_avg_accum_prod(const float *a, const float *b, int n, size_t cells, double *acc, cudaStream_t st);
 // Adjoint of a batch (k_adjoint, one CTA per event in turn): per-event
 // gradients dtheta [n][4] = (dL/dw, dL/dalpha, dL/dR, dL/da; the last two
