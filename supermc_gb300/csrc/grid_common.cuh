@@ -50,6 +50,19 @@ struct KSum {
   __device__ __forceinline__ DF df() const { return {s, -c}; }
 };
 
+// Relative half width of the band around a cut dc <= rho2 inside which the
+// FP32 distance does not decide a cell (the FP64 test does).  The FP32 grid
+// coordinates and source positions that reach a cell are at most
+// M = (grid extent) + rho in magnitude and each off by 2^-24 M, so
+// |dc_FP32 - dc| <= 7.2e-7 rho M + 2.4e-7 rho^2; the band is three times
+// that relative to rho^2, never wider than 1e-4.
+__device__ __forceinline__ float cut_band(const DevParams &P, double rho2) {
+  const double rho = sqrt(rho2);
+  const double ext = fmax(fmax(fabs(P.xmin), fabs(P.xmin + (P.nx - 1) * P.dx)),
+                          fmax(fabs(P.ymin), fabs(P.ymin + (P.ny - 1) * P.dy)));
+  return rho > 0 ? (float)fmin(1e-4, 2.2e-6 * (ext + rho) / rho + 7.2e-7) : 1e-4f;
+}
+
 // exact per-cell inclusion, FP64 as the reference evaluates it
 static __device__ __noinline__ bool cell_in_exact(const DevParams &P, double sx, double sy, int kind, int i, int j) {
   double xg = __dadd_rn(P.xmin, __dmul_rn((double)i, P.dx));
@@ -92,7 +105,7 @@ __device__ __forceinline__ bool post_cell(const DevParams &P, int np, float a0, 
     // a zero thickness reads the zero first row / column of the table
     // (src/MCnucl.cpp:937-944): the interpolation is exactly 0 there
     if (t1 == 0.f || t2 == 0.f) return true;
-    const float dT = (float)P.kln_dT;
+    const float dT = P.kln_dT_f;
     float di = t1 / dT, dj = t2 / dT;
     const int tm = P.kln_tmax;
     if (di < 0.f || di >= tm - 2 || dj < 0.f || dj >= tm - 2) return false;

@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
   const int tid = threadIdx.x;
   const double w = P.width;
   const float inv2w2 = (float)(1.0 / (2.0 * P.w2));
-  const float lim = (float)(25.0 * P.w2), lim_lo = lim * (1.f - 1e-4f), lim_hi = lim * (1.f + 1e-4f);
+  const float lim = (float)(25.0 * P.w2), band_g = cut_band(P, 25.0 * P.w2);
+  const float lim_lo = lim * (1.f - band_g), lim_hi = lim * (1.f + band_g);
   const float inv_dy = (float)(1.0 / P.dy), ymin_f = (float)P.ymin;
   const int hmax = P.splat_mw;
   for (int i = tid; i < nx; i += kAT) xg[i] = (float)(P.xmin + i * P.dx);

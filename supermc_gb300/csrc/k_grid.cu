@@ -108,8 +108,10 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
   const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
   const int nx = P.nx, ny = P.ny, nyp = L.nyp, np = L.np;
   const float inv2w2 = (float)(1.0 / (2.0 * P.w2));
-  const float lim = (float)(25.0 * P.w2), lim_lo = lim * (1.f - 1e-4f), lim_hi = lim * (1.f + 1e-4f);
-  const float dsq = (float)P.dsq, dsq_lo = dsq * (1.f - 1e-4f), dsq_hi = dsq * (1.f + 1e-4f);
+  const float lim = (float)(25.0 * P.w2), band_g = cut_band(P, 25.0 * P.w2);
+  const float lim_lo = lim * (1.f - band_g), lim_hi = lim * (1.f + band_g);
+  const float dsq = (float)P.dsq, band_d = cut_band(P, P.dsq);
+  const float dsq_lo = dsq * (1.f - band_d), dsq_hi = dsq * (1.f + band_d);
   const float inv_dy = (float)(1.0 / P.dy), ymin_f = (float)P.ymin;
 
   for (int i = tid; i < nx; i += kGT) xg[i] = (float)(P.xmin + i * P.dx);
@@ -285,17 +287,18 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
         red[wid * 64 + 3] = make_float2(d.hi, d.lo);
       }
       __syncthreads();
-      if (tid == 0) {
-        double sa = 0, sb = 0, sc = 0, sd = 0;
-        for (int w = 0; w < kWarps; w++) {
-          sa += (double)red[w * 64].x + (double)red[w * 64].y;
-          sb += (double)red[w * 64 + 1].x + (double)red[w * 64 + 1].y;
-          sc += (double)red[w * 64 + 2].x + (double)red[w * 64 + 2].y;
-          sd += (double)red[w * 64 + 3].x + (double)red[w * 64 + 3].y;
+      if (tid < 32) {   // lane k < 4 adds sum k (FP64, warp order), lanes 1, 2 divide
+        double t = 0;
+        if (lane < 4)
+          for (int w = 0; w < kWarps; w++) t += (double)red[w * 64 + lane].x + (double)red[w * 64 + lane].y;
+        const double sa = __shfl_sync(0xffffffffu, t, 0), sd = __shfl_sync(0xffffffffu, t, 3);
+        if (lane == 0) {
+          s_cm[0] = sa;
+          // MCnucl.cpp:812-816, on the density before the NBD fluctuations (:819)
+          if (!((NBD ? sd : sa) * P.dx * P.dy >= 1e-15) && s_status == 0) s_status = 5;
+        } else if (lane < 3) {
+          s_cm[lane] = t / sa;
         }
-        s_cm[0] = sa; s_cm[1] = sb / sa; s_cm[2] = sc / sa;
-        // MCnucl.cpp:812-816, on the density before the NBD fluctuations (:819)
-        if (!((NBD ? sd : sa) * P.dx * P.dy >= 1e-15) && s_status == 0) s_status = 5;
       }
       __syncthreads();
     }

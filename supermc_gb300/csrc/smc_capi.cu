@@ -747,6 +747,7 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
     int tmax = p.tmax > 1 ? p.tmax : 71;
     P.kln_tmax = (p.shape_of_nucleons >= 2) ? sub * (tmax - 1) + 1 : tmax;   // MCnucl.cpp:915-919
     P.kln_dT = 10.0 / sigin / 1 / ((p.shape_of_nucleons >= 2) ? sub : 1);
+    P.kln_dT_f = (float)P.kln_dT;
   }
   smc_info &I = c->info;
   I.nx = P.nx; I.ny = P.ny; I.sigin = sigin; I.dsq = P.dsq; I.width = width; I.sigma_gg = P.sigma_gg;

@@ -98,6 +98,7 @@ struct DevParams {
   int ecc_from, ecc_to;
   int kln_tmax;
   double kln_dT;
+  float kln_dT_f;           // (float)kln_dT, read per cell
   const float *kln_table;   // [tmax][tmax] (device)
   int want_ta, want_tb;     // thickness planes requested
   int splat_mw;             // widest splat window in columns (+ margin)
