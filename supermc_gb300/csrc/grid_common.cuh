@@ -302,13 +302,20 @@ __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, co
   // warps take (row, 32-column block) items of the bounding box, lanes the columns
   const int nbj = rec.jmax > rec.jmin ? (rec.jmax - rec.jmin + 31) >> 5 : 0;
   const int nitem = rec.imax > rec.imin ? (rec.imax - rec.imin) * nbj : 0;
-  // the next item's density is loaded before the current one is processed
+  // the next item's density is loaded before the current one is processed;
+  // (ib, jb): row and column block of the warp's next item
+  int ib = nbj > 0 ? wid / nbj : 0, jb = wid - ib * nbj;
   auto fetch = [&](int c, int &i, int &j) -> float {
-    if (c >= nitem) return 0.f;
-    const int ib = c / nbj;
-    i = rec.imin + ib;
-    j = rec.jmin + ((c - ib * nbj) << 5) + lane;
-    return j < rec.jmax ? rho[(size_t)i * ny + j] : 0.f;
+    float v = 0.f;
+    if (c < nitem) {
+      i = rec.imin + ib;
+      j = rec.jmin + (jb << 5) + lane;
+      if (j < rec.jmax) v = rho[(size_t)i * ny + j];
+    }
+    jb += NT / 32;   // nbj >= 1 whenever there are items: at most NT/32 steps
+    if (nbj > 0)
+      while (jb >= nbj) { jb -= nbj; ib++; }
+    return v;
   };
   int i_next = 0, j_next = 0;
   float d_next = fetch(wid, i_next, j_next);
@@ -340,23 +347,34 @@ __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, co
       }
       if (n >= LO && n >= from && n <= to) {
         const int q = n - LO;
-        // r^2 e^{in theta} = z^n r^{2-n};  r^n e^{in theta} = z^n (r^3 e^{i theta} for n = 1)
-        float s2 = n == 1 ? r : 1.f;
-#pragma unroll
-        for (int k = 2; k < n; k++) s2 *= inv_r;
-        a_re2[q] += zr * s2 * d;
-        a_im2[q] += zi * s2 * d;
+        // r^2 e^{in theta} = z^n r^{2-n};  r^n e^{in theta} = z^n (r^3 e^{i theta} for n = 1).
+        // n = 2: the r^2 and r^n sums coincide (taken from a_ren, a_imn and a_norm below)
         if (n == 1) {
+          a_re2[q] += zr * r * d;
+          a_im2[q] += zi * r * d;
           a_ren[q] += zr * r2 * d;
           a_imn[q] += zi * r2 * d;
           a_np[q] += rp[3] * d;
         } else {
+          if (n > 2) {
+            float s2 = inv_r;
+#pragma unroll
+            for (int k = 3; k < n; k++) s2 *= inv_r;
+            const float sd = s2 * d;
+            a_re2[q] += zr * sd;
+            a_im2[q] += zi * sd;
+            a_np[q] += rp[n] * d;
+          }
           a_ren[q] += zr * d;
           a_imn[q] += zi * d;
-          a_np[q] += rp[n] * d;
         }
       }
     }
+  }
+  if (LO <= 2 && HI >= 2) {   // order 2: r^2 e^{2i theta} = z^2, and r^2 = r2
+    a_re2[2 - LO] = a_ren[2 - LO];
+    a_im2[2 - LO] = a_imn[2 - LO];
+    a_np[2 - LO] = a_norm;
   }
   // ---- block reduction in double-float (each accumulator retires as it is reduced)
   constexpr int NV = 10 + 5 * NO;
