@@ -89,7 +89,7 @@ struct Kahan {
 // the centre of mass and the rotation the sources receive.
 __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events, EventRec *recs, Source *srcs,
                                                        AvgSrc *state, const float *rho, int order, int mode,
-                                                       double4 *frame) {
+                                                       AvgFrame *frame) {
   __shared__ float2 red[kAT / 32];
   __shared__ double s_par[4];   // X, Y, cos, sin
   __shared__ int s_box[4];      // the event's new window bounds: imin, imax, jmin, jmax
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
     const double SX = block_sum_df(sx.s, sx.c, red);
     const double SY = block_sum_df(sy.s, sy.c, red);
     if (!(W > 0)) {   // empty density: nothing to move (uniform over the block)
-      if (frame && tid == 0) frame[e] = make_double4(0.0, 0.0, 1.0, 0.0);
+      if (frame && tid == 0) frame[e] = AvgFrame{0.0, 0.0, 1.0, 0.0};
       continue;
     }
     const double X = SX / W, Y = SY / W;
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
     }
     __syncthreads();
     const double cx = s_par[0], cy = s_par[1], cphi = s_par[2], sphi = s_par[3];
-    if (frame && tid == 0) frame[e] = make_double4(cx, cy, cphi, sphi);
+    if (frame && tid == 0) frame[e] = AvgFrame{cx, cy, cphi, sphi};
     if (mode == 2) continue;
     // ---- transform the sources (FP64, reference rounding)
     const double c4w = 4 * P.width, c4q = 4 * P.quark_width;
@@ -340,7 +340,7 @@ __device__ __forceinline__ float binned_value(const float *G, int nx, int ny, fl
 }
 
 __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const EventRec *recs, const float *rho,
-                                                   const double4 *frame, const int *order, const int *seg,
+                                                   const AvgFrame *frame, const int *order, const int *seg,
                                                    int nbins, float2 *acc) {
   __shared__ float4 s_fr[256];
   __shared__ int s_ev[256];
@@ -367,8 +367,8 @@ __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const EventRec 
         e = order[q0 + tid];
         const EventRec r = recs[e];
         if (resample) {
-          const double4 f = frame[e];
-          fr = make_float4((float)f.z, (float)f.w, (float)f.x - xmin, (float)f.y - ymin);
+          const AvgFrame f = frame[e];
+          fr = make_float4((float)f.c, (float)f.s, (float)f.x - xmin, (float)f.y - ymin);
           float lo_x = 1e30f, hi_x = -1e30f, lo_y = 1e30f, hi_y = -1e30f;
 #pragma unroll
           for (int corner = 0; corner < 4; corner++) {
@@ -435,7 +435,7 @@ cudaError_t launch_avg_bins(const EventRec *recs, int n, const int *edges, int n
   return cudaGetLastError();
 }
 
-cudaError_t launch_avg_binned(const DevParams &P, const EventRec *recs, const float *rho, const double4 *frame,
+cudaError_t launch_avg_binned(const DevParams &P, const EventRec *recs, const float *rho, const AvgFrame *frame,
                               const int *order, const int *seg, int nbins, float2 *acc, cudaStream_t st) {
   dim3 grid((P.ny + 15) / 16, (P.nx + 15) / 16);
   k_avg_binned<<<grid, 256, 0, st>>>(P, recs, rho, frame, order, seg, nbins, acc);
@@ -448,7 +448,7 @@ cudaError_t launch_avg_init(const DevParams &P, int n, const EventRec *recs, con
   return cudaGetLastError();
 }
 cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Source *srcs, AvgSrc *state,
-                                 const float *rho, int order, int mode, int grid, cudaStream_t st, double4 *frame) {
+                                 const float *rho, int order, int mode, int grid, cudaStream_t st, AvgFrame *frame) {
   k_avg_transform<<<grid, kAT, 0, st>>>(P, n, recs, srcs, state, rho, order, mode, frame);
   return cudaGetLastError();
 }

@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
   __shared__ double s_cm[3];
 
   const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
-  const int nx = P.nx, ny = P.ny, nyp = L.nyp;
+  const int nx = P.nx, ny = P.ny;
   const float inv2w2 = (float)(1.0 / (2.0 * P.w2));
   const float lim = (float)(25.0 * P.w2), band_g = cut_band(P, 25.0 * P.w2);
   const float lim_lo = lim * (1.f - band_g), lim_hi = lim * (1.f + band_g);
@@ -522,7 +522,7 @@ template <int LO, int HI>
 __global__ void __launch_bounds__(kCT) k_moments(DevParams P, int n_events, const EventRec *recs,
                                                  const Source *srcs, const float *rho_ev, const double *cm_ev,
                                                  double *out_ecc, EventQueue q) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(1024) unsigned char smem[];   // the same symbol as the splat's
   const int nx = P.nx, ny = P.ny;
   uint32_t *mask = reinterpret_cast<uint32_t *>(smem);
   float *xo = reinterpret_cast<float *>(smem + sizeof(uint32_t) * (size_t)nx * ((ny + 31) / 32));

@@ -246,7 +246,7 @@ struct Ctx {
   DevBuf<smc::AvgSrc> avg_state;
   // binned averages: event frames, bin order, bin segments and counts,
   // bin edges, per-bin compensated sums
-  DevBuf<double4> avg_frame;
+  DevBuf<smc::AvgFrame> avg_frame;
   DevBuf<int> avg_order, avg_seg, avg_count, avg_edges;
   DevBuf<float2> avg_bins;
   DevBuf<float> avg_rho, avg_ta, avg_tb, avg_aux;

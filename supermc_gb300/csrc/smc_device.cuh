@@ -137,6 +137,12 @@ __device__ __forceinline__ int queue_next(const EventQueue &q, int k, int *s_k) 
 }
 __device__ __forceinline__ int queue_event(const EventQueue &q, int k) { return q.order ? q.order[k] : k; }
 
+// Averaged mode: an event's frame, the centre of mass (x, y) and the
+// rotation (cos, sin) that brings its participant plane to the x axis.
+struct alignas(16) AvgFrame {
+  double x, y, c, s;
+};
+
 // Per-event record written by the sampling/pairing stage.
 struct EventRec {
   double b;

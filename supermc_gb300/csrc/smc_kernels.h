@@ -47,13 +47,13 @@ cudaError_t launch_avg_init(const DevParams &P, int n, const EventRec *recs, con
                             int grid, cudaStream_t st);
 cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Source *srcs, AvgSrc *state,
                                  const float *rho, int order, int mode, int grid, cudaStream_t st,
-                                 double4 *frame = nullptr);
+                                 AvgFrame *frame = nullptr);
 // centrality bins of a chunk (order[], seg[nbins + 1], counts[nbins] +=)
 cudaError_t launch_avg_bins(const EventRec *recs, int n, const int *edges, int nbins, int *order, int *seg,
                             int *counts, cudaStream_t st);
 // per-bin compensated sums acc [nbins][nx][ny] of the chunk's densities,
 // bilinearly resampled in each event's frame (frame != NULL) or as they are
-cudaError_t launch_avg_binned(const DevParams &P, const EventRec *recs, const float *rho, const double4 *frame,
+cudaError_t launch_avg_binned(const DevParams &P, const EventRec *recs, const float *rho, const AvgFrame *frame,
                               const int *order, const int *seg, int nbins, float2 *acc, cudaStream_t st);
 cudaError_t launch_avg_accum(const float *rho, int n, size_t cells, double *acc, cudaStream_t st);
 // averaged mode's derived grids: source views (0: rho_binary, 1: spectators)
