@@ -19,6 +19,8 @@ namespace smc {
 
 constexpr int kNT = 256;   // threads per CTA; also the candidate batch size
 constexpr int kSlab = 32;  // z slabs of the hard-core search, at most
+static_assert(kSlab * (kNT / 32) == kNT, "one slab-mask word per thread is cleared");
+static_assert(kMaxA <= kNT, "one nucleon per thread");
 static_assert(kMaxA % 4 == 0, "float4 rows");
 
 // Per-event constants, derived once by thread 0 from the event's parameters
