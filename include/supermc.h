@@ -95,6 +95,15 @@ typedef struct smc_params {
                                             min(T_A, T_B) (2); 3-5 rejected */
   double cc_fluctuation_gamma_theta;     /* Gamma scale (cc_fluctuation_Gamma_theta) */
   double cc_fluctuation_k;               /* NBD shape of model 1 (cc_fluctuation_k)  */
+  double kln_exact_band;                 /* MC-KLN: the per-cell table cell
+                                            floor(T/dT) (src/MCnucl.cpp:659-
+                                            670) is taken from FP64 thickness
+                                            sums where T/dT lies within this
+                                            relative distance of an integer
+                                            (<= 0: the error bound of the FP32
+                                            sums, so every cell is decided as
+                                            in FP64; larger values only move
+                                            more cells to the FP64 path)    */
 } smc_params;
 
 /* Derived constants (MCnucl::MCnucl, src/MCnucl.cpp:22-154). */

@@ -20,6 +20,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libsmc_oracle.so")
+# where the reference's source tree lies on the machine that builds the
+# reference checker (the only setting that names it; absent elsewhere)
+REF_ROOT = os.environ.get("SUPERMC_REFERENCE_ROOT", "/root/reference")
 REF_SO = os.path.join(HERE, "_ref", "libsmc_ref.so")
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -38,8 +41,9 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
-def build_reference(ref_root: str = "/root/reference") -> str | None:
+def build_reference(ref_root: str | None = None) -> str | None:
     """Build the reference checker when its source tree is present."""
+    ref_root = ref_root or REF_ROOT
     if not os.path.isdir(os.path.join(ref_root, "src")):
         return None
     repo = os.path.dirname(HERE)
@@ -325,10 +329,45 @@ class OracleEvent:
         self.lib.smco_event_populate_philox(self.h, ctypes.byref(nA), ctypes.byref(nB), b, seed, event, attempt)
 
 
+def _kln_rows_worker(args):
+    """Rows of the MC-KLN table by the oracle's FP64 quadrature (pool worker)."""
+    ecm, lam, dT, rows, tmax, rule = args
+    orc = Oracle()
+    k = KLN()
+    orc.lib.smco_kln_init(ctypes.byref(k), ecm, lam)
+    out = []
+    for i in rows:
+        row = [0.0] * tmax
+        if i > 0:
+            for j in range(1, tmax):
+                row[j] = orc.lib.smco_kln_dndy(ctypes.byref(k), dT * i, dT * j, *rule)
+        out.append((i, row))
+    return out
+
+
+def kln_table(ecm: float, lam: float, dT: float, tmax: int, rule=(48, 64, 32), procs: int | None = None):
+    """The whole MC-KLN dN/dy table [tmax][tmax] (MCnucl::makeTable,
+    src/MCnucl.cpp:911-960) by the oracle's FP64 Gauss-Legendre quadrature of
+    KLNModel::func, rows spread over a process pool (spawned, so that it is
+    safe after a CUDA context exists).  Row and column 0 are zero."""
+    import multiprocessing as mp
+    procs = procs or max(1, os.cpu_count() or 1)
+    rows = list(range(tmax))
+    chunks = [rows[k::procs] for k in range(procs)]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        parts = pool.map(_kln_rows_worker, [(ecm, lam, dT, c, tmax, tuple(rule)) for c in chunks])
+    tab = np.zeros((tmax, tmax))
+    for part in parts:
+        for i, row in part:
+            tab[i] = row
+    return tab
+
+
 class Reference:
     """The reference's own code (compiled from source) with injected inputs."""
 
-    def __init__(self, params_text: str, eos_dir: str = "/root/reference/EOS", workdir: str | None = None):
+    def __init__(self, params_text: str, eos_dir: str | None = None, workdir: str | None = None):
+        eos_dir = eos_dir or os.path.join(REF_ROOT, "EOS")
         if not os.path.exists(REF_SO):
             raise FileNotFoundError(REF_SO)
         lib = ctypes.CDLL(REF_SO)

@@ -62,6 +62,7 @@ class SmcParams(ctypes.Structure):
         ("ws_inverse_cdf", ctypes.c_int),
         ("cc_fluctuation_model", ctypes.c_int), ("cc_fluctuation_gamma_theta", ctypes.c_double),
         ("cc_fluctuation_k", ctypes.c_double),
+        ("kln_exact_band", ctypes.c_double),
     ]
 
 

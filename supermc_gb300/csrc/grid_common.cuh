@@ -14,9 +14,40 @@ namespace smc {
 struct GroupSrc {
   double x, y;
   float xf, yf, weight;
-  int16_t xl, xr, yl, yr;
+  float gi0;               // x = xmin + (gi0 + gfx) dx: grid cell and fraction in [0, 1)
+  float gfy, gj0;          // the same along y (8-byte aligned: read together by the
+                           // accumulating lanes)
+  float gfx;
   int16_t kind, plane;
+  int16_t xl, xr, yl, yr;
 };
+static_assert(offsetof(GroupSrc, gfy) % 8 == 0, "column offsets read as one 8-byte word");
+
+// A source position in grid units split into its cell (exact in FP32) and
+// the fraction within it, (v - vmin)/d - cell, from the FP64 position: the
+// FP32 distance (k - cell) - fraction from the source to grid point k then
+// errs by at most 2^-25 + 2^-24 |distance| grid units, where a difference of
+// FP32 coordinates errs by 2^-24 of the coordinates' magnitude.
+__device__ __forceinline__ void grid_offset(double v, double vmin, double inv_d, float &cell, float &frac) {
+  const double g = (v - vmin) * inv_d;
+  const double c = floor(g);
+  cell = (float)c;
+  frac = (float)(g - c);
+}
+
+// 2^a (PTX ex2.approx.ftz.f32, relative error below 2^-22)
+__device__ __forceinline__ float ex2f(float a) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
+
+// exp(-d^2 / 2w^2) of a grid distance d = (k - cell) - frac in grid units:
+// 2^(-d^2 c) with c = spacing^2 log2(e) / (2 w^2)
+__device__ __forceinline__ float gauss_grid(float k, float cell, float frac, float c) {
+  const float d = (k - cell) - frac;
+  return ex2f(-(d * d) * c);
+}
 
 // ---------------------------------------------------- double-float sums
 struct DF {
@@ -84,15 +115,47 @@ __device__ __forceinline__ float six_point(float x, float y, float v00, float v0
   return axx * x * x + axy * x * y + ayy * y * y + bx * x + by * y + v00;
 }
 
+// Per-cell results of post_cell
+enum CellCode : int {
+  CELL_OK = 0,
+  CELL_TABLE = 1,       // MC-KLN thickness beyond the dN/dy table (status 4)
+  CELL_UNDECIDED = 8,   // MC-KLN: the FP32 thickness leaves the table cell
+                        // floor(T/dT) undecided; it is decided from FP64 sums
+                        // of the planes flagged below
+  CELL_NEED_A = 16, CELL_NEED_B = 32
+};
+
+// The six-point interpolation of the dN/dy table in table cell (ii, jj) at
+// offsets (fi, fj) in lattice units (src/MCnucl.cpp:672-676)
+__device__ __forceinline__ float kln_interp(const DevParams &P, int ii, int jj, float fi, float fj) {
+  const int tm = P.kln_tmax;
+  const float *T = P.kln_table + ii * tm + jj;
+  return six_point(fi, fj, __ldg(T), __ldg(T + 1), __ldg(T + 2), __ldg(T + tm), __ldg(T + tm + 1),
+                   __ldg(T + 2 * tm));
+}
+
+// Relative error bound of an event's FP32 thickness sums: the per-term
+// bound P.kln_band plus one rounding (2^-24) per added term, at most
+// max(Npart1, Npart2) terms.
+__device__ __forceinline__ float kln_event_band(const DevParams &P, const EventRec &rec) {
+  return fmaf((float)max(rec.npart1, rec.npart2), 5.9604645e-8f, P.kln_band);
+}
+
 // Per-cell post-op of the splat planes a0..a2 (np planes): the density v and
 // the thickness outputs t1, t2 (MCnucl::setDensity, src/MCnucl.cpp:654-811).
 //   model 5 (Glauber): v = a0; planes 1, 2 are T_A, T_B when requested
 //   model 7: v = sqrt(T_A T_B)
 //   model 1 (MC-KLN): planes are T_A, T_B; v = dN/dy from the six-point
-//     interpolation in the table; false when the thickness lies beyond it
-//     (the reference exits there, src/MCnucl.cpp:665-670)
-__device__ __forceinline__ bool post_cell(const DevParams &P, int np, float a0, float a1, float a2, float &v,
-                                          float &t1, float &t2) {
+//     interpolation in the table at di = T_A/dT, dj = T_B/dT, table cell
+//     (floor di, floor dj); CELL_TABLE when the thickness lies beyond the
+//     table (the reference exits there, src/MCnucl.cpp:665-670).  The FP32
+//     thickness is within a relative `band` of the reference's FP64 sum;
+//     when di or dj is that close to an integer the table cell (or, for a
+//     cell with a zero thickness, whose value is 0 in any table cell, the
+//     bound test) is undecided in FP32: CELL_UNDECIDED with the planes to
+//     redo in FP64.
+__device__ __forceinline__ int post_cell(const DevParams &P, int np, float a0, float a1, float a2, float band,
+                                         float &v, float &t1, float &t2) {
   v = t1 = t2 = 0.f;
   const int model = P.which_mc_model;
   if (model == 5) {
@@ -101,20 +164,117 @@ __device__ __forceinline__ bool post_cell(const DevParams &P, int np, float a0, 
   } else if (model == 7) {
     v = sqrtf(a0 * a1);
   } else {
-    t1 = a0; t2 = a1;
+    // a nonzero thickness is at least one source's value at the cut; below
+    // half of that only rounding residues of the tensor-core corner
+    // subtraction remain: the reference's sum there is exactly 0
+    t1 = a0 < P.kln_tzero ? 0.f : a0;
+    t2 = a1 < P.kln_tzero ? 0.f : a1;
+    // T/dT as T (1/dT): within 2 ulp of the quotient, inside the band
+    const float di = t1 * P.kln_inv_dT_f, dj = t2 * P.kln_inv_dT_f;
+    const float fi = di - floorf(di), fj = dj - floorf(dj);
+    const float bi = fmaf(band, di, 1e-7f), bj = fmaf(band, dj, 1e-7f);
+    const int tm = P.kln_tmax;
+    const bool both = t1 > 0.f && t2 > 0.f;
+    const bool near_a = t1 > 0.f && (fi < bi || fi > 1.f - bi) && (both || di > tm - 3);
+    const bool near_b = t2 > 0.f && (fj < bj || fj > 1.f - bj) && (both || dj > tm - 3);
+    if (near_a || near_b) return CELL_UNDECIDED | (near_a ? CELL_NEED_A : 0) | (near_b ? CELL_NEED_B : 0);
+    if (di >= tm - 2 || dj >= tm - 2) return CELL_TABLE;
     // a zero thickness reads the zero first row / column of the table
     // (src/MCnucl.cpp:937-944): the interpolation is exactly 0 there
-    if (t1 == 0.f || t2 == 0.f) return true;
-    const float dT = P.kln_dT_f;
-    float di = t1 / dT, dj = t2 / dT;
-    const int tm = P.kln_tmax;
-    if (di < 0.f || di >= tm - 2 || dj < 0.f || dj >= tm - 2) return false;
-    int ii = (int)floorf(di), jj = (int)floorf(dj);
-    const float *T = P.kln_table + ii * tm + jj;
-    v = six_point(di - ii, dj - jj, __ldg(T), __ldg(T + 1), __ldg(T + 2), __ldg(T + tm), __ldg(T + tm + 1),
-                  __ldg(T + 2 * tm));
+    if (!both) return CELL_OK;
+    v = kln_interp(P, (int)di, (int)dj, fi, fj);
   }
-  return true;
+  return CELL_OK;
+}
+
+// The thickness of plane `pl` (0: T_A, 1: T_B) at the cell (i, j) in FP64,
+// summed as the reference sums it (MCnucl::setThickness,
+// src/MCnucl.cpp:432-478; Particle::getSmoothTn, src/Particle.cpp:122-132):
+// every thickness record of the plane whose window holds the cell adds
+// peak exp(-r^2/2w^2) unless r > 5w (disk nucleons: 10/sigma_in unless
+// dc > dsq, added one by one in FP64 as the reference adds them).  The
+// plane's records are S[base, base + n), x-sorted, so those of row i sit in
+// a few 32-record chunks.  Called by a whole warp (lanes over the records);
+// every lane returns the sum.
+__device__ __forceinline__ double thickness_fp64(const DevParams &P, const Source *S, int base, int n, int pl, int i,
+                                                 int j) {
+  const int lane = threadIdx.x & 31;
+  const double xg = __dadd_rn(P.xmin, __dmul_rn((double)i, P.dx));
+  const double yg = __dadd_rn(P.ymin, __dmul_rn((double)j, P.dy));
+  const double cut = __dmul_rn(5., P.width), cut2 = cut * cut;
+  const double inv2w2 = 1.0 / (2.0 * P.w2);
+  double sum = 0.0;
+  int ndisk = 0;
+  for (int k0 = 0; k0 < n; k0 += 32) {
+    double t = 0.0;
+    bool in = false, disk_hit = false;
+    if (k0 + lane < n) {
+      const Source &s = S[base + k0 + lane];
+      if ((s.kind & 15) == SRC_THICK && s.plane == pl && i >= s.xl && i < s.xr && j >= s.yl && j < s.yr) {
+        in = true;
+        const double dc = sq_dist_rn(s.x, s.y, xg, yg);
+        if (s.kind & 16) {
+          disk_hit = !(dc > P.dsq);
+        } else {
+          // r = sqrt(dc) > 5w decided on dc away from the cut
+          const bool keep = dc < cut2 * (1 - 1e-12) ? true
+                            : dc > cut2 * (1 + 1e-12) ? false
+                                                      : !(__dsqrt_rn(dc) > cut);
+          if (keep) t = P.peak * exp(-dc * inv2w2);
+        }
+      }
+    }
+    if (!__ballot_sync(0xffffffffu, in)) continue;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    sum += __shfl_sync(0xffffffffu, t, 0);
+    ndisk += __popc(__ballot_sync(0xffffffffu, disk_hit));
+  }
+  if (ndisk) {   // disk nucleons: n equal terms, added in turn
+    const double c = 10.0 / P.sigin;
+    for (int k = 0; k < ndisk; k++) sum += c;
+  }
+  return sum;
+}
+
+// The MC-KLN cell from thickness values taken as decided in FP64 (the
+// planes redone in FP64, the others already decided by their FP32 value),
+// the table cell as the reference takes it (di = T_A/dT in FP64,
+// src/MCnucl.cpp:659-676); t1, t2 receive the thickness outputs.
+__device__ __forceinline__ int kln_cell_fp64(const DevParams &P, double ta, double tb, float &v, float &t1,
+                                             float &t2) {
+  const double di = ta / P.kln_dT, dj = tb / P.kln_dT;
+  t1 = (float)ta;
+  t2 = (float)tb;
+  v = 0.f;
+  const int tm = P.kln_tmax;
+  if (di >= tm - 2 || dj >= tm - 2) return CELL_TABLE;
+  if (ta == 0.0 || tb == 0.0) return CELL_OK;
+  const int ii = (int)floor(di), jj = (int)floor(dj);
+  v = kln_interp(P, ii, jj, (float)(di - ii), (float)(dj - jj));
+  return CELL_OK;
+}
+
+// Warp-wide completion of post_cell: every lane passes its cell (i, j),
+// code and thickness values; the undecided cells of the warp are redone one
+// at a time by the whole warp, each flagged plane from FP64 sums over its
+// thickness records (MC-KLN records: [projectile participants][target
+// participants] at the end of the splat records).  All 32 lanes call it.
+__device__ __forceinline__ void kln_resolve_warp(const DevParams &P, const EventRec &rec, const Source *S, int i,
+                                                 int j, int &code, float &v, float &t1, float &t2) {
+  unsigned m = __ballot_sync(0xffffffffu, (code & CELL_UNDECIDED) != 0);
+  const int lane = threadIdx.x & 31;
+  const int base0 = rec.nsplat - rec.npart1 - rec.npart2, base1 = base0 + rec.npart1;
+  while (m) {
+    const int src = __ffs(m) - 1;
+    m &= m - 1u;
+    const int ci = __shfl_sync(0xffffffffu, i, src), cj = __shfl_sync(0xffffffffu, j, src);
+    const int need = __shfl_sync(0xffffffffu, code, src);
+    double ta = (double)__shfl_sync(0xffffffffu, t1, src), tb = (double)__shfl_sync(0xffffffffu, t2, src);
+    if (need & CELL_NEED_A) ta = thickness_fp64(P, S, base0, rec.npart1, 0, ci, cj);
+    if (need & CELL_NEED_B) tb = thickness_fp64(P, S, base1, rec.npart2, 1, ci, cj);
+    if (lane == src) code = kln_cell_fp64(P, ta, tb, v, t1, t2);
+  }
 }
 
 // Column interval [ja, jb) of row i that the reference includes for source

@@ -82,6 +82,62 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
   return L;
 }
 
+// column steps of 32 cells whose MC-KLN fix-up marks one 64-bit word holds
+constexpr int kPendSteps = 32;
+
+// a thread's centre-of-mass sums and the density sum before fluctuations
+struct CmSums {
+  KSum c0, c1, c2, pre;
+};
+
+// The MC-KLN cells of row i, columns s0 + 32 k + lane, that post_cell left
+// undecided (pend: two bits per step k, the planes to redo), finished by the
+// whole warp in step and lane order: the flagged thickness sums redone in
+// FP64 (thickness_fp64), then each cell's owner lane writes its outputs and
+// adds it to its centre-of-mass sums (so the sums keep one deterministic
+// order).  t_a, t_b: the strip's T_A and T_B rows.  The sums go in and come
+// back by value (their addresses are never taken, so they stay in registers
+// in the caller's loops).
+template <bool NBD>
+static __device__ __noinline__ CmSums kln_finish_row(const DevParams &P, const EventRec &rec, const Source *S,
+                                                     const float *t_a, const float *t_b, int i, int s0, uint64_t pend,
+                                                     float *rho, float *ta, float *tb, float xi, const float *yg,
+                                                     CmSums cs, int *s_status) {
+  const int lane = threadIdx.x & 31, ny = P.ny;
+  for (int k = 0; k < kPendSteps; k++) {
+    const unsigned need = (unsigned)(pend >> (2 * k)) & 3u;
+    unsigned m = __ballot_sync(0xffffffffu, need != 0);
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1u;
+      const int j = s0 + 32 * k + src;
+      const unsigned nd = __shfl_sync(0xffffffffu, need, src);
+      // the FP32 values as post_cell took them (below kln_tzero: zero)
+      const float a0 = t_a[j] < P.kln_tzero ? 0.f : t_a[j], a1 = t_b[j] < P.kln_tzero ? 0.f : t_b[j];
+      const double da = (nd & 1u) ? thickness_fp64(P, S, rec.nsplat - rec.npart1 - rec.npart2, rec.npart1, 0, i, j)
+                                  : (double)a0;
+      const double db = (nd & 2u) ? thickness_fp64(P, S, rec.nsplat - rec.npart2, rec.npart2, 1, i, j) : (double)a1;
+      if (lane == src) {
+        float v, t1, t2;
+        if (kln_cell_fp64(P, da, db, v, t1, t2) == CELL_TABLE) *s_status = 4;
+        if (NBD) {
+          cs.pre.add(v);
+          v = nbd_cell(P, rec.ev, (uint32_t)(i * ny + j), v, t1, t2);
+        }
+        rho[(size_t)i * ny + j] = v;
+        if (ta) ta[(size_t)i * ny + j] = t1;
+        if (tb) tb[(size_t)i * ny + j] = t2;
+        if (v != 0.f) {
+          cs.c0.add(v);
+          cs.c1.add(xi * v);
+          cs.c2.add(yg[j] * v);
+        }
+      }
+    }
+  }
+  return cs;
+}
+
 // NBD: the per-cell negative-binomial fluctuations (a separate instance, so
 // that the common case carries none of their registers)
 template <int LO, int HI, bool NBD>
@@ -107,7 +163,10 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
 
   const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
   const int nx = P.nx, ny = P.ny, nyp = L.nyp, np = L.np;
-  const float inv2w2 = (float)(1.0 / (2.0 * P.w2));
+  // Gaussian factors 2^(-d^2 c) of grid distances d (gauss_grid)
+  const float cx = (float)(P.dx * P.dx * 1.4426950408889634 / (2.0 * P.w2));
+  const float cy = (float)(P.dy * P.dy * 1.4426950408889634 / (2.0 * P.w2));
+  const double inv_dx64 = 1.0 / P.dx, inv_dy64 = 1.0 / P.dy;
   const float lim = (float)(25.0 * P.w2), band_g = cut_band(P, 25.0 * P.w2);
   const float lim_lo = lim * (1.f - band_g), lim_hi = lim * (1.f + band_g);
   const float dsq = (float)P.dsq, band_d = cut_band(P, P.dsq);
@@ -128,6 +187,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
     if (tid == 0) s_status = rec.status;
     KSum cm0, cm1, cm2, pre;   // pre: the density before NBD fluctuations (the zero-dN/dy test)
     const bool full = out_rho || ta || tb;
+    const float kband = kln_event_band(P, rec);
     __syncthreads();
 
     for (int r0 = 0; r0 < nx; r0 += kR) {
@@ -162,6 +222,8 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
               const Source &s = S[list[g0 + t]];
               GroupSrc g;
               g.x = s.x; g.y = s.y; g.xf = (float)s.x; g.yf = (float)s.y; g.weight = s.weight;
+              grid_offset(s.x, P.xmin, inv_dx64, g.gi0, g.gfx);
+              grid_offset(s.y, P.ymin, inv_dy64, g.gj0, g.gfy);
               g.xl = s.xl; g.xr = s.xr; g.yl = s.yl; g.yr = s.yr;
               g.kind = s.kind; g.plane = s.plane;
               grp[t] = g;
@@ -192,7 +254,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
               if (r < rows && i >= g.xl && i < g.xr) {
                 const bool disk = g.kind & 16;
                 const float dx = xg[i] - g.xf, dx2 = dx * dx;
-                exw = disk ? g.weight : g.weight * __expf(-dx2 * inv2w2);
+                exw = disk ? g.weight : g.weight * gauss_grid((float)i, g.gi0, g.gfx, cx);
                 int jb;
                 row_interval(P, g, i, dx2, disk ? dsq_lo : lim_lo, disk ? dsq_hi : lim_hi, yg, inv_dy, ymin_f, ja,
                              jb);
@@ -209,7 +271,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
             // unit visits only the sources that reach its block, in order
             for (int u = wid; u < (nyp / 32) * kSplit; u += kWarps) {
               const int jb = u / kSplit, j = jb * 32 + lane, rh = (u - jb * kSplit) * kRU;
-              const float yj = yg[j];
+              const float jf = (float)j;
               for (int pl = 0; pl < np; pl++) {
                 float *ab = acc + ((size_t)pl * kR + rh) * nyp + j;
                 float a[kRU];
@@ -222,8 +284,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
                     const int q = h * 32 + __ffs(m) - 1;
                     m &= m - 1u;
                     const GroupSrc &g = grp[q];
-                    const float dy = yj - g.yf;
-                    const float ey = (g.kind & 16) ? 1.f : __expf(-dy * dy * inv2w2);
+                    const float ey = (g.kind & 16) ? 1.f : gauss_grid(jf, g.gj0, g.gfy, cy);
 #pragma unroll
                     for (int r4 = 0; r4 < kRU; r4 += 4) {
                       const int o = q * kR + rh + r4;
@@ -252,25 +313,43 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
         const int jlo = full ? 0 : rec.jmin, jhi = full ? ny : rec.jmax;
         for (int rr = wid; rr < rows; rr += kWarps) {
           const int i = r0 + rr;
-          for (int j = jlo + lane; j < jhi; j += 32) {
-            float v = 0.f, t1 = 0.f, t2 = 0.f;
-            if (active) {
-              const float a0 = acc[rr * nyp + j];
-              const float a1 = np > 1 ? acc[(kR + rr) * nyp + j] : 0.f;
-              const float a2 = np > 2 ? acc[(2 * kR + rr) * nyp + j] : 0.f;
-              if (!post_cell(P, np, a0, a1, a2, v, t1, t2)) s_status = 4;
-              if (NBD) {
-                pre.add(v);
-                v = nbd_cell(P, rec.ev, (uint32_t)(i * ny + j), v, t1, t2);
+          // segments of up to 32 column steps: the MC-KLN cells left
+          // undecided in FP32 are marked (the planes to redo, two bits per
+          // step) and finished by the warp after the segment, outside the
+          // per-cell loop
+          for (int s0 = jlo; s0 < jhi; s0 += 32 * kPendSteps) {
+            const int s1 = min(jhi, s0 + 32 * kPendSteps);
+            uint64_t pend = 0;
+            for (int j = s0 + lane; j < s1; j += 32) {
+              float v = 0.f, t1 = 0.f, t2 = 0.f;
+              if (active) {
+                const float a0 = acc[rr * nyp + j];
+                const float a1 = np > 1 ? acc[(kR + rr) * nyp + j] : 0.f;
+                const float a2 = np > 2 ? acc[(2 * kR + rr) * nyp + j] : 0.f;
+                const int code = post_cell(P, np, a0, a1, a2, kband, v, t1, t2);
+                if (code & CELL_UNDECIDED) {
+                  pend |= (uint64_t)((code & (CELL_NEED_A | CELL_NEED_B)) >> 4) << (2 * ((j - s0) >> 5));
+                  continue;
+                }
+                if (code == CELL_TABLE) s_status = 4;
+                if (NBD) {
+                  pre.add(v);
+                  v = nbd_cell(P, rec.ev, (uint32_t)(i * ny + j), v, t1, t2);
+                }
+              }
+              rho[(size_t)i * ny + j] = v;
+              if (ta) ta[(size_t)i * ny + j] = t1;
+              if (tb) tb[(size_t)i * ny + j] = t2;
+              if (v != 0.f) {
+                cm0.add(v);
+                cm1.add(xg[i] * v);
+                cm2.add(yg[j] * v);
               }
             }
-            rho[(size_t)i * ny + j] = v;
-            if (ta) ta[(size_t)i * ny + j] = t1;
-            if (tb) tb[(size_t)i * ny + j] = t2;
-            if (v != 0.f) {
-              cm0.add(v);
-              cm1.add(xg[i] * v);
-              cm2.add(yg[j] * v);
+            if (P.which_mc_model == 1 && __any_sync(0xffffffffu, pend != 0)) {
+              const CmSums cs = kln_finish_row<NBD>(P, rec, S, acc + rr * nyp, acc + (kR + rr) * nyp, i, s0, pend,
+                                                    rho, ta, tb, xg[i], yg, CmSums{cm0, cm1, cm2, pre}, &s_status);
+              cm0 = cs.c0; cm1 = cs.c1; cm2 = cs.c2; pre = cs.pre;
             }
           }
         }

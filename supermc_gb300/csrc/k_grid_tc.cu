@@ -83,6 +83,7 @@ constexpr int kErrMmaTimeout = 8;        // per-event status when that limit is 
 // A splat source held in shared memory.
 struct CSrc {
   float xf, yf, w;
+  float gi0, gfx, gj0, gfy;   // grid cell and fraction of the position (grid_offset)
   int16_t xl, xr, yl, yr, kind, plane;
   int idx;   // index in the event's source array (FP64 position for the exact test)
 };
@@ -157,7 +158,10 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
 
   const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
   const int nx = P.nx, ny = P.ny;
-  const float inv2w2 = (float)(1.0 / (2.0 * P.w2));
+  // Gaussian factors 2^(-d^2 c) of grid distances d (gauss_grid)
+  const float cx = (float)(P.dx * P.dx * 1.4426950408889634 / (2.0 * P.w2));
+  const float cy = (float)(P.dy * P.dy * 1.4426950408889634 / (2.0 * P.w2));
+  const double inv_dx64 = 1.0 / P.dx, inv_dy64 = 1.0 / P.dy;
   const float lim = (float)(25.0 * P.w2), band_g = cut_band(P, 25.0 * P.w2);
   const float lim_lo = lim * (1.f - band_g), lim_hi = lim * (1.f + band_g);
   const float inv_dy = (float)(1.0 / P.dy), ymin_f = (float)P.ymin;
@@ -197,6 +201,7 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
     float *tb = out_tb ? out_tb + (size_t)e * nx * ny : nullptr;
     int *corr = corr_scratch + (size_t)blockIdx.x * np * nx * ny;   // [plane][i][j], this CTA's
     const bool full = out_rho || ta || tb;
+    const float kband = kln_event_band(P, rec);
     if (tid == 0) s_status = rec.status;
     KSum cm0, cm1, cm2, pre;   // pre: the density before NBD fluctuations (the zero-dN/dy test)
     const bool any = rec.imax > rec.imin && rec.jmax > rec.jmin;
@@ -232,7 +237,11 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
       }
       for (int t = tid; t < count; t += kTT) {
         const Source &s = S[lo + list[t]];
-        cache[t] = CSrc{(float)s.x, (float)s.y, s.weight, s.xl, s.xr, s.yl, s.yr, s.kind, s.plane, lo + list[t]};
+        CSrc c{(float)s.x, (float)s.y, s.weight, 0.f, 0.f, 0.f, 0.f, s.xl, s.xr, s.yl, s.yr, s.kind, s.plane,
+               lo + list[t]};
+        grid_offset(s.x, P.xmin, inv_dx64, c.gi0, c.gfx);
+        grid_offset(s.y, P.ymin, inv_dy64, c.gj0, c.gfy);
+        cache[t] = c;
       }
       if (tid == 0) s_ncache = count;
       __syncthreads();
@@ -258,16 +267,12 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
         cut_interval(P, &S[cs.idx].x, cs.kind, cs.yf, i, dx * dx, lim_lo, lim_hi, yg, inv_dy, ymin_f, cs.yl,
                      cs.yr, ja, jb);
         if (ja <= cs.yl && jb >= cs.yr) continue;
-        const float exw = cs.w * __expf(-dx * dx * inv2w2) * inv_corr_unit;
+        const float exw = cs.w * gauss_grid((float)i, cs.gi0, cs.gfx, cx) * inv_corr_unit;
         int *crow = corr + ((size_t)cs.plane * nx + i) * ny;
-        for (int j = cs.yl; j < ja; j++) {
-          const float d = yg[j] - cs.yf;
-          atomicAdd(&crow[j], __float2int_rn(exw * __expf(-d * d * inv2w2)));
-        }
-        for (int j = jb; j < cs.yr; j++) {
-          const float d = yg[j] - cs.yf;
-          atomicAdd(&crow[j], __float2int_rn(exw * __expf(-d * d * inv2w2)));
-        }
+        for (int j = cs.yl; j < ja; j++)
+          atomicAdd(&crow[j], __float2int_rn(exw * gauss_grid((float)j, cs.gj0, cs.gfy, cy)));
+        for (int j = jb; j < cs.yr; j++)
+          atomicAdd(&crow[j], __float2int_rn(exw * gauss_grid((float)j, cs.gj0, cs.gfy, cy)));
       }
       __syncthreads();
     }
@@ -346,10 +351,7 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
                 float v = 0.f;
                 if (q < kc) {
                   const CSrc &cs = src_of(p, c0 + q);
-                  if (i >= cs.xl && i < cs.xr) {
-                    const float d = xg[i] - cs.xf;
-                    v = cs.w * __expf(-d * d * inv2w2);
-                  }
+                  if (i >= cs.xl && i < cs.xr) v = cs.w * gauss_grid((float)i, cs.gi0, cs.gfx, cx);
                 }
                 const float h = tc::to_tf32(v);
                 Ah[idx] = h;
@@ -364,10 +366,7 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
                 float v = 0.f;
                 if (q < kc) {
                   const CSrc &cs = src_of(p, c0 + q);
-                  if (j >= cs.yl && j < cs.yr) {
-                    const float d = yg[j] - cs.yf;
-                    v = __expf(-d * d * inv2w2);
-                  }
+                  if (j >= cs.yl && j < cs.yr) v = gauss_grid((float)j, cs.gj0, cs.gfy, cy);
                 }
                 const float h = tc::to_tf32(v);
                 Bh[idx] = h;
@@ -431,13 +430,26 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
         }
         __syncthreads();
         // ---- 4. post-op of the owned cells, outputs and centre-of-mass sums
-        if (i_own < nx) {
+        // (a warp owns 32 rows of the same columns: the loop is warp-uniform,
+        // as the MC-KLN fix-up needs)
+        {
           const float *sr = stage + (size_t)r_own * kSP + kQ * hc;
           for (int k = 0; k < kQ; k++) {
             const int j = c_lo + k;
             if (j >= c_hi) break;
+            const bool inwin = i_own < rec.imax && j < rec.jmax;   // rec.imax <= nx
+            float v = 0.f, t1 = 0.f, t2 = 0.f;
+            int code = CELL_OK;
+            if (inwin) {
+              const float a0 = (used & 1u) ? fmaxf(sr[k], 0.f) : 0.f;
+              const float a1 = np > 1 && (used & 2u) ? fmaxf(sr[kTM * kSP + k], 0.f) : 0.f;
+              code = post_cell(P, np, a0, a1, 0.f, kband, v, t1, t2);
+            }
+            if (P.which_mc_model == 1) kln_resolve_warp(P, rec, S, i_own, j, code, v, t1, t2);
+            if (code == CELL_TABLE) s_status = 4;
+            if (i_own >= nx) continue;
             const size_t g = (size_t)i_own * ny + j;
-            if (i_own >= rec.imax || j >= rec.jmax) {   // beyond every window: zero
+            if (!inwin) {   // beyond every window: zero
               if (full) {
                 rho[g] = 0.f;
                 if (ta) ta[g] = 0.f;
@@ -445,11 +457,6 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
               }
               continue;
             }
-            const float a0 = (used & 1u) ? fmaxf(sr[k], 0.f) : 0.f;
-            const float a1 = np > 1 && (used & 2u) ? fmaxf(sr[kTM * kSP + k], 0.f) : 0.f;
-            const float a2 = 0.f;
-            float v, t1, t2;
-            if (!post_cell(P, np, a0, a1, a2, v, t1, t2)) s_status = 4;
             if (P.nbd) {
               pre.add(v);
               v = nbd_cell(P, rec.ev, (uint32_t)g, v, t1, t2);

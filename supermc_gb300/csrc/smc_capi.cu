@@ -342,8 +342,11 @@ smc_status build_kln_table(Ctx *c) {
   gauss_legendre01(npt, xp, wp);
   gauss_legendre01(nkt, xk, wk);
   gauss_legendre01(nphi, xf, wf);
+  // cos(2 pi x) of the phi nodes up to the middle (the rule is symmetric)
+  std::vector<double> cf(nphi / 2 + 1);
+  for (int f = 0; f <= nphi / 2 && f < nphi; f++) cf[f] = std::cos(2 * M_PI * xf[f]);
   std::vector<double> nodes;
-  for (auto *v : {&xp, &wp, &xk, &wk, &xf, &wf}) nodes.insert(nodes.end(), v->begin(), v->end());
+  for (auto *v : {&xp, &wp, &xk, &wk, &xf, &wf, &cf}) nodes.insert(nodes.end(), v->begin(), v->end());
   double *d_nodes = nullptr;
   CK(cudaMalloc(&d_nodes, sizeof(double) * nodes.size()));
   CK(cudaMemcpyAsync(d_nodes, nodes.data(), sizeof(double) * nodes.size(), cudaMemcpyHostToDevice, c->st));
@@ -363,6 +366,7 @@ smc_status build_kln_table(Ctx *c) {
   K.npt = npt; K.nkt = nkt; K.nphi = nphi;
   K.xp = d_nodes; K.wp = d_nodes + npt; K.xk = K.wp + npt; K.wk = K.xk + nkt; K.xf = K.wk + nkt;
   K.wf = K.xf + nphi;
+  K.cf = K.wf + nphi;
   int tmax = c->info.kln_tmax;
   CK(c->kln64.ensure((size_t)tmax * tmax));
   CK(c->kln32.ensure((size_t)tmax * tmax));
@@ -748,6 +752,26 @@ smc_status smc_create(const smc_params *params, void **ctx_out) {
     P.kln_tmax = (p.shape_of_nucleons >= 2) ? sub * (tmax - 1) + 1 : tmax;   // MCnucl.cpp:915-919
     P.kln_dT = 10.0 / sigin / 1 / ((p.shape_of_nucleons >= 2) ? sub : 1);
     P.kln_dT_f = (float)P.kln_dT;
+    P.kln_inv_dT_f = (float)(1.0 / P.kln_dT);
+    // Relative error bound of a Gaussian term of the splats' FP32 thickness
+    // against the FP64 one.  A source sits at grid cell + fraction (FP64
+    // split, the fraction rounded by 2^-25 grid units), and the grid
+    // distance d = (k - cell) - fraction errs by 2^-25 + 2^-24 |d|; the
+    // exponent d^2 c (c = spacing^2 log2(e) / 2w^2 rounded, two products)
+    // then errs by 2^-24 (c |d| + 5 d^2 c) per axis, at most 2^-24 (c
+    // 5w/spacing + 5 x 12.5 log2(e)) in all (r <= 5w), times ln 2 relative;
+    // ex2.approx adds 2^-22 per factor, the weight and the two products an
+    // ulp each, the tensor cores' split-TF32 products below 1e-6.  Plus the
+    // quotient by dT (T times the rounded 1/dT: 2 ulp) and a margin.  The
+    // kernels add one rounding per summed term, at most max(Npart1, Npart2)
+    // terms per event.  Disk nucleons add one constant per term.
+    const double u = std::ldexp(1.0, -24), ln2 = std::log(2.0);
+    const double cg = std::max(p.dx, p.dy) * std::max(p.dx, p.dy) / (2 * width * width) / ln2;
+    const double expo = u * (cg * 5 * width / std::min(p.dx, p.dy) + 5 * 12.5 / ln2) * ln2;
+    const double terms = p.shape_of_nucleons == 1 ? 1e-7 : expo + 2 * std::ldexp(1.0, -22) + 3 * u + 1e-6;
+    P.kln_band = (float)(terms + 1e-6);
+    if (p.kln_exact_band > P.kln_band) P.kln_band = (float)p.kln_exact_band;
+    P.kln_tzero = (float)(0.5 * (p.shape_of_nucleons == 1 ? 10.0 / sigin : P.peak * std::exp(-12.5)));
   }
   smc_info &I = c->info;
   I.nx = P.nx; I.ny = P.ny; I.sigin = sigin; I.dsq = P.dsq; I.width = width; I.sigma_gg = P.sigma_gg;

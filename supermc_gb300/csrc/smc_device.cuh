@@ -98,7 +98,13 @@ struct DevParams {
   int ecc_from, ecc_to;
   int kln_tmax;
   double kln_dT;
-  float kln_dT_f;           // (float)kln_dT, read per cell
+  float kln_dT_f;           // (float)kln_dT
+  float kln_inv_dT_f;       // (float)(1 / kln_dT), read per cell
+  // bound on the relative error of a term of the splats' FP32 thickness sums
+  // against the reference's FP64 terms (a cell whose T/dT lies within the
+  // event's bound of an integer takes its table cell from FP64 sums), and
+  // half the smallest nonzero thickness a source adds (its value at the cut)
+  float kln_band, kln_tzero;
   const float *kln_table;   // [tmax][tmax] (device)
   int want_ta, want_tb;     // thickness planes requested
   int splat_mw;             // widest splat window in columns (+ margin)

@@ -9,6 +9,7 @@ struct KlnDev {
   double ecm, lambda, y, ptmin, ptmax, lambda_qcd2, alpha_max, beta0, fac, prefactor;
   int npt, nkt, nphi;
   const double *xp, *wp, *xk, *wk, *xf, *wf;   // Gauss-Legendre nodes on [0,1]
+  const double *cf;                            // cos(2 pi xf[f]), f <= nphi / 2
 };
 
 size_t sample_pair_smem();

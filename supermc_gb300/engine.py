@@ -47,6 +47,7 @@ def smc_params_from(vals: dict[str, float], seed: int = 1) -> _lib.SmcParams:
     p.cc_fluctuation_model = int(v["cc_fluctuation_model"])
     p.cc_fluctuation_gamma_theta = v["cc_fluctuation_gamma_theta"]
     p.cc_fluctuation_k = v["cc_fluctuation_k"]
+    p.kln_exact_band = v["kln_exact_band"]
     return p
 
 

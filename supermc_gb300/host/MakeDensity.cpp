@@ -31,7 +31,7 @@ const Default kDefaults[] = {
     // extensions (0: the reference's hard-coded value)
     {"proj_R", 0}, {"proj_a", 0}, {"targ_R", 0}, {"targ_a", 0}, {"proj_d_min", 0}, {"targ_d_min", 0},
     {"siginNN_override", 0}, {"kln_npt", 48}, {"kln_nkt", 64}, {"kln_nphi", 32}, {"max_attempts", 0},
-    {"max_collisions", 0}, {"ws_inverse_cdf", 0},
+    {"max_collisions", 0}, {"ws_inverse_cdf", 0}, {"kln_exact_band", 0},
 };
 
 double val(const ParameterReader &p, const char *name) {
@@ -97,6 +97,7 @@ smc_params params_from(const ParameterReader &p) {
   s.cc_fluctuation_model = (int)val(p, "cc_fluctuation_model");
   s.cc_fluctuation_gamma_theta = val(p, "cc_fluctuation_Gamma_theta");
   s.cc_fluctuation_k = val(p, "cc_fluctuation_k");
+  s.kln_exact_band = val(p, "kln_exact_band");
   return s;
 }
 

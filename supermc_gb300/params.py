@@ -50,6 +50,9 @@ EXTENSION_KEYS: dict[str, float] = {
     "max_attempts": 0, "max_collisions": 0,
     # Woods-Saxon radii by inverse CDF (differentiable in R and a)
     "ws_inverse_cdf": 0,
+    # MC-KLN: relative band around table-cell boundaries decided from FP64
+    # thickness sums (0: the FP32 error bound)
+    "kln_exact_band": 0.0,
 }
 
 

@@ -1,12 +1,12 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a container that holds the reference source tree (default
-/root/reference): it builds oracle/_ref/libsmc_ref.so from those sources
+Run in a container that holds the reference source tree (--ref, default
+the SUPERMC_REFERENCE_ROOT setting of oracle/oracle.py): it builds oracle/_ref/libsmc_ref.so from those sources
 (oracle/Makefile.ref) and drives the reference's own code through the
 injection harness (oracle/ref_harness.cpp).  The fixtures then pin the
 oracle and the GPU path on machines without the reference.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref <reference tree>]
 """
 from __future__ import annotations
 
@@ -21,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
-from oracle.oracle import Reference, build_reference  # noqa: E402
+from oracle.oracle import REF_ROOT, Reference, build_reference  # noqa: E402
 from supermc_gb300.params import parameters_text, read_parameters  # noqa: E402
 
 # parameter sets (parameters.dat keys) of the fixtures
@@ -39,7 +39,7 @@ SYSTEMS = {
 }
 
 
-EOS_DIR = "/root/reference/EOS"
+EOS_DIR = os.path.join(REF_ROOT, "EOS")
 
 
 def ref_for(args, extra=()):
@@ -227,7 +227,7 @@ def make_text(out):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=REF_ROOT)
     ap.add_argument("--nev", type=int, default=1500)
     ap.add_argument("--only", choices=["constants", "sampler", "inject", "average", "kln", "native", "text"],
                     help="regenerate one fixture only")

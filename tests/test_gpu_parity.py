@@ -265,10 +265,13 @@ def test_kln_table_vs_oracle(oracle):
     dT = eng.info.kln_dT
     for i, j in rng.integers(1, 211, size=(12, 2)):
         want = oracle.lib.smco_kln_dndy(ctypes.byref(k), i * dT, j * dT, 48, 64, 32)
-        assert tab[i, j] == pytest.approx(want, rel=2e-5)
+        assert tab[i, j] == pytest.approx(want, rel=1e-9)
 
 
 def test_kln_events_vs_oracle(oracle):
+    """Injected MC-KLN events at sigma_in(2.76 TeV), at the Glauber bars (the
+    GPU's table equals the oracle's own, tests/test_gpu_kln.py, where the
+    benchmark workload runs against the oracle's table)."""
     from oracle.oracle import _ptr
     vals = values(SYSTEMS["pbpb2760"], which_mc_model=1, sub_model=7, **{"lambda": 0.288})
     eng = engine(vals)
@@ -285,8 +288,8 @@ def test_kln_events_vs_oracle(oracle):
         assert ev.thickness() == 0 and ev.density() == 0
         for w, key in ((0, "ta"), (1, "tb"), (2, "rho")):
             ref = ev.grid(w)
-            assert np.abs(out[key][k] - ref).max() <= 1e-4 * ref.max()
-        np.testing.assert_allclose(out["ecc"][k], ev.eccentricities(1, 9, bs[k]), rtol=1e-5, atol=1e-5)
+            assert np.abs(out[key][k] - ref).max() <= GRID_RTOL * ref.max()
+        assert_ecc_close(out["ecc"][k], ev.eccentricities(1, 9, bs[k]))
 
 
 @pytest.mark.parametrize("model,over", [
