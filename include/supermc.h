@@ -394,8 +394,8 @@ smc_status smc_write_nucleon_tables(const double *xy, const uint8_t *wounded, in
  * smc_status).  Work is queued on cuda_stream (NULL: the legacy default
  * stream) and is complete when that stream is.
  *   - Intermediate data use one static 24 MiB device array: each event needs
- *     64 + 48 * (2 (A + B) + max_collisions) bytes (max_collisions defaults to
- *     2048 here), e.g. at most 180 Pb+Pb events per call; larger n returns
+ *     64 + 64 * (2 (A + B) + max_collisions) bytes (max_collisions defaults to
+ *     2048 here), e.g. at most 136 Pb+Pb events per call; larger n returns
  *     SMC_ERR_SCRATCH_LIMIT.
  *   - All calls share that array: calls that overlap on the GPU (other
  *     streams, other threads) race.  Nothing in it needs clearing.

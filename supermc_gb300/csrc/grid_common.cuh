@@ -15,6 +15,7 @@ struct GroupSrc {
   double x, y;
   float xf, yf, weight;
   float gi0;               // x = xmin + (gi0 + gfx) dx: grid cell and fraction in [0, 1)
+                           // (Source::gi0 .. gfy)
   float gfy, gj0;          // the same along y (8-byte aligned: read together by the
                            // accumulating lanes)
   float gfx;
@@ -22,18 +23,6 @@ struct GroupSrc {
   int16_t xl, xr, yl, yr;
 };
 static_assert(offsetof(GroupSrc, gfy) % 8 == 0, "column offsets read as one 8-byte word");
-
-// A source position in grid units split into its cell (exact in FP32) and
-// the fraction within it, (v - vmin)/d - cell, from the FP64 position: the
-// FP32 distance (k - cell) - fraction from the source to grid point k then
-// errs by at most 2^-25 + 2^-24 |distance| grid units, where a difference of
-// FP32 coordinates errs by 2^-24 of the coordinates' magnitude.
-__device__ __forceinline__ void grid_offset(double v, double vmin, double inv_d, float &cell, float &frac) {
-  const double g = (v - vmin) * inv_d;
-  const double c = floor(g);
-  cell = (float)c;
-  frac = (float)(g - c);
-}
 
 // 2^a (PTX ex2.approx.ftz.f32, relative error below 2^-22)
 __device__ __forceinline__ float ex2f(float a) {

@@ -180,6 +180,7 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
       }
       s.x = x;
       s.y = y;
+      set_grid_offsets(s, P);
       // splat windows from the new geometry (src/MCnucl.cpp:829-832, :732-735, :450-453);
       // mask-only records keep their empty window
       if (kind == 3) continue;

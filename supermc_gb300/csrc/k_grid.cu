@@ -166,7 +166,6 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
   // Gaussian factors 2^(-d^2 c) of grid distances d (gauss_grid)
   const float cx = (float)(P.dx * P.dx * 1.4426950408889634 / (2.0 * P.w2));
   const float cy = (float)(P.dy * P.dy * 1.4426950408889634 / (2.0 * P.w2));
-  const double inv_dx64 = 1.0 / P.dx, inv_dy64 = 1.0 / P.dy;
   const float lim = (float)(25.0 * P.w2), band_g = cut_band(P, 25.0 * P.w2);
   const float lim_lo = lim * (1.f - band_g), lim_hi = lim * (1.f + band_g);
   const float dsq = (float)P.dsq, band_d = cut_band(P, P.dsq);
@@ -222,8 +221,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
               const Source &s = S[list[g0 + t]];
               GroupSrc g;
               g.x = s.x; g.y = s.y; g.xf = (float)s.x; g.yf = (float)s.y; g.weight = s.weight;
-              grid_offset(s.x, P.xmin, inv_dx64, g.gi0, g.gfx);
-              grid_offset(s.y, P.ymin, inv_dy64, g.gj0, g.gfy);
+              g.gi0 = s.gi0; g.gfx = s.gfx; g.gj0 = s.gj0; g.gfy = s.gfy;
               g.xl = s.xl; g.xr = s.xr; g.yl = s.yl; g.yr = s.yr;
               g.kind = s.kind; g.plane = s.plane;
               grp[t] = g;

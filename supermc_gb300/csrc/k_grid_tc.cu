@@ -161,7 +161,6 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
   // Gaussian factors 2^(-d^2 c) of grid distances d (gauss_grid)
   const float cx = (float)(P.dx * P.dx * 1.4426950408889634 / (2.0 * P.w2));
   const float cy = (float)(P.dy * P.dy * 1.4426950408889634 / (2.0 * P.w2));
-  const double inv_dx64 = 1.0 / P.dx, inv_dy64 = 1.0 / P.dy;
   const float lim = (float)(25.0 * P.w2), band_g = cut_band(P, 25.0 * P.w2);
   const float lim_lo = lim * (1.f - band_g), lim_hi = lim * (1.f + band_g);
   const float inv_dy = (float)(1.0 / P.dy), ymin_f = (float)P.ymin;
@@ -237,11 +236,8 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
       }
       for (int t = tid; t < count; t += kTT) {
         const Source &s = S[lo + list[t]];
-        CSrc c{(float)s.x, (float)s.y, s.weight, 0.f, 0.f, 0.f, 0.f, s.xl, s.xr, s.yl, s.yr, s.kind, s.plane,
-               lo + list[t]};
-        grid_offset(s.x, P.xmin, inv_dx64, c.gi0, c.gfx);
-        grid_offset(s.y, P.ymin, inv_dy64, c.gj0, c.gfy);
-        cache[t] = c;
+        cache[t] = CSrc{(float)s.x, (float)s.y, s.weight, s.gi0, s.gfx, s.gj0, s.gfy, s.xl, s.xr, s.yl, s.yr,
+                        s.kind, s.plane, lo + list[t]};
       }
       if (tid == 0) s_ncache = count;
       __syncthreads();

@@ -1014,6 +1014,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
             }
             const int pos = box_src ? p : mask_base + p;
             if (stan) stan[pos] = nucleon_tangent(tio.ntan, e, AB, k);
+            set_grid_offsets(s, P);
             S[pos] = s;
           }
           if (thick_src) {
@@ -1027,6 +1028,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
             s.weight = disk_n ? disk_val : peak;
             s.bx = s.by = 0.f;
             if (stan) stan[thick_base + p] = nucleon_tangent(tio.ntan, e, AB, k);
+            set_grid_offsets(s, P);
             S[thick_base + p] = s;
           }
         }
@@ -1077,6 +1079,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
             stan[coll_base + pos] = make_float4(0.5f * (ta.x + tb.x), 0.5f * (ta.y + tb.y), 0.5f * (ta.z + tb.z),
                                            0.5f * (ta.w + tb.w));
           }
+          set_grid_offsets(s, P);
           S[coll_base + pos] = s;
           pos++;
         }
@@ -1109,6 +1112,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
           s.plane = w;
           s.weight = disk_n ? disk_val : peak;
           s.bx = s.by = 0.f;
+          set_grid_offsets(s, P);
           S[nsrc + woff + __popc(bal & ((1u << (tid & 31)) - 1u))] = s;
         }
         nsrc += tot;

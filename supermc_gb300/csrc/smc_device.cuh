@@ -33,8 +33,12 @@ struct Source {
   int16_t kind, plane;   // SrcKind, accumulator plane
   float weight;          // multiplies exp(-r^2/2w^2)
   float bx, by;          // construction point of a participant box (kind bit SRC_RAW_BASE)
+  // the position in grid units, split into a cell (exact in FP32) and the
+  // fraction within it: x = xmin + (gi0 + gfx) dx, y = ymin + (gj0 + gfy) dy
+  // (set_grid_offsets; the splats' Gaussian arguments are taken from them)
+  float gi0, gfx, gj0, gfy;
 };
-static_assert(sizeof(Source) == 48, "Source layout");
+static_assert(sizeof(Source) == 64, "Source layout");
 
 // Averaged-mode state of one source: construction position and the
 // current bounding box with Box2D's centre (src/Box2D.h:16-63).
@@ -326,6 +330,24 @@ static __device__ __noinline__ float nbd_cell(const DevParams &P, uint64_t ev, u
 #endif
 
 // ------------------------------------------------------- exact helpers
+#ifdef __CUDACC__
+// A position in grid units split into its cell (exact in FP32) and the
+// fraction within it, (v - vmin)/d - cell, from the FP64 position: the FP32
+// distance (k - cell) - fraction from the position to grid point k then errs
+// by at most 2^-25 + 2^-24 |distance| grid units, where a difference of FP32
+// coordinates errs by 2^-24 of the coordinates' magnitude.
+__device__ __forceinline__ void grid_offset(double v, double vmin, double d, float &cell, float &frac) {
+  const double g = (v - vmin) / d;
+  const double c = floor(g);
+  cell = (float)c;
+  frac = (float)(g - c);
+}
+__device__ __forceinline__ void set_grid_offsets(Source &s, const DevParams &P) {
+  grid_offset(s.x, P.xmin, P.dx, s.gi0, s.gfx);
+  grid_offset(s.y, P.ymin, P.dy, s.gj0, s.gfy);
+}
+#endif
+
 // (int)((v - mn)/d) as the reference computes it in FP64 (C++ truncation
 // toward zero).  FP64 division is slow on this part, so the FP32 estimate
 // is used whenever it is provably on the same side of every integer.

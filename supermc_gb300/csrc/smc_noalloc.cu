@@ -12,7 +12,7 @@
 //
 // Limits and rules (also stated in include/supermc.h):
 //   * the scratch array is kNoAllocScratchBytes (24 MiB); a call needs
-//     64 + 48 * (2 (A + B) + max_collisions) bytes per event, with
+//     64 + 64 * (2 (A + B) + max_collisions) bytes per event, with
 //     max_collisions = 2048 unless the parameters set it; larger requests
 //     are refused with SMC_ERR_SCRATCH_LIMIT;
 //   * every call shares the array and it keeps the last call's contents; the
