@@ -146,6 +146,13 @@ typedef struct smc_outputs {
                            (pair midpoints) in the reference's order
                            (MCnucl::createBinaryCollisions, src/MCnucl.cpp:
                            326-352); the first ncoll rows of each event     */
+  double *orientation;  /* [n][4] cos(theta), phi of the projectile, then of
+                           the target: the orientation Nucleus::populate
+                           draws for the accepted attempt (src/Nucleus.cpp:
+                           192-197; it rotates deformed nuclei); zero for
+                           injected nuclei.  The deformed layout of the
+                           eccentricity files carries it
+                           (smc_write_ecc_deformed)                          */
 } smc_outputs;
 
 /* MCnucl::MCnucl + MakeDensity::MakeDensity: validates the configuration,
@@ -366,6 +373,16 @@ smc_status smc_kln_table(void *ctx, double *host_table, int capacity);
  * smc_write_density_4col: MakeDensity::dumpDensity4Col (:2573-2595): a
  *   header with Npart and the grid size, then rapidity, x, y, value per cell. */
 smc_status smc_write_ecc(const double *ecc, int n, int from_order, int to_order, const char *pattern);
+/* smc_write_ecc in the layout dumpEccentricities writes when a nucleus is
+ * deformed (proj_deformed or targ_deformed = 1; src/MakeDensity.cpp:
+ * 2435-2455, 2483-2492): each line of every file ends in four more fields
+ * (%16.8g), cos(theta) and phi of the projectile, then of the target, from
+ * orientation[n][4] (smc_outputs.orientation).  The reference prints the
+ * members MCnucl::lastCx1, lastPh1, lastCx2, lastPh2 there, which its code
+ * never assigns (src/MCnucl.h:90), so its files hold whatever those members
+ * contain; here they hold the orientations the names describe. */
+smc_status smc_write_ecc_deformed(const double *ecc, const double *orientation, int n, int from_order,
+                                  int to_order, const char *pattern);
 smc_status smc_write_density_block(const double *grid, int nx, int ny, const char *filename);
 smc_status smc_write_density_4col(const double *grid, int nx, int ny, double xmin, double ymin, double dx, double dy,
                                   double rapidity, double npart, const char *filename);

@@ -28,7 +28,7 @@ EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "sm
            "smc_set_grid_path", "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_write_ecc",
            "smc_write_density_block", "smc_write_density_4col", "smc_inject_noalloc", "smc_average",
            "smc_average_binned", "smc_adjoint", "smc_autotune", "smc_generate_graph", "smc_average_profiles",
-           "smc_write_binary_table", "smc_write_nucleon_tables"]
+           "smc_write_binary_table", "smc_write_nucleon_tables", "smc_write_ecc_deformed"]
 
 
 class SmcError(RuntimeError):
@@ -88,7 +88,7 @@ class SmcOutputs(ctypes.Structure):
         ("ecc", ctypes.c_void_p), ("rho", ctypes.c_void_p), ("ta", ctypes.c_void_p), ("tb", ctypes.c_void_p),
         ("npart", ctypes.c_void_p), ("ncoll", ctypes.c_void_p), ("b", ctypes.c_void_p),
         ("attempts", ctypes.c_void_p), ("positions", ctypes.c_void_p), ("wounded", ctypes.c_void_p),
-        ("tangents", ctypes.c_void_p), ("collisions", ctypes.c_void_p),
+        ("tangents", ctypes.c_void_p), ("collisions", ctypes.c_void_p), ("orientation", ctypes.c_void_p),
     ]
 
 
@@ -140,6 +140,7 @@ def load() -> ctypes.CDLL:
     lib.smc_set_timing.argtypes = [vp, ctypes.c_int]
     lib.smc_set_grid_path.argtypes = [vp, ctypes.c_int]
     lib.smc_write_ecc.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
+    lib.smc_write_ecc_deformed.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
     lib.smc_write_density_block.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
     lib.smc_write_density_4col.argtypes = [vp, ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 6 + [ctypes.c_char_p]
     lib.smc_get_stats.argtypes = [vp, ctypes.POINTER(SmcStats)]

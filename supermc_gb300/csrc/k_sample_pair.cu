@@ -1150,6 +1150,20 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
       r.imin = imin; r.imax = imax; r.jmin = jmin; r.jmax = jmax;
       r.ev = ev;
       recs[e] = r;
+      // Nucleus::populate's (cx, phi) of both nuclei (src/Nucleus.cpp:192-196),
+      // in FP64 from the attempt's uniforms; zero for injected nuclei
+      if (tio.orient) {
+        double o[4] = {0.0, 0.0, 0.0, 0.0};
+        if (!inject && status == 0) {
+          for (int w = 0; w < 2; w++) {
+            double o0, o1;
+            uniform2(P.seed, ev, stream_id(attempt, ST_EVENT), 1 + w, o0, o1);
+            o[2 * w] = 1.0 - 2.0 * o0;
+            o[2 * w + 1] = 2 * M_PI * o1;
+          }
+        }
+        for (int k = 0; k < 4; k++) tio.orient[4 * (size_t)e + k] = o[k];
+      }
     }
     __syncthreads();
   }

@@ -228,7 +228,7 @@ struct Ctx {
   // position tangents (differentiable sampling): inverse-CDF tables, the
   // per-nucleon and per-source tangents, injected tangents, and the set the
   // next sampler launch uses
-  DevBuf<double> icdf_tab[2], ntan, inj_tp, inj_tt;
+  DevBuf<double> icdf_tab[2], ntan, inj_tp, inj_tt, orient;
   DevBuf<float4> stan;
   smc::TangentIO tio{};
   std::vector<double> h_adj;
@@ -392,6 +392,7 @@ smc_status ensure_buffers(Ctx *c, int n, const smc_outputs *out) {
     if (out->wounded) CK(c->wounded.ensure((size_t)n * (c->info.A + c->info.B)));
     if (out->tangents) CK(c->ntan.ensure((size_t)n * 4 * (c->info.A + c->info.B)));
     if (out->collisions) CK(c->coll.ensure((size_t)n * 2 * P.max_coll));
+    if (out->orientation) CK(c->orient.ensure((size_t)n * 4));
   }
   if (!out->ecc || out->device == 0) CK(c->ecc.ensure((size_t)n * smc::kEccLen));
   return SMC_OK;
@@ -517,8 +518,10 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
   double *pos = out->positions ? (dev ? out->positions + (size_t)off * 2 * AB : c->pos.p) : nullptr;
   uint8_t *wnd = out->wounded ? (dev ? out->wounded + (size_t)off * AB : c->wounded.p) : nullptr;
   double *tg = out->tangents ? (dev ? out->tangents + (size_t)off * 4 * AB : c->ntan.p) : nullptr;
+  double *ori = out->orientation ? (dev ? out->orientation + (size_t)off * 4 : c->orient.p) : nullptr;
   smc::TangentIO tio = c->tio;
   if (tg) tio.ntan = tg;
+  tio.orient = ori;
   int grid1 = std::max(1, std::min(n, c->sms * c->occ1));
   int grid2 = std::max(1, std::min(n, c->sms * c->occ2));
   if (!rho) CK(c->scratch.ensure((size_t)(plain ? 1 : grid2) * g));
@@ -526,6 +529,7 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
     for (int e = 0; e < n; e++) {
       smc::TangentIO te{};
       te.ntan = tg ? tg + (size_t)e * 4 * AB : nullptr;
+      te.orient = ori ? ori + (size_t)e * 4 : nullptr;
       CK(timed(c, 0, [&] {
         return smc::launch_sample_pair_mixed(
             P, first_event + e, 1, inj_p ? inj_p + (size_t)e * 2 * c->info.A : nullptr,
@@ -587,6 +591,9 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
     if (out->collisions)
       CK(cudaMemcpyAsync(out->collisions + (size_t)off * 2 * P.max_coll, coll, sizeof(double) * n * 2 * P.max_coll,
                          cudaMemcpyDeviceToHost, c->st));
+    if (out->orientation)
+      CK(cudaMemcpyAsync(out->orientation + (size_t)off * 4, ori, sizeof(double) * n * 4, cudaMemcpyDeviceToHost,
+                         c->st));
     if (out->npart || out->ncoll || out->b || out->attempts) {
       c->h_recs.resize(n);
       CK(cudaMemcpyAsync(c->h_recs.data(), c->recs.p, sizeof(EventRec) * n, cudaMemcpyDeviceToHost, c->st));
@@ -1328,6 +1335,7 @@ smc_status enqueue_batch(Ctx *c, int n, const smc_outputs *out, int *launches) {
     uint8_t *wnd = out->wounded ? out->wounded + (size_t)off * AB : nullptr;
     smc::TangentIO tio{};
     tio.ntan = out->tangents ? out->tangents + (size_t)off * 4 * AB : nullptr;
+    tio.orient = out->orientation ? out->orientation + (size_t)off * 4 : nullptr;
     const int grid1 = std::max(1, std::min(m, c->sms * c->occ1));
     CK(smc::launch_sample_pair_mixed(P, off, m, nullptr, nullptr, nullptr, c->recs.p, c->srcs.p, pos, wnd, nullptr,
                                      nullptr, nullptr, grid1, c->st, &tio, c->ev_base.p, c->tickets.p + 2));

@@ -75,6 +75,9 @@ struct TangentIO {
   const double *inj_proj, *inj_targ;
   double *ntan;
   float4 *stan;
+  // per event [n][4]: the orientations (cos theta, phi) of the projectile
+  // and the target drawn by the accepted attempt (NULL: not written)
+  double *orient;
 };
 
 // The parameters that differ between the systems of a mixed batch (the

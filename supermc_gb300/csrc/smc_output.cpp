@@ -19,22 +19,21 @@ namespace {
 constexpr int kEccLen = 49;
 
 // writes a line of the per-order file (order in 1..9) or, for order 10, the
-// line with all orders; fields as in dumpEccentricities (non-deformed nuclei)
-void ecc_line(FILE *f, const double *e, int order) {
+// line with all orders; fields as in dumpEccentricities, plus the four
+// orientation fields of the deformed layout when ori is given
+void ecc_line(FILE *f, const double *e, int order, const double *ori) {
   if (order < 10) {
     const double *o = e + 5 * (order - 1);
     std::fprintf(f, "%16.8g%16.8g%16.8g%16.8g%16.8g", o[0], o[1], o[2], o[3], o[4]);
   } else {
     for (int k = 0; k < 45; k++) std::fprintf(f, "%16.8g", e[k]);
   }
-  std::fprintf(f, "%10.5g%10.5g%16.8g%16.8g\n", e[45], e[46], e[47], e[48]);
+  std::fprintf(f, "%10.5g%10.5g%16.8g%16.8g", e[45], e[46], e[47], e[48]);
+  if (ori) std::fprintf(f, "%16.8g%16.8g%16.8g%16.8g", ori[0], ori[1], ori[2], ori[3]);
+  std::fprintf(f, "\n");
 }
 
-}  // namespace
-
-extern "C" {
-
-smc_status smc_write_ecc(const double *ecc, int n, int from_order, int to_order, const char *pattern) {
+smc_status write_ecc(const double *ecc, const double *ori, int n, int from_order, int to_order, const char *pattern) {
   if (!pattern || n < 0 || (n > 0 && !ecc) || from_order < 1 || to_order > 9 || from_order > to_order)
     return SMC_ERR_ARGUMENT;
   char path[4096];
@@ -43,10 +42,24 @@ smc_status smc_write_ecc(const double *ecc, int n, int from_order, int to_order,
     if (std::snprintf(path, sizeof(path), pattern, which) >= (int)sizeof(path)) return SMC_ERR_ARGUMENT;
     FILE *f = std::fopen(path, "a");
     if (!f) return SMC_ERR_ARGUMENT;
-    for (int e = 0; e < n; e++) ecc_line(f, ecc + (size_t)e * kEccLen, which);
+    for (int e = 0; e < n; e++) ecc_line(f, ecc + (size_t)e * kEccLen, which, ori ? ori + 4 * (size_t)e : nullptr);
     std::fclose(f);
   }
   return SMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+smc_status smc_write_ecc(const double *ecc, int n, int from_order, int to_order, const char *pattern) {
+  return write_ecc(ecc, nullptr, n, from_order, to_order, pattern);
+}
+
+smc_status smc_write_ecc_deformed(const double *ecc, const double *orientation, int n, int from_order, int to_order,
+                                  const char *pattern) {
+  if (n > 0 && !orientation) return SMC_ERR_ARGUMENT;
+  return write_ecc(ecc, orientation, n, from_order, to_order, pattern);
 }
 
 smc_status smc_write_density_block(const double *grid, int nx, int ny, const char *filename) {

@@ -52,7 +52,7 @@ def smc_params_from(vals: dict[str, float], seed: int = 1) -> _lib.SmcParams:
 
 
 OUTPUT_NAMES = ("ecc", "rho", "ta", "tb", "npart", "ncoll", "b", "attempts", "positions", "wounded", "tangents",
-                "collisions")
+                "collisions", "orientation")
 # keys that describe one collision system of a mixed batch
 SYSTEM_KEYS = ("aproj", "atarg", "proj_deformed", "targ_deformed", "ecm", "sigininn_override", "proj_r", "proj_a",
                "targ_r", "targ_a", "proj_d_min", "targ_d_min")
@@ -93,7 +93,8 @@ class Engine:
                   "b": ((n,), np.float64), "attempts": ((n,), np.int32),
                   "positions": ((n, AB, 2), np.float64), "wounded": ((n, AB), np.uint8),
                   "tangents": ((n, AB, 4), np.float64),
-                  "collisions": ((n, self.info.max_collisions, 2), np.float64)}
+                  "collisions": ((n, self.info.max_collisions, 2), np.float64),
+                  "orientation": ((n, 4), np.float64)}
         return {k: np.zeros(*shapes[k]) for k in want}
 
     @staticmethod

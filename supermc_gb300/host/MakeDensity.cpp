@@ -121,14 +121,22 @@ void MakeDensity::generateEccTable(int nevent) {
   ensure_data_dir();
   const int from = (int)val(*reader_, "ecc_from_order"), to = (int)val(*reader_, "ecc_to_order");
   const bool sd = val(*reader_, "use_sd") != 0;
-  std::vector<double> ecc;
+  // dumpEccentricities' deformed layout (src/MakeDensity.cpp:2249-2251)
+  const bool deformed = val(*reader_, "proj_deformed") == 1 || val(*reader_, "targ_deformed") == 1;
+  std::vector<double> ecc, ori;
   for (int done = 0; done < nevent; done += batch_) {
     const int n = std::min(batch_, nevent - done);
     ecc.resize((size_t)n * 49);
+    ori.resize((size_t)n * 4);
     smc_outputs out{};
     out.ecc = ecc.data();
+    if (deformed) out.orientation = ori.data();
     check(smc_generate(ctx_, (uint64_t)done, n, &out), "smc_generate");
-    if (sd) check(smc_write_ecc(ecc.data(), n, from, to, "data/sn_ecc_eccp_%d.dat"), "smc_write_ecc");
+    if (sd && deformed)
+      check(smc_write_ecc_deformed(ecc.data(), ori.data(), n, from, to, "data/sn_ecc_eccp_%d.dat"),
+            "smc_write_ecc_deformed");
+    else if (sd)
+      check(smc_write_ecc(ecc.data(), n, from, to, "data/sn_ecc_eccp_%d.dat"), "smc_write_ecc");
   }
 }
 

@@ -9,11 +9,22 @@ import numpy as np
 from . import _lib
 
 
-def write_ecc(ecc, from_order: int, to_order: int, pattern: str = "data/sn_ecc_eccp_%d.dat") -> None:
-    """Appends the MakeDensity::dumpEccentricities lines of ecc[n][49]."""
+def write_ecc(ecc, from_order: int, to_order: int, pattern: str = "data/sn_ecc_eccp_%d.dat",
+              orientation=None) -> None:
+    """Appends the MakeDensity::dumpEccentricities lines of ecc[n][49]; with
+    orientation[n][4] (cos theta, phi of each nucleus) the deformed-nucleus
+    layout."""
     e = np.ascontiguousarray(np.atleast_2d(ecc), dtype=np.float64)
     lib = _lib.load()
-    _lib.check(lib.smc_write_ecc(_lib.ptr(e), e.shape[0], from_order, to_order, pattern.encode()), "smc_write_ecc")
+    if orientation is None:
+        _lib.check(lib.smc_write_ecc(_lib.ptr(e), e.shape[0], from_order, to_order, pattern.encode()),
+                   "smc_write_ecc")
+        return
+    o = np.ascontiguousarray(np.atleast_2d(orientation), dtype=np.float64)
+    if o.shape != (e.shape[0], 4):
+        raise ValueError("orientation must be [n][4]")
+    _lib.check(lib.smc_write_ecc_deformed(_lib.ptr(e), _lib.ptr(o), e.shape[0], from_order, to_order,
+                                          pattern.encode()), "smc_write_ecc_deformed")
 
 
 def write_density_block(grid, filename: str) -> None:

@@ -156,6 +156,27 @@ def make_native_tables(out, nev):
     np.savez_compressed(os.path.join(out, "ecc_native.npz"), **data)
 
 
+# further systems at the reference's own geometry (tests/systems.py NATIVE_SYSTEMS)
+NATIVE_SYSTEM_ARGS = {
+    "ppb5020": ["Aproj=1", "Atarg=208", "ecm=5020"],
+    "dau200": ["Aproj=2", "Atarg=197", "ecm=200"],
+    "cucu200": ["Aproj=63", "Atarg=63", "ecm=200"],
+    "uu200": ["Aproj=238", "Atarg=238", "ecm=200", "proj_deformed=1", "targ_deformed=1"],
+}
+
+
+def make_native_systems(out, nev):
+    """The reference's op-9 table (its own drand48 sampler) for p+Pb, d+Au,
+    Cu+Cu and deformed U+U: the 49 columns of each sn_ecc_eccp_10.dat line
+    (a deformed run appends four more, dropped here)."""
+    data = {}
+    for name, extra in NATIVE_SYSTEM_ARGS.items():
+        ref, _ = ref_for(["auau200"], extra + ["ecc_from_order=2", "ecc_to_order=5"])
+        ref.srand(7)
+        data[name] = ref.generate_ecc_table(nev)[:, :49]
+    np.savez_compressed(os.path.join(out, "ecc_native_systems.npz"), **data)
+
+
 def make_kln(out):
     ref, vals = ref_for(["pbpb2760"], ["which_mc_model=1", "sub_model=7", "lambda=0.288"])
     ref.lib.refh_kln_setup(2760.0, 0.288)
@@ -199,15 +220,19 @@ def make_constants(out):
 
 def make_text(out):
     """Raw text files of the stock reference binary: the eccentricity files of
-    operation 9 (4 Au+Au events, orders 2..5) and the block / 4-column density
-    files of operation 1 (2 events on a 13x13 grid)."""
+    operation 9 (4 Au+Au events, orders 2..5; 3 deformed U+U events, orders
+    2..3, keys "deformed/<name>") and the block / 4-column density files of
+    operation 1 (2 events on a 13x13 grid)."""
     import subprocess
     import tempfile
     ref, vals = ref_for(["auau200"])
     exe = os.path.join(REPO, "oracle", "_ref", "superMC.e")
     texts = {}
-    for op, args in ((9, ["nev=4", "ecc_from_order=2", "ecc_to_order=5"]),
-                     (1, ["nev=2", "maxx=3", "maxy=3", "dx=0.5", "dy=0.5", "use_block=1", "use_4col=1"])):
+    runs = ((9, "", ["nev=4", "ecc_from_order=2", "ecc_to_order=5"]),
+            (1, "", ["nev=2", "maxx=3", "maxy=3", "dx=0.5", "dy=0.5", "use_block=1", "use_4col=1"]),
+            (9, "deformed/", ["nev=3", "ecc_from_order=2", "ecc_to_order=3", "Aproj=238", "Atarg=238",
+                              "proj_deformed=1", "targ_deformed=1"]))
+    for op, key, args in runs:
         wd = tempfile.mkdtemp(prefix="smc_text_", dir=ref.workdir)
         os.makedirs(os.path.join(wd, "data"))
         os.symlink(os.path.join(ref.workdir, "tables"), os.path.join(wd, "tables"))
@@ -215,11 +240,12 @@ def make_text(out):
         with open(os.path.join(wd, "parameters.dat"), "w") as f:
             f.write(parameters_text(vals))
         subprocess.run([exe, f"operation={op}", "randomSeed=7"] + args, cwd=wd, check=True, capture_output=True)
-        names = ([f"sn_ecc_eccp_{k}.dat" for k in (2, 3, 4, 5, 10)] if op == 9 else
+        orders = (2, 3, 10) if key else (2, 3, 4, 5, 10)
+        names = ([f"sn_ecc_eccp_{k}.dat" for k in orders] if op == 9 else
                  [f"sd_event_{e}_{kind}.dat" for e in (1, 2) for kind in ("block", "4col")])
         for name in names:
             with open(os.path.join(wd, "data", name)) as f:
-                texts[name] = f.read()
+                texts[key + name] = f.read()
     texts["grid"] = {"xmin": -3.0, "ymin": -3.0, "dx": 0.5, "dy": 0.5, "nx": 13, "ny": 13}
     with open(os.path.join(out, "text_outputs.json"), "w") as f:
         json.dump(texts, f, indent=0)
@@ -229,7 +255,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=REF_ROOT)
     ap.add_argument("--nev", type=int, default=1500)
-    ap.add_argument("--only", choices=["constants", "sampler", "inject", "average", "kln", "native", "text"],
+    ap.add_argument("--only", choices=["constants", "sampler", "inject", "average", "kln", "native",
+                                       "native_systems", "text"],
                     help="regenerate one fixture only")
     a = ap.parse_args()
     if build_reference(a.ref) is None:
@@ -239,6 +266,7 @@ def main():
     steps = {"constants": lambda: make_constants(HERE), "sampler": lambda: make_sampler(HERE),
              "inject": lambda: make_inject(HERE), "average": lambda: make_average(HERE),
              "kln": lambda: make_kln(HERE), "native": lambda: make_native_tables(HERE, a.nev),
+             "native_systems": lambda: make_native_systems(HERE, a.nev),
              "text": lambda: make_text(HERE)}
     for k, f in steps.items():
         if a.only in (None, k):

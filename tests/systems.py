@@ -12,6 +12,41 @@ AUAU200 = dict(BASE, Aproj=197, Atarg=197, ecm=200)
 PBPB2760 = dict(BASE, Aproj=208, Atarg=208, ecm=2760)
 SYSTEMS = {"auau200": AUAU200, "pbpb2760": PBPB2760}
 
+# Further collision systems, at the reference's own nuclear geometry (its
+# hard-coded R, a, deformation and 0.9 fm hard core, src/Nucleus.cpp:65-111)
+# so that their distributions can be compared with the reference's sampler:
+# p+Pb, d+Au (Hulthen deuteron), Cu+Cu, deformed U+U.
+NATIVE_SYSTEMS = {
+    "ppb5020": dict(BASE, Aproj=1, Atarg=208, ecm=5020),
+    "dau200": dict(BASE, Aproj=2, Atarg=197, ecm=200),
+    "cucu200": dict(BASE, Aproj=63, Atarg=63, ecm=200),
+    "uu200": dict(BASE, Aproj=238, Atarg=238, ecm=200, proj_deformed=1, targ_deformed=1),
+}
+
+
+def _ws(R, a):
+    return dict(proj_r=R, proj_a=a, targ_r=R, targ_a=a)
+
+
+# The same systems with Woods-Saxon parameters given by the optional keys
+# (the reference has no keys for them): Cu+Cu R=4.2 a=0.596, deformed U+U
+# R=6.81 a=0.55, and Au+Au R=6.38 a=0.535 with a 0.4 fm hard core at
+# sigma_NN = 42 mb.
+OVERRIDE_SYSTEMS = {
+    "cucu200_R42": dict(NATIVE_SYSTEMS["cucu200"], **_ws(4.2, 0.596)),
+    "uu200_R681": dict(NATIVE_SYSTEMS["uu200"], **_ws(6.81, 0.55)),
+    "auau_R638_dmin04_sig42": dict(AUAU200, sigininn_override=42.0, proj_d_min=0.4, targ_d_min=0.4,
+                                   **_ws(6.38, 0.535)),
+}
+ALL_SYSTEMS = dict(SYSTEMS, **NATIVE_SYSTEMS, **OVERRIDE_SYSTEMS)
+
+
+def oracle_nuclei(oracle, vals):
+    """The oracle's projectile and target nuclei of a parameter set (mass
+    number, deformation and the optional Woods-Saxon / hard-core keys)."""
+    return tuple(oracle.nucleus(int(vals[f"a{w}"]), int(vals[f"{w}_deformed"]), vals[f"{w}_r"], vals[f"{w}_a"],
+                                vals[f"{w}_d_min"]) for w in ("proj", "targ"))
+
 
 def values(system: dict, **over) -> dict:
     d = dict(system)

@@ -83,3 +83,32 @@ def test_generated_events_round_trip_through_the_writers(tmp_path):
     sd = out["rho"][0].astype(np.float64) * eng.values["finalfactor"]
     write_density_block(sd, str(tmp_path / "sd_event_1_block.dat"))
     np.testing.assert_allclose(np.loadtxt(tmp_path / "sd_event_1_block.dat"), sd, rtol=1e-11, atol=0)
+
+
+def test_deformed_eccentricity_layout(lib, texts, tmp_path):
+    """dumpEccentricities with a deformed nucleus appends four fields to every
+    line (src/MakeDensity.cpp:2435-2455, 2483-2492).  The reference prints
+    MCnucl::lastCx1, lastPh1, lastCx2, lastPh2 there, members its code never
+    assigns, so the stock binary's files hold stray memory in those 64
+    characters; every other byte must be the reference's, and the four fields
+    hold the given orientations (%16.8g)."""
+    ref10 = texts["deformed/sn_ecc_eccp_10.dat"]
+    vals = np.loadtxt(io.StringIO(ref10), ndmin=2)
+    assert vals.shape[1] == 53
+    ecc = np.ascontiguousarray(vals[:, :49])
+    n = len(ecc)
+    ori = np.ascontiguousarray(np.column_stack([np.linspace(-0.9, 0.8, n), np.linspace(0.1, 6.2, n),
+                                                np.linspace(0.3, -0.4, n), np.linspace(3.0, 1.0, n)]))
+    pattern = str(tmp_path / "sn_ecc_eccp_%d.dat").encode()
+    _lib.check(lib.smc_write_ecc_deformed(_lib.ptr(ecc), _lib.ptr(ori), n, 2, 3, pattern), "smc_write_ecc_deformed")
+    for order in (2, 3, 10):
+        name = f"sn_ecc_eccp_{order}.dat"
+        got = (tmp_path / name).read_text().splitlines()
+        want = texts["deformed/" + name].splitlines()
+        assert len(got) == len(want) == n
+        for k in range(n):
+            assert len(got[k]) == len(want[k]), (name, k)
+            assert got[k][:-64] == want[k][:-64], (name, k)
+            assert got[k][-64:] == "".join("%16.8g" % v for v in ori[k]), (name, k)
+    with pytest.raises(Exception):
+        _lib.check(lib.smc_write_ecc_deformed(_lib.ptr(ecc), None, n, 2, 3, pattern), "smc_write_ecc_deformed")
