@@ -7,6 +7,8 @@
 //   six-point lookup    src/arsenal.cpp:33-54 (used at src/MCnucl.cpp:654-687)
 //   eps_n, <r^n>        src/MakeDensity.cpp:2244-2511, hot-spot mask src/MCnucl.cpp:1303-1323
 #pragma once
+#include <climits>
+
 #include "smc_device.cuh"
 
 namespace smc {
@@ -188,19 +190,31 @@ __device__ __forceinline__ int post_cell(const DevParams &P, int np, float a0, f
 __device__ __forceinline__ double thickness_fp64(const DevParams &P, const Source *S, int base, int n, int pl, int i,
                                                  int j) {
   const int lane = threadIdx.x & 31;
+  // the chunks holding a record whose row window reaches row i: all window
+  // rows loaded at once (independent loads), one bit per chunk
+  constexpr int kMaxChunks = (kMaxA + 31) / 32;
+  uint32_t chunks = 0;
+#pragma unroll
+  for (int c = 0; c < kMaxChunks; c++) {
+    const int k = 32 * c + lane;
+    const bool in = k < n && i >= S[base + k].xl && i < S[base + k].xr;
+    if (__ballot_sync(0xffffffffu, in)) chunks |= 1u << c;
+  }
   const double xg = __dadd_rn(P.xmin, __dmul_rn((double)i, P.dx));
   const double yg = __dadd_rn(P.ymin, __dmul_rn((double)j, P.dy));
   const double cut = __dmul_rn(5., P.width), cut2 = cut * cut;
   const double inv2w2 = 1.0 / (2.0 * P.w2);
   double sum = 0.0;
   int ndisk = 0;
-  for (int k0 = 0; k0 < n; k0 += 32) {
+  while (chunks) {
+    const int c = __ffs(chunks) - 1;
+    chunks &= chunks - 1u;
+    const int k = 32 * c + lane;
     double t = 0.0;
-    bool in = false, disk_hit = false;
-    if (k0 + lane < n) {
-      const Source &s = S[base + k0 + lane];
+    bool disk_hit = false;
+    if (k < n) {
+      const Source &s = S[base + k];
       if ((s.kind & 15) == SRC_THICK && s.plane == pl && i >= s.xl && i < s.xr && j >= s.yl && j < s.yr) {
-        in = true;
         const double dc = sq_dist_rn(s.x, s.y, xg, yg);
         if (s.kind & 16) {
           disk_hit = !(dc > P.dsq);
@@ -213,7 +227,6 @@ __device__ __forceinline__ double thickness_fp64(const DevParams &P, const Sourc
         }
       }
     }
-    if (!__ballot_sync(0xffffffffu, in)) continue;
 #pragma unroll
     for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
     sum += __shfl_sync(0xffffffffu, t, 0);
@@ -242,6 +255,82 @@ __device__ __forceinline__ int kln_cell_fp64(const DevParams &P, double ta, doub
   const int ii = (int)floor(di), jj = (int)floor(dj);
   v = kln_interp(P, ii, jj, (float)(di - ii), (float)(dj - jj));
   return CELL_OK;
+}
+
+// a thread's centre-of-mass sums and the density sum before fluctuations
+struct CmSums {
+  KSum c0, c1, c2, pre;
+};
+
+// An MC-KLN cell that post_cell left undecided, held in a CTA's list until
+// the end of its event: the cell, the planes to redo, the FP32 thickness
+// values post_cell took, then the density before (v) and after (vout) the
+// per-cell fluctuations
+struct PendCell {
+  int i, j, need;
+  float t1, t2, v, vout;
+};
+
+// Appends an undecided cell to the event's list; false when the list is full
+// (the caller then decides the cell on its own path).
+__device__ __forceinline__ bool kln_defer(PendCell *list, int *count, int cap, int i, int j, int code, float t1,
+                                          float t2) {
+  const int slot = atomicAdd(count, 1);
+  if (slot >= cap) return false;
+  list[slot] = PendCell{i, j, (code >> 4) & 3, t1, t2, 0.f, 0.f};
+  return true;
+}
+
+// The event's listed cells, decided from FP64 thickness sums of their
+// flagged planes: the warps take the cells in turn (each a warp-wide FP64
+// sum), lane 0 writes the cell's outputs and its values into the list.
+template <int NWARPS>
+static __device__ __noinline__ void kln_finish_listed(const DevParams &P, const EventRec &rec, const Source *S,
+                                                  PendCell *list, int n, float *rho, float *ta, float *tb,
+                                                  int *s_status) {
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, ny = P.ny;
+  const int base0 = rec.nsplat - rec.npart1 - rec.npart2, base1 = base0 + rec.npart1;
+  for (int q = wid; q < n; q += NWARPS) {
+    const PendCell c = list[q];
+    const double da = (c.need & 1) ? thickness_fp64(P, S, base0, rec.npart1, 0, c.i, c.j) : (double)c.t1;
+    const double db = (c.need & 2) ? thickness_fp64(P, S, base1, rec.npart2, 1, c.i, c.j) : (double)c.t2;
+    if (lane == 0) {
+      float v, t1, t2;
+      if (kln_cell_fp64(P, da, db, v, t1, t2) == CELL_TABLE) *s_status = 4;
+      const size_t g = (size_t)c.i * ny + c.j;
+      const float vout = P.nbd ? nbd_cell(P, rec.ev, (uint32_t)g, v, t1, t2) : v;
+      rho[g] = vout;
+      if (ta) ta[g] = t1;
+      if (tb) tb[g] = t2;
+      list[q].v = v;
+      list[q].vout = vout;
+    }
+  }
+}
+
+// Adds the listed cells to one thread's centre-of-mass sums in cell order
+// (so that the sums do not depend on the order the cells were listed in);
+// the sums go in and come back by value.
+static __device__ __noinline__ CmSums kln_add_listed(const PendCell *list, int n, int ny, const float *xg,
+                                                     const float *yg, CmSums cs) {
+  long long last = -1;
+  for (int k = 0; k < n; k++) {
+    long long best = LLONG_MAX;
+    int at = -1;
+    for (int q = 0; q < n; q++) {
+      const long long key = (long long)list[q].i * ny + list[q].j;
+      if (key > last && key < best) { best = key; at = q; }
+    }
+    last = best;
+    const PendCell &c = list[at];
+    cs.pre.add(c.v);
+    if (c.vout != 0.f) {
+      cs.c0.add(c.vout);
+      cs.c1.add(xg[c.i] * c.vout);
+      cs.c2.add(yg[c.j] * c.vout);
+    }
+  }
+  return cs;
 }
 
 // Warp-wide completion of post_cell: every lane passes its cell (i, j),

@@ -85,11 +85,6 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
 // column steps of 32 cells whose MC-KLN fix-up marks one 64-bit word holds
 constexpr int kPendSteps = 32;
 
-// a thread's centre-of-mass sums and the density sum before fluctuations
-struct CmSums {
-  KSum c0, c1, c2, pre;
-};
-
 // The MC-KLN cells of row i, columns s0 + 32 k + lane, that post_cell left
 // undecided (pend: two bits per step k, the planes to redo), finished by the
 // whole warp in step and lane order: the flagged thickness sums redone in

@@ -79,6 +79,7 @@ constexpr uint32_t kLboA = kTM * 16, kLboB = kTN * 16, kSbo = 128;
 constexpr uint32_t kTmemCols = 4 * kTN;
 constexpr uint32_t kMaxPolls = 1u << 24; // MMA completion wait limit
 constexpr int kErrMmaTimeout = 8;        // per-event status when that limit is hit
+constexpr int kPendCapTc = 128;          // undecided MC-KLN cells an event's list holds
 
 // A splat source held in shared memory.
 struct CSrc {
@@ -154,6 +155,10 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
   __shared__ uint32_t s_tmem;
   __shared__ int s_wcnt[kTW];
   __shared__ int s_status, s_dead, s_ncache;
+  // the event's undecided MC-KLN cells, decided together at its end by all
+  // warps (a cell that finds the list full is decided at once by its warp)
+  __shared__ PendCell s_pend[kPendCapTc];
+  __shared__ int s_npend;
   __shared__ double s_cm[3];
 
   const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
@@ -201,7 +206,10 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
     int *corr = corr_scratch + (size_t)blockIdx.x * np * nx * ny;   // [plane][i][j], this CTA's
     const bool full = out_rho || ta || tb;
     const float kband = kln_event_band(P, rec);
-    if (tid == 0) s_status = rec.status;
+    if (tid == 0) {
+      s_status = rec.status;
+      s_npend = 0;
+    }
     KSum cm0, cm1, cm2, pre;   // pre: the density before NBD fluctuations (the zero-dN/dy test)
     const bool any = rec.imax > rec.imin && rec.jmax > rec.jmin;
     const int ti0 = rec.imin, tj0 = rec.jmin;
@@ -441,9 +449,14 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
               const float a1 = np > 1 && (used & 2u) ? fmaxf(sr[kTM * kSP + k], 0.f) : 0.f;
               code = post_cell(P, np, a0, a1, 0.f, kband, v, t1, t2);
             }
+            bool listed = false;
+            if ((code & CELL_UNDECIDED) && kln_defer(s_pend, &s_npend, kPendCapTc, i_own, j, code, t1, t2)) {
+              listed = true;
+              code = CELL_OK;
+            }
             if (P.which_mc_model == 1) kln_resolve_warp(P, rec, S, i_own, j, code, v, t1, t2);
             if (code == CELL_TABLE) s_status = 4;
-            if (i_own >= nx) continue;
+            if (i_own >= nx || listed) continue;
             const size_t g = (size_t)i_own * ny + j;
             if (!inwin) {   // beyond every window: zero
               if (full) {
@@ -468,6 +481,18 @@ __global__ void __launch_bounds__(kTT, 1) k_grid_tc(DevParams P, int n_events, c
           }
         }
         __syncthreads();   // the cache window and the list are reused by the next tile
+      }
+    }
+    // ---- the listed MC-KLN cells (s_npend is final after the tiles' last barrier)
+    if (P.which_mc_model == 1) {
+      const int npend = min(s_npend, kPendCapTc);
+      if (npend > 0) {
+        kln_finish_listed<kTW>(P, rec, S, s_pend, npend, rho, ta, tb, &s_status);
+        __syncthreads();
+        if (tid == 0) {
+          const CmSums cs = kln_add_listed(s_pend, npend, ny, xg, yg, CmSums{cm0, cm1, cm2, pre});
+          cm0 = cs.c0; cm1 = cs.c1; cm2 = cs.c2; pre = cs.pre;
+        }
       }
     }
     // ---- centre of mass
