@@ -192,7 +192,10 @@ def run_reference(args, vals) -> dict:
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "events/s", "cores": procs, "kind": "port",
                              "sample": f"{per_proc} events per process x {procs} processes per step; "
-                                       f"dN/dy table built once by the FP64 quadrature ({t_tab:.0f} s, untimed)"},
+                                       f"dN/dy table built once by the FP64 quadrature ({t_tab:.0f} s, untimed)",
+                             "note": "the oracle's C restatement of the reference's op-9 loop (the reference's "
+                                     "own binary is not built on this aarch64 host); on x86 the port takes "
+                                     "about 1.4x the reference binary's time per event"},
             "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -204,6 +207,8 @@ def cpu_baseline(vals, table, target_s: float = 12.0) -> dict:
     n2 = min(n2, 4000)
     nev, dt = _oracle_worker((vals, table, n2, 7))
     return {"value": nev / dt, "unit": "events/s", "cores": 1, "kind": "port",
+            "note": "the oracle's C restatement of the reference's op-9 loop; on x86 it takes about 1.4x the "
+                    "reference binary's time per event",
             "sample": f"{nev} events of the workload on one core ({dt:.1f} s), oracle op-9 loop with the "
                       "same dN/dy table"}
 
@@ -250,7 +255,9 @@ MIXED_SYSTEMS = [   # (share, parameters): p+Pb, d+Au, Cu+Cu, deformed U+U, Au+A
 
 
 def mixed_batch(dev, stream, n: int) -> dict:
-    """events/s of one mixed-system batch of n events, events in HBM."""
+    """events/s of one mixed-system batch of n events (shares 1:2:2:2:3), as
+    one CUDA graph (smc_generate_mixed_graph: captured by a first call, then
+    replayed), events in HBM; the eager batch beside it."""
     import numpy as np
     import torch
     from supermc_gb300.engine import Engine
@@ -264,19 +271,25 @@ def mixed_batch(dev, stream, n: int) -> dict:
     systems = [p for _, p in MIXED_SYSTEMS]
     bufs = {"ecc": torch.empty((n, 49), dtype=torch.float64, device=dev),
             "npart": torch.empty((n, 2), dtype=torch.int32, device=dev)}
-    eng.generate_mixed(systems, sel, first_event=0, device_bufs=bufs)
+    def timed(first, graph):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.generate_mixed(systems, sel, first_event=first, device_bufs=bufs, graph=graph)
+        b.record(stream)
+        torch.cuda.synchronize()
+        return n / (a.elapsed_time(b) / 1e3)
+    eng.generate_mixed(systems, sel, first_event=0, device_bufs=bufs, graph=True)   # eager + capture
     torch.cuda.synchronize()
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    eng.generate_mixed(systems, sel, first_event=n, device_bufs=bufs)
-    b.record(stream)
-    torch.cuda.synchronize()
-    rate = n / (a.elapsed_time(b) / 1e3)
+    rates = [timed(n * (k + 1), True) for k in range(3)]
+    eager = timed(n * 5, False)
     eng.close()
-    return {"value": rate, "unit": "events/s", "events": n,
+    return {"value": statistics.median(rates), "unit": "events/s", "events": n,
+            "counts": counts.tolist(),
             "systems": "p+Pb 5.02 TeV, d+Au, Cu+Cu, deformed U+U, Au+Au (200 GeV) in shares 1:2:2:2:3, "
-                       "MC-Glauber 261x261, one smc_generate_mixed call",
+                       "MC-Glauber 261x261",
+            "launch": "one CUDA graph per batch (smc_generate_mixed_graph), median of 3 replays",
+            "eager_value": eager,
             "splat": "tensor cores" if tuning["tensor_cores"] else "CUDA cores", "chunk": tuning["chunk"]}
 
 
@@ -305,18 +318,29 @@ def differentiable_batch(stream, n: int = 4096) -> dict:
     eng.generate(0, n, want=("ecc",))
     eng.adjoint(0, n, g_eps=g)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    eng.generate(0, n, want=("ecc",))
-    t1 = time.perf_counter()
+
+    def timed(fn):   # CUDA events on the engine's stream around one call, median of 3
+        out = []
+        for _ in range(3):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r = fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            out.append(a.elapsed_time(b) / 1e3)
+        return statistics.median(out), r
+    t_fwd, _ = timed(lambda: eng.generate(0, n, want=("ecc",)))
     eng.reset_stats()
     eng.set_timing(True)
-    grad, _ = eng.adjoint(0, n, g_eps=g)
-    t2 = time.perf_counter()
+    t_fb, (grad, _) = timed(lambda: eng.adjoint(0, n, g_eps=g))
     st = eng.stats()
     eng.close()
-    return {"forward": n / (t1 - t0), "forward_backward": n / (t2 - t1), "unit": "events/s", "events": n,
-            "adjoint_kernel_ms": st["post_ms"], "grad_mean_eps2": {"w": grad[0], "alpha": grad[1], "R": grad[2],
-                                                                   "a": grad[3]},
+    return {"forward": n / t_fwd, "forward_backward": n / t_fb, "unit": "events/s", "events": n,
+            "timing": "CUDA events on the engine's stream around one call (host copies of the results "
+                      "included), median of 3",
+            "adjoint_kernel_ms": st["post_ms"] / 3, "grad_mean_eps2": {"w": grad[0], "alpha": grad[1],
+                                                                      "R": grad[2], "a": grad[3]},
             "workload": "Pb+Pb 2.76 TeV, sigma_NN=64 mb, radii by inverse CDF, w=0.5 fm, alpha=0.118, 261x261",
             "splat": "tensor cores" if tuning["tensor_cores"] else "CUDA cores", "chunk": tuning["chunk"]}
 
@@ -367,6 +391,34 @@ def binned_average(stream, n: int) -> dict:
                                          "peak_kind": peak_kind}}
         eng.close()
     return out
+
+
+def grid_output_leg(eng, n: int) -> dict:
+    """Operation 1 (MakeDensity::generate_profile_ebe, src/MakeDensity.cpp:
+    574-694): every event's density grid and eccentricities copied to pinned
+    host memory inside the call (smc_generate with host outputs)."""
+    import ctypes
+    import torch
+    from supermc_gb300 import _lib
+    hb = {"ecc": torch.empty((n, 49), dtype=torch.float64, pin_memory=True),
+          "rho": torch.empty((n, eng.nx, eng.ny), dtype=torch.float32, pin_memory=True)}
+    hnp = {k: v.numpy() for k, v in hb.items()}
+
+    def step(first):
+        o = eng._outputs(hnp, False)
+        _lib.check(eng.lib.smc_generate(eng.h, first, n, ctypes.byref(o)), "smc_generate")
+    step(10 ** 9)
+    times = []
+    for k in range(3):
+        t0 = time.perf_counter()
+        step(10 ** 9 + (k + 1) * n)
+        times.append(time.perf_counter() - t0)
+    dt = statistics.median(times)
+    bytes_ev = 4 * eng.nx * eng.ny
+    return {"value": n / dt, "unit": "events/s", "events": n, "density_bytes_per_event": bytes_ev,
+            "density_GB_per_s": bytes_ev * n / dt / 1e9,
+            "note": "smc_generate with pinned host outputs (FP32 density + eps line per event), "
+                    "wall clock per call, median of 3"}
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -501,6 +553,7 @@ def run_gpu(args, vals) -> dict | None:
     # proportions 1:2:2:2:3, MC-Glauber), one smc_generate_mixed call
     mixed = mixed_batch(dev, stream, args.mixed_events)
     diff = differentiable_batch(stream) if args.side_workloads else None
+    grids = grid_output_leg(eng, args.grid_events) if args.side_workloads else None
     binned = binned_average(stream, args.binned_events) if args.side_workloads else None
 
     # ---- plain per-event path, same workload (sample)
@@ -518,7 +571,7 @@ def run_gpu(args, vals) -> dict | None:
 
     # ---- roofline of the dominant kernel (the thickness/density splat)
     hbm_peak, tf_peak, peak_kind = peaks()
-    ecc = bufs["ecc"].double().cpu().numpy()
+    from supermc_gb300.params import derive
     npart = bufs["npart"].cpu().numpy()
     nsrc = float(npart.sum(axis=1).mean())     # MC-KLN: T_A, T_B sources are the participants
     flops_per_event = 2.0 * eng.nx * eng.ny * nsrc
@@ -534,12 +587,31 @@ def run_gpu(args, vals) -> dict | None:
             "peak_kind": f"bf16 dense, {peak_kind}",
             "sample_kernel_ms_per_launch": st["sample_ms"] / max(1, st["sample_launches"]),
             "grid_kernel_ms_per_launch": grid_launch_ms}
+    # the work a splat must do: each thickness source adds to the cells within
+    # its cut (r <= 5w: pi (5w)^2 / (dx dy) cells), one multiply-add each
+    d = derive(vals)
+    disk_cells = math.pi * (5 * d.width) ** 2 / (vals["dx"] * vals["dy"])
+    useful = nsrc * disk_cells
+    roof["useful"] = {"fma_per_event": useful, "tflops": 2 * useful * events_per_launch / (grid_launch_ms / 1e3) / 1e12,
+                      "work": "N_src x cells within r <= 5w, one FMA each (the splat's own work; the dense count "
+                              "above also spans the cells outside the cut)"}
     try:
         with open(os.path.join(HERE, "profiles", "traffic.json")) as f:
             tr = json.load(f)
         key = "k_grid_tc_bytes_per_event" if tc_used else "k_grid_cc_bytes_per_event"
         if key in tr:
             roof["traffic"] = tr[key] * events_per_launch
+        ikey = "k_grid_tc_warp_inst_per_event" if tc_used else "k_grid_cc_warp_inst_per_event"
+        if ikey in tr:
+            # instruction issue: 4 schedulers per SM, one warp instruction each per clock
+            sms = torch.cuda.get_device_properties(dev).multi_processor_count
+            mhz = clk.get("sm_mhz") or 2070.0
+            peak_inst = sms * 4 * mhz * 1e6
+            inst = tr[ikey] * events_per_launch / (grid_launch_ms / 1e3)
+            roof["issue"] = {"bound": "issue", "achieved": inst / 1e9, "peak": peak_inst / 1e9,
+                             "unit": "G warp instructions/s", "frac": inst / peak_inst,
+                             "warp_inst_per_event": tr[ikey],
+                             "source": "instructions per event from one ncu capture (profiles/)"}
     except Exception:
         pass
 
@@ -551,7 +623,9 @@ def run_gpu(args, vals) -> dict | None:
     err = eps_error(eng, vals, otab)
     line = {"metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 (FP64 pairing/CM/moment totals)",
+            "vs_baseline": None,
+            "dtype": "f32 splat, dN/dy lookup and moments (double-float moment sums); f64 pairing, "
+                     "centre-of-mass shift, dN/dy table and the table cells FP32 leaves undecided",
             "data": "synthetic (Monte-Carlo events from Philox streams)",
             "config": {"workload": WORKLOAD_NAME, "events_per_step": n, "grid": [eng.nx, eng.ny],
                        "parallelism": f"event data parallel, {world} GPU(s)",
@@ -567,6 +641,7 @@ def run_gpu(args, vals) -> dict | None:
                           "batched_over_plain": value / plain},
             "mixed_batch": mixed,
             "differentiable": diff,
+            "grid_output_op1": grids,
             "binned_average_501": binned,
             "batched_by_splat_path": {"tensor_cores": paths[True], "cuda_cores": paths[False], "unit": "events/s",
                                       "events": n, "note": "eager smc_generate with each splat (smc_set_grid_path)"},
@@ -589,14 +664,16 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--events", type=int, default=EVENTS_PER_STEP)
     ap.add_argument("--plain-events", type=int, default=200)
-    ap.add_argument("--mixed-events", type=int, default=20000)
-    ap.add_argument("--binned-events", type=int, default=32768)
+    ap.add_argument("--mixed-events", type=int, default=100000)
+    ap.add_argument("--binned-events", type=int, default=1000000, help="per system (Pb+Pb and O+O)")
+    ap.add_argument("--grid-events", type=int, default=4096, help="operation-1 leg: events per call")
     ap.add_argument("--side-workloads", type=int, default=1, help="differentiable and 501^2 binned workloads")
     ap.add_argument("--graph", type=int, default=1, help="time the batch as a CUDA graph (smc_generate_graph)")
     ap.add_argument("--autotune", type=int, default=1, help="tune the launch configuration before timing")
     ap.add_argument("--grid-path", default="auto", choices=["auto", "tc", "cc"],
                     help="with --autotune 0: the splat (tensor-core or CUDA-core)")
-    ap.add_argument("--ref-events", type=int, default=1600, help="reference arm: events per step (all cores)")
+    ap.add_argument("--ref-events", type=int, default=EVENTS_PER_STEP,
+                    help="reference arm: events per step (all cores)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--seed", type=int, default=1)
     args = ap.parse_args()

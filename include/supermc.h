@@ -212,6 +212,17 @@ smc_status smc_generate_mixed(void *ctx, const smc_params *systems, int nsys, ui
  * (out->device != 0); the results equal smc_generate's. */
 smc_status smc_generate_graph(void *ctx, uint64_t first_event, int n, const smc_outputs *out);
 
+/* smc_generate_mixed as one CUDA graph: the whole mixed batch (every
+ * chunk's sampling with its systems and heavy-systems-first order, splat,
+ * eccentricities and the device-side status reduction) is captured on the
+ * first call for a given n, system table, per-event systems, output set and
+ * launch configuration -- that call runs eagerly -- and replayed by later
+ * calls with new event ids.  Device outputs only (out->device != 0); the
+ * results equal smc_generate_mixed's.  The reference runs one system per
+ * process (src/main.cpp:35-61); no counterpart. */
+smc_status smc_generate_mixed_graph(void *ctx, const smc_params *systems, int nsys, uint64_t first_event, int n,
+                                    const int *system_of_event, const smc_outputs *out);
+
 /* Plain per-event path: the same results as smc_generate, one event per
  * kernel launch sequence (the unbatched baseline). */
 smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_outputs *out);

@@ -2,6 +2,7 @@
 // derived constants (MCnucl::MCnucl, src/MCnucl.cpp:22-154), device buffers,
 // batching and the two-stage launch sequence.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -239,6 +240,20 @@ struct Ctx {
   int graph_n = 0, graph_chunk = 0, graph_launches = 0;
   bool graph_tc = false;
   smc_outputs graph_out{};
+  // the context's device buffers a captured batch uses (a buffer that a
+  // later eager call had to grow is reallocated: the graph is captured again)
+  std::array<const void *, 12> graph_bufs{}, mgraph_bufs{};
+  // captured mixed-system batch (smc_generate_mixed_graph): its system table,
+  // per-event systems and event order on the device, and what it was
+  // captured for
+  cudaGraphExec_t mgraph = nullptr;
+  int mgraph_n = 0, mgraph_chunk = 0, mgraph_launches = 0;
+  bool mgraph_tc = false;
+  smc_outputs mgraph_out{};
+  std::vector<smc_params> mgraph_sys;
+  std::vector<int> mgraph_ev;
+  DevBuf<smc::SystemDev> mg_sys;
+  DevBuf<int> mg_ev, mg_order;
   DevBuf<uint64_t> ev_base;
   DevBuf<int> worst;
   uint64_t *h_first = nullptr;
@@ -819,6 +834,8 @@ void smc_destroy(void *ctx) {
   c->icdf_tab[0].release(); c->icdf_tab[1].release(); c->ntan.release(); c->inj_tp.release(); c->inj_tt.release();
   c->stan.release();
   if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->mgraph) cudaGraphExecDestroy(c->mgraph);
+  c->mg_sys.release(); c->mg_ev.release(); c->mg_order.release();
   c->ev_base.release(); c->worst.release();
   if (c->h_first) cudaFreeHost(c->h_first);
   if (c->h_worst) cudaFreeHost(c->h_worst);
@@ -880,19 +897,21 @@ smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_
   return run(c, first_event, n, out, nullptr, nullptr, nullptr, true);
 }
 
-smc_status smc_generate_mixed(void *ctx, const smc_params *systems, int nsys, uint64_t first_event, int n,
-                              const int *system_of_event, const smc_outputs *out) {
-  if (ctx && static_cast<Ctx *>(ctx)->prm.ws_inverse_cdf) return SMC_ERR_CONFIG;
-  if (out && out->tangents) return SMC_ERR_ARGUMENT;
-  if (!ctx || !out || !systems || nsys < 1 || nsys > 64 || n < 0 || (n > 0 && !system_of_event))
-    return SMC_ERR_ARGUMENT;
+// The per-system table of a mixed batch (and each system's cost, A + B, and
+// the largest A + B), after checking that the systems differ from the
+// context's parameters only where a mixed batch allows it.
+smc_status mixed_systems(Ctx *c, const smc_params *systems, int nsys, int n, const int *system_of_event,
+                         const smc_outputs *out, std::vector<smc::SystemDev> &sys, std::vector<int> &cost,
+                         int &max_ab) {
+  if (c->prm.ws_inverse_cdf) return SMC_ERR_CONFIG;
+  if (out->tangents) return SMC_ERR_ARGUMENT;
+  if (!systems || nsys < 1 || nsys > 64 || n < 0 || (n > 0 && !system_of_event)) return SMC_ERR_ARGUMENT;
   if (out->positions || out->wounded) return SMC_ERR_ARGUMENT;   // per-system shapes
-  Ctx *c = static_cast<Ctx *>(ctx);
   const smc_params &q = c->prm;
   if (q.which_mc_model == 1 || q.shape_of_nucleons != 4) return SMC_ERR_CONFIG;
-  std::vector<smc::SystemDev> sys(nsys);
-  std::vector<int> cost(nsys);
-  int max_ab = c->info.A + c->info.B;
+  sys.assign(nsys, smc::SystemDev{});
+  cost.assign(nsys, 0);
+  max_ab = c->info.A + c->info.B;
   for (int k = 0; k < nsys; k++) {
     const smc_params &p = systems[k];
     smc_status v = validate(p);
@@ -919,7 +938,29 @@ smc_status smc_generate_mixed(void *ctx, const smc_params *systems, int nsys, ui
   }
   for (int e = 0; e < n; e++)
     if (system_of_event[e] < 0 || system_of_event[e] >= nsys) return SMC_ERR_ARGUMENT;
-  smc_status s = set_thickness_flags(c, out);
+  return SMC_OK;
+}
+
+// The order in which the CTAs take the events of chunk [off, off + m): heavy
+// systems first.
+void mixed_order(const std::vector<int> &cost, const int *system_of_event, int off, int m, std::vector<int> &order) {
+  order.resize(m);
+  for (int e = 0; e < m; e++) order[e] = e;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return cost[system_of_event[off + a]] > cost[system_of_event[off + b]];
+  });
+}
+
+smc_status smc_generate_mixed(void *ctx, const smc_params *systems, int nsys, uint64_t first_event, int n,
+                              const int *system_of_event, const smc_outputs *out) {
+  if (!ctx || !out) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  std::vector<smc::SystemDev> sys;
+  std::vector<int> cost;
+  int max_ab = 0;
+  smc_status s = mixed_systems(c, systems, nsys, n, system_of_event, out, sys, cost, max_ab);
+  if (s) return s;
+  s = set_thickness_flags(c, out);
   if (s) return s;
   if (n == 0) return SMC_OK;
   CK(cudaSetDevice(c->device));
@@ -933,12 +974,7 @@ smc_status smc_generate_mixed(void *ctx, const smc_params *systems, int nsys, ui
   std::vector<int> order, evs;
   for (int off = 0; off < n; off += c->chunk) {
     const int m = std::min(c->chunk, n - off);
-    // the CTAs take the chunk's events heavy systems first
-    order.resize(m);
-    for (int e = 0; e < m; e++) order[e] = e;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-      return cost[system_of_event[off + a]] > cost[system_of_event[off + b]];
-    });
+    mixed_order(cost, system_of_event, off, m, order);   // heavy systems first
     s = ensure_buffers(c, m, out);
     if (!s && (c->mix_ev.ensure(m) != cudaSuccess || c->mix_order.ensure(m) != cudaSuccess)) s = SMC_ERR_CUDA;
     if (!s && (cudaMemcpyAsync(c->mix_ev.p, system_of_event + off, sizeof(int) * m, cudaMemcpyHostToDevice, c->st) !=
@@ -1318,7 +1354,15 @@ smc_status smc_average_binned(void *ctx, uint64_t first_event, int n, int order,
 // synchronisation: event ids from the device value ev_base, the worst
 // event status reduced on the device and copied to h_worst at the end.
 // Buffers must already have their sizes (no allocation: it is captured).
-smc_status enqueue_batch(Ctx *c, int n, const smc_outputs *out, int *launches) {
+// The device buffers of the context that a captured batch reads or writes.
+std::array<const void *, 12> batch_buffers(const Ctx *c) {
+  return {c->recs.p, c->srcs.p, c->scratch.p, c->ecc.p, c->status.p, c->ev_order.p, c->tickets.p, c->corr_ev.p,
+          c->rho_ev.p, c->cm_ev.p, c->ev_base.p, c->worst.p};
+}
+
+smc_status enqueue_batch(Ctx *c, int n, const smc_outputs *out, int *launches,
+                         const smc::SystemDev *systems = nullptr, const int *ev_sys = nullptr,
+                         const int *order = nullptr) {
   const DevParams &P = c->P;
   const size_t g = (size_t)P.nx * P.ny;
   const int AB = c->info.A + c->info.B;
@@ -1337,8 +1381,9 @@ smc_status enqueue_batch(Ctx *c, int n, const smc_outputs *out, int *launches) {
     tio.ntan = out->tangents ? out->tangents + (size_t)off * 4 * AB : nullptr;
     tio.orient = out->orientation ? out->orientation + (size_t)off * 4 : nullptr;
     const int grid1 = std::max(1, std::min(m, c->sms * c->occ1));
-    CK(smc::launch_sample_pair_mixed(P, off, m, nullptr, nullptr, nullptr, c->recs.p, c->srcs.p, pos, wnd, nullptr,
-                                     nullptr, nullptr, grid1, c->st, &tio, c->ev_base.p, c->tickets.p + 2));
+    CK(smc::launch_sample_pair_mixed(P, off, m, nullptr, nullptr, nullptr, c->recs.p, c->srcs.p, pos, wnd, systems,
+                                     ev_sys ? ev_sys + off : nullptr, order ? order + off : nullptr, grid1, c->st,
+                                     &tio, c->ev_base.p, c->tickets.p + 2));
     CK(launch_splat(c, P, m, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p));
     nl += 3 + ((c->use_tc && smc::grid_tc_supported(P) && !P.no_moments) ? 1 : 0);
     int *np = out->npart ? out->npart + 2 * off : nullptr;
@@ -1425,7 +1470,7 @@ smc_status smc_generate_graph(void *ctx, uint64_t first_event, int n, const smc_
   smc_status s = set_thickness_flags(c, out);
   if (s) return s;
   const bool same = c->graph && c->graph_n == n && c->graph_chunk == c->chunk && c->graph_tc == c->use_tc &&
-                    std::memcmp(&c->graph_out, out, sizeof(smc_outputs)) == 0;
+                    std::memcmp(&c->graph_out, out, sizeof(smc_outputs)) == 0 && c->graph_bufs == batch_buffers(c);
   if (!same) {
     // this call runs eagerly (sizing every buffer), then the batch is captured
     if (c->graph) {
@@ -1460,12 +1505,98 @@ smc_status smc_generate_graph(void *ctx, uint64_t first_event, int n, const smc_
     c->graph_tc = c->use_tc;
     c->graph_out = *out;
     c->graph_launches = launches;
+    c->graph_bufs = batch_buffers(c);
     return s;
   }
   *c->h_first = first_event;
   CK(cudaGraphLaunch(c->graph, c->st));
   CK(cudaStreamSynchronize(c->st));
   c->stats.launches += c->graph_launches;
+  c->stats.events += n;
+  return status_error(*c->h_worst);
+}
+
+smc_status smc_generate_mixed_graph(void *ctx, const smc_params *systems, int nsys, uint64_t first_event, int n,
+                                    const int *system_of_event, const smc_outputs *out) {
+  if (!ctx || !out || n < 0 || !out->device) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  if (n == 0) return SMC_OK;
+  CK(cudaSetDevice(c->device));
+  const bool same = c->mgraph && c->mgraph_n == n && c->mgraph_chunk == c->chunk && c->mgraph_tc == c->use_tc &&
+                    std::memcmp(&c->mgraph_out, out, sizeof(smc_outputs)) == 0 && (int)c->mgraph_sys.size() == nsys &&
+                    std::memcmp(c->mgraph_sys.data(), systems, sizeof(smc_params) * nsys) == 0 &&
+                    std::memcmp(c->mgraph_ev.data(), system_of_event, sizeof(int) * n) == 0 &&
+                    c->mgraph_bufs == batch_buffers(c);
+  if (!same) {
+    if (c->mgraph) {
+      cudaGraphExecDestroy(c->mgraph);
+      c->mgraph = nullptr;
+    }
+    // this call runs eagerly (checks the systems, sizes every buffer), then
+    // the batch is captured with its own copies of the system table and of
+    // each chunk's system list and event order
+    smc_status s = smc_generate_mixed(ctx, systems, nsys, first_event, n, system_of_event, out);
+    if (s && s != SMC_ERR_ZERO_DNDY) return s;
+    std::vector<smc::SystemDev> sys;
+    std::vector<int> cost, order, all_order(n);
+    int max_ab = 0;
+    smc_status v = mixed_systems(c, systems, nsys, n, system_of_event, out, sys, cost, max_ab);
+    if (v) return v;
+    for (int off = 0; off < n; off += c->chunk) {
+      const int m = std::min(c->chunk, n - off);
+      mixed_order(cost, system_of_event, off, m, order);
+      std::copy(order.begin(), order.end(), all_order.begin() + off);
+    }
+    CK(c->mg_sys.ensure(nsys));
+    CK(c->mg_ev.ensure(n));
+    CK(c->mg_order.ensure(n));
+    CK(cudaMemcpyAsync(c->mg_sys.p, sys.data(), sizeof(smc::SystemDev) * nsys, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->mg_ev.p, system_of_event, sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->mg_order.p, all_order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
+    CK(c->ev_base.ensure(1));
+    CK(c->worst.ensure(1));
+    if (!c->h_first) CK(cudaHostAlloc(&c->h_first, sizeof(uint64_t), cudaHostAllocDefault));
+    if (!c->h_worst) CK(cudaHostAlloc(&c->h_worst, sizeof(int), cudaHostAllocDefault));
+    CK(c->scratch.ensure((size_t)c->sms * c->occ2 * c->P.nx * c->P.ny));
+    CK(cudaStreamSynchronize(c->st));
+    const int saved_max_src = c->P.max_src;
+    c->P.max_src = 2 * max_ab + c->P.max_coll;   // as the eager call sized the sources
+    cudaGraph_t graph = nullptr;
+    const cudaError_t eb = cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal);
+    int launches = 0;
+    smc_status se = SMC_ERR_CUDA;
+    cudaError_t ee = cudaErrorUnknown;
+    if (eb == cudaSuccess) {
+      const bool timing = c->timing;
+      c->timing = false;
+      se = enqueue_batch(c, n, out, &launches, c->mg_sys.p, c->mg_ev.p, c->mg_order.p);
+      c->timing = timing;
+      ee = cudaStreamEndCapture(c->st, &graph);
+    }
+    c->P.max_src = saved_max_src;
+    if (eb != cudaSuccess) return SMC_ERR_CUDA;
+    if (se) {
+      if (graph) cudaGraphDestroy(graph);
+      return se;
+    }
+    CK(ee);
+    const cudaError_t ei = cudaGraphInstantiate(&c->mgraph, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ei);
+    c->mgraph_n = n;
+    c->mgraph_chunk = c->chunk;
+    c->mgraph_tc = c->use_tc;
+    c->mgraph_out = *out;
+    c->mgraph_sys.assign(systems, systems + nsys);
+    c->mgraph_ev.assign(system_of_event, system_of_event + n);
+    c->mgraph_launches = launches;
+    c->mgraph_bufs = batch_buffers(c);
+    return s;
+  }
+  *c->h_first = first_event;
+  CK(cudaGraphLaunch(c->mgraph, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->stats.launches += c->mgraph_launches;
   c->stats.events += n;
   return status_error(*c->h_worst);
 }

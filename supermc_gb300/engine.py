@@ -120,12 +120,14 @@ class Engine:
         return bufs
 
     def generate_mixed(self, systems: list[dict], system_of_event, first_event: int = 0,
-                       want=("ecc", "npart", "ncoll", "b"), device_bufs: dict | None = None):
+                       want=("ecc", "npart", "ncoll", "b"), device_bufs: dict | None = None, graph: bool = False):
         """Events of several collision systems in one batch.  systems are
         parameters.dat key sets: the nucleus and energy keys (SYSTEM_KEYS)
         start from their defaults, every other key is this engine's unless
         given (only the impact-parameter range and the Npart cut may differ
-        besides); system_of_event[e] selects event first_event + e's system."""
+        besides); system_of_event[e] selects event first_event + e's system.
+        graph: the batch as one CUDA graph (smc_generate_mixed_graph; device
+        buffers only)."""
         nsys = len(systems)
         arr = (_lib.SmcParams * nsys)()
         for k, sysv in enumerate(systems):
@@ -144,8 +146,14 @@ class Engine:
         else:
             bufs = self._host_buffers(n, want)
             o = self._outputs(bufs, False)
-        _lib.check(self.lib.smc_generate_mixed(self.h, arr, nsys, first_event, n, _lib.ptr(sel), ctypes.byref(o)),
-                   "smc_generate_mixed")
+        if graph:
+            if device_bufs is None:
+                raise ValueError("a graph-captured mixed batch writes device buffers")
+            _lib.check(self.lib.smc_generate_mixed_graph(self.h, arr, nsys, first_event, n, _lib.ptr(sel),
+                                                         ctypes.byref(o)), "smc_generate_mixed_graph")
+        else:
+            _lib.check(self.lib.smc_generate_mixed(self.h, arr, nsys, first_event, n, _lib.ptr(sel),
+                                                   ctypes.byref(o)), "smc_generate_mixed")
         return bufs
 
     def generate_graph_into(self, first_event: int, n: int, device_bufs: dict) -> None:

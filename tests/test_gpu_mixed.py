@@ -52,3 +52,31 @@ def test_mixed_batch_rejects_incompatible_systems():
         eng.generate_mixed([dict(MIXED[0], dx=0.2)], np.zeros(4, np.int32))
     with pytest.raises(SmcError):   # system index out of range
         eng.generate_mixed(MIXED[:2], np.array([0, 1, 2], np.int32))
+
+
+@pytest.mark.parametrize("tensor_cores", [False, True])
+def test_mixed_graph_replays_equal_eager_batches(tensor_cores):
+    """smc_generate_mixed_graph: the first call runs eagerly and captures the
+    batch; replays with new event ids equal smc_generate_mixed on those ids.
+    An eager call that grows the context's buffers in between makes the next
+    call capture again (the old graph's buffers are gone)."""
+    import torch
+    base = values(dict(BASE, **MIXED[-1]), ecc_from_order=2, ecc_to_order=5)
+    n = 5 * 40
+    sel = np.random.default_rng(8).permutation(np.arange(n) % len(MIXED)).astype(np.int32)
+    eng = engine(base, seed=23)
+    eng.set_grid_path(tensor_cores)
+    dev = torch.device("cuda", 0)
+
+    def bufs():
+        return {"ecc": torch.zeros((n, 49), dtype=torch.float64, device=dev),
+                "npart": torch.zeros((n, 2), dtype=torch.int32, device=dev),
+                "ncoll": torch.zeros((n,), dtype=torch.int32, device=dev)}
+    g = bufs()
+    for first in (0, 5000, 9000):
+        eng.generate_mixed(MIXED, sel, first_event=first, device_bufs=g, graph=True)
+        ref = eng.generate_mixed(MIXED, sel, first_event=first, want=("ecc", "npart", "ncoll"))
+        for key in ("ecc", "npart", "ncoll"):
+            np.testing.assert_array_equal(g[key].cpu().numpy(), ref[key], err_msg=f"{first} {key}")
+        if first == 5000:
+            eng.generate(0, 4 * n)   # grows the context's buffers
