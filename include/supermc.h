@@ -428,7 +428,13 @@ smc_status smc_write_nucleon_tables(const double *xy, const uint8_t *wounded, in
  *   - All calls share that array: calls that overlap on the GPU (other
  *     streams, other threads) race.  Nothing in it needs clearing.
  *   - The first call on a device looks up the array's device address with
- *     that device current; make it before any stream capture.
+ *     that device current; make it before any stream capture.  Under lazy
+ *     module loading (the CUDA default) that first call also loads the
+ *     module, which commits the 24 MiB on the device: make it before the
+ *     caller's pool takes the device memory, or set CUDA_MODULE_LOADING=EAGER.
+ *   - max_collisions defaults to 2048 here, not smc_inject's 4096: an event
+ *     with more binary collisions gets SMC_ERR_CAPACITY in d_status (set
+ *     max_collisions to take such events, at fewer events per call).
  *   - MC-Glauber (which_mc_model 5) and sqrt(T_A T_B) (7) only.
  * Allocates nothing: no cudaMalloc, cudaFree or allocating library call. */
 smc_status smc_inject_noalloc(const smc_params *params, int n, const double *d_xy_proj,
