@@ -223,6 +223,17 @@ smc_status smc_generate_graph(void *ctx, uint64_t first_event, int n, const smc_
 smc_status smc_generate_mixed_graph(void *ctx, const smc_params *systems, int nsys, uint64_t first_event, int n,
                                     const int *system_of_event, const smc_outputs *out);
 
+/* MCnucl::generateNuclei(b) + getBinaryCollision (src/MCnucl.cpp:208-308)
+ * for one event: both nuclei drawn from the Philox streams of (seed,
+ * event) at the given impact parameter, then paired (one attempt, no
+ * centrality cut, no retry).  xy_proj [A][2], xy_targ [B][2] (host) receive
+ * the nucleons (each nucleus sorted by x), npart [2] Npart1, Npart2, *ncoll
+ * the binary collisions (0: none), orientation [4] cos(theta), phi of each
+ * nucleus (Nucleus::populate, src/Nucleus.cpp:192-197); npart, ncoll and
+ * orientation may be NULL.  The nuclei then go through smc_inject. */
+smc_status smc_sample_nuclei(void *ctx, uint64_t event, double b, double *xy_proj, double *xy_targ, int *npart,
+                             int *ncoll, double *orientation);
+
 /* Plain per-event path: the same results as smc_generate, one event per
  * kernel launch sequence (the unbatched baseline). */
 smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_outputs *out);

@@ -29,7 +29,7 @@ EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "sm
            "smc_write_density_block", "smc_write_density_4col", "smc_inject_noalloc", "smc_average",
            "smc_average_binned", "smc_adjoint", "smc_autotune", "smc_generate_graph", "smc_average_profiles",
            "smc_write_binary_table", "smc_write_nucleon_tables", "smc_write_ecc_deformed",
-           "smc_generate_mixed_graph"]
+           "smc_generate_mixed_graph", "smc_sample_nuclei"]
 
 
 class SmcError(RuntimeError):
@@ -139,6 +139,7 @@ def load() -> ctypes.CDLL:
     lib.smc_generate_mixed_graph.argtypes = [vp, ctypes.POINTER(SmcParams), ctypes.c_int, ctypes.c_uint64,
                                              ctypes.c_int, vp, ctypes.POINTER(SmcOutputs)]
     lib.smc_inject.argtypes = [vp, ctypes.c_int, vp, vp, vp, ctypes.POINTER(SmcOutputs)]
+    lib.smc_sample_nuclei.argtypes = [vp, ctypes.c_uint64, ctypes.c_double, vp, vp, vp, vp, vp]
     lib.smc_kln_table.argtypes = [vp, vp, ctypes.c_int]
     lib.smc_set_timing.argtypes = [vp, ctypes.c_int]
     lib.smc_set_grid_path.argtypes = [vp, ctypes.c_int]

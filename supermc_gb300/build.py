@@ -17,8 +17,11 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libsupermc_gb300.so")
 HOST = os.path.join(HERE, "host")
-HOST_SOURCES = ["ParameterReader.cpp", "MakeDensity.cpp", "main.cpp"]
+HOST_SOURCES = ["ParameterReader.cpp", "MakeDensity.cpp", "MCnucl.cpp", "main.cpp"]
 EXE = os.path.join(OUT_DIR, "superMC")
+# one event through the MCnucl call surface (host/MCnucl.h), for its test
+MCNUCL_SOURCES = ["ParameterReader.cpp", "MakeDensity.cpp", "MCnucl.cpp", "mcnucl_event.cpp"]
+MCNUCL_EXE = os.path.join(OUT_DIR, "mcnucl_event")
 SOURCES = ["smc_capi.cu", "k_sample_pair.cu", "k_grid.cu", "k_kln.cu", "k_average.cu", "smc_noalloc.cu", "k_grid_tc.cu", "k_adjoint.cu", "smc_output.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -67,21 +70,27 @@ def build(verbose: bool = False, force: bool = False) -> str:
     return LIB
 
 
-def build_host(force: bool = False) -> str:
-    """The C++ drop-in driver ``_build/superMC`` (ParameterReader,
-    MakeDensity, main over the C ABI), linked to the library."""
-    srcs = [os.path.join(HOST, f) for f in HOST_SOURCES]
+def _host_exe(exe: str, sources: list[str], force: bool) -> str:
+    srcs = [os.path.join(HOST, f) for f in sources]
     deps = srcs + [os.path.join(HOST, h) for h in os.listdir(HOST) if h.endswith(".h")] + [LIB]
-    if not force and not _stale(EXE, deps):
-        return EXE
+    if not force and not _stale(exe, deps):
+        return exe
     cxx = shutil.which("g++") or "g++"
-    tmp = EXE + ".tmp"
+    tmp = exe + ".tmp"
     r = subprocess.run([cxx, "-O2", "-std=c++17", "-Wall", "-o", tmp, *srcs, "-L" + OUT_DIR, "-lsupermc_gb300",
                         "-Wl,-rpath,$ORIGIN"], capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError("host build failed:\n" + r.stdout + r.stderr)
-    os.replace(tmp, EXE)
-    return EXE
+    os.replace(tmp, exe)
+    return exe
+
+
+def build_host(force: bool = False) -> str:
+    """The C++ drop-in driver ``_build/superMC`` (ParameterReader,
+    MakeDensity, MCnucl, main over the C ABI) and ``_build/mcnucl_event``
+    (one event through the MCnucl call surface), linked to the library."""
+    _host_exe(MCNUCL_EXE, MCNUCL_SOURCES, force)
+    return _host_exe(EXE, HOST_SOURCES, force)
 
 
 if __name__ == "__main__":

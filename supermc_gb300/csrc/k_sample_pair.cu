@@ -782,11 +782,16 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
       if (attempt >= P.max_attempts) { status = 3; break; }
       // impact parameter (MakeDensity.cpp:2149)
       if (tid == 0) {
-        if (inject) sm.b = inj_b ? inj_b[e] : 0.0;
-        else {
-          double u, unused;
-          uniform2(P.seed, ev, stream_id(attempt, ST_EVENT), 0, u, unused);
-          sm.b = sqrt((P.bmax * P.bmax - P.bmin * P.bmin) * u + P.bmin * P.bmin);
+        // a given impact parameter (injected nuclei, or nuclei drawn at a
+        // given b: MCnucl::generateNuclei(b)), else drawn
+        if (inj_b) sm.b = inj_b[e];
+        else if (inject) sm.b = 0.0;
+        if (!inject) {
+          if (!inj_b) {
+            double u, unused;
+            uniform2(P.seed, ev, stream_id(attempt, ST_EVENT), 0, u, unused);
+            sm.b = sqrt((P.bmax * P.bmax - P.bmin * P.bmin) * u + P.bmin * P.bmin);
+          }
           // nucleus orientations (cos theta, phi), rounded to float
           for (int w = 0; w < 2; w++) {
             double o0, o1;

@@ -1497,6 +1497,48 @@ smc_status smc_generate_mixed_graph(void *ctx, const smc_params *systems, int ns
   return status_error(*c->h_worst);
 }
 
+smc_status smc_sample_nuclei(void *ctx, uint64_t event, double b, double *xy_proj, double *xy_targ, int *npart,
+                             int *ncoll, double *orientation) {
+  if (!ctx || !xy_proj || !xy_targ) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  CK(cudaSetDevice(c->device));
+  const int A = c->info.A, B = c->info.B;
+  CK(c->recs.ensure(1));
+  CK(c->srcs.ensure(c->P.max_src));
+  CK(c->pos.ensure((size_t)2 * (A + B)));
+  CK(c->inj_b.ensure(1));
+  CK(cudaMemcpyAsync(c->inj_b.p, &b, sizeof(double), cudaMemcpyHostToDevice, c->st));
+  // one attempt at the given b, no centrality cut: an event without a
+  // collision ends with the retry status after its first attempt
+  DevParams P = c->P;
+  P.max_attempts = 1;
+  P.npmin = 0;
+  P.npmax = 1 << 30;
+  CK(smc::launch_sample_pair_mixed(P, event, 1, nullptr, nullptr, c->inj_b.p, c->recs.p, c->srcs.p, c->pos.p,
+                                   nullptr, nullptr, nullptr, nullptr, 1, c->st));
+  std::vector<double> pos((size_t)2 * (A + B));
+  EventRec r{};
+  CK(cudaMemcpyAsync(pos.data(), c->pos.p, sizeof(double) * pos.size(), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(&r, c->recs.p, sizeof(EventRec), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (r.status != 0 && r.status != 3) return status_error(r.status);
+  std::copy(pos.begin(), pos.begin() + 2 * A, xy_proj);
+  std::copy(pos.begin() + 2 * A, pos.end(), xy_targ);
+  if (npart) { npart[0] = r.npart1; npart[1] = r.npart2; }
+  if (ncoll) *ncoll = r.ncoll;
+  if (orientation) {
+    // the attempt's orientations, as the sampler draws them (whether or not
+    // the event has a collision)
+    for (int w = 0; w < 2; w++) {
+      double o[2];
+      smc::uniform2(c->P.seed, event, smc::stream_id(0, smc::ST_EVENT), 1 + w, o[0], o[1]);
+      orientation[2 * w] = 1.0 - 2.0 * o[0];
+      orientation[2 * w + 1] = 2 * M_PI * o[1];
+    }
+  }
+  return SMC_OK;
+}
+
 smc_status smc_set_grid_path(void *ctx, int tensor_cores) {
   if (!ctx) return SMC_ERR_ARGUMENT;
   static_cast<Ctx *>(ctx)->use_tc = tensor_cores != 0;

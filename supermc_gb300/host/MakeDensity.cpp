@@ -27,6 +27,7 @@ const Default kDefaults[] = {
     {"ecc_from_order", 1}, {"ecc_to_order", 9}, {"use_sd", 1}, {"use_ed", 1}, {"use_4col", 0}, {"use_block", 1},
     {"maxx", 15.0}, {"maxy", 15.0}, {"dx", 0.1}, {"dy", 0.1}, {"cc_fluctuation_model", 6},
     {"cc_fluctuation_Gamma_theta", 0.75}, {"cc_fluctuation_k", 0.75}, {"generate_reaction_plane_avg_profile", 1}, {"cutdSdy", 0},
+    {"cutdSdy_lowerBound", 593.51}, {"cutdSdy_upperBound", 889.53},
     {"output_TATB", 1}, {"output_rho_binary", 1}, {"output_TA", 1}, {"output_spectator_density", 1},
     // extensions (0: the reference's hard-coded value)
     {"proj_R", 0}, {"proj_a", 0}, {"targ_R", 0}, {"targ_a", 0}, {"proj_d_min", 0}, {"targ_d_min", 0},
@@ -107,8 +108,6 @@ MakeDensity::MakeDensity(ParameterReader *reader) : reader_(reader) {
   check(smc_get_info(ctx_, &info_), "smc_get_info");
   if (val(*reader_, "use_ed"))
     std::fprintf(stderr, "supermc_gb300: use_ed = 1: energy-density outputs (equation of state) are not produced\n");
-  if (val(*reader_, "cutdSdy"))
-    std::fprintf(stderr, "supermc_gb300: cutdSdy is not applied\n");
 }
 
 MakeDensity::~MakeDensity() { smc_destroy(ctx_); }
@@ -144,7 +143,13 @@ void MakeDensity::generate_profile_ebe(int nevent) {
   ensure_data_dir();
   const bool sd = val(*reader_, "use_sd") != 0, block = val(*reader_, "use_block") != 0,
              four = val(*reader_, "use_4col") != 0;
-  const double ff = params_.final_factor;
+  // cutdSdy: an event whose dS/dy = sum getRho dx dy lies outside
+  // [cutdSdy_lowerBound, cutdSdy_upperBound] is dropped after its pairing
+  // (its binary.dat lines stay) and does not count (src/MakeDensity.cpp:
+  // 601-617, :683-684, gettotaldSdy :2557-2567)
+  const bool cut = val(*reader_, "cutdSdy") == 1;
+  const double cut_lo = val(*reader_, "cutdSdy_lowerBound"), cut_hi = val(*reader_, "cutdSdy_upperBound");
+  const double ff = params_.final_factor, area = params_.dx * params_.dy;
   const size_t g = (size_t)info_.nx * info_.ny;
   const int AB = info_.A + info_.B, mc = info_.max_collisions;
   const int batch = std::max(1, std::min(batch_, 1024));   // host grids of one call
@@ -153,8 +158,10 @@ void MakeDensity::generate_profile_ebe(int nevent) {
   std::vector<double> grid(g), pos, coll;
   std::vector<uint8_t> wounded;
   char name[256];
-  for (int done = 0; done < nevent; done += batch) {
-    const int n = std::min(batch, nevent - done);
+  int event = 0;                 // events written
+  uint64_t generated = 0;        // event ids used
+  while (event < nevent) {
+    const int n = std::min(batch, cut ? batch : nevent - event);
     rho.resize((size_t)n * g);
     npart.resize((size_t)n * 2);
     ncoll.resize(n);
@@ -168,22 +175,26 @@ void MakeDensity::generate_profile_ebe(int nevent) {
     out.positions = pos.data();
     out.wounded = wounded.data();
     out.collisions = coll.data();
-    check(smc_generate(ctx_, (uint64_t)done, n, &out), "smc_generate");
-    // MCnucl::dumpBinaryTable("data/binary.dat") after each event's pairing
-    // (src/MakeDensity.cpp:598; src/MCnucl.cpp:1175-1207)
-    for (int e = 0; e < n; e++) {
+    check(smc_generate(ctx_, generated, n, &out), "smc_generate");
+    generated += n;
+    for (int e = 0; e < n && event < nevent; e++) {
+      // MCnucl::dumpBinaryTable("data/binary.dat") after each event's pairing
+      // (src/MakeDensity.cpp:598; src/MCnucl.cpp:1175-1207)
       check(smc_write_binary_table(coll.data() + (size_t)e * mc * 2, std::min(ncoll[e], mc), "data/binary.dat"),
             "smc_write_binary_table");
-      if (done + e + 1 == nevent)
+      if (cut) {
+        double total = 0.0;
+        for (size_t k = 0; k < g; k++) total += (double)rho[(size_t)e * g + k] * area;
+        if (total < cut_lo || total > cut_hi) continue;
+      }
+      event++;
+      if (event == nevent)
         check(smc_write_nucleon_tables(pos.data() + (size_t)e * AB * 2, wounded.data() + (size_t)e * AB, info_.A,
                                        info_.B, "data/wounded.data", "data/nucl1.data", "data/nucl2.data"),
               "smc_write_nucleon_tables");
-    }
-    if (!sd) continue;
-    for (int e = 0; e < n; e++) {
+      if (!sd) continue;
       // MakeDensity::setSd (src/MakeDensity.cpp:2514-2522)
       for (size_t k = 0; k < g; k++) grid[k] = (double)rho[(size_t)e * g + k] * ff;
-      const int event = done + e + 1;
       if (four) {
         std::snprintf(name, sizeof(name), "data/sd_event_%d_4col.dat", event);
         check(smc_write_density_4col(grid.data(), info_.nx, info_.ny, -params_.maxx, -params_.maxy, params_.dx,

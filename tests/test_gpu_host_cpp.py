@@ -79,3 +79,23 @@ def test_operation_3_averages(tmp_path):
                        ("rho_binary_fromSd_order_2", "rho_binary"), ("spectator_density_B_fromSd_order_2", "spectator_b")):
         got = np.loadtxt(tmp_path / "data" / f"{fname}_block.dat")
         np.testing.assert_allclose(got, prof[key][0], rtol=1e-11, atol=1e-300, err_msg=fname)
+
+
+def test_operation_1_cut_on_total_entropy(tmp_path):
+    """cutdSdy = 1: only events with lower <= sum getRho dx dy <= upper are
+    written and counted; every generated event's collisions still reach
+    binary.dat (src/MakeDensity.cpp:598-617)."""
+    lo, hi = 60.0, 140.0
+    p = _run(tmp_path, operation=1, nev=4, cutdSdy=1, cutdSdy_lowerBound=lo, cutdSdy_upperBound=hi, use_4col=0)
+    n = 400
+    out = _engine(p).generate(0, n, want=("rho", "ncoll", "collisions"))
+    total = out["rho"].astype(np.float64).sum(axis=(1, 2)) * (0.1 * 0.1)
+    keep = np.flatnonzero((total >= lo) & (total <= hi))[:4]
+    assert len(keep) == 4
+    for k, e in enumerate(keep):
+        assert (tmp_path / "data" / f"sd_event_{k + 1}_block.dat").exists()
+        block = np.loadtxt(tmp_path / "data" / f"sd_event_{k + 1}_block.dat")
+        np.testing.assert_allclose(block, out["rho"][e].astype(np.float64) * 40.0, rtol=1e-11)
+    assert not (tmp_path / "data" / "sd_event_5_block.dat").exists()
+    lines = [f"{x:10.3g}{y:10.3g}" for e in range(keep[-1] + 1) for x, y in out["collisions"][e][:out["ncoll"][e]]]
+    assert (tmp_path / "data" / "binary.dat").read_text() == "".join(l + "\n" for l in lines)
