@@ -56,7 +56,9 @@ typedef struct smc_params {
   int shape_of_nucleons;    /* 1 disk, 2 Gaussian from sigma, 4 user width  */
   int shape_of_entropy;     /* 1 disk, 2 Gaussian                           */
   int collision_criterion;  /* 1 disk (d^2 <= sigma/pi), 2 Gaussian profile */
-  int Aproj, Atarg;         /* mass numbers (1 = p, 2 = d, else Woods-Saxon)*/
+  int Aproj, Atarg;         /* mass numbers (1 = p, 2 = d, else Woods-Saxon
+                               or a configuration table:
+                               smc_set_configurations)                     */
   int proj_deformed, targ_deformed;
   double ecm;               /* sqrt(s) [GeV]; sigma_in from Regge fits      */
   double alpha;             /* (1-alpha)/2 WN + alpha BC                    */
@@ -234,6 +236,34 @@ smc_status smc_generate_mixed_graph(void *ctx, const smc_params *systems, int ns
 smc_status smc_sample_nuclei(void *ctx, uint64_t event, double b, double *xy_proj, double *xy_targ, int *npart,
                              int *ncoll, double *orientation);
 
+/* Light-nucleus configurations (Nucleus::readin_helium3_position ..
+ * readin_oxygen_position and GetNucleonPosition, src/Nucleus.cpp:383-478,
+ * 555-574): every nucleus of mass number A (3 <= A <= 256) of this
+ * context -- projectile, target, the systems of a mixed batch -- takes one
+ * configuration of xyz [nconf][A][3] (nucleus-frame x, y, z in fm, host
+ * memory) per event instead of Woods-Saxon sampling: configuration
+ * floor(u nconf) with u from the event's Philox stream 7 (the reference:
+ * rand() % nconf), rotated by the nucleus orientation (Point3D::rotate),
+ * shifted by +-b/2 and not recentred (src/Nucleus.cpp:210-236).
+ * nconf = 0 removes A's table.  Non-finite positions: SMC_ERR_ARGUMENT.
+ * The table is copied to the device; captured graphs are re-captured. */
+smc_status smc_set_configurations(void *ctx, int A, const double *xyz, int nconf);
+
+/* The light-nucleus configuration files in the reference's layout for A
+ * (one configuration per record, whitespace-separated fields): A = 3
+ * (tables/he3_plaintext.dat): 9 coordinates and 4 further fields; A = 12
+ * (tables/carbon_plaintext.dat): 2 fields and 36 coordinates; any other A
+ * (tables/he4_plaintext.dat, tables/oxygen_plaintext.dat): 3 A coordinates.
+ * Records are read until the file ends.  smc_read_configurations needs no
+ * GPU: *nconf receives the file's configuration count and xyz [capacity][A][3]
+ * the first capacity of them (SMC_ERR_CAPACITY when more are in the file;
+ * xyz may be NULL with capacity 0 to count).  A file that cannot be opened,
+ * holds no complete record or ends inside one: SMC_ERR_ARGUMENT.
+ * smc_load_configurations reads a file and passes it to
+ * smc_set_configurations. */
+smc_status smc_read_configurations(int A, const char *path, double *xyz, int capacity, int *nconf);
+smc_status smc_load_configurations(void *ctx, int A, const char *path);
+
 /* Plain per-event path: the same results as smc_generate, one event per
  * kernel launch sequence (the unbatched baseline). */
 smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_outputs *out);
@@ -406,6 +436,25 @@ smc_status smc_write_ecc(const double *ecc, int n, int from_order, int to_order,
 smc_status smc_write_ecc_deformed(const double *ecc, const double *orientation, int n, int from_order,
                                   int to_order, const char *pattern);
 smc_status smc_write_density_block(const double *grid, int nx, int ny, const char *filename);
+
+/* Binary counterparts of the text files (no reference counterpart: the
+ * reference writes text only, src/MakeDensity.cpp:2432-2609): NumPy .npy
+ * files (format 1.0, little-endian, C order; numpy.load reads them), one
+ * array per text file holding the text file's columns at full precision.
+ * smc_write_npy: data [shape[0]]..[shape[ndim-1]] of elem_bytes 4 (float)
+ * or 8 (double), 1 <= ndim <= 4; with append != 0 an existing file this
+ * function wrote with the same type and trailing dimensions grows by
+ * shape[0] rows (the text writers append the same way), any other existing
+ * file: SMC_ERR_ARGUMENT.  A density block is [nx][ny] (the rows of
+ * sd_event_<n>_block.dat), the collision table [ncoll][2] (binary.dat).
+ * smc_write_ecc_npy: sn_ecc_eccp_<order>.npy [n][9] (the per-order line's
+ * Re, Im (r^2), Re, Im (r^n), <r^n>, then Npart, Ncoll, dN/dy, b) and
+ * sn_ecc_eccp_10.npy [n][49]; with orientation (not NULL) the deformed
+ * layout's four more columns; appends like smc_write_ecc. */
+smc_status smc_write_npy(const char *filename, const void *data, int elem_bytes, int ndim, const int64_t *shape,
+                         int append);
+smc_status smc_write_ecc_npy(const double *ecc, const double *orientation, int n, int from_order, int to_order,
+                             const char *pattern);
 smc_status smc_write_density_4col(const double *grid, int nx, int ny, double xmin, double ymin, double dx, double dy,
                                   double rapidity, double npart, const char *filename);
 /* MCnucl::dumpBinaryTable (src/MCnucl.cpp:1175-1189): appends one line per

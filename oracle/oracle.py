@@ -83,6 +83,7 @@ class Nucleus(ctypes.Structure):
         ("beta2", ctypes.c_double), ("beta4", ctypes.c_double),
         ("d_min", ctypes.c_double), ("rmax_cut", ctypes.c_double), ("rw_max", ctypes.c_double),
         ("icdf", ctypes.c_int),
+        ("conf", _D), ("nconf", ctypes.c_int),
     ]
 
 
@@ -170,10 +171,18 @@ class Oracle:
                                            ctypes.c_int, ctypes.c_uint64, _D]
 
     # ---- helpers ---------------------------------------------------------
-    def nucleus(self, A, deformed=0, R=0.0, a=0.0, dmin=0.0, icdf=0) -> Nucleus:
+    def nucleus(self, A, deformed=0, R=0.0, a=0.0, dmin=0.0, icdf=0, conf=None) -> Nucleus:
+        """conf: light-nucleus configurations [nconf][A][3] (kept alive by
+        the returned structure)."""
         n = Nucleus()
         self.lib.smco_nucleus_init(ctypes.byref(n), A, deformed, R, a, dmin)
         n.icdf = icdf
+        if conf is not None:
+            t = np.ascontiguousarray(np.asarray(conf, dtype=np.float64))
+            assert t.ndim == 3 and t.shape[1:] == (A, 3), t.shape
+            n._conf_keep = t
+            n.conf = _ptr(t)
+            n.nconf = t.shape[0]
         return n
 
     def ws_icdf(self, R, a, u):
@@ -345,6 +354,20 @@ def _kln_rows_worker(args):
     return out
 
 
+def read_configurations(path: str, A: int) -> np.ndarray:
+    """A light-nucleus configuration file in the reference's layout for A
+    (src/Nucleus.cpp:383-478: he3 records hold 9 coordinates and 4 further
+    fields, carbon records 2 fields and 36 coordinates, the others 3 A
+    coordinates), as [nconf][A][3]."""
+    lead, trail = (2 if A == 12 else 0), (4 if A == 3 else 0)
+    rec = lead + 3 * A + trail
+    with open(path) as f:
+        vals = np.array(f.read().split(), dtype=np.float64)
+    if len(vals) == 0 or len(vals) % rec:
+        raise ValueError(f"{path}: {len(vals)} fields, not whole records of {rec}")
+    return vals.reshape(-1, rec)[:, lead:lead + 3 * A].reshape(-1, A, 3).copy()
+
+
 def kln_table(ecm: float, lam: float, dT: float, tmax: int, rule=(48, 64, 32), procs: int | None = None):
     """The whole MC-KLN dN/dy table [tmax][tmax] (MCnucl::makeTable,
     src/MCnucl.cpp:911-960) by the oracle's FP64 Gauss-Legendre quadrature of
@@ -366,8 +389,15 @@ def kln_table(ecm: float, lam: float, dT: float, tmax: int, rule=(48, 64, 32), p
 class Reference:
     """The reference's own code (compiled from source) with injected inputs."""
 
-    def __init__(self, params_text: str, eos_dir: str | None = None, workdir: str | None = None):
+    LIGHT_TABLES = ("he3_plaintext.dat", "he4_plaintext.dat", "carbon_plaintext.dat", "oxygen_plaintext.dat")
+
+    def __init__(self, params_text: str, eos_dir: str | None = None, workdir: str | None = None,
+                 tables_dir: str | None = None):
+        """tables_dir: where the reference's light-nucleus configuration files
+        are (default: the reference tree's tables/); the Nucleus constructor
+        reads them from tables/ of the work directory."""
         eos_dir = eos_dir or os.path.join(REF_ROOT, "EOS")
+        tables_dir = tables_dir or os.path.join(REF_ROOT, "tables")
         if not os.path.exists(REF_SO):
             raise FileNotFoundError(REF_SO)
         lib = ctypes.CDLL(REF_SO)
@@ -402,6 +432,11 @@ class Reference:
         lib.refh_kln_dndy.restype = ctypes.c_double
         lib.refh_kln_dndy.argtypes = [ctypes.c_double] * 3
         self.workdir = workdir or tempfile.mkdtemp(prefix="smc_ref_")
+        os.makedirs(os.path.join(self.workdir, "tables"), exist_ok=True)
+        for f in self.LIGHT_TABLES:
+            src, dst = os.path.join(tables_dir, f), os.path.join(self.workdir, "tables", f)
+            if os.path.exists(src) and not os.path.lexists(dst):
+                os.symlink(os.path.abspath(src), dst)
         cwd = os.getcwd()
         rc = lib.refh_init(self.workdir.encode(), eos_dir.encode(), params_text.encode())
         os.chdir(cwd)  # the harness chdir()s into its work dir; callers keep theirs

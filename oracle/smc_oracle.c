@@ -55,7 +55,7 @@ void smco_uniform2(uint64_t seed, uint64_t event, uint32_t stream, uint32_t slot
 }
 
 /* stream ids (low byte of the stream word; the retry attempt is above) */
-enum { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5, ST_NBD = 6 };
+enum { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5, ST_NBD = 6, ST_CONF = 7 };
 static uint32_t stream_id(int attempt, int sid) { return ((uint32_t)attempt << 8) | (uint32_t)sid; }
 
 /* ================================================================== */
@@ -482,7 +482,19 @@ static void populate_drand48(smco_event *e, int w, const smco_nucleus *n, double
   int A = n->A;
   reserve(e, w, A);
   e->n[w] = 0;
-  if (A == 1) {
+  if (n->conf && A >= 3) {
+    /* Nucleus::GetNucleonPosition (Nucleus.cpp:555-574): configuration
+     * rand() % nconf, each nucleon rotated; constructed in place
+     * (:210-236) */
+    const double *cfg = n->conf + (size_t)(rand() % n->nconf) * 3 * A;
+    for (int i = 0; i < A; i++) {
+      double x = cfg[3 * i], y = cfg[3 * i + 1], z = cfg[3 * i + 2];
+      rotate3(&x, &y, &z, cx, phi);
+      particle_draws();
+      construct(e, &e->nuc[w][i], x + xc, y + yc, z);
+    }
+    e->n[w] = A;
+  } else if (A == 1) {
     particle_draws();
     construct(e, &e->nuc[w][0], xc, yc, 0.0);
     e->n[w] = 1;
@@ -580,7 +592,20 @@ static int populate_philox(smco_event *e, int w, const smco_nucleus *n, double x
   double px[256], py[256], pz[256], pu[256];
   if (A > 256) return -1;
   int cnt = 0;
-  if (A == 1) {
+  if (n->conf && A >= 3) {
+    /* configuration floor(u nconf) from the nucleus's own stream (the
+     * reference: rand() % nconf), rotated in FP64, not recentred */
+    double u[2];
+    smco_uniform2(seed, event, stream_id(attempt, ST_CONF), (uint32_t)w, u);
+    int k = (int)(u[0] * n->nconf);
+    if (k > n->nconf - 1) k = n->nconf - 1;
+    const double *cfg = n->conf + (size_t)k * 3 * A;
+    for (int i = 0; i < A; i++) {
+      px[i] = cfg[3 * i]; py[i] = cfg[3 * i + 1]; pz[i] = cfg[3 * i + 2];
+      rotate3(&px[i], &py[i], &pz[i], cx, phi);
+    }
+    cnt = A;
+  } else if (A == 1) {
     px[0] = 0; py[0] = 0; pz[0] = 0;
     cnt = 1;
   } else if (A == 2) {

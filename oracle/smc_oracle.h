@@ -40,6 +40,11 @@ typedef struct {
   double rmax_cut;      /* proposal sphere radius, R + 2.5                  */
   double rw_max;        /* 1/(1+exp(-R/a))                                  */
   int icdf;             /* 1: radii by inverse CDF (spherical A > 2)        */
+  /* light-nucleus configurations [nconf][A][3] (NULL: Woods-Saxon); an
+   * event takes one, rotated and shifted, not recentred
+   * (Nucleus.cpp:210-236, 555-574) */
+  const double *conf;
+  int nconf;
 } smco_nucleus;
 /* inverse-CDF Woods-Saxon radius for the uniform u, with dr/dR, dr/da
  * (either may be NULL) */

@@ -29,7 +29,8 @@ EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "sm
            "smc_write_density_block", "smc_write_density_4col", "smc_inject_noalloc", "smc_average",
            "smc_average_binned", "smc_adjoint", "smc_autotune", "smc_generate_graph", "smc_average_profiles",
            "smc_write_binary_table", "smc_write_nucleon_tables", "smc_write_ecc_deformed",
-           "smc_generate_mixed_graph", "smc_sample_nuclei"]
+           "smc_generate_mixed_graph", "smc_sample_nuclei", "smc_set_configurations",
+           "smc_load_configurations", "smc_read_configurations", "smc_write_npy", "smc_write_ecc_npy"]
 
 
 class SmcError(RuntimeError):
@@ -140,6 +141,11 @@ def load() -> ctypes.CDLL:
                                              ctypes.c_int, vp, ctypes.POINTER(SmcOutputs)]
     lib.smc_inject.argtypes = [vp, ctypes.c_int, vp, vp, vp, ctypes.POINTER(SmcOutputs)]
     lib.smc_sample_nuclei.argtypes = [vp, ctypes.c_uint64, ctypes.c_double, vp, vp, vp, vp, vp]
+    lib.smc_set_configurations.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int]
+    lib.smc_load_configurations.argtypes = [vp, ctypes.c_int, ctypes.c_char_p]
+    lib.smc_read_configurations.argtypes = [ctypes.c_int, ctypes.c_char_p, vp, ctypes.c_int, vp]
+    lib.smc_write_npy.argtypes = [ctypes.c_char_p, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int]
+    lib.smc_write_ecc_npy.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
     lib.smc_kln_table.argtypes = [vp, vp, ctypes.c_int]
     lib.smc_set_timing.argtypes = [vp, ctypes.c_int]
     lib.smc_set_grid_path.argtypes = [vp, ctypes.c_int]

@@ -67,7 +67,8 @@ struct alignas(16) SampleSmem {
   double bmean[2];   // block means broadcast by block_mean2_f
   long long lred[32];
   double b;
-  float ori[2][2];   // nucleus orientations (cos theta, phi) of the attempt
+  double ori[2][2];   // nucleus orientations (cos theta, phi) of the attempt
+  int cfg_idx[2];     // configuration of each table nucleus
   SampleConsts sc;
 };
 
@@ -76,6 +77,17 @@ __device__ __forceinline__ float sph2(float ct) { return (3.0f * ct * ct - 1.0f)
 __device__ __forceinline__ float sph4(float ct) {
   float c2 = ct * ct;
   return (35.0f * c2 * c2 - 30.0f * c2 + 3.0f) * 0.10578554691520431f;
+}
+
+// Point3D::rotate (src/MathBasics.cpp:41-50), FP64
+__device__ __forceinline__ void rotate3d(double &x, double &y, double &z, double cth, double phi) {
+  double sphi, cphi;
+  sincos(phi, &sphi, &cphi);
+  const double sth = sqrt(fmax(0.0, 1.0 - cth * cth));
+  const double x0 = x, y0 = y, z0 = z;
+  x = cth * cphi * x0 - sphi * y0 + sth * cphi * z0;
+  y = cth * sphi * x0 + cphi * y0 + sth * sphi * z0;
+  z = -sth * x0 + cth * z0;
 }
 
 // Point3D::rotate (src/MathBasics.cpp:41-50)
@@ -469,19 +481,23 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
 // Places nucleus w: nucleus-frame positions -> centre-of-mass removed in
 // FP64 -> shifted by xc along x -> sorted by x (the reference sorts by the
 // left box edge x-4w, src/Nucleus.cpp:314, the same order).
+// With cfg (a light nucleus's configuration, [A][3]) the positions are the
+// configuration rotated by (cth, phi) in FP64 and shifted by xc, not
+// recentred (src/Nucleus.cpp:210-236, 555-574).
 // With ntan (this nucleus's [A][4] rows of the per-nucleon tangents) the
 // position tangents follow the same order: injected ones as given, those
 // of inverse-CDF radii as (dr/dp)/r times the nucleus-frame point minus
 // their mean over the nucleus (the centre-of-mass shift), else zero.
 __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const double *inj_xy,
-                             const NucleusDev &nu, const double *inj_tan, double *ntan) {
+                             const NucleusDev &nu, const double *inj_tan, double *ntan,
+                             const double *cfg = nullptr, double cth = 1.0, double phi = 0.0) {
   const int tid = threadIdx.x;
   double px = 0, py = 0;
   float rx = 0.f, ry = 0.f;
   float tg[4] = {0.f, 0.f, 0.f, 0.f};
   if (ntan && inj_xy && inj_tan && tid < A)
     for (int c = 0; c < 4; c++) tg[c] = (float)inj_tan[4 * tid + c];
-  if (ntan && !inj_xy && nu.icdf && !nu.deformed && A > 2) {
+  if (ntan && !inj_xy && !cfg && nu.icdf && !nu.deformed && A > 2) {
     double sR = 0, sa = 0;
     float x = 0.f, y = 0.f;
     if (tid < A) {
@@ -501,6 +517,15 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
   }
   if (inj_xy) {
     if (tid < A) { px = inj_xy[2 * tid]; py = inj_xy[2 * tid + 1]; }
+  } else if (cfg) {
+    if (tid < A) {
+      double x = cfg[3 * tid], y = cfg[3 * tid + 1], z = cfg[3 * tid + 2];
+      rotate3d(x, y, z, cth, phi);
+      px = x + xc;
+      py = y;
+      rx = (float)x;
+      ry = (float)y;
+    }
   } else {
     double mxa, mya;   // centre of mass
     block_mean2_f(tid < A ? sm.ax[w][tid] : 0.f, tid < A ? sm.ay[w][tid] : 0.f, A, sm.red2, sm.bmean, mxa, mya);
@@ -792,12 +817,17 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
             uniform2(P.seed, ev, stream_id(attempt, ST_EVENT), 0, u, unused);
             sm.b = sqrt((P.bmax * P.bmax - P.bmin * P.bmin) * u + P.bmin * P.bmin);
           }
-          // nucleus orientations (cos theta, phi), rounded to float
+          // nucleus orientations (cos theta, phi)
           for (int w = 0; w < 2; w++) {
             double o0, o1;
             uniform2(P.seed, ev, stream_id(attempt, ST_EVENT), 1 + w, o0, o1);
-            sm.ori[w][0] = (float)(1.0 - 2.0 * o0);
-            sm.ori[w][1] = (float)(2 * M_PI * o1);
+            sm.ori[w][0] = 1.0 - 2.0 * o0;
+            sm.ori[w][1] = 2 * M_PI * o1;
+            // a table nucleus's configuration (the reference: rand() % nconf)
+            if (P.nuc[w].conf) {
+              uniform2(P.seed, ev, stream_id(attempt, ST_CONF), (uint32_t)w, o0, o1);
+              sm.cfg_idx[w] = min((int)(o0 * P.nuc[w].nconf), P.nuc[w].nconf - 1);
+            }
           }
         }
       }
@@ -814,8 +844,12 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
                        itan ? itan + (size_t)e * 4 * nu.A : nullptr, ntan);
           continue;
         }
-        const float ctr = sm.ori[w][0], phir = sm.ori[w][1];
-        if (nu.A == 1) {
+        // rounded to float for the FP32 samplers
+        const float ctr = (float)sm.ori[w][0], phir = (float)sm.ori[w][1];
+        const double *cfg = nu.conf ? nu.conf + (size_t)sm.cfg_idx[w] * 3 * nu.A : nullptr;
+        if (cfg) {
+          // placed from the table below
+        } else if (nu.A == 1) {
           if (tid == 0) { sm.ax[w][0] = 0.f; sm.ay[w][0] = 0.f; sm.az[w][0] = 0.f; }
           __syncthreads();
         } else if (nu.A == 2) {
@@ -832,7 +866,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
         } else {
           ok = ok && sample_ws(sm, nu, w, P.seed, ev, attempt, ctr, phir);
         }
-        place_sorted(sm, w, nu.A, xc, nullptr, nu, nullptr, ntan);
+        place_sorted(sm, w, nu.A, xc, nullptr, nu, nullptr, ntan, cfg, sm.ori[w][0], sm.ori[w][1]);
       }
       if (!ok) { status = 3; break; }
       // ---- pairing: thread i tests projectile i against every target
@@ -1009,8 +1043,9 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
             // a Woods-Saxon nucleon is constructed at its nucleus-frame
             // position and then moved (Nucleus::populate,
             // src/Nucleus.cpp:274-309, Particle::setX/setY): its base box
-            // stays there, and the averaged mode's rotation brings it back
-            if (!inject && (w == 0 ? A : B) > 2) {
+            // stays there, and the averaged mode's rotation brings it back;
+            // light nuclei are constructed in place (:199-236)
+            if (!inject && (w == 0 ? A : B) > 2 && !P.nuc[w].conf) {
               s.kind |= SRC_RAW_BASE;
               s.bx = sm.ax[w][i];
               s.by = sm.ay[w][i];

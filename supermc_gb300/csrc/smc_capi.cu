@@ -4,9 +4,12 @@
 #include <algorithm>
 #include <array>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <map>
 #include <new>
 #include <vector>
 
@@ -157,6 +160,12 @@ struct Ctx {
   // next sampler launch uses
   DevBuf<double> icdf_tab[2], ntan, inj_tp, inj_tt, orient;
   DevBuf<float4> stan;
+  // light-nucleus configuration tables by mass number: [n][A][3] on the device
+  struct ConfTab {
+    DevBuf<double> xyz;
+    int n = 0;
+  };
+  std::map<int, ConfTab> conf;
   smc::TangentIO tio{};
   std::vector<double> h_adj;
   // captured batch (smc_generate_graph): the instantiated graph and what it
@@ -729,6 +738,7 @@ void smc_destroy(void *ctx) {
   c->adj_rho.release(); c->adj_lam.release(); c->adj_grho.release(); c->adj_geps.release(); c->adj_out.release();
   c->icdf_tab[0].release(); c->icdf_tab[1].release(); c->ntan.release(); c->inj_tp.release(); c->inj_tt.release();
   c->stan.release();
+  for (auto &t : c->conf) t.second.xyz.release();
   if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->mgraph) cudaGraphExecDestroy(c->mgraph);
   c->mg_sys.release(); c->mg_ev.release(); c->mg_order.release();
@@ -793,6 +803,14 @@ smc_status smc_generate_plain(void *ctx, uint64_t first_event, int n, const smc_
   return run(c, first_event, n, out, nullptr, nullptr, nullptr, true);
 }
 
+// A nucleus takes its mass number's configuration table, if the context has one.
+void attach_configurations(const Ctx *c, smc::NucleusDev &n) {
+  auto it = c->conf.find(n.A);
+  const bool on = n.A >= 3 && it != c->conf.end() && it->second.n > 0;
+  n.conf = on ? it->second.xyz.p : nullptr;
+  n.nconf = on ? it->second.n : 0;
+}
+
 // The per-system table of a mixed batch (and each system's cost, A + B, and
 // the largest A + B), after checking that the systems differ from the
 // context's parameters only where a mixed batch allows it.
@@ -825,6 +843,8 @@ smc_status mixed_systems(Ctx *c, const smc_params *systems, int nsys, int n, con
     const double sigin = p.sigin_override > 0 ? p.sigin_override : sigma_inelastic(p.ecm);
     d.nuc[0] = make_nucleus(p.Aproj, p.proj_deformed, p.proj_R, p.proj_a, p.proj_d_min);
     d.nuc[1] = make_nucleus(p.Atarg, p.targ_deformed, p.targ_R, p.targ_a, p.targ_d_min);
+    attach_configurations(c, d.nuc[0]);
+    attach_configurations(c, d.nuc[1]);
     d.dsq = 0.1 * sigin / M_PI;   // MCnucl.cpp:120
     d.sigin = sigin;
     d.sigma_gg = sigma_gg_from(sigin, c->P.width);
@@ -1537,6 +1557,73 @@ smc_status smc_sample_nuclei(void *ctx, uint64_t event, double b, double *xy_pro
     }
   }
   return SMC_OK;
+}
+
+smc_status smc_set_configurations(void *ctx, int A, const double *xyz, int nconf) {
+  if (!ctx || A < 3 || A > smc::kMaxA || nconf < 0 || (nconf > 0 && !xyz)) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  const size_t cnt = (size_t)nconf * A * 3;
+  for (size_t k = 0; k < cnt; k++)
+    if (!std::isfinite(xyz[k])) return SMC_ERR_ARGUMENT;
+  CK(cudaSetDevice(c->device));
+  // the work queued on the old table ends before it is replaced
+  CK(cudaStreamSynchronize(c->st));
+  Ctx::ConfTab &t = c->conf[A];
+  if (nconf == 0) {
+    t.xyz.release();
+    t.n = 0;
+  } else {
+    if (t.xyz.n < cnt) t.xyz.release();   // no stale table if the allocation fails
+    t.n = 0;
+    CK(t.xyz.ensure(cnt));
+    CK(cudaMemcpy(t.xyz.p, xyz, sizeof(double) * cnt, cudaMemcpyHostToDevice));
+    t.n = nconf;
+  }
+  attach_configurations(c, c->P.nuc[0]);
+  attach_configurations(c, c->P.nuc[1]);
+  // captured batches hold the old parameters
+  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  if (c->mgraph) { cudaGraphExecDestroy(c->mgraph); c->mgraph = nullptr; }
+  return SMC_OK;
+}
+
+smc_status smc_read_configurations(int A, const char *path, double *xyz, int capacity, int *nconf) {
+  if (!path || !nconf || A < 3 || A > smc::kMaxA || capacity < 0 || (capacity > 0 && !xyz))
+    return SMC_ERR_ARGUMENT;
+  *nconf = 0;
+  std::ifstream in(path);
+  if (!in.is_open()) return SMC_ERR_ARGUMENT;
+  // the reference's record layouts (src/Nucleus.cpp:383-478): fields before
+  // and after the 3 A coordinates of one configuration
+  const int lead = A == 12 ? 2 : 0, trail = A == 3 ? 4 : 0;
+  std::vector<double> rec((size_t)3 * A);
+  int n = 0;
+  for (;;) {
+    double v;
+    int got = 0;
+    for (int k = 0; k < lead && (in >> v); k++) got++;
+    for (int k = 0; k < 3 * A && (in >> rec[k]); k++) got++;
+    for (int k = 0; k < trail && (in >> v); k++) got++;
+    if (got == 0 && in.eof()) break;
+    if (got != lead + 3 * A + trail) return SMC_ERR_ARGUMENT;   // a record cut short, or not a number
+    if (n < capacity) std::copy(rec.begin(), rec.end(), xyz + (size_t)n * 3 * A);
+    if (n == INT_MAX) return SMC_ERR_ARGUMENT;
+    n++;
+  }
+  *nconf = n;
+  if (n == 0) return SMC_ERR_ARGUMENT;
+  return n > capacity ? SMC_ERR_CAPACITY : SMC_OK;
+}
+
+smc_status smc_load_configurations(void *ctx, int A, const char *path) {
+  if (!ctx) return SMC_ERR_ARGUMENT;
+  int n = 0;
+  smc_status s = smc_read_configurations(A, path, nullptr, 0, &n);
+  if (s != SMC_OK && s != SMC_ERR_CAPACITY) return s;
+  std::vector<double> xyz((size_t)n * 3 * A);
+  s = smc_read_configurations(A, path, xyz.data(), n, &n);
+  if (s) return s;
+  return smc_set_configurations(ctx, A, xyz.data(), n);
 }
 
 smc_status smc_set_grid_path(void *ctx, int tensor_cores) {

@@ -65,6 +65,13 @@ struct NucleusDev {
   const double *icdf;
   int icdf_m, icdf_nb;
   double icdf_h, icdf_ntot, icdf_dntot_R, icdf_dntot_a;
+  // configuration table of a light nucleus ([nconf][A][3] nucleus-frame
+  // positions, fm; NULL: Woods-Saxon sampling).  Each event takes one
+  // configuration, rotates it by the nucleus orientation and shifts it,
+  // without recentring (Nucleus::populate and GetNucleonPosition,
+  // src/Nucleus.cpp:210-236, 555-574)
+  const double *conf;
+  int nconf;
 };
 
 // Position tangents of the differentiable sampling mode: injected per
@@ -243,7 +250,9 @@ __host__ __device__ __forceinline__ void uniform2f(uint64_t seed, uint64_t event
   u1 = u53f(c[2], c[3]);
 }
 
-enum StreamId : uint32_t { ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5, ST_NBD = 6 };
+enum StreamId : uint32_t {
+  ST_EVENT = 0, ST_PROJ = 1, ST_TARG = 2, ST_DEUT = 3, ST_COLL = 4, ST_FLUCT = 5, ST_NBD = 6, ST_CONF = 7
+};
 __host__ __device__ __forceinline__ uint32_t stream_id(int attempt, uint32_t sid) {
   return ((uint32_t)attempt << 8) | sid;
 }

@@ -279,6 +279,24 @@ class Engine:
         _lib.check(self.lib.smc_kln_table(self.h, _lib.ptr(out), t * t), "smc_kln_table")
         return out
 
+    def set_configurations(self, A: int, xyz) -> None:
+        """Light nuclei of mass number A from a table of configurations,
+        xyz [nconf][A][3] in fm (None or an empty table: Woods-Saxon again);
+        smc_set_configurations."""
+        if xyz is None or len(xyz) == 0:
+            _lib.check(self.lib.smc_set_configurations(self.h, A, None, 0), "smc_set_configurations")
+            return
+        t = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64))
+        if t.ndim != 3 or t.shape[1:] != (A, 3):
+            raise ValueError(f"configurations for A={A}: shape [nconf][{A}][3], got {t.shape}")
+        _lib.check(self.lib.smc_set_configurations(self.h, A, _lib.ptr(t), t.shape[0]), "smc_set_configurations")
+
+    def load_configurations(self, A: int, path: str) -> None:
+        """set_configurations from a file in the reference's layout for A
+        (tables/he3_plaintext.dat, he4_plaintext.dat, carbon_plaintext.dat,
+        oxygen_plaintext.dat); smc_load_configurations."""
+        _lib.check(self.lib.smc_load_configurations(self.h, A, str(path).encode()), "smc_load_configurations")
+
     def autotune(self, n_events: int = 8192) -> dict:
         """Times the splat paths and events per launch on this context's
         workload and keeps the fastest (smc_autotune)."""

@@ -7,6 +7,12 @@ namespace smc {
 MCnucl::MCnucl(ParameterReader *reader) {
   params_ = params_from(*reader);
   check(smc_create(&params_, &ctx_), "smc_create");
+  try {
+    load_light_tables(ctx_, params_);
+  } catch (...) {
+    smc_destroy(ctx_);
+    throw;
+  }
   check(smc_get_info(ctx_, &info_), "smc_get_info");
   npmin_ = params_.npmin;
   npmax_ = params_.npmax;

@@ -32,7 +32,7 @@ const Default kDefaults[] = {
     // extensions (0: the reference's hard-coded value)
     {"proj_R", 0}, {"proj_a", 0}, {"targ_R", 0}, {"targ_a", 0}, {"proj_d_min", 0}, {"targ_d_min", 0},
     {"siginNN_override", 0}, {"kln_npt", 48}, {"kln_nkt", 64}, {"kln_nphi", 32}, {"max_attempts", 0},
-    {"max_collisions", 0}, {"ws_inverse_cdf", 0}, {"kln_exact_band", 0},
+    {"max_collisions", 0}, {"ws_inverse_cdf", 0}, {"kln_exact_band", 0}, {"use_binary", 0},
 };
 
 double val(const ParameterReader &p, const char *name) {
@@ -102,10 +102,29 @@ smc_params params_from(const ParameterReader &p) {
   return s;
 }
 
+void load_light_tables(void *ctx, const smc_params &p) {
+  const int masses[2] = {p.Aproj, p.Atarg};
+  for (int w = 0; w < 2; w++) {
+    const int A = masses[w];
+    const char *file = A == 3 ? "tables/he3_plaintext.dat" : A == 4 ? "tables/he4_plaintext.dat"
+                     : A == 12 ? "tables/carbon_plaintext.dat" : A == 16 ? "tables/oxygen_plaintext.dat" : nullptr;
+    if (!file || (w == 1 && A == masses[0])) continue;   // one table per mass number
+    smc_status s = smc_load_configurations(ctx, A, file);
+    if (s != SMC_OK) throw Error(s, std::string("Error: ") + file + " does not find (or holds no configuration)");
+  }
+}
+
 MakeDensity::MakeDensity(ParameterReader *reader) : reader_(reader) {
   params_ = params_from(*reader);
   check(smc_create(&params_, &ctx_), "smc_create");
+  try {
+    load_light_tables(ctx_, params_);
+  } catch (...) {
+    smc_destroy(ctx_);
+    throw;
+  }
   check(smc_get_info(ctx_, &info_), "smc_get_info");
+  binary_ = val(*reader_, "use_binary") == 1;
   if (val(*reader_, "use_ed"))
     std::fprintf(stderr, "supermc_gb300: use_ed = 1: energy-density outputs (equation of state) are not produced\n");
 }
@@ -114,6 +133,88 @@ MakeDensity::~MakeDensity() { smc_destroy(ctx_); }
 
 void MakeDensity::check(smc_status s, const char *what) const {
   if (s != SMC_OK) throw Error(s, what);
+}
+
+namespace {
+
+// use_binary = 1: each table goes to a NumPy .npy file of the same name in
+// place of the text file, with the text file's columns at full precision
+void write_block(const double *grid, int nx, int ny, const char *stem, bool binary) {
+  char name[512];
+  std::snprintf(name, sizeof(name), "%s_block.%s", stem, binary ? "npy" : "dat");
+  if (binary) {
+    const int64_t shape[2] = {nx, ny};
+    MakeDensity::check_status(smc_write_npy(name, grid, 8, 2, shape, 0), "smc_write_npy");
+  } else {
+    MakeDensity::check_status(smc_write_density_block(grid, nx, ny, name), "smc_write_density_block");
+  }
+}
+
+void write_4col(const double *grid, int nx, int ny, const smc_params &p, double npart, const char *stem,
+                bool binary) {
+  char name[512];
+  std::snprintf(name, sizeof(name), "%s_4col.%s", stem, binary ? "npy" : "dat");
+  if (!binary) {
+    MakeDensity::check_status(
+        smc_write_density_4col(grid, nx, ny, -p.maxx, -p.maxy, p.dx, p.dy, 0.0, npart, name),
+        "smc_write_density_4col");
+    return;
+  }
+  std::vector<double> rows((size_t)nx * ny * 4);
+  for (int i = 0; i < nx; i++)
+    for (int j = 0; j < ny; j++) {
+      double *r = rows.data() + ((size_t)i * ny + j) * 4;
+      r[0] = 0.0;
+      r[1] = -p.maxx + i * p.dx;
+      r[2] = -p.maxy + j * p.dy;
+      r[3] = grid[(size_t)i * ny + j];
+    }
+  const int64_t shape[2] = {(int64_t)nx * ny, 4};
+  MakeDensity::check_status(smc_write_npy(name, rows.data(), 8, 2, shape, 0), "smc_write_npy");
+}
+
+}  // namespace
+
+void MakeDensity::check_status(smc_status s, const char *what) {
+  if (s != SMC_OK) throw Error(s, what);
+}
+
+void MakeDensity::setSd(const float *rho, double *sd) const {
+  const size_t g = (size_t)info_.nx * info_.ny;
+  for (size_t k = 0; k < g; k++) sd[k] = (double)rho[k] * params_.final_factor;
+}
+
+double MakeDensity::gettotaldSdy(const float *rho) const {
+  const size_t g = (size_t)info_.nx * info_.ny;
+  double sum = 0.0;
+  for (size_t k = 0; k < g; k++) sum += (double)rho[k] * params_.dx * params_.dy;
+  return sum;
+}
+
+void MakeDensity::dumpDensityBlock(const char *filename, const double *grid) const {
+  check(smc_write_density_block(grid, info_.nx, info_.ny, filename), "smc_write_density_block");
+}
+
+void MakeDensity::dumpDensity4Col(const char *filename, const double *grid, double npart) const {
+  check(smc_write_density_4col(grid, info_.nx, info_.ny, -params_.maxx, -params_.maxy, params_.dx, params_.dy, 0.0,
+                               npart, filename),
+        "smc_write_density_4col");
+}
+
+void MakeDensity::dumpEccentricities(const char *base_filename, const double *ecc, int n, int from_order,
+                                     int to_order, const double *orientation) const {
+  if (!base_filename) throw Error(SMC_ERR_ARGUMENT, "dumpEccentricities: no file name");
+  std::string pattern;
+  for (const char *c = base_filename; *c; c++) {
+    pattern += *c;
+    if (*c == '%') pattern += '%';   // a literal '%' of the name
+  }
+  pattern += "_%d.dat";
+  if (orientation)
+    check(smc_write_ecc_deformed(ecc, orientation, n, from_order, to_order, pattern.c_str()),
+          "smc_write_ecc_deformed");
+  else
+    check(smc_write_ecc(ecc, n, from_order, to_order, pattern.c_str()), "smc_write_ecc");
 }
 
 void MakeDensity::generateEccTable(int nevent) {
@@ -131,12 +232,28 @@ void MakeDensity::generateEccTable(int nevent) {
     out.ecc = ecc.data();
     if (deformed) out.orientation = ori.data();
     check(smc_generate(ctx_, (uint64_t)done, n, &out), "smc_generate");
-    if (sd && deformed)
+    if (sd && binary_)
+      check(smc_write_ecc_npy(ecc.data(), deformed ? ori.data() : nullptr, n, from, to, "data/sn_ecc_eccp_%d.npy"),
+            "smc_write_ecc_npy");
+    else if (sd && deformed)
       check(smc_write_ecc_deformed(ecc.data(), ori.data(), n, from, to, "data/sn_ecc_eccp_%d.dat"),
             "smc_write_ecc_deformed");
     else if (sd)
       check(smc_write_ecc(ecc.data(), n, from, to, "data/sn_ecc_eccp_%d.dat"), "smc_write_ecc");
   }
+}
+
+// wounded.data / nucl1.data / nucl2.data as .npy: participants [k][3]
+// (x, y, nucleus 1 or 2), projectile [A][2], target [B][2]
+void MakeDensity::write_nucleon_npy(const double *xy, const uint8_t *wounded) {
+  const int A = info_.A, B = info_.B;
+  std::vector<double> part;
+  for (int k = 0; k < A + B; k++)
+    if (wounded[k]) part.insert(part.end(), {xy[2 * k], xy[2 * k + 1], k < A ? 1.0 : 2.0});
+  const int64_t sp[2] = {(int64_t)(part.size() / 3), 3}, s1[2] = {A, 2}, s2[2] = {B, 2};
+  check(smc_write_npy("data/wounded.npy", part.data(), 8, 2, sp, 0), "smc_write_npy");
+  check(smc_write_npy("data/nucl1.npy", xy, 8, 2, s1, 0), "smc_write_npy");
+  check(smc_write_npy("data/nucl2.npy", xy + 2 * (size_t)A, 8, 2, s2, 0), "smc_write_npy");
 }
 
 void MakeDensity::generate_profile_ebe(int nevent) {
@@ -180,31 +297,33 @@ void MakeDensity::generate_profile_ebe(int nevent) {
     for (int e = 0; e < n && event < nevent; e++) {
       // MCnucl::dumpBinaryTable("data/binary.dat") after each event's pairing
       // (src/MakeDensity.cpp:598; src/MCnucl.cpp:1175-1207)
-      check(smc_write_binary_table(coll.data() + (size_t)e * mc * 2, std::min(ncoll[e], mc), "data/binary.dat"),
-            "smc_write_binary_table");
+      const int nc = std::min(ncoll[e], mc);
+      if (binary_) {
+        const int64_t shape[2] = {nc, 2};
+        check(smc_write_npy("data/binary.npy", coll.data() + (size_t)e * mc * 2, 8, 2, shape, 1), "smc_write_npy");
+      } else {
+        check(smc_write_binary_table(coll.data() + (size_t)e * mc * 2, nc, "data/binary.dat"),
+              "smc_write_binary_table");
+      }
       if (cut) {
         double total = 0.0;
         for (size_t k = 0; k < g; k++) total += (double)rho[(size_t)e * g + k] * area;
         if (total < cut_lo || total > cut_hi) continue;
       }
       event++;
-      if (event == nevent)
+      if (event == nevent && binary_)
+        write_nucleon_npy(pos.data() + (size_t)e * AB * 2, wounded.data() + (size_t)e * AB);
+      else if (event == nevent)
         check(smc_write_nucleon_tables(pos.data() + (size_t)e * AB * 2, wounded.data() + (size_t)e * AB, info_.A,
                                        info_.B, "data/wounded.data", "data/nucl1.data", "data/nucl2.data"),
               "smc_write_nucleon_tables");
       if (!sd) continue;
       // MakeDensity::setSd (src/MakeDensity.cpp:2514-2522)
       for (size_t k = 0; k < g; k++) grid[k] = (double)rho[(size_t)e * g + k] * ff;
-      if (four) {
-        std::snprintf(name, sizeof(name), "data/sd_event_%d_4col.dat", event);
-        check(smc_write_density_4col(grid.data(), info_.nx, info_.ny, -params_.maxx, -params_.maxy, params_.dx,
-                                     params_.dy, 0.0, (double)(npart[2 * e] + npart[2 * e + 1]), name),
-              "smc_write_density_4col");
-      }
-      if (block) {
-        std::snprintf(name, sizeof(name), "data/sd_event_%d_block.dat", event);
-        check(smc_write_density_block(grid.data(), info_.nx, info_.ny, name), "smc_write_density_block");
-      }
+      std::snprintf(name, sizeof(name), "data/sd_event_%d", event);
+      if (four)
+        write_4col(grid.data(), info_.nx, info_.ny, params_, (double)(npart[2 * e] + npart[2 * e + 1]), name, binary_);
+      if (block) write_block(grid.data(), info_.nx, info_.ny, name, binary_);
     }
   }
 }
@@ -252,16 +371,9 @@ void MakeDensity::generate_profile_average(int nevent) {
     for (int q = 0; q < no; q++) {
       const double *m = grid[k].data() + (size_t)q * g;
       const int order = from + q;
-      if (four) {
-        std::snprintf(name, sizeof(name), "data/%s_%d_4col.dat", stem[k], order);
-        check(smc_write_density_4col(m, info_.nx, info_.ny, -params_.maxx, -params_.maxy, params_.dx, params_.dy,
-                                     0.0, 0.0, name),
-              "smc_write_density_4col");
-      }
-      if (block) {
-        std::snprintf(name, sizeof(name), "data/%s_%d_block.dat", stem[k], order);
-        check(smc_write_density_block(m, info_.nx, info_.ny, name), "smc_write_density_block");
-      }
+      std::snprintf(name, sizeof(name), "data/%s_%d", stem[k], order);
+      if (four) write_4col(m, info_.nx, info_.ny, params_, 0.0, name, binary_);
+      if (block) write_block(m, info_.nx, info_.ny, name, binary_);
     }
   }
 }

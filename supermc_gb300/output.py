@@ -43,3 +43,30 @@ def write_density_4col(grid, xmin: float, ymin: float, dx: float, dy: float, npa
     lib = _lib.load()
     _lib.check(lib.smc_write_density_4col(_lib.ptr(g), g.shape[0], g.shape[1], xmin, ymin, dx, dy, rapidity, npart,
                                           filename.encode()), "smc_write_density_4col")
+
+
+def write_npy(array, filename: str, append: bool = False) -> None:
+    """A float32 / float64 array as a NumPy .npy file through smc_write_npy
+    (append: grow an appendable file of the same type and trailing shape)."""
+    a = np.ascontiguousarray(array)
+    if a.dtype not in (np.float32, np.float64):
+        a = a.astype(np.float64)
+    shape = np.array(a.shape, dtype=np.int64)
+    lib = _lib.load()
+    _lib.check(lib.smc_write_npy(filename.encode(), a.ctypes.data, a.itemsize, a.ndim, shape.ctypes.data,
+                                 1 if append else 0), "smc_write_npy")
+
+
+def write_ecc_npy(ecc, from_order: int, to_order: int, pattern: str = "data/sn_ecc_eccp_%d.npy",
+                  orientation=None) -> None:
+    """write_ecc's tables as .npy files (smc_write_ecc_npy): the same
+    columns at full precision, appended."""
+    e = np.ascontiguousarray(np.atleast_2d(ecc), dtype=np.float64)
+    o = None
+    if orientation is not None:
+        o = np.ascontiguousarray(np.atleast_2d(orientation), dtype=np.float64)
+        if o.shape != (e.shape[0], 4):
+            raise ValueError("orientation must be [n][4]")
+    lib = _lib.load()
+    _lib.check(lib.smc_write_ecc_npy(_lib.ptr(e), None if o is None else _lib.ptr(o), e.shape[0], from_order,
+                                     to_order, pattern.encode()), "smc_write_ecc_npy")

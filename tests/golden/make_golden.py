@@ -40,6 +40,7 @@ SYSTEMS = {
 
 
 EOS_DIR = os.path.join(REF_ROOT, "EOS")
+TABLES_DIR = os.path.join(REF_ROOT, "tables")
 
 
 def ref_for(args, extra=()):
@@ -177,6 +178,50 @@ def make_native_systems(out, nev):
     np.savez_compressed(os.path.join(out, "ecc_native_systems.npz"), **data)
 
 
+def make_light(out, nev):
+    """Light nuclei from configuration tables.
+    light_nuclei_drand48.npz: Nucleus::populate of 3He, 4He and 12C from the
+    reference's own tables (srand48 / srand seeds 3, 11, 19): the nucleons,
+    and the one configuration each draw used (index rand() % nconf, its
+    [A][3] positions) -- what the oracle needs to redo the draw.
+    ecc_light_systems.npz: the reference's op-9 table (its own sampler) for
+    the systems of tests/systems.py LIGHT_SYSTEMS with the seeded synthetic
+    tables of synthetic_configurations written in the reference's layout."""
+    import ctypes
+    import tempfile
+    sys.path.insert(0, os.path.dirname(HERE))
+    from systems import LIGHT_FILES, LIGHT_SYSTEMS, synthetic_configurations, write_configurations
+    from oracle.oracle import read_configurations
+    libc = ctypes.CDLL(None)
+    libc.srand.argtypes = [ctypes.c_uint]
+    pin = {}
+    for A in (3, 4, 12):
+        tab = read_configurations(os.path.join(TABLES_DIR, LIGHT_FILES[A]), A)
+        ref, _ = ref_for(["auau200"], [f"Aproj={A}"])
+        pin[f"A{A}_nconf"] = np.array(len(tab))
+        for seed in (3, 11, 19):
+            ref.srand(seed)
+            pin[f"A{A}_s{seed}_pos"] = ref.populate(0, 2.5)
+            libc.srand(seed)
+            k = libc.rand() % len(tab)
+            pin[f"A{A}_s{seed}_idx"] = np.array(k)
+            pin[f"A{A}_s{seed}_conf"] = tab[k]
+    np.savez_compressed(os.path.join(out, "light_nuclei_drand48.npz"), **pin)
+    data = {}
+    for name, sysd in LIGHT_SYSTEMS.items():
+        tdir = tempfile.mkdtemp(prefix="smc_light_")
+        for A in {sysd["Aproj"], sysd["Atarg"]}:
+            if A in LIGHT_FILES:
+                write_configurations(os.path.join(tdir, LIGHT_FILES[A]), A, synthetic_configurations(A))
+        extra = [f"Aproj={sysd['Aproj']}", f"Atarg={sysd['Atarg']}", f"ecm={sysd['ecm']}", "ecc_from_order=2",
+                 "ecc_to_order=5"]
+        vals = read_parameters(None, list(SYSTEMS["auau200"]) + extra, strict=False)
+        ref = Reference(parameters_text(vals), eos_dir=EOS_DIR, tables_dir=tdir)
+        ref.srand(7)
+        data[name] = ref.generate_ecc_table(nev)[:, :49]
+    np.savez_compressed(os.path.join(out, "ecc_light_systems.npz"), **data)
+
+
 def make_kln(out):
     ref, vals = ref_for(["pbpb2760"], ["which_mc_model=1", "sub_model=7", "lambda=0.288"])
     ref.lib.refh_kln_setup(2760.0, 0.288)
@@ -256,17 +301,19 @@ def main():
     ap.add_argument("--ref", default=REF_ROOT)
     ap.add_argument("--nev", type=int, default=1500)
     ap.add_argument("--only", choices=["constants", "sampler", "inject", "average", "kln", "native",
-                                       "native_systems", "text"],
+                                       "native_systems", "light", "text"],
                     help="regenerate one fixture only")
     a = ap.parse_args()
     if build_reference(a.ref) is None:
         sys.exit(f"reference tree not found at {a.ref}")
-    global EOS_DIR
+    global EOS_DIR, TABLES_DIR
     EOS_DIR = os.path.join(a.ref, "EOS")
+    TABLES_DIR = os.path.join(a.ref, "tables")
     steps = {"constants": lambda: make_constants(HERE), "sampler": lambda: make_sampler(HERE),
              "inject": lambda: make_inject(HERE), "average": lambda: make_average(HERE),
              "kln": lambda: make_kln(HERE), "native": lambda: make_native_tables(HERE, a.nev),
              "native_systems": lambda: make_native_systems(HERE, a.nev),
+             "light": lambda: make_light(HERE, a.nev),
              "text": lambda: make_text(HERE)}
     for k, f in steps.items():
         if a.only in (None, k):

@@ -40,12 +40,57 @@ OVERRIDE_SYSTEMS = {
 }
 ALL_SYSTEMS = dict(SYSTEMS, **NATIVE_SYSTEMS, **OVERRIDE_SYSTEMS)
 
+# Light nuclei from configuration tables (src/Nucleus.cpp:150-164, 210-236):
+# 3He+Au, 12C+Au and O+O at 200 GeV, with the synthetic tables below.
+LIGHT_SYSTEMS = {
+    "he3au200": dict(BASE, Aproj=3, Atarg=197, ecm=200),
+    "cau200": dict(BASE, Aproj=12, Atarg=197, ecm=200),
+    "oo200": dict(BASE, Aproj=16, Atarg=16, ecm=200),
+}
+# the reference's file for each light mass number (read from tables/)
+LIGHT_FILES = {3: "he3_plaintext.dat", 4: "he4_plaintext.dat", 12: "carbon_plaintext.dat",
+               16: "oxygen_plaintext.dat"}
 
-def oracle_nuclei(oracle, vals):
+
+def synthetic_configurations(A: int, nconf: int = 1500):
+    """A seeded stand-in for a light nucleus's configuration table:
+    [nconf][A][3] positions (fm) from an isotropic Gaussian with the
+    nucleus's rms charge radius, each configuration's centre of mass at the
+    origin (as in the reference's tables)."""
+    import numpy as np
+    rms = {3: 1.97, 4: 1.68, 12: 2.47, 16: 2.70}.get(A, 1.2 * A ** (1.0 / 3.0))
+    rng = np.random.default_rng(7000 + A)
+    x = rng.normal(0.0, rms / np.sqrt(3.0), size=(nconf, A, 3))
+    return x - x.mean(axis=1, keepdims=True)
+
+
+def write_configurations(path, A: int, xyz):
+    """A configuration table in the reference's file layout for A
+    (src/Nucleus.cpp:383-478): he3 records carry 4 further fields after the
+    9 coordinates, carbon records 2 fields before the 36, the others none;
+    17 significant digits, so the file reads back exactly."""
+    lead, trail = (2 if A == 12 else 0), (4 if A == 3 else 0)
+    with open(path, "w") as f:
+        for k, conf in enumerate(xyz):
+            fields = ["0.0"] * lead + ["%.17g" % v for v in conf.reshape(-1)] + ["0.0"] * (trail - 1 if trail else 0)
+            if trail:
+                fields.append(str(k + 1))
+            f.write(" ".join(fields) + "\n")
+
+
+def light_engine_tables(vals):
+    """{A: table} of the light nuclei of a parameter set."""
+    return {A: synthetic_configurations(A) for A in {int(vals["aproj"]), int(vals["atarg"])} if A in LIGHT_FILES}
+
+
+def oracle_nuclei(oracle, vals, tables=None):
     """The oracle's projectile and target nuclei of a parameter set (mass
-    number, deformation and the optional Woods-Saxon / hard-core keys)."""
+    number, deformation and the optional Woods-Saxon / hard-core keys);
+    tables {A: [nconf][A][3]}: configuration tables of light nuclei."""
+    tables = tables or {}
     return tuple(oracle.nucleus(int(vals[f"a{w}"]), int(vals[f"{w}_deformed"]), vals[f"{w}_r"], vals[f"{w}_a"],
-                                vals[f"{w}_d_min"]) for w in ("proj", "targ"))
+                                vals[f"{w}_d_min"], conf=tables.get(int(vals[f"a{w}"])))
+                 for w in ("proj", "targ"))
 
 
 def values(system: dict, **over) -> dict:

@@ -112,3 +112,54 @@ def test_deformed_eccentricity_layout(lib, texts, tmp_path):
             assert got[k][-64:] == "".join("%16.8g" % v for v in ori[k]), (name, k)
     with pytest.raises(Exception):
         _lib.check(lib.smc_write_ecc_deformed(_lib.ptr(ecc), None, n, 2, 3, pattern), "smc_write_ecc_deformed")
+
+
+def test_npy_files_read_by_numpy(lib, tmp_path):
+    """smc_write_npy: numpy.load gives the array back; appends grow the
+    first dimension; a mismatched append is refused."""
+    from supermc_gb300.output import write_npy
+    rng = np.random.default_rng(4)
+    for dt in (np.float32, np.float64):
+        for shape in ((7,), (5, 9), (3, 4, 6)):
+            a = rng.normal(size=shape).astype(dt)
+            f = str(tmp_path / f"a_{np.dtype(dt).name}_{len(shape)}.npy")
+            write_npy(a, f)
+            b = np.load(f)
+            assert b.dtype == dt and b.shape == a.shape
+            np.testing.assert_array_equal(b, a)
+    f = str(tmp_path / "grow.npy")
+    a, b = rng.normal(size=(4, 3)), rng.normal(size=(2, 3))
+    write_npy(a, f, append=True)
+    write_npy(b, f, append=True)
+    np.testing.assert_array_equal(np.load(f), np.concatenate([a, b]))
+    with pytest.raises(_lib.SmcError):   # other trailing shape
+        write_npy(rng.normal(size=(2, 4)), f, append=True)
+    with pytest.raises(_lib.SmcError):   # other type
+        write_npy(rng.normal(size=(2, 3)).astype(np.float32), f, append=True)
+    (tmp_path / "text.npy").write_text("not a npy file\n" * 20)
+    with pytest.raises(_lib.SmcError):
+        write_npy(a, str(tmp_path / "text.npy"), append=True)
+    np.testing.assert_array_equal(np.load(f), np.concatenate([a, b]))   # untouched by the refusals
+
+
+@pytest.mark.parametrize("deformed", [False, True])
+def test_ecc_npy_holds_the_text_columns(lib, tmp_path, deformed):
+    """sn_ecc_eccp_<order>.npy holds the columns of the text lines; the text
+    is those values printed to 8 (Npart, Ncoll: 5) significant digits."""
+    from supermc_gb300.output import write_ecc, write_ecc_npy
+    rng = np.random.default_rng(9)
+    n = 12
+    ecc = rng.normal(size=(n, 49))
+    ecc[:, 45:47] = rng.integers(2, 400, size=(n, 2))
+    ori = np.column_stack([rng.uniform(-1, 1, n), rng.uniform(0, 6.28, n)] * 2) if deformed else None
+    for half in (slice(0, 5), slice(5, n)):   # two appends
+        write_ecc(ecc[half], 2, 4, str(tmp_path / "e_%d.dat"), orientation=None if ori is None else ori[half])
+        write_ecc_npy(ecc[half], 2, 4, str(tmp_path / "e_%d.npy"), orientation=None if ori is None else ori[half])
+    for order in (2, 3, 4, 10):
+        b = np.load(tmp_path / f"e_{order}.npy")
+        t = np.loadtxt(tmp_path / f"e_{order}.dat", ndmin=2)
+        cols = (list(range(5 * (order - 1), 5 * order)) if order < 10 else list(range(45))) + [45, 46, 47, 48]
+        want = ecc[:, cols] if ori is None else np.column_stack([ecc[:, cols], ori])
+        np.testing.assert_array_equal(b, want)
+        assert t.shape == b.shape
+        np.testing.assert_allclose(t, b, rtol=6e-8, atol=1e-300)
