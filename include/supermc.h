@@ -155,6 +155,20 @@ typedef struct smc_outputs {
                            injected nuclei.  The deformed layout of the
                            eccentricity files carries it
                            (smc_write_ecc_deformed)                          */
+  /* The fields below are not produced by the graph-captured batches
+   * (smc_generate_graph, smc_generate_mixed_graph: SMC_ERR_ARGUMENT). */
+  float *rho_pt;        /* [n][nx][ny][nbins] MC-KLN p_T-differential dN/dy
+                           d^2p_T per cell (MCnucl::setDensity(iy, ipt) for
+                           every bin, src/MCnucl.cpp:626-687, getRho(iy, i,
+                           j, ipt)); needs smc_kln_pt_table first (nbins are
+                           its bins; ignored before it)                      */
+  float *rho_binary;    /* [n][nx][ny] binary-collision density
+                           (MCnucl::calculate_rho_binary, src/MCnucl.cpp:
+                           481-531): a unit-normalised Gaussian (or disk) per
+                           collision, r <= 5w                                */
+  float *spectator_a, *spectator_b;   /* [n][nx][ny] spectator densities of
+                           the projectile and the target
+                           (MCnucl::calculate_spectator_density, :534-614)   */
 } smc_outputs;
 
 /* MCnucl::MCnucl + MakeDensity::MakeDensity: validates the configuration,
@@ -411,6 +425,17 @@ smc_status smc_reset_stats(void *ctx);
 /* MC-KLN dN/dy table (MCnucl::makeTable, src/MCnucl.cpp:911-960): copies the
  * current table ([tmax][tmax] doubles, rapidity slice 0) to host. */
 smc_status smc_kln_table(void *ctx, double *host_table, int capacity);
+/* MCnucl::makeTable(ptmin, dpt, iPtmax) (src/MCnucl.cpp:967-1025): the
+ * p_T-differential table dN/dy d^2p_T at p_T = pt_min + k d_pt, k < nbins
+ * (the PT_Min, d_PT, MaxPT of src/MakeDensity.cpp:67-71), on the nodes
+ * (i dT, j dT) of the p_T-integrated table: KLNModel::getdNdy at fixed p_T
+ * (src/KLNModel.cpp:96-124, the (k_T, phi) integral of func_simpson,
+ * :281-322), built on the GPU in FP64 by the k_T and phi Gauss-Legendre
+ * rules of the p_T-integrated table (the reference integrates by adaptive
+ * Simpson to 1e-4 relative).  The table stays in the context for
+ * smc_outputs.rho_pt.  host_table (may be NULL): receives it,
+ * [tmax][tmax][nbins] doubles (capacity in doubles).  MC-KLN only. */
+smc_status smc_kln_pt_table(void *ctx, double pt_min, double d_pt, int nbins, double *host_table, size_t capacity);
 
 /* Text outputs in the reference's layouts (host code, no GPU), so that the
  * reference's downstream tools read the results unchanged.
@@ -471,6 +496,24 @@ smc_status smc_write_binary_table(const double *xy, int ncoll, const char *filen
  * file name may be NULL. */
 smc_status smc_write_nucleon_tables(const double *xy, const uint8_t *wounded, int A, int B, const char *participants,
                                     const char *proj, const char *targ);
+/* MCnucl::dumpparticipantTable (src/MCnucl.cpp:1213-1220): appends the
+ * event's participants (the wounded.data lines, Nucleus::dumpParticipants,
+ * src/Nucleus.cpp:753-764) to `filename` (the Jet mode's
+ * ParticipantTable_event_<n>.dat). */
+smc_status smc_write_participant_table(const double *xy, const uint8_t *wounded, int A, int B, const char *filename);
+/* MCnucl::getSpectators + dumpSpectatorsTable (src/MCnucl.cpp:1223-1265):
+ * the non-participants, projectile then target in nucleon order, x, y and
+ * the beam rapidity +Y (projectile) or -Y (target) of sqrt(s) = ecm
+ * (scientific, 4 digits); `filename` overwritten (Spectators_event_<n>.dat). */
+smc_status smc_write_spectator_table(const double *xy, const uint8_t *wounded, int A, int B, double ecm,
+                                     const char *filename);
+/* MakeDensity::dumpDensity5Col / dumpDesityptCol (src/MakeDensity.cpp:
+ * 2612-2661): the header "% <npart>= .. xmax= .. ymax= .. Ptmax= ..", then
+ * one line per cell (x-major) of its nbins p_T values times `scale`
+ * (finalFactor for setSd), %22.12e each.  data [nx][ny][nbins]
+ * (smc_outputs.rho_pt of one event). */
+smc_status smc_write_density_pt(const float *data, int nx, int ny, int nbins, double npart, double scale,
+                                const char *filename);
 
 /* smc_inject without any device allocation.  No counterpart in the
  * reference (which allocates host arrays freely); it exists for callers that

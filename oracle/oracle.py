@@ -153,6 +153,9 @@ class Oracle:
         lib.smco_kln_init.argtypes = [ctypes.POINTER(KLN), ctypes.c_double, ctypes.c_double]
         lib.smco_kln_integrand.restype = ctypes.c_double
         lib.smco_kln_integrand.argtypes = [ctypes.POINTER(KLN), ctypes.c_double, ctypes.c_double, _D]
+        lib.smco_kln_dndy_pt.restype = ctypes.c_double
+        lib.smco_kln_dndy_pt.argtypes = [ctypes.POINTER(KLN), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_int, ctypes.c_int]
         lib.smco_kln_dndy.restype = ctypes.c_double
         lib.smco_kln_dndy.argtypes = [ctypes.POINTER(KLN), ctypes.c_double, ctypes.c_double,
                                       ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -429,6 +432,8 @@ class Reference:
         lib.refh_kln_prepare.argtypes = [ctypes.c_double] * 3
         lib.refh_kln_integrand.restype = ctypes.c_double
         lib.refh_kln_integrand.argtypes = [ctypes.c_double] * 6
+        lib.refh_kln_dndy_pt.restype = ctypes.c_double
+        lib.refh_kln_dndy_pt.argtypes = [ctypes.c_double] * 4
         lib.refh_kln_dndy.restype = ctypes.c_double
         lib.refh_kln_dndy.argtypes = [ctypes.c_double] * 3
         self.workdir = workdir or tempfile.mkdtemp(prefix="smc_ref_")

@@ -379,6 +379,8 @@ void refh_kln_prepare(double y, double ta, double tb) {
   g_kln->getdNdy(y, ta, tb, -1.0, 1);
 }
 double refh_kln_dndy(double y, double ta, double tb) { return g_kln->getdNdy(y, ta, tb, -1.0, 1); }
+// dN/dy d^2p_T at fixed p_T (the adaptive-Simpson path, src/KLNModel.cpp:115-119)
+double refh_kln_dndy_pt(double y, double ta, double tb, double pt) { return g_kln->getdNdy(y, ta, tb, pt, 1); }
 double refh_kln_norm() { return KLNModel::Norm; }
 
 }  // extern "C"

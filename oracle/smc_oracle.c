@@ -1669,6 +1669,49 @@ double smco_kln_dndy(const smco_kln *k, double ta, double tb, int npt, int nkt, 
   return 1.0 * k->g2hfac * Norm * sum * 9. / 32.;
 }
 
+/* KLNModel::getdNdy at a fixed p_T (src/KLNModel.cpp:96-124, the pt > 0
+ * branch): g2hfac Norm 9/32 times the integral of func_simpson (:281-322)
+ * over k_T in [0, pt] and phi in [0, 2 pi] -- alpha_s(max(k1^2, k2^2,
+ * m_T^2)) phi_A(k1^2) phi_B(k2^2) k_T / m_T^2 / 4 with m_T = p_T --
+ * taken by the Gauss-Legendre rules of nkt and nphi nodes (the reference
+ * integrates by adaptive Simpson, relative precision 1e-4: SimpsonPrecision,
+ * :27).  The rows of MCnucl::makeTable(ptmin, dpt, iPtmax),
+ * src/MCnucl.cpp:967-1025. */
+double smco_kln_dndy_pt(const smco_kln *k, double ta, double tb, double pt, int nkt, int nphi) {
+  double *xk = (double *)malloc(sizeof(double) * 2 * (nkt + nphi));
+  double *wk = xk + nkt, *xf = wk + nkt, *wf = xf + nphi;
+  smco_gauss_legendre01(nkt, xk, wk);
+  smco_gauss_legendre01(nphi, xf, wf);
+  double mt = pt;
+  double x1 = mt / k->ecm * exp(k->y), x2 = mt / k->ecm / exp(k->y);
+  double sum = 0;
+  if (!(x1 > 1.0 || x2 > 1.0) && pt > 0) {
+    double qs2a = ta * 2. / 1.53 * pow(0.01 / x1, k->lambda);
+    double qs2b = tb * 2. / 1.53 * pow(0.01 / x2, k->lambda);
+    for (int b = 0; b < nkt; b++) {
+      double kt = pt * xk[b], sb = 0;
+      for (int c = 0; c < nphi; c++) {
+        double phi = 2 * M_PI * xf[c];
+        double ktsq1 = 0.25 * (pt * pt + kt * kt + 2 * kt * pt * cos(phi));
+        double ktsq2 = 0.25 * (pt * pt + kt * kt - 2 * pt * kt * cos(phi));
+        double fnc = kln_wave(k, qs2a, x1, ktsq1) * kln_wave(k, qs2b, x2, ktsq2);
+        double scale = ktsq1 > ktsq2 ? ktsq1 : ktsq2;
+        double alp = kln_alpha(k, scale > mt * mt ? scale : mt * mt);
+        double result = alp * fnc;
+        result *= kt;
+        result /= mt * mt;
+        result /= 4.0;
+        sb += wf[c] * (2 * M_PI) * result;
+      }
+      sum += wk[b] * pt * sb;
+    }
+  }
+  free(xk);
+  double CF = (3.0 * 3.0 - 1.0) / (2 * 3.0);
+  double Norm = 2. / CF / (KLN_HBARC * KLN_HBARC);
+  return 1.0 * k->g2hfac * Norm * sum * 9. / 32.;
+}
+
 /* ================================================================== */
 /* op-9 event loop (MakeDensity.cpp:2108-2240) for CPU-baseline timing  */
 long smco_run_ecc_table(const smco_params *p, const smco_nucleus *nA, const smco_nucleus *nB,

@@ -182,6 +182,7 @@ void smco_gauss_legendre01(int n, double *x, double *w);
  * (npt x nkt x nphi on the unit cube), times g2hfac*Norm*9/32
  * (KLNModel.cpp:97-125) */
 double smco_kln_dndy(const smco_kln *k, double ta, double tb, int npt, int nkt, int nphi);
+double smco_kln_dndy_pt(const smco_kln *k, double ta, double tb, double pt, int nkt, int nphi);
 
 /* ------------------------------------------------------------------ */
 /* whole event loop (MakeDensity::generateEccTable, MakeDensity.cpp:2108)

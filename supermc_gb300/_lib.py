@@ -30,7 +30,9 @@ EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "sm
            "smc_average_binned", "smc_adjoint", "smc_autotune", "smc_generate_graph", "smc_average_profiles",
            "smc_write_binary_table", "smc_write_nucleon_tables", "smc_write_ecc_deformed",
            "smc_generate_mixed_graph", "smc_sample_nuclei", "smc_set_configurations",
-           "smc_load_configurations", "smc_read_configurations", "smc_write_npy", "smc_write_ecc_npy"]
+           "smc_load_configurations", "smc_read_configurations", "smc_write_npy", "smc_write_ecc_npy",
+           "smc_kln_pt_table", "smc_write_participant_table", "smc_write_spectator_table",
+           "smc_write_density_pt"]
 
 
 class SmcError(RuntimeError):
@@ -91,6 +93,8 @@ class SmcOutputs(ctypes.Structure):
         ("npart", ctypes.c_void_p), ("ncoll", ctypes.c_void_p), ("b", ctypes.c_void_p),
         ("attempts", ctypes.c_void_p), ("positions", ctypes.c_void_p), ("wounded", ctypes.c_void_p),
         ("tangents", ctypes.c_void_p), ("collisions", ctypes.c_void_p), ("orientation", ctypes.c_void_p),
+        ("rho_pt", ctypes.c_void_p), ("rho_binary", ctypes.c_void_p), ("spectator_a", ctypes.c_void_p),
+        ("spectator_b", ctypes.c_void_p),
     ]
 
 
@@ -147,6 +151,7 @@ def load() -> ctypes.CDLL:
     lib.smc_write_npy.argtypes = [ctypes.c_char_p, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int]
     lib.smc_write_ecc_npy.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
     lib.smc_kln_table.argtypes = [vp, vp, ctypes.c_int]
+    lib.smc_kln_pt_table.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, vp, ctypes.c_size_t]
     lib.smc_set_timing.argtypes = [vp, ctypes.c_int]
     lib.smc_set_grid_path.argtypes = [vp, ctypes.c_int]
     lib.smc_write_ecc.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
@@ -158,6 +163,10 @@ def load() -> ctypes.CDLL:
     lib.smc_write_nucleon_tables.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p,
                                              ctypes.c_char_p]
     lib.smc_reset_stats.argtypes = [vp]
+    lib.smc_write_participant_table.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
+    lib.smc_write_spectator_table.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_char_p]
+    lib.smc_write_density_pt.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_char_p]
     lib.smc_average.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                 ctypes.c_int, vp, vp, ctypes.POINTER(ctypes.c_int)]
     lib.smc_inject_noalloc.argtypes = [ctypes.POINTER(SmcParams), ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]

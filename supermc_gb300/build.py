@@ -22,7 +22,7 @@ EXE = os.path.join(OUT_DIR, "superMC")
 # one event through the MCnucl call surface (host/MCnucl.h), for its test
 MCNUCL_SOURCES = ["ParameterReader.cpp", "MakeDensity.cpp", "MCnucl.cpp", "mcnucl_event.cpp"]
 MCNUCL_EXE = os.path.join(OUT_DIR, "mcnucl_event")
-SOURCES = ["smc_capi.cu", "k_sample_pair.cu", "k_grid.cu", "k_kln.cu", "k_average.cu", "smc_noalloc.cu", "k_grid_tc.cu", "k_adjoint.cu", "smc_output.cpp"]
+SOURCES = ["smc_capi.cu", "k_sample_pair.cu", "k_grid.cu", "k_kln.cu", "k_kln_cells.cu", "k_average.cu", "smc_noalloc.cu", "k_grid_tc.cu", "k_adjoint.cu", "smc_output.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]

@@ -460,18 +460,20 @@ __device__ __forceinline__ void cut_interval(const DevParams &P, const double *s
 // The hot-spot region of dumpEccentricities as a bit mask over the grid
 // (one bit per cell, rows of ceil(ny/32) words): the union of the
 // participant boxes on the reference's lattice (ranges mx0..my1 of the
-// participant sources, src/MakeDensity.cpp:2341-2359).
+// participant sources, src/MakeDensity.cpp:2341-2359).  NT: threads of the
+// block (0: blockDim.x).
 template <int NT>
 __device__ __forceinline__ void hotspot_mask(const DevParams &P, const EventRec &rec, const Source *S, uint32_t *mask) {
   const int tid = threadIdx.x;
+  const int nt = NT > 0 ? NT : (int)blockDim.x;
   const int nx = P.nx, ny = P.ny;
   const int nw = (ny + 31) / 32;
-  for (int k = tid; k < nx * nw; k += NT) mask[k] = 0;
+  for (int k = tid; k < nx * nw; k += nt) mask[k] = 0;
   __syncthreads();
   // sources in chunks of 32 per warp; the lanes then take the (source, row)
   // pairs of the chunk's boxes, so that all lanes set bits
   const int lane = tid & 31;
-  for (int s0 = (tid >> 5) * 32; s0 < rec.nsrc; s0 += NT) {
+  for (int s0 = (tid >> 5) * 32; s0 < rec.nsrc; s0 += nt) {
     int r0 = 0, r1 = 0, c0 = 0, c1 = 0;
     if (s0 + lane < rec.nsrc) {
       const Source &src = S[s0 + lane];
@@ -519,10 +521,14 @@ __device__ __forceinline__ void hotspot_mask(const DevParams &P, const EventRec 
   __syncthreads();
 }
 
+// The eccentricity pass of dumpEccentricities over the event's density
+// (centre of mass already known: xo, yo are the grid coordinates relative
+// to it).  NT: threads of the block (0: blockDim.x).
 template <int LO, int HI, int NT>
 __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, const Source *S, const float *rho, uint32_t *mask,
                         const float *xo, const float *yo, float2 *red, double tot0, double *ecc_out) {
   const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+  const int nt = NT > 0 ? NT : (int)blockDim.x, nwarps = nt / 32;
   const int ny = P.ny;
   const int nw = (ny + 31) / 32;
   // ---- eccentricity mask from the participant boxes
@@ -537,8 +543,10 @@ __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, co
 #pragma unroll
   for (int k = 0; k < NO; k++) a_re2[k] = a_im2[k] = a_ren[k] = a_imn[k] = a_np[k] = 0.f;
   const int from = P.ecc_from, to = P.ecc_to;
-  // warps take (row, 32-column block) items of the bounding box, lanes the columns
-  const int nbj = rec.jmax > rec.jmin ? (rec.jmax - rec.jmin + 31) >> 5 : 0;
+  // warps take (row, 32-column block) items of the bounding box, lanes the
+  // columns; blocks aligned to 32 columns (one mask word per item)
+  const int jlo = rec.jmin & ~31;
+  const int nbj = rec.jmax > rec.jmin ? (rec.jmax - jlo + 31) >> 5 : 0;
   const int nitem = rec.imax > rec.imin ? (rec.imax - rec.imin) * nbj : 0;
   // the next item's density is loaded before the current one is processed;
   // (ib, jb): row and column block of the warp's next item
@@ -547,20 +555,20 @@ __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, co
     float v = 0.f;
     if (c < nitem) {
       i = rec.imin + ib;
-      j = rec.jmin + (jb << 5) + lane;
-      if (j < rec.jmax) v = rho[(size_t)i * ny + j];
+      j = jlo + (jb << 5) + lane;
+      if (j >= rec.jmin && j < rec.jmax) v = rho[(size_t)i * ny + j];
     }
-    jb += NT / 32;   // nbj >= 1 whenever there are items: at most NT/32 steps
+    jb += nwarps;   // nbj >= 1 whenever there are items: at most nwarps steps
     if (nbj > 0)
       while (jb >= nbj) { jb -= nbj; ib++; }
     return v;
   };
   int i_next = 0, j_next = 0;
   float d_next = fetch(wid, i_next, j_next);
-  for (int c = wid; c < nitem; c += NT / 32) {
+  for (int c = wid; c < nitem; c += nwarps) {
     const int i = i_next, j = j_next;
     const float d = d_next;
-    d_next = fetch(c + NT / 32, i_next, j_next);
+    d_next = fetch(c + nwarps, i_next, j_next);
     if (d == 0.f) continue;
     float x = xo[i], y = yo[j];
     float r2 = x * x + y * y;
@@ -573,7 +581,9 @@ __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, co
     for (int k = 1; k < 10; k++) a_rn[k] += rp[k] * d;
     bool imp = (mask[i * nw + (j >> 5)] >> (j & 31)) & 1u;
     if (!imp) continue;
-    float inv_r = r > 0.f ? 1.f / r : 0.f;
+    // 1/r only enters the r^2-weighted sums of orders >= 3 (approximate
+    // reciprocal square root, 2^-22 relative)
+    const float inv_r = r2 > 0.f ? rsqrtf(r2) : 0.f;
     a_norm += r2 * d;
     float zr = x, zi = y;   // z^n
 #pragma unroll
@@ -635,7 +645,7 @@ __device__ __noinline__ void moments(const DevParams &P, const EventRec &rec, co
   __shared__ double s_tot[64];
   if (tid < NV) {
     double t = 0;
-    for (int w = 0; w < NT / 32; w++) t += (double)red[w * 64 + tid].x + (double)red[w * 64 + tid].y;
+    for (int w = 0; w < nwarps; w++) t += (double)red[w * 64 + tid].x + (double)red[w * 64 + tid].y;
     s_tot[tid] = t;
   }
   __syncthreads();

@@ -230,18 +230,19 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
 //     src/MCnucl.cpp:534-614): the spectators, projectile into plane 1,
 //     target into plane 2.
 // Both cut at dc <= 25 w^2 (dc <= dsq for disks), the SRC_COLL rule; every
-// other record becomes a mask-only record with an empty window.
+// other record becomes a mask-only record with an empty window.  The view's
+// record carries the bounding box of its own windows.
 __global__ void k_avg_view(DevParams P, int n_events, const EventRec *recs, const Source *in, Source *out, int mode,
                            EventRec *vrecs) {
   const bool disk = P.shape_of_nucleons == 1;
   const float w_unit = disk ? (float)(10.0 / P.sigin) : (float)P.peak;
+  __shared__ int s_box[4];   // the view's window bounds: imin, imax, jmin, jmax
   for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
     const int ns = recs[e].nsrc;
-    if (threadIdx.x == 0) {   // the view's splat sources may lie anywhere in the records
-      EventRec r = recs[e];
-      r.nsplat = ns;
-      vrecs[e] = r;
+    if (threadIdx.x == 0) {
+      s_box[0] = P.nx; s_box[1] = 0; s_box[2] = P.ny; s_box[3] = 0;
     }
+    __syncthreads();
     for (int k = threadIdx.x; k < ns; k += blockDim.x) {
       Source s = in[(size_t)e * P.max_src + k];
       const int kind = s.kind & 15;
@@ -256,8 +257,20 @@ __global__ void k_avg_view(DevParams P, int n_events, const EventRec *recs, cons
         s.kind = 3;
         s.xl = s.xr = s.yl = s.yr = 0;
       }
+      if (s.kind != 3 && s.xr > s.xl && s.yr > s.yl) {
+        atomicMin(&s_box[0], (int)s.xl); atomicMax(&s_box[1], (int)s.xr);
+        atomicMin(&s_box[2], (int)s.yl); atomicMax(&s_box[3], (int)s.yr);
+      }
       out[(size_t)e * P.max_src + k] = s;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) {   // the view's splat sources may lie anywhere in the records
+      EventRec r = recs[e];
+      r.nsplat = ns;
+      r.imin = s_box[0]; r.imax = s_box[1]; r.jmin = s_box[2]; r.jmax = s_box[3];
+      vrecs[e] = r;
+    }
+    __syncthreads();
   }
 }
 

@@ -43,7 +43,7 @@ static_assert(kRU % 4 == 0, "units are read four rows at a time");
 // number of included columns (0: the source misses the row)
 struct GridLayout {
   int nyp, mw, np;
-  size_t off_acc, off_list, off_grp, off_exw, off_ja, off_len, off_cmask, off_xg, off_yg, off_red, total;
+  size_t off_acc, off_list, off_grp, off_exw, off_ja, off_len, off_xg, off_yg, off_red, total;
 };
 
 __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np) {
@@ -63,7 +63,6 @@ __host__ __device__ inline GridLayout grid_layout(int nx, int ny, int mw, int np
   L.off_exw = o; o += sizeof(float) * kGS * kR;
   L.off_ja = o; o += sizeof(int) * kGS * kR;
   L.off_len = o; o += sizeof(int) * kGS * kR;
-  L.off_cmask = o; o += sizeof(uint32_t) * kGW * np * (L.nyp / 32);
   o = (o + 15) / 16 * 16;
   L.off_xg = o; o += sizeof(float) * 2 * nx;   // grid x, then x - x_cm
   L.off_yg = o; o += sizeof(float) * 2 * L.nyp;
@@ -149,11 +148,11 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
   float *p_exw = reinterpret_cast<float *>(smem + L.off_exw);
   int *p_ja = reinterpret_cast<int *>(smem + L.off_ja);
   int *p_len = reinterpret_cast<int *>(smem + L.off_len);
-  uint32_t *cmask = reinterpret_cast<uint32_t *>(smem + L.off_cmask);   // [block][plane][kGW]: sources reaching it
   float *xg = reinterpret_cast<float *>(smem + L.off_xg);
   float *yg = reinterpret_cast<float *>(smem + L.off_yg);
   float2 *red = reinterpret_cast<float2 *>(smem + L.off_red);
   __shared__ int s_status;
+  __shared__ int s_wcnt[kWarps];
   __shared__ double s_cm[3];
 
   const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
@@ -187,8 +186,10 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
     for (int r0 = 0; r0 < nx; r0 += kR) {
       const int rows = min(kR, nx - r0);
       const bool active = r0 + rows > rec.imin && r0 < rec.imax;
+      // fresh: no group accumulated yet (the accumulators are not read back,
+      // and a strip no source reaches has no valid accumulators)
+      bool fresh = true;
       if (active) {
-        for (int k = tid; k < np * kR * nyp; k += kGT) acc[k] = 0.f;
         for (int c0 = 0; c0 < rec.nsplat; c0 += kGT) {   // the splat sources lead the records
           // compact the sources of this chunk that reach the strip
           int k = c0 + tid;
@@ -198,20 +199,21 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
             hit = s.xl < r0 + rows && s.xr > r0 && s.yr > s.yl && (s.kind & 15) < 3;   // kinds >= 3: no splat
           }
           unsigned bal = __ballot_sync(0xffffffffu, hit);
-          __syncthreads();
-          if (lane == 0) list[kGT - 1 - wid] = __popc(bal);
+          if (lane == 0) s_wcnt[wid] = __popc(bal);
           __syncthreads();
           int off = 0, tot = 0;
           for (int q = 0; q < kWarps; q++) {
-            int cq = list[kGT - 1 - q];
+            int cq = s_wcnt[q];
             off += q < wid ? cq : 0;
             tot += cq;
           }
-          __syncthreads();
           if (hit) list[off + __popc(bal & ((1u << lane) - 1u))] = k;
           __syncthreads();
           for (int g0 = 0; g0 < tot; g0 += kGS) {
             const int gn = min(kGS, tot - g0);
+            // row factors and included column intervals, one per (source,
+            // row); the row-0 thread of a source also stores it for the
+            // accumulating warps
             for (int t = tid; t < gn; t += kGT) {
               const Source &s = S[list[g0 + t]];
               GroupSrc g;
@@ -222,25 +224,9 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
               grp[t] = g;
             }
             __syncthreads();
-            // per (32-column block, plane): the group's sources whose window reaches it
-            for (int it = wid; it < (nyp / 32) * np; it += kWarps) {
-              const int jb0 = (it / np) * 32, pl = it - (it / np) * np;
-#pragma unroll
-              for (int h = 0; h < kGW; h++) {
-                const int q = h * 32 + lane;
-                bool in = false;
-                if (q < gn) {
-                  const GroupSrc &g = grp[q];
-                  in = g.plane == pl && g.yr > jb0 && g.yl < jb0 + 32 && g.yr > g.yl;
-                }
-                const unsigned b = __ballot_sync(0xffffffffu, in);
-                if (lane == 0) cmask[it * kGW + h] = b;
-              }
-            }
-            // row factors and included column intervals, one per (source, row)
             for (int t = tid; t < gn * kR; t += kGT) {
               const int q = t / kR, r = t - q * kR;
-              const GroupSrc &g = grp[q];
+              const GroupSrc g = grp[q];
               const int i = r0 + r;
               float exw = 0.f;
               int ja = 0, len = 0;
@@ -265,14 +251,29 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
             for (int u = wid; u < (nyp / 32) * kSplit; u += kWarps) {
               const int jb = u / kSplit, j = jb * 32 + lane, rh = (u - jb * kSplit) * kRU;
               const float jf = (float)j;
+              // the group's sources whose window reaches this block: lane q
+              // of word h tests source 32 h + q
+              int qpl[kGW];
+              bool qin[kGW];
+#pragma unroll
+              for (int h = 0; h < kGW; h++) {
+                const int q = h * 32 + lane;
+                qin[h] = false;
+                qpl[h] = 0;
+                if (q < gn) {
+                  const GroupSrc &g = grp[q];
+                  qin[h] = g.yr > jb * 32 && g.yl < jb * 32 + 32 && g.yr > g.yl;
+                  qpl[h] = g.plane;
+                }
+              }
               for (int pl = 0; pl < np; pl++) {
                 float *ab = acc + ((size_t)pl * kR + rh) * nyp + j;
                 float a[kRU];
 #pragma unroll
-                for (int r = 0; r < kRU; r++) a[r] = ab[r * nyp];
+                for (int r = 0; r < kRU; r++) a[r] = fresh ? 0.f : ab[r * nyp];
 #pragma unroll
                 for (int h = 0; h < kGW; h++) {
-                  uint32_t m = cmask[(jb * np + pl) * kGW + h];
+                  uint32_t m = __ballot_sync(0xffffffffu, qin[h] && qpl[h] == pl);
                   while (m) {
                     const int q = h * 32 + __ffs(m) - 1;
                     m &= m - 1u;
@@ -295,6 +296,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
                 for (int r = 0; r < kRU; r++) ab[r * nyp] = a[r];
               }
             }
+            fresh = false;
             __syncthreads();
           }
         }
@@ -313,9 +315,12 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
           for (int s0 = jlo; s0 < jhi; s0 += 32 * kPendSteps) {
             const int s1 = min(jhi, s0 + 32 * kPendSteps);
             uint64_t pend = 0;
+            // the lane's sums over the segment's cells in FP32 (at most
+            // kPendSteps terms), added to the compensated sums after it
+            float p0 = 0.f, p1 = 0.f, p2 = 0.f, pp = 0.f;
             for (int j = s0 + lane; j < s1; j += 32) {
               float v = 0.f, t1 = 0.f, t2 = 0.f;
-              if (active) {
+              if (active && !fresh) {
                 const float a0 = acc[rr * nyp + j];
                 const float a1 = np > 1 ? acc[(kR + rr) * nyp + j] : 0.f;
                 const float a2 = np > 2 ? acc[(2 * kR + rr) * nyp + j] : 0.f;
@@ -326,19 +331,20 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
                 }
                 if (code == CELL_TABLE) s_status = 4;
                 if (NBD) {
-                  pre.add(v);
+                  pp += v;
                   v = nbd_cell(P, rec.ev, (uint32_t)(i * ny + j), v, t1, t2);
                 }
               }
               rho[(size_t)i * ny + j] = v;
               if (ta) ta[(size_t)i * ny + j] = t1;
               if (tb) tb[(size_t)i * ny + j] = t2;
-              if (v != 0.f) {
-                cm0.add(v);
-                cm1.add(xg[i] * v);
-                cm2.add(yg[j] * v);
-              }
+              p0 += v;
+              p2 += yg[j] * v;
             }
+            cm0.add(p0);
+            cm1.add(xg[i] * p0);
+            cm2.add(p2);
+            if (NBD) pre.add(pp);
             if (P.which_mc_model == 1 && __any_sync(0xffffffffu, pend != 0)) {
               const CmSums cs = kln_finish_row<NBD>(P, rec, S, acc + rr * nyp, acc + (kR + rr) * nyp, i, s0, pend,
                                                     rho, ta, tb, xg[i], yg, CmSums{cm0, cm1, cm2, pre}, &s_status);
@@ -347,8 +353,8 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
           }
         }
       }
-      __syncthreads();
     }
+    __syncthreads();   // the post-op's reads of the strip are done (the reductions reuse its memory)
     // ---- centre of mass
     {
       DF a = df_warp_sum(cm0.df()), b = df_warp_sum(cm1.df()), c = df_warp_sum(cm2.df()), d = df_warp_sum(pre.df());

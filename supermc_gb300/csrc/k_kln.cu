@@ -108,4 +108,85 @@ cudaError_t launch_kln_table(const KlnDev &K, int tmax, double dT, double *table
   return cudaGetLastError();
 }
 
+// p_T-differential dN/dy d^2p_T table (MCnucl::makeTable(ptmin, dpt, iPtmax),
+// src/MCnucl.cpp:967-1025): at every node (T_A, T_B) = (i dT, j dT) and
+// p_T bin p (p_T = ptmin + p dpt), KLNModel::getdNdy at fixed p_T
+// (src/KLNModel.cpp:96-124): prefactor times the (k_T, phi) integral of
+// KLNModel::func_simpson (:281-322) over k_T in [0, p_T], phi in [0, 2 pi],
+// which the reference takes by adaptive Simpson (relative precision 1e-4)
+// and which is taken here by the tensor-product Gauss-Legendre rule of the
+// p_T-integrated table (k_T and phi nodes), in FP64.  One CTA per node; the
+// warps take the p_T bins in turn, the lanes the k_T nodes, and each bin's
+// sum is reduced in a fixed order.  Layout [tmax][tmax][nbins].
+__global__ void __launch_bounds__(kKT) k_kln_pt_table(KlnDev K, int tmax, double dT, double ptmin, double dpt,
+                                                      int nbins, double *table64, float *table32) {
+  __shared__ double s_cos[kMaxNodes / 2 + 1], s_fw[kMaxNodes / 2 + 1], s_kx[kMaxNodes], s_kw[kMaxNodes];
+  const int node = blockIdx.x;
+  const int i = node / tmax, j = node % tmax;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  double *out64 = table64 + (size_t)node * nbins;
+  float *out32 = table32 + (size_t)node * nbins;
+  if (i == 0 || j == 0) {   // MCnucl.cpp:1006-1012
+    for (int p = tid; p < nbins; p += kKT) { out64[p] = 0.0; out32[p] = 0.f; }
+    return;
+  }
+  const double ta = dT * i, tb = dT * j;
+  const double inv_l2 = 1.0 / K.lambda_qcd2, inv_amax = 1.0 / K.alpha_max;
+  auto alpha_s = [&](double q2) {
+    if (q2 <= K.lambda_qcd2) return K.alpha_max;
+    const double v = 1.0 / (K.beta0 * log(q2 * inv_l2));
+    return K.alpha_max < v ? K.alpha_max : v;
+  };
+  const int nh = K.nphi / 2, nf = nh + (K.nphi & 1);
+  for (int f = tid; f < nf; f += kKT) {
+    s_cos[f] = K.cf[f];
+    s_fw[f] = f < nh ? 2.0 * K.wf[f] : K.wf[f];
+  }
+  for (int k = tid; k < K.nkt; k += kKT) { s_kx[k] = K.xk[k]; s_kw[k] = K.wk[k]; }
+  __syncthreads();
+  for (int p = wid; p < nbins; p += kKT / 32) {
+    const double pt = ptmin + p * dpt;
+    const double x1 = pt / K.ecm * exp(K.y), x2 = pt / K.ecm / exp(K.y);
+    double acc = 0.0;
+    if (!(x1 > 1.0 || x2 > 1.0) && pt > 0.0) {
+      const double qa = ta * 2. / 1.53 * pow(0.01 / x1, K.lambda);   // KLNModel::SaturationScale
+      const double qb = tb * 2. / 1.53 * pow(0.01 / x2, K.lambda);
+      const double fab = K.fac * pow(1.0 - x1, 4.) / alpha_s(qa) * (K.fac * pow(1.0 - x2, 4.) / alpha_s(qb));
+      const double pt2 = pt * pt;
+      for (int k = lane; k < K.nkt; k += 32) {
+        const double kt = pt * s_kx[k];
+        const double base = 0.25 * (pt2 + kt * kt), cross = 0.5 * kt * pt;
+        double sum = 0.0;
+        for (int f = 0; f < nf; f++) {
+          const double c = s_cos[f];
+          const double k1 = base + cross * c, k2 = base - cross * c;
+          double num = fab, den = 1.0;
+          if (k1 > qa) { num *= qa; den *= k1; }
+          if (k2 > qb) { num *= qb; den *= k2; }
+          const double scale = fmax(fmax(k1, k2), pt2);
+          double d = inv_amax;
+          if (scale > K.lambda_qcd2) d = fmax(d, K.beta0 * log(scale * inv_l2));
+          sum += s_fw[f] * (num / (den * d));
+        }
+        // (pt dk)(2 pi dphi) kt / (4 pt^2) = pi kt / (2 pt) per unit of the [0,1] rules
+        acc += sum * (M_PI * kt / (2.0 * pt)) * s_kw[k];
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      const double v = K.prefactor * acc;
+      out64[p] = v;
+      out32[p] = (float)v;
+    }
+  }
+}
+
+cudaError_t launch_kln_pt_table(const KlnDev &K, int tmax, double dT, double ptmin, double dpt, int nbins,
+                                double *table64, float *table32, cudaStream_t st) {
+  if (K.nkt > kMaxNodes || K.nphi > kMaxNodes || nbins < 1) return cudaErrorInvalidValue;
+  k_kln_pt_table<<<tmax * tmax, kKT, 0, st>>>(K, tmax, dT, ptmin, dpt, nbins, table64, table32);
+  return cudaGetLastError();
+}
+
 }  // namespace smc

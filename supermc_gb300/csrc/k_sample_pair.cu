@@ -1159,8 +1159,10 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
       }
       __syncthreads();
     }
-    // bounding box of all windows
-    for (int k = tid; k < nsrc; k += kNT) {
+    // bounding box of the splat windows (the density is zero outside them;
+    // the records after the splat sources -- mask-only participant boxes,
+    // collisions kept for other views, spectators -- do not widen it)
+    for (int k = tid; k < nsplat; k += kNT) {
       Source s = S[k];
       if (s.xr > s.xl && s.yr > s.yl) {
         imin = min(imin, (int)s.xl); imax = max(imax, (int)s.xr);

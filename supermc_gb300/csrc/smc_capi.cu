@@ -151,6 +151,14 @@ struct Ctx {
   DevBuf<uint8_t> wounded;
   DevBuf<double> kln64;
   DevBuf<float> kln32;
+  // p_T-differential table (smc_kln_pt_table) [tmax][tmax][pt_nbins], its
+  // bins, and the per-event thickness and p_T-differential staging buffers
+  DevBuf<double> pt64;
+  DevBuf<float> pt32, pt_ta, pt_tb, rho_pt;
+  // staging of the per-event binary-collision and spectator densities
+  DevBuf<float> ev_aux;
+  int pt_nbins = 0;
+  double pt_min = 0, pt_step = 0;
   // adjoint: forward densities, per-CTA adjoint grids, staged cotangents,
   // per-event gradients
   DevBuf<float> adj_rho, adj_lam, adj_grho;
@@ -284,7 +292,10 @@ smc_status validate(const smc_params &p) {
   return SMC_OK;
 }
 
-smc_status build_kln_table(Ctx *c) {
+// The quadrature of the MC-KLN tables (Gauss-Legendre nodes on [0,1] in
+// p_T, k_T, phi; KLNModel's constants, src/KLNModel.cpp:27-90): the node
+// arrays are copied to *d_nodes (device memory the caller frees).
+smc_status kln_quadrature(Ctx *c, smc::KlnDev &K, double **d_nodes_out) {
   const smc_params &p = c->prm;
   int npt = p.kln_npt > 0 ? p.kln_npt : 48, nkt = p.kln_nkt > 0 ? p.kln_nkt : 64,
       nphi = p.kln_nphi > 0 ? p.kln_nphi : 32;
@@ -299,8 +310,9 @@ smc_status build_kln_table(Ctx *c) {
   for (auto *v : {&xp, &wp, &xk, &wk, &xf, &wf, &cf}) nodes.insert(nodes.end(), v->begin(), v->end());
   double *d_nodes = nullptr;
   CK(cudaMalloc(&d_nodes, sizeof(double) * nodes.size()));
+  *d_nodes_out = d_nodes;
   CK(cudaMemcpyAsync(d_nodes, nodes.data(), sizeof(double) * nodes.size(), cudaMemcpyHostToDevice, c->st));
-  smc::KlnDev K{};
+  K = smc::KlnDev{};
   K.ecm = p.ecm;
   K.lambda = p.lambda;
   K.y = 0.0;
@@ -317,6 +329,17 @@ smc_status build_kln_table(Ctx *c) {
   K.xp = d_nodes; K.wp = d_nodes + npt; K.xk = K.wp + npt; K.wk = K.xk + nkt; K.xf = K.wk + nkt;
   K.wf = K.xf + nphi;
   K.cf = K.wf + nphi;
+  return SMC_OK;
+}
+
+smc_status build_kln_table(Ctx *c) {
+  smc::KlnDev K;
+  double *d_nodes = nullptr;
+  smc_status s = kln_quadrature(c, K, &d_nodes);
+  if (s) {
+    if (d_nodes) cudaFree(d_nodes);
+    return s;
+  }
   int tmax = c->info.kln_tmax;
   CK(c->kln64.ensure((size_t)tmax * tmax));
   CK(c->kln32.ensure((size_t)tmax * tmax));
@@ -343,6 +366,7 @@ smc_status ensure_buffers(Ctx *c, int n, const smc_outputs *out) {
     if (out->tangents) CK(c->ntan.ensure((size_t)n * 4 * (c->info.A + c->info.B)));
     if (out->collisions) CK(c->coll.ensure((size_t)n * 2 * P.max_coll));
     if (out->orientation) CK(c->orient.ensure((size_t)n * 4));
+    if (out->rho_pt && c->pt_nbins > 0) CK(c->rho_pt.ensure((size_t)n * g * c->pt_nbins));
   }
   if (!out->ecc || out->device == 0) CK(c->ecc.ensure((size_t)n * smc::kEccLen));
   return SMC_OK;
@@ -465,6 +489,18 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
   float *rho = out->rho ? (dev ? out->rho + (size_t)off * g : c->rho.p) : nullptr;
   float *ta = out->ta ? (dev ? out->ta + (size_t)off * g : c->ta.p) : nullptr;
   float *tb = out->tb ? (dev ? out->tb + (size_t)off * g : c->tb.p) : nullptr;
+  // p_T-differential densities: read the splat's thickness outputs
+  const bool want_pt = out->rho_pt && c->pt_nbins > 0 && P.which_mc_model == 1;
+  const size_t gpt = g * (size_t)c->pt_nbins;
+  float *rho_pt = want_pt ? (dev ? out->rho_pt + (size_t)off * gpt : c->rho_pt.p) : nullptr;
+  if (want_pt && !ta) {
+    CK(c->pt_ta.ensure((size_t)n * g));
+    ta = c->pt_ta.p;
+  }
+  if (want_pt && !tb) {
+    CK(c->pt_tb.ensure((size_t)n * g));
+    tb = c->pt_tb.p;
+  }
   double *pos = out->positions ? (dev ? out->positions + (size_t)off * 2 * AB : c->pos.p) : nullptr;
   uint8_t *wnd = out->wounded ? (dev ? out->wounded + (size_t)off * AB : c->wounded.p) : nullptr;
   double *tg = out->tangents ? (dev ? out->tangents + (size_t)off * 4 * AB : c->ntan.p) : nullptr;
@@ -505,6 +541,58 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
       return launch_splat(c, P, n, c->recs.p, c->srcs.p, rho, ta, tb, c->scratch.p, ecc, c->status.p);
     }));
   }
+  // per-event binary-collision and spectator densities: views of the
+  // event's records splatted on their own (MCnucl::calculate_rho_binary,
+  // calculate_spectator_density, src/MCnucl.cpp:481-614)
+  const bool want_rhob = out->rho_binary != nullptr, want_spect = out->spectator_a || out->spectator_b;
+  float *rhob = nullptr, *spa = nullptr, *spb = nullptr;
+  if (want_rhob || want_spect) {
+    CK(c->avg_view.ensure((size_t)n * P.max_src));
+    CK(c->avg_vrecs.ensure(n));
+    CK(c->avg_status.ensure(n));
+    CK(c->scratch.ensure((size_t)c->sms * c->occ2 * g));
+    if (!dev) CK(c->ev_aux.ensure((size_t)n * g * 3));
+    rhob = want_rhob ? (dev ? out->rho_binary + (size_t)off * g : c->ev_aux.p) : nullptr;
+    // both spectator planes are splatted; a plane not asked for lands in staging
+    if (want_spect) {
+      if (!dev || !out->spectator_a || !out->spectator_b) CK(c->ev_aux.ensure((size_t)n * g * 3));
+      spa = dev && out->spectator_a ? out->spectator_a + (size_t)off * g : c->ev_aux.p + (size_t)n * g;
+      spb = dev && out->spectator_b ? out->spectator_b + (size_t)off * g : c->ev_aux.p + (size_t)n * g * 2;
+    }
+    const int grid3 = std::max(1, std::min(n, c->sms * 4));
+    if (want_rhob) {
+      DevParams Pv = P;
+      Pv.which_mc_model = 5;   // the plane is written out as it is
+      Pv.nbd = 0;
+      Pv.n_planes = 1;
+      Pv.want_ta = Pv.want_tb = 0;
+      Pv.no_moments = 1;
+      CK(smc::launch_avg_view(Pv, n, c->recs.p, c->srcs.p, c->avg_view.p, 0, c->avg_vrecs.p, grid3, c->st));
+      CK(timed(c, 2, [&] {
+        return launch_splat(c, Pv, n, c->avg_vrecs.p, c->avg_view.p, rhob, nullptr, nullptr, c->scratch.p, c->ecc.p,
+                            c->avg_status.p);   // (a view's own status is not the event's)
+      }));
+    }
+    if (want_spect) {
+      DevParams Pv = P;
+      Pv.which_mc_model = 5;   // planes 1, 2 are written out as they are
+      Pv.n_planes = 3;
+      Pv.want_ta = Pv.want_tb = 1;
+      Pv.no_moments = 1;
+      Pv.nbd = 0;
+      CK(smc::launch_avg_view(Pv, n, c->recs.p, c->srcs.p, c->avg_view.p, 1, c->avg_vrecs.p, grid3, c->st));
+      CK(timed(c, 2, [&] {
+        return launch_splat(c, Pv, n, c->avg_vrecs.p, c->avg_view.p, nullptr, spa, spb, c->scratch.p, c->ecc.p,
+                            c->avg_status.p);
+      }));
+    }
+  }
+  if (want_pt) {
+    CK(timed(c, 2, [&] {
+      return smc::launch_kln_pt_cells(P, n, c->recs.p, c->srcs.p, ta, tb, c->pt32.p, c->pt_nbins, rho_pt,
+                                      c->status.p, std::max(1, std::min(n, c->sms * 4)), c->st);
+    }));
+  }
   double *coll = out->collisions ? (dev ? out->collisions + (size_t)off * 2 * P.max_coll : c->coll.p) : nullptr;
   if (coll) {
     k_collisions<<<(n + 7) / 8, 256, 0, c->st>>>(c->recs.p, c->srcs.p, n, P.max_src, P.max_coll, coll);
@@ -530,6 +618,18 @@ smc_status run_chunk(Ctx *c, uint64_t first_event, int off, int n, const smc_out
     if (out->rho) CK(cudaMemcpyAsync(out->rho + (size_t)off * g, rho, sizeof(float) * n * g, cudaMemcpyDeviceToHost, c->st));
     if (out->ta) CK(cudaMemcpyAsync(out->ta + (size_t)off * g, ta, sizeof(float) * n * g, cudaMemcpyDeviceToHost, c->st));
     if (out->tb) CK(cudaMemcpyAsync(out->tb + (size_t)off * g, tb, sizeof(float) * n * g, cudaMemcpyDeviceToHost, c->st));
+    if (want_pt)
+      CK(cudaMemcpyAsync(out->rho_pt + (size_t)off * gpt, rho_pt, sizeof(float) * n * gpt, cudaMemcpyDeviceToHost,
+                         c->st));
+    if (out->rho_binary)
+      CK(cudaMemcpyAsync(out->rho_binary + (size_t)off * g, rhob, sizeof(float) * n * g, cudaMemcpyDeviceToHost,
+                         c->st));
+    if (out->spectator_a)
+      CK(cudaMemcpyAsync(out->spectator_a + (size_t)off * g, spa, sizeof(float) * n * g, cudaMemcpyDeviceToHost,
+                         c->st));
+    if (out->spectator_b)
+      CK(cudaMemcpyAsync(out->spectator_b + (size_t)off * g, spb, sizeof(float) * n * g, cudaMemcpyDeviceToHost,
+                         c->st));
     if (out->positions)
       CK(cudaMemcpyAsync(out->positions + (size_t)off * 2 * AB, pos, sizeof(double) * n * 2 * AB,
                          cudaMemcpyDeviceToHost, c->st));
@@ -594,8 +694,15 @@ smc_status run(Ctx *c, uint64_t first_event, int n, const smc_outputs *out, cons
   if (n == 0) return SMC_OK;
   CK(cudaSetDevice(c->device));
   smc_status worst = SMC_OK;
-  for (int off = 0; off < n; off += c->chunk) {
-    int m = std::min(c->chunk, n - off);
+  // p_T-differential densities take [nx][ny][bins] floats per event: their
+  // chunks are kept to about 2^29 values
+  int chunk = c->chunk;
+  if (out->rho_pt && c->pt_nbins > 0) {
+    const size_t per_ev = (size_t)c->P.nx * c->P.ny * c->pt_nbins;
+    chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)chunk, ((size_t)1 << 29) / per_ev));
+  }
+  for (int off = 0; off < n; off += chunk) {
+    int m = std::min(chunk, n - off);
     smc_status s = ensure_buffers(c, m, out);
     if (s) return s;
     const double *ip = nullptr, *it = nullptr, *ib = nullptr;
@@ -730,6 +837,8 @@ void smc_destroy(void *ctx) {
   c->tb.release(); c->scratch.release(); c->status.release(); c->npart.release(); c->ncoll.release();
   c->attempts.release(); c->wounded.release(); c->rho_ev.release(); c->corr_ev.release(); c->cm_ev.release();
   c->mix_sys.release(); c->mix_ev.release(); c->mix_order.release(); c->kln64.release(); c->kln32.release();
+  c->pt64.release(); c->pt32.release(); c->pt_ta.release(); c->pt_tb.release(); c->rho_pt.release();
+  c->ev_aux.release();
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
   c->avg_ta.release(); c->avg_tb.release(); c->avg_aux.release(); c->avg_view.release(); c->avg_vrecs.release(); c->avg_status.release();
   c->avg_frame.release(); c->avg_order.release(); c->avg_seg.release(); c->avg_count.release();
@@ -774,7 +883,9 @@ static smc_status set_thickness_flags(Ctx *c, const smc_outputs *out) {
   const bool nbd_thick = P.nbd == 2 && P.which_mc_model == 5;
   P.want_ta = out->ta != nullptr || nbd_thick;
   P.want_tb = out->tb != nullptr || nbd_thick;
-  P.want_binary = out->collisions != nullptr;   // collision records whatever the model
+  // collision records whatever the model (collision positions, rho_binary)
+  P.want_binary = out->collisions != nullptr || out->rho_binary != nullptr;
+  P.want_spect = out->spectator_a != nullptr || out->spectator_b != nullptr;   // spectator records
   if ((out->ta || out->tb) && P.which_mc_model == 7) return SMC_ERR_CONFIG;
   // splat planes: Glauber rho (+ T_A, T_B on request); MC-KLN T_A, T_B;
   // sqrt(T_A T_B) scaling rho_A, rho_B
@@ -1093,8 +1204,10 @@ smc_status smc_average_profiles(void *ctx, uint64_t first_event, int n, const do
         CK(smc::launch_avg_accum_prod(c->avg_ta.p, c->avg_tb.p, m, g, acc_of(K_TATB, f, q), c->st));
       if (want[K_RHOB][f]) {   // MCnucl::calculate_rho_binary on the moved collisions
         DevParams Pv = P;
+        Pv.which_mc_model = 5;   // the plane is written out as it is
         Pv.n_planes = 1;
         Pv.want_ta = Pv.want_tb = 0;
+        Pv.nbd = 0;
         CK(smc::launch_avg_view(Pv, m, c->recs.p, c->srcs.p, c->avg_view.p, 0, c->avg_vrecs.p, grid3, c->st));
         CK(launch_splat(c, Pv, m, c->avg_vrecs.p, c->avg_view.p, c->avg_aux.p, nullptr, nullptr, c->scratch.p, c->ecc.p,
                         c->avg_status.p));   // (a view's own status, e.g. zero density, is not the event's)
@@ -1105,6 +1218,7 @@ smc_status smc_average_profiles(void *ctx, uint64_t first_event, int n, const do
         Pv.which_mc_model = 5;   // planes 1, 2 are written out as they are
         Pv.n_planes = 3;
         Pv.want_ta = Pv.want_tb = 1;
+        Pv.nbd = 0;
         CK(smc::launch_avg_view(Pv, m, c->recs.p, c->srcs.p, c->avg_view.p, 1, c->avg_vrecs.p, grid3, c->st));
         CK(launch_splat(c, Pv, m, c->avg_vrecs.p, c->avg_view.p, nullptr, c->avg_aux.p, c->avg_aux.p + (size_t)m * g,
                         c->scratch.p, c->ecc.p, c->avg_status.p));
@@ -1380,6 +1494,7 @@ smc_status smc_autotune(void *ctx, int n_events, smc_tuning *out) {
 
 smc_status smc_generate_graph(void *ctx, uint64_t first_event, int n, const smc_outputs *out) {
   if (!ctx || !out || n < 0 || !out->device) return SMC_ERR_ARGUMENT;
+  if (out->rho_pt || out->rho_binary || out->spectator_a || out->spectator_b) return SMC_ERR_ARGUMENT;
   Ctx *c = static_cast<Ctx *>(ctx);
   if (n == 0) return SMC_OK;
   CK(cudaSetDevice(c->device));
@@ -1435,6 +1550,7 @@ smc_status smc_generate_graph(void *ctx, uint64_t first_event, int n, const smc_
 smc_status smc_generate_mixed_graph(void *ctx, const smc_params *systems, int nsys, uint64_t first_event, int n,
                                     const int *system_of_event, const smc_outputs *out) {
   if (!ctx || !out || n < 0 || !out->device) return SMC_ERR_ARGUMENT;
+  if (out->rho_pt || out->rho_binary || out->spectator_a || out->spectator_b) return SMC_ERR_ARGUMENT;
   Ctx *c = static_cast<Ctx *>(ctx);
   if (n == 0) return SMC_OK;
   CK(cudaSetDevice(c->device));
@@ -1658,6 +1774,40 @@ smc_status smc_kln_table(void *ctx, double *host_table, int capacity) {
   if ((size_t)capacity < n) return SMC_ERR_ARGUMENT;
   CK(cudaMemcpyAsync(host_table, c->kln64.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
+  return SMC_OK;
+}
+
+smc_status smc_kln_pt_table(void *ctx, double pt_min, double d_pt, int nbins, double *host_table, size_t capacity) {
+  if (!ctx || nbins < 1 || nbins > 4096 || !(d_pt > 0) || !(pt_min > 0)) return SMC_ERR_ARGUMENT;
+  Ctx *c = static_cast<Ctx *>(ctx);
+  if (c->P.which_mc_model != 1 || !c->kln64.p) return SMC_ERR_CONFIG;
+  const int tmax = c->info.kln_tmax;
+  const size_t n = (size_t)tmax * tmax * nbins;
+  if (host_table && capacity < n) return SMC_ERR_ARGUMENT;
+  CK(cudaSetDevice(c->device));
+  if (c->pt_nbins != nbins || c->pt_min != pt_min || c->pt_step != d_pt) {
+    smc::KlnDev K;
+    double *d_nodes = nullptr;
+    smc_status s = kln_quadrature(c, K, &d_nodes);
+    cudaError_t e = s ? cudaSuccess : c->pt64.ensure(n);
+    if (!s && e == cudaSuccess) e = c->pt32.ensure(n);
+    if (!s && e == cudaSuccess)
+      e = smc::launch_kln_pt_table(K, tmax, c->info.kln_dT, pt_min, d_pt, nbins, c->pt64.p, c->pt32.p, c->st);
+    if (!s && e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (d_nodes) cudaFree(d_nodes);
+    if (s) return s;
+    if (e != cudaSuccess) {
+      c->pt_nbins = 0;
+      return SMC_ERR_CUDA;
+    }
+    c->pt_nbins = nbins;
+    c->pt_min = pt_min;
+    c->pt_step = d_pt;
+  }
+  if (host_table) {
+    CK(cudaMemcpyAsync(host_table, c->pt64.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
   return SMC_OK;
 }
 

@@ -77,5 +77,13 @@ cudaError_t launch_adjoint(const DevParams &P, int n_events, const EventRec *rec
                            int *ticket = nullptr);
 cudaError_t launch_kln_table(const KlnDev &K, int tmax, double dT, double *table64, float *table32,
                              cudaStream_t st);
+// p_T-differential table [tmax][tmax][nbins] (k_kln_pt_table)
+cudaError_t launch_kln_pt_table(const KlnDev &K, int tmax, double dT, double ptmin, double dpt, int nbins,
+                                double *table64, float *table32, cudaStream_t st);
+// per-cell p_T-differential densities out [n][nx][ny][nbins] from the
+// events' thickness grids ta, tb [n][nx][ny] and the FP32 table
+cudaError_t launch_kln_pt_cells(const DevParams &P, int n, const EventRec *recs, const Source *srcs, const float *ta,
+                                const float *tb, const float *table, int nbins, float *out, int *status, int grid,
+                                cudaStream_t st);
 
 }  // namespace smc

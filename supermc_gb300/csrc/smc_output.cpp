@@ -15,6 +15,7 @@
 // header dictionary, little-endian C-order data), one array per text file
 // with the text file's columns and full precision.
 #include <cstdint>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -250,6 +251,44 @@ smc_status smc_write_nucleon_tables(const double *xy, const uint8_t *wounded, in
     for (int k = k0; k < k1; k++) std::fprintf(f, "%10.3g%10.3g\n", xy[2 * k], xy[2 * k + 1]);
     std::fclose(f);
   }
+  return SMC_OK;
+}
+
+smc_status smc_write_participant_table(const double *xy, const uint8_t *wounded, int A, int B, const char *filename) {
+  if (!xy || !wounded || !filename || A < 0 || B < 0) return SMC_ERR_ARGUMENT;
+  FILE *f = std::fopen(filename, "a");
+  if (!f) return SMC_ERR_ARGUMENT;
+  for (int k = 0; k < A + B; k++)
+    if (wounded[k]) std::fprintf(f, "%10.3g   %10.3g   %d\n", xy[2 * k], xy[2 * k + 1], k < A ? 1 : 2);
+  std::fclose(f);
+  return SMC_OK;
+}
+
+smc_status smc_write_spectator_table(const double *xy, const uint8_t *wounded, int A, int B, double ecm,
+                                     const char *filename) {
+  if (!xy || !wounded || !filename || A < 0 || B < 0) return SMC_ERR_ARGUMENT;
+  FILE *f = std::fopen(filename, "w");
+  if (!f) return SMC_ERR_ARGUMENT;
+  // the spectators' rapidity, +Y for the projectile, -Y for the target
+  const double vz = std::sqrt(1. - 1. / ((ecm / 2.) * (ecm / 2.)));
+  const double Y = 0.5 * std::log((1. + vz) / (1. - vz + 1e-100));
+  for (int k = 0; k < A + B; k++)
+    if (!wounded[k]) std::fprintf(f, "%10.4e  %.4e  %.4e\n", xy[2 * k], xy[2 * k + 1], k < A ? Y : -Y);
+  std::fclose(f);
+  return SMC_OK;
+}
+
+smc_status smc_write_density_pt(const float *data, int nx, int ny, int nbins, double npart, double scale,
+                                const char *filename) {
+  if (!data || !filename || nx < 1 || ny < 1 || nbins < 1) return SMC_ERR_ARGUMENT;
+  FILE *f = std::fopen(filename, "w");
+  if (!f) return SMC_ERR_ARGUMENT;
+  std::fprintf(f, "%% <npart>= %g xmax= %d ymax= %d Ptmax= %d\n", npart, nx, ny, nbins);
+  for (size_t c = 0; c < (size_t)nx * ny; c++) {
+    for (int p = 0; p < nbins; p++) std::fprintf(f, "%22.12e", (double)data[c * nbins + p] * scale);
+    std::fprintf(f, "\n");
+  }
+  std::fclose(f);
   return SMC_OK;
 }
 

@@ -52,7 +52,7 @@ def smc_params_from(vals: dict[str, float], seed: int = 1) -> _lib.SmcParams:
 
 
 OUTPUT_NAMES = ("ecc", "rho", "ta", "tb", "npart", "ncoll", "b", "attempts", "positions", "wounded", "tangents",
-                "collisions", "orientation")
+                "collisions", "orientation", "rho_pt", "rho_binary", "spectator_a", "spectator_b")
 # keys that describe one collision system of a mixed batch
 SYSTEM_KEYS = ("aproj", "atarg", "proj_deformed", "targ_deformed", "ecm", "sigininn_override", "proj_r", "proj_a",
                "targ_r", "targ_a", "proj_d_min", "targ_d_min")
@@ -72,6 +72,7 @@ class Engine:
         _lib.check(self.lib.smc_get_info(self.h, ctypes.byref(info)), "smc_get_info")
         self.info = info
         self.nx, self.ny, self.A, self.B = info.nx, info.ny, info.A, info.B
+        self.pt_bins = 0
 
     def close(self):
         if getattr(self, "h", None):
@@ -94,7 +95,9 @@ class Engine:
                   "positions": ((n, AB, 2), np.float64), "wounded": ((n, AB), np.uint8),
                   "tangents": ((n, AB, 4), np.float64),
                   "collisions": ((n, self.info.max_collisions, 2), np.float64),
-                  "orientation": ((n, 4), np.float64)}
+                  "orientation": ((n, 4), np.float64),
+                  "rho_pt": ((n, self.nx, self.ny, max(1, self.pt_bins)), np.float32),
+                  "rho_binary": (g, np.float32), "spectator_a": (g, np.float32), "spectator_b": (g, np.float32)}
         return {k: np.zeros(*shapes[k]) for k in want}
 
     @staticmethod
@@ -272,6 +275,18 @@ class Engine:
         _lib.check(self.lib.smc_adjoint(self.h, first_event, n, _lib.ptr(xp), _lib.ptr(xt), _lib.ptr(bb),
                                         ctypes.byref(ct), _lib.ptr(grad)), "smc_adjoint")
         return grad, per
+
+    def kln_pt_table(self, pt_min: float = 0.1, d_pt: float = 0.1, nbins: int = 20) -> np.ndarray:
+        """The p_T-differential dN/dy d^2p_T table [tmax][tmax][nbins] at
+        p_T = pt_min + k d_pt (smc_kln_pt_table; MCnucl::makeTable(ptmin,
+        dpt, iPtmax)); afterwards the "rho_pt" output holds every event's
+        per-cell values of these bins."""
+        t = self.info.kln_tmax
+        out = np.zeros((t, t, nbins))
+        _lib.check(self.lib.smc_kln_pt_table(self.h, pt_min, d_pt, nbins, _lib.ptr(out), out.size),
+                   "smc_kln_pt_table")
+        self.pt_bins = nbins
+        return out
 
     def kln_table(self) -> np.ndarray:
         t = self.info.kln_tmax

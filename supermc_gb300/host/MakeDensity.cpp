@@ -29,6 +29,8 @@ const Default kDefaults[] = {
     {"cc_fluctuation_Gamma_theta", 0.75}, {"cc_fluctuation_k", 0.75}, {"generate_reaction_plane_avg_profile", 1}, {"cutdSdy", 0},
     {"cutdSdy_lowerBound", 593.51}, {"cutdSdy_upperBound", 889.53},
     {"output_TATB", 1}, {"output_rho_binary", 1}, {"output_TA", 1}, {"output_spectator_density", 1},
+    {"output_rhob", 0}, {"PT_flag", 1}, {"mixedMode", 0}, {"PT_Min", 0.1}, {"PT_Max", 2}, {"d_PT", 0.1},
+    {"use_5col", 0}, {"use_ptCol", 0},
     // extensions (0: the reference's hard-coded value)
     {"proj_R", 0}, {"proj_a", 0}, {"targ_R", 0}, {"targ_a", 0}, {"proj_d_min", 0}, {"targ_d_min", 0},
     {"siginNN_override", 0}, {"kln_npt", 48}, {"kln_nkt", 64}, {"kln_nphi", 32}, {"max_attempts", 0},
@@ -264,13 +266,29 @@ void MakeDensity::generate_profile_ebe(int nevent) {
   // [cutdSdy_lowerBound, cutdSdy_upperBound] is dropped after its pairing
   // (its binary.dat lines stay) and does not count (src/MakeDensity.cpp:
   // 601-617, :683-684, gettotaldSdy :2557-2567)
-  const bool cut = val(*reader_, "cutdSdy") == 1;
+  // PT_flag > 0: the p_T-integrated profiles; PT_flag < 0 or mixedMode > 0:
+  // the p_T-differential ones of MC-KLN as well (MakeDensity::MakeDensity,
+  // src/MakeDensity.cpp:106-119; :563-688).  Their files are written when
+  // use_5col / use_ptCol are set: the reference reads those switches into
+  // locals that shadow the ones it tests (:556-567), so its operation 1
+  // writes none.  The cut on dS/dy applies with PT_flag > 0 only (:604-617).
+  const bool pt_inte = val(*reader_, "PT_flag") > 0;
+  const bool want_pt = (!pt_inte || val(*reader_, "mixedMode") > 0) && params_.which_mc_model == 1;
+  const bool five = val(*reader_, "use_5col") != 0, ptcol = val(*reader_, "use_ptCol") != 0;
+  int nbins = 0;
+  if (want_pt) {
+    const double ptmin = val(*reader_, "PT_Min"), ptmax = val(*reader_, "PT_Max"), dpt = val(*reader_, "d_PT");
+    nbins = (int)((ptmax - ptmin) / dpt + 0.1) + 1;   // MaxPT, src/MakeDensity.cpp:71
+    check(smc_kln_pt_table(ctx_, ptmin, dpt, nbins, nullptr, 0), "smc_kln_pt_table");
+  }
+  const bool cut = val(*reader_, "cutdSdy") == 1 && pt_inte;
   const double cut_lo = val(*reader_, "cutdSdy_lowerBound"), cut_hi = val(*reader_, "cutdSdy_upperBound");
   const double ff = params_.final_factor, area = params_.dx * params_.dy;
   const size_t g = (size_t)info_.nx * info_.ny;
   const int AB = info_.A + info_.B, mc = info_.max_collisions;
-  const int batch = std::max(1, std::min(batch_, 1024));   // host grids of one call
-  std::vector<float> rho;
+  // host grids of one call (the p_T-differential ones hold nbins per cell)
+  const int batch = std::max(1, std::min(batch_, want_pt ? 32 : 1024));
+  std::vector<float> rho, rho_pt;
   std::vector<int> npart, ncoll;
   std::vector<double> grid(g), pos, coll;
   std::vector<uint8_t> wounded;
@@ -292,6 +310,10 @@ void MakeDensity::generate_profile_ebe(int nevent) {
     out.positions = pos.data();
     out.wounded = wounded.data();
     out.collisions = coll.data();
+    if (want_pt) {
+      rho_pt.resize((size_t)n * g * nbins);
+      out.rho_pt = rho_pt.data();
+    }
     check(smc_generate(ctx_, generated, n, &out), "smc_generate");
     generated += n;
     for (int e = 0; e < n && event < nevent; e++) {
@@ -318,12 +340,147 @@ void MakeDensity::generate_profile_ebe(int nevent) {
                                        info_.B, "data/wounded.data", "data/nucl1.data", "data/nucl2.data"),
               "smc_write_nucleon_tables");
       if (!sd) continue;
+      const double np = (double)(npart[2 * e] + npart[2 * e + 1]);
+      if (want_pt && (five || ptcol)) {   // setSd of the p_T bins, dumpDensity5Col / dumpDesityptCol
+        const float *d = rho_pt.data() + (size_t)e * g * nbins;
+        if (five) {
+          std::snprintf(name, sizeof(name), "data/sd_event_%d_5col.dat", event);
+          check(smc_write_density_pt(d, info_.nx, info_.ny, nbins, np, ff, name), "smc_write_density_pt");
+        }
+        if (ptcol) {
+          std::snprintf(name, sizeof(name), "data/sd_event_%d_ptCol.dat", event);
+          check(smc_write_density_pt(d, info_.nx, info_.ny, nbins, np, ff, name), "smc_write_density_pt");
+        }
+      }
+      if (!pt_inte) continue;
       // MakeDensity::setSd (src/MakeDensity.cpp:2514-2522)
       for (size_t k = 0; k < g; k++) grid[k] = (double)rho[(size_t)e * g + k] * ff;
       std::snprintf(name, sizeof(name), "data/sd_event_%d", event);
-      if (four)
-        write_4col(grid.data(), info_.nx, info_.ny, params_, (double)(npart[2 * e] + npart[2 * e + 1]), name, binary_);
+      if (four) write_4col(grid.data(), info_.nx, info_.ny, params_, np, name, binary_);
       if (block) write_block(grid.data(), info_.nx, info_.ny, name, binary_);
+    }
+  }
+}
+
+void MakeDensity::generate_profile_ebe_Jet(int nevent) {
+  // the reference's constructor exits for operation 2 with PT_flag < 0
+  // (src/MakeDensity.cpp:121-131)
+  if (val(*reader_, "PT_flag") < 0)
+    throw Error(SMC_ERR_CONFIG, "This option is not supported: Operation=2, PTinte<0");
+  ensure_data_dir();
+  const int from = (int)val(*reader_, "ecc_from_order"), to = (int)val(*reader_, "ecc_to_order");
+  const bool sd = val(*reader_, "use_sd") != 0, block = val(*reader_, "use_block") != 0,
+             four = val(*reader_, "use_4col") != 0;
+  const bool rhob_on = val(*reader_, "output_rho_binary") != 0, ta_on = val(*reader_, "output_TA") != 0,
+             nb_on = val(*reader_, "output_rhob") != 0, spect_on = val(*reader_, "output_spectator_density") != 0;
+  const bool thick_ok = params_.which_mc_model != 7;   // sqrt(T_A T_B) has no thickness planes here
+  if ((ta_on || nb_on) && !thick_ok)
+    std::fprintf(stderr, "supermc_gb300: output_TA / output_rhob: not produced for which_mc_model 7\n");
+  const bool deformed = val(*reader_, "proj_deformed") == 1 || val(*reader_, "targ_deformed") == 1;
+  const bool cut = val(*reader_, "cutdSdy") == 1;
+  const double cut_lo = val(*reader_, "cutdSdy_lowerBound"), cut_hi = val(*reader_, "cutdSdy_upperBound");
+  const double ff = params_.final_factor, area = params_.dx * params_.dy;
+  const size_t g = (size_t)info_.nx * info_.ny;
+  const int A = info_.A, B = info_.B, AB = A + B, mc = info_.max_collisions;
+  const int batch = std::max(1, std::min(batch_, 256));   // host grids of one call
+  const bool want_t = (ta_on || nb_on) && thick_ok;
+  std::vector<float> rho, ta, tb, rb, spa, spb;
+  std::vector<int> npart, ncoll;
+  std::vector<double> grid(g), pos, coll, ecc, ori;
+  std::vector<uint8_t> wounded;
+  char name[256], pattern[256];
+  int event = 1;                 // the event number of the files (events that passed the cut + 1)
+  uint64_t generated = 0;        // event ids used
+  while (event <= nevent) {
+    const int n = std::min(batch, cut ? batch : nevent - event + 1);
+    rho.resize((size_t)n * g);
+    npart.resize((size_t)n * 2);
+    ncoll.resize(n);
+    pos.resize((size_t)n * AB * 2);
+    wounded.resize((size_t)n * AB);
+    coll.resize((size_t)n * mc * 2);
+    ecc.resize((size_t)n * 49);
+    ori.resize((size_t)n * 4);
+    smc_outputs out{};
+    out.rho = rho.data();
+    out.ecc = ecc.data();
+    out.npart = npart.data();
+    out.ncoll = ncoll.data();
+    out.positions = pos.data();
+    out.wounded = wounded.data();
+    out.collisions = coll.data();
+    if (deformed) out.orientation = ori.data();
+    if (want_t) {
+      ta.resize((size_t)n * g);
+      tb.resize((size_t)n * g);
+      out.ta = ta.data();
+      out.tb = tb.data();
+    }
+    if (rhob_on) {
+      rb.resize((size_t)n * g);
+      out.rho_binary = rb.data();
+    }
+    if (spect_on) {
+      spa.resize((size_t)n * g);
+      spb.resize((size_t)n * g);
+      out.spectator_a = spa.data();
+      out.spectator_b = spb.data();
+    }
+    check(smc_generate(ctx_, generated, n, &out), "smc_generate");
+    generated += n;
+    for (int e = 0; e < n && event <= nevent; e++) {
+      const double *xy = pos.data() + (size_t)e * AB * 2;
+      const uint8_t *wd = wounded.data() + (size_t)e * AB;
+      const double np = (double)(npart[2 * e] + npart[2 * e + 1]);
+      // the event's tables, written after its pairing whatever the cut
+      // decides (src/MakeDensity.cpp:299-305); an event that fails the cut
+      // leaves them under the number the next event reuses
+      std::snprintf(name, sizeof(name), "data/ParticipantTable_event_%d.dat", event);
+      check(smc_write_participant_table(xy, wd, A, B, name), "smc_write_participant_table");
+      std::snprintf(name, sizeof(name), "data/Spectators_event_%d.dat", event);
+      check(smc_write_spectator_table(xy, wd, A, B, params_.ecm, name), "smc_write_spectator_table");
+      std::snprintf(name, sizeof(name), "data/BinaryCollisionTable_event_%d.dat", event);
+      const int nc = std::min(ncoll[e], mc);
+      check(smc_write_binary_table(coll.data() + (size_t)e * mc * 2, nc, name), "smc_write_binary_table");
+      // MCnucl::dumpBinaryTable also rewrites the nucleon tables (src/MCnucl.cpp:1191-1207)
+      check(smc_write_nucleon_tables(xy, wd, A, B, "data/wounded.data", "data/nucl1.data", "data/nucl2.data"),
+            "smc_write_nucleon_tables");
+      if (cut) {
+        double total = 0.0;
+        for (size_t k = 0; k < g; k++) total += (double)rho[(size_t)e * g + k] * area;
+        if (total < cut_lo || total > cut_hi) continue;
+      }
+      auto grids = [&](const float *src, double scale, const char *stem_fmt) {
+        for (size_t k = 0; k < g; k++) grid[k] = (double)src[k] * scale;
+        std::snprintf(name, sizeof(name), stem_fmt, event);
+        if (four) write_4col(grid.data(), info_.nx, info_.ny, params_, np, name, binary_);
+        if (block) write_block(grid.data(), info_.nx, info_.ny, name, binary_);
+      };
+      if (sd) {
+        std::snprintf(pattern, sizeof(pattern), "data/sn_ecc_eccp_%%d_event_%d.dat", event);
+        const double *er = ecc.data() + (size_t)e * 49;
+        if (deformed)
+          check(smc_write_ecc_deformed(er, ori.data() + (size_t)e * 4, 1, from, to, pattern), "smc_write_ecc_deformed");
+        else
+          check(smc_write_ecc(er, 1, from, to, pattern), "smc_write_ecc");
+        grids(rho.data() + (size_t)e * g, ff, "data/sd_event_%d");
+      }
+      if (rhob_on) grids(rb.data() + (size_t)e * g, 1.0, "data/rho_binary_event_%d");
+      if (ta_on && thick_ok) {
+        grids(ta.data() + (size_t)e * g, 1.0, "data/nuclear_thickness_TA_event_%d");
+        grids(tb.data() + (size_t)e * g, 1.0, "data/nuclear_thickness_TB_event_%d");
+      }
+      if (nb_on && thick_ok) {   // net baryon density T_A + T_B
+        for (size_t k = 0; k < g; k++) grid[k] = (double)ta[(size_t)e * g + k] + (double)tb[(size_t)e * g + k];
+        std::snprintf(name, sizeof(name), "data/rhob_event_%d", event);
+        if (four) write_4col(grid.data(), info_.nx, info_.ny, params_, np, name, binary_);
+        if (block) write_block(grid.data(), info_.nx, info_.ny, name, binary_);
+      }
+      if (spect_on) {
+        grids(spa.data() + (size_t)e * g, 1.0, "data/spectator_density_A_event_%d");
+        grids(spb.data() + (size_t)e * g, 1.0, "data/spectator_density_B_event_%d");
+      }
+      event++;
     }
   }
 }

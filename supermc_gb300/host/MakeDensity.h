@@ -4,6 +4,11 @@
 //   generateEccTable          operation 9: data/sn_ecc_eccp_<order>.dat
 //   generate_profile_ebe      operation 1: data/sd_event_<n>_block.dat / _4col.dat,
 //                             data/binary.dat, wounded.data, nucl1.data, nucl2.data
+//   generate_profile_ebe_Jet  operation 2: per event data/ParticipantTable_event_<n>.dat,
+//                             Spectators_event_<n>.dat, BinaryCollisionTable_event_<n>.dat,
+//                             sn_ecc_eccp_<order>_event_<n>.dat, sd_event_<n>_block/_4col,
+//                             rho_binary_event_<n>_*, nuclear_thickness_TA/TB_event_<n>_*,
+//                             rhob_event_<n>_*, spectator_density_A/B_event_<n>_*
 //   generate_profile_average  operation 3: data/sdAvg[_RP]_order_<n>_block.dat / _4col.dat and
 //                             the TATB, rho_binary, nuclear_thickness, spectator_density means
 // With the key use_binary = 1 (no reference counterpart) each of these tables
@@ -45,6 +50,7 @@ class MakeDensity {
 
   void generateEccTable(int nevent);           // src/MakeDensity.cpp:2103-2200
   void generate_profile_ebe(int nevent);       // :501-694
+  void generate_profile_ebe_Jet(int nevent);   // :148-498 (operation 2)
   void generate_profile_average(int nevent);   // :736-2103 (integrated-p_T entropy means)
   // The per-event helpers the operations use, on the library's results:
   // setSd (src/MakeDensity.cpp:2514-2522): sd = getRho * finalFactor

@@ -17,6 +17,7 @@ int main(int argc, char *argv[]) {
     const clock_t start = clock();
     switch (operation) {
       case 1: dens.generate_profile_ebe(nevent); break;
+      case 2: dens.generate_profile_ebe_Jet(nevent); break;
       case 3: dens.generate_profile_average(nevent); break;
       case 9: dens.generateEccTable(nevent); break;
       default:

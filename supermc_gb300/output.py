@@ -70,3 +70,33 @@ def write_ecc_npy(ecc, from_order: int, to_order: int, pattern: str = "data/sn_e
     lib = _lib.load()
     _lib.check(lib.smc_write_ecc_npy(_lib.ptr(e), None if o is None else _lib.ptr(o), e.shape[0], from_order,
                                      to_order, pattern.encode()), "smc_write_ecc_npy")
+
+
+def write_participant_table(positions, wounded, A: int, filename: str) -> None:
+    """MCnucl::dumpparticipantTable (appended): the event's participants,
+    positions [A+B][2] and wounded [A+B] as the generator returns them."""
+    xy = np.ascontiguousarray(positions, dtype=np.float64)
+    w = np.ascontiguousarray(wounded, dtype=np.uint8)
+    lib = _lib.load()
+    _lib.check(lib.smc_write_participant_table(_lib.ptr(xy), _lib.ptr(w), A, len(w) - A, filename.encode()),
+               "smc_write_participant_table")
+
+
+def write_spectator_table(positions, wounded, A: int, ecm: float, filename: str) -> None:
+    """MCnucl::dumpSpectatorsTable: the non-participants with the beam
+    rapidity of sqrt(s) = ecm."""
+    xy = np.ascontiguousarray(positions, dtype=np.float64)
+    w = np.ascontiguousarray(wounded, dtype=np.uint8)
+    lib = _lib.load()
+    _lib.check(lib.smc_write_spectator_table(_lib.ptr(xy), _lib.ptr(w), A, len(w) - A, ecm, filename.encode()),
+               "smc_write_spectator_table")
+
+
+def write_density_pt(rho_pt, npart: float, filename: str, scale: float = 1.0) -> None:
+    """MakeDensity::dumpDensity5Col / dumpDesityptCol of one event's
+    p_T-differential grid [nx][ny][nbins] (times scale: finalFactor for the
+    entropy density)."""
+    d = np.ascontiguousarray(rho_pt, dtype=np.float32)
+    lib = _lib.load()
+    _lib.check(lib.smc_write_density_pt(_lib.ptr(d), d.shape[0], d.shape[1], d.shape[2], npart, scale,
+                                        filename.encode()), "smc_write_density_pt")

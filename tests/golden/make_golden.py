@@ -252,6 +252,19 @@ def make_kln(out):
                         **{"lookup_rho_" + k: v for k, v in dig.items()})
 
 
+def make_kln_pt(out):
+    """KLNModel::getdNdy at fixed p_T (adaptive Simpson, the rows of
+    MCnucl::makeTable(ptmin, dpt, iPtmax)) at a few (T_A, T_B, p_T)."""
+    ref, vals = ref_for(["pbpb2760"], ["which_mc_model=1", "sub_model=7", "lambda=0.288"])
+    ref.lib.refh_kln_setup(2760.0, 0.288)
+    pts, vals_out = [], []
+    for ta, tb in [(0.3, 0.9), (1.7, 2.2), (4.4, 0.5), (9.0, 7.5)]:
+        for pt in (0.1, 0.5, 1.0, 1.5, 2.0):
+            pts.append([ta, tb, pt])
+            vals_out.append(ref.lib.refh_kln_dndy_pt(0.0, ta, tb, pt))
+    np.savez_compressed(os.path.join(out, "kln_pt.npz"), points=np.array(pts), values=np.array(vals_out))
+
+
 def make_constants(out):
     ref, _ = ref_for(["auau200"])
     c = {"sigma_in": {str(e): ref.lib.refh_sigma_in(e) for e in (62.4, 200.0, 2760.0, 3670.0, 5020.0, 5520.0)},
@@ -276,7 +289,10 @@ def make_text(out):
     runs = ((9, "", ["nev=4", "ecc_from_order=2", "ecc_to_order=5"]),
             (1, "", ["nev=2", "maxx=3", "maxy=3", "dx=0.5", "dy=0.5", "use_block=1", "use_4col=1"]),
             (9, "deformed/", ["nev=3", "ecc_from_order=2", "ecc_to_order=3", "Aproj=238", "Atarg=238",
-                              "proj_deformed=1", "targ_deformed=1"]))
+                              "proj_deformed=1", "targ_deformed=1"]),
+            (2, "jet/", ["nev=2", "maxx=3", "maxy=3", "dx=0.5", "dy=0.5", "use_block=1", "use_4col=1", "use_ed=0",
+                         "ecc_from_order=2", "ecc_to_order=3", "output_rho_binary=1", "output_TA=1",
+                         "output_rhob=1", "output_spectator_density=1"]))
     for op, key, args in runs:
         wd = tempfile.mkdtemp(prefix="smc_text_", dir=ref.workdir)
         os.makedirs(os.path.join(wd, "data"))
@@ -285,6 +301,15 @@ def make_text(out):
         with open(os.path.join(wd, "parameters.dat"), "w") as f:
             f.write(parameters_text(vals))
         subprocess.run([exe, f"operation={op}", "randomSeed=7"] + args, cwd=wd, check=True, capture_output=True)
+        if op == 2:
+            # Jet mode: the file set, and the per-event tables (formats)
+            names = ["ParticipantTable_event_1.dat", "Spectators_event_1.dat", "BinaryCollisionTable_event_1.dat",
+                     "sn_ecc_eccp_2_event_1.dat", "sn_ecc_eccp_10_event_1.dat"]
+            texts[key + "files"] = sorted(os.listdir(os.path.join(wd, "data")))
+            for name in names:
+                with open(os.path.join(wd, "data", name)) as f:
+                    texts[key + name] = f.read()
+            continue
         orders = (2, 3, 10) if key else (2, 3, 4, 5, 10)
         names = ([f"sn_ecc_eccp_{k}.dat" for k in orders] if op == 9 else
                  [f"sd_event_{e}_{kind}.dat" for e in (1, 2) for kind in ("block", "4col")])
@@ -300,7 +325,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=REF_ROOT)
     ap.add_argument("--nev", type=int, default=1500)
-    ap.add_argument("--only", choices=["constants", "sampler", "inject", "average", "kln", "native",
+    ap.add_argument("--only", choices=["constants", "sampler", "inject", "average", "kln", "kln_pt", "native",
                                        "native_systems", "light", "text"],
                     help="regenerate one fixture only")
     a = ap.parse_args()
@@ -311,7 +336,7 @@ def main():
     TABLES_DIR = os.path.join(a.ref, "tables")
     steps = {"constants": lambda: make_constants(HERE), "sampler": lambda: make_sampler(HERE),
              "inject": lambda: make_inject(HERE), "average": lambda: make_average(HERE),
-             "kln": lambda: make_kln(HERE), "native": lambda: make_native_tables(HERE, a.nev),
+             "kln": lambda: make_kln(HERE), "kln_pt": lambda: make_kln_pt(HERE), "native": lambda: make_native_tables(HERE, a.nev),
              "native_systems": lambda: make_native_systems(HERE, a.nev),
              "light": lambda: make_light(HERE, a.nev),
              "text": lambda: make_text(HERE)}

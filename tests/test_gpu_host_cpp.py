@@ -1,6 +1,7 @@
 """The C++ drop-in driver (supermc_gb300/_build/superMC, the reference's
 main over the C ABI) writes the same files as the Python host over the same
-calls: operations 9, 1 and 3."""
+calls: operations 9, 1 (also p_T-differential), 2 (Jet mode) and 3."""
+import io
 import os
 import subprocess
 
@@ -99,3 +100,68 @@ def test_operation_1_cut_on_total_entropy(tmp_path):
     assert not (tmp_path / "data" / "sd_event_5_block.dat").exists()
     lines = [f"{x:10.3g}{y:10.3g}" for e in range(keep[-1] + 1) for x, y in out["collisions"][e][:out["ncoll"][e]]]
     assert (tmp_path / "data" / "binary.dat").read_text() == "".join(l + "\n" for l in lines)
+
+
+def test_operation_2_jet_mode(tmp_path):
+    """Operation 2 (MakeDensity::generate_profile_ebe_Jet, src/MakeDensity.cpp:
+    148-498): the per-event tables and grids, the reference's file set (its
+    quarks.data aside), contents equal to the events the library generates."""
+    import json
+    from supermc_gb300.output import write_density_block
+    p = _run(tmp_path, operation=2, nev=3, use_4col=1, output_rho_binary=1, output_TA=1, output_rhob=1,
+             output_spectator_density=1, ecc_to_order=3)
+    out = _engine(p).generate(0, 3, want=("rho", "ecc", "npart", "ncoll", "collisions", "positions", "wounded",
+                                          "ta", "tb", "rho_binary", "spectator_a", "spectator_b"))
+    names = set(os.listdir(tmp_path / "data"))
+    with open(os.path.join(os.path.dirname(__file__), "golden", "text_outputs.json")) as f:
+        ref_names = set(json.load(f)["jet/files"]) - {"quarks.data"}
+    # the reference's files of events 1 and 2 (it ran two); the same kinds for event 3
+    assert ref_names <= names
+    assert {n.replace("_event_3", "_event_1") for n in names if "_event_3" in n} <= ref_names
+    A = 197
+    vz = np.sqrt(1.0 - 1.0 / 100.0 ** 2)
+    Y = 0.5 * np.log((1 + vz) / (1 - vz + 1e-100))
+    for e in range(3):
+        n = e + 1
+        pos, wnd = out["positions"][e], out["wounded"][e].astype(bool)
+        want = "".join(f"{x:10.3g}   {y:10.3g}   {1 if k < A else 2}\n" for k, (x, y) in enumerate(pos) if wnd[k])
+        assert (tmp_path / "data" / f"ParticipantTable_event_{n}.dat").read_text() == want
+        want = "".join(f"{x:10.4e}  {y:.4e}  {(Y if k < A else -Y):.4e}\n" for k, (x, y) in enumerate(pos)
+                       if not wnd[k])
+        assert (tmp_path / "data" / f"Spectators_event_{n}.dat").read_text() == want
+        lines = [f"{x:10.3g}{y:10.3g}\n" for x, y in out["collisions"][e][:out["ncoll"][e]]]
+        assert (tmp_path / "data" / f"BinaryCollisionTable_event_{n}.dat").read_text() == "".join(lines)
+        got = np.loadtxt(tmp_path / "data" / f"sn_ecc_eccp_10_event_{n}.dat", ndmin=2)
+        np.testing.assert_allclose(got[0], out["ecc"][e], rtol=1e-7, atol=1e-12)
+        for stem, grid in (("sd", out["rho"][e] * 40.0), ("rho_binary", out["rho_binary"][e]),
+                           ("nuclear_thickness_TA", out["ta"][e]), ("nuclear_thickness_TB", out["tb"][e]),
+                           ("rhob", out["ta"][e].astype(np.float64) + out["tb"][e]),
+                           ("spectator_density_A", out["spectator_a"][e]),
+                           ("spectator_density_B", out["spectator_b"][e])):
+            write_density_block(np.asarray(grid, dtype=np.float64) if stem != "sd" else
+                                out["rho"][e].astype(np.float64) * 40.0, str(tmp_path / "ref_block.dat"))
+            assert (tmp_path / "data" / f"{stem}_event_{n}_block.dat").read_text() == \
+                (tmp_path / "ref_block.dat").read_text(), (stem, n)
+
+
+def test_operation_1_pt_differential(tmp_path):
+    """PT_flag < 0 with MC-KLN: the p_T-differential table and per-event
+    densities (MCnucl::makeTable(ptmin, dpt, iPtmax), setDensity(iy, ipt));
+    use_5col writes sd_event_<n>_5col.dat (dumpDensity5Col: setSd of every
+    bin per cell), and no p_T-integrated profile is written."""
+    kln = dict(which_mc_model=1, sub_model=7, **{"lambda": 0.288}, cc_fluctuation_model=0, maxx=6, maxy=6, dx=0.2,
+               dy=0.2)
+    p = _run(tmp_path, operation=1, nev=2, PT_flag=-1, use_5col=1, **kln)
+    eng = _engine(p)
+    eng.kln_pt_table(0.1, 0.1, 20)
+    out = eng.generate(0, 2, want=("rho_pt", "npart"))
+    names = sorted(os.listdir(tmp_path / "data"))
+    assert not any(n.endswith("_block.dat") for n in names), names
+    for e in range(2):
+        text = (tmp_path / "data" / f"sd_event_{e + 1}_5col.dat").read_text()
+        head, body = text.split("\n", 1)
+        assert head == "%% <npart>= %g xmax= 61 ymax= 61 Ptmax= 20" % out["npart"][e].sum()
+        got = np.loadtxt(io.StringIO(body), ndmin=2)
+        want = out["rho_pt"][e].reshape(61 * 61, 20).astype(np.float64) * 40.0
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=0)
+        assert got.max() > 0

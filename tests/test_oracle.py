@@ -142,6 +142,20 @@ def test_kln_quadrature_near_bases(oracle, golden):
         assert got == pytest.approx(want, rel=5e-3)
 
 
+def test_kln_pt_rule_matches_reference_simpson(oracle, golden):
+    """dN/dy d^2p_T at fixed p_T (MCnucl::makeTable(ptmin, dpt, iPtmax)):
+    the oracle's Gauss-Legendre rule (64 k_T x 32 phi nodes) against the
+    reference's adaptive Simpson integral (relative precision 1e-4)."""
+    import ctypes
+    from oracle.oracle import KLN
+    g = golden("kln_pt.npz")
+    k = KLN()
+    oracle.lib.smco_kln_init(ctypes.byref(k), 2760.0, 0.288)
+    for (ta, tb, pt), want in zip(g["points"], g["values"]):
+        got = oracle.lib.smco_kln_dndy_pt(ctypes.byref(k), ta, tb, pt, 64, 32)
+        assert got == pytest.approx(want, rel=5e-4), (ta, tb, pt)
+
+
 def test_kln_lookup_matches_reference(oracle, golden):
     from oracle.oracle import _ptr
     g = golden("kln.npz")

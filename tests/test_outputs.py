@@ -163,3 +163,53 @@ def test_ecc_npy_holds_the_text_columns(lib, tmp_path, deformed):
         np.testing.assert_array_equal(b, want)
         assert t.shape == b.shape
         np.testing.assert_allclose(t, b, rtol=6e-8, atol=1e-300)
+
+
+def test_jet_mode_tables(lib, texts, tmp_path):
+    """Operation 2's per-event tables (src/MakeDensity.cpp:148-498):
+    ParticipantTable_event_<n>.dat (MCnucl::dumpparticipantTable, appended),
+    Spectators_event_<n>.dat (MCnucl::dumpSpectatorsTable, beam rapidity of
+    sqrt(s) = 200 GeV), BinaryCollisionTable_event_<n>.dat, and the
+    per-event eccentricity files, written again from the values the
+    reference's own files hold."""
+    part = np.loadtxt(io.StringIO(texts["jet/ParticipantTable_event_1.dat"]), ndmin=2)
+    ids = part[:, 2].astype(int)
+    A, B = int((ids == 1).sum()), int((ids == 2).sum())
+    xy = np.ascontiguousarray(part[:, :2])
+    wounded = np.ones(A + B, dtype=np.uint8)
+    out = str(tmp_path / "part.dat").encode()
+    _lib.check(lib.smc_write_participant_table(_lib.ptr(xy), _lib.ptr(wounded), A, B, out),
+               "smc_write_participant_table")
+    assert (tmp_path / "part.dat").read_text() == texts["jet/ParticipantTable_event_1.dat"]
+
+    spec = np.loadtxt(io.StringIO(texts["jet/Spectators_event_1.dat"]), ndmin=2)
+    A, B = int((spec[:, 2] > 0).sum()), int((spec[:, 2] < 0).sum())
+    xy = np.ascontiguousarray(spec[:, :2])
+    none = np.zeros(A + B, dtype=np.uint8)
+    out = str(tmp_path / "spec.dat").encode()
+    _lib.check(lib.smc_write_spectator_table(_lib.ptr(xy), _lib.ptr(none), A, B, 200.0, out),
+               "smc_write_spectator_table")
+    assert (tmp_path / "spec.dat").read_text() == texts["jet/Spectators_event_1.dat"]
+
+    coll = np.ascontiguousarray(np.loadtxt(io.StringIO(texts["jet/BinaryCollisionTable_event_1.dat"]), ndmin=2))
+    out = str(tmp_path / "coll.dat").encode()
+    _lib.check(lib.smc_write_binary_table(_lib.ptr(coll), len(coll), out), "smc_write_binary_table")
+    assert (tmp_path / "coll.dat").read_text() == texts["jet/BinaryCollisionTable_event_1.dat"]
+
+    ecc = np.ascontiguousarray(np.loadtxt(io.StringIO(texts["jet/sn_ecc_eccp_10_event_1.dat"]), ndmin=2))
+    pattern = str(tmp_path / "sn_ecc_eccp_%d_event_1.dat").encode()
+    _lib.check(lib.smc_write_ecc(_lib.ptr(ecc), 1, 2, 3, pattern), "smc_write_ecc")
+    for name in ("sn_ecc_eccp_2_event_1.dat", "sn_ecc_eccp_10_event_1.dat"):
+        assert (tmp_path / name).read_text() == texts["jet/" + name], name
+
+
+def test_pt_differential_layout(lib, tmp_path):
+    """MakeDensity::dumpDensity5Col / dumpDesityptCol (src/MakeDensity.cpp:
+    2612-2661): a header line, then the p_T bins of one cell per line."""
+    data = np.arange(2 * 3 * 4, dtype=np.float32).reshape(2, 3, 4) * 0.5 + 0.25
+    out = str(tmp_path / "pt.dat").encode()
+    _lib.check(lib.smc_write_density_pt(_lib.ptr(data), 2, 3, 4, 17.0, 40.0, out), "smc_write_density_pt")
+    lines = (tmp_path / "pt.dat").read_text().split("\n")
+    assert lines[0] == "% <npart>= 17 xmax= 2 ymax= 3 Ptmax= 4"
+    assert lines[1] == "".join("%22.12e" % (v * 40.0) for v in data[0, 0])
+    assert len(lines) == 2 + 6 and lines[-1] == ""
