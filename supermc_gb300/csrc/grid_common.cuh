@@ -118,11 +118,13 @@ enum CellCode : int {
 
 // The six-point interpolation of the dN/dy table in table cell (ii, jj) at
 // offsets (fi, fj) in lattice units (src/MCnucl.cpp:672-676)
+// (sixPoint2dInterp, src/arsenal.cpp:33-54, with the cell's coefficients
+// taken in FP64 from the table once per context: two 16-byte loads and five
+// FMAs per cell)
 __device__ __forceinline__ float kln_interp(const DevParams &P, int ii, int jj, float fi, float fj) {
-  const int tm = P.kln_tmax;
-  const float *T = P.kln_table + ii * tm + jj;
-  return six_point(fi, fj, __ldg(T), __ldg(T + 1), __ldg(T + 2), __ldg(T + tm), __ldg(T + tm + 1),
-                   __ldg(T + 2 * tm));
+  const float4 *c = P.kln_coef + 2 * ((size_t)ii * P.kln_tmax + jj);
+  const float4 a = __ldg(c), b = __ldg(c + 1);   // axx, axy, ayy, bx | by, v00
+  return fmaf(fmaf(a.x, fi, fmaf(a.y, fj, a.w)), fi, fmaf(fmaf(a.z, fj, b.x), fj, b.y));
 }
 
 // Relative error bound of an event's FP32 thickness sums: the per-term

@@ -151,6 +151,7 @@ struct Ctx {
   DevBuf<uint8_t> wounded;
   DevBuf<double> kln64;
   DevBuf<float> kln32;
+  DevBuf<float4> kln_coef;
   // p_T-differential table (smc_kln_pt_table) [tmax][tmax][pt_nbins], its
   // bins, and the per-event thickness and p_T-differential staging buffers
   DevBuf<double> pt64;
@@ -345,6 +346,28 @@ smc_status build_kln_table(Ctx *c) {
   CK(c->kln32.ensure((size_t)tmax * tmax));
   CK(smc::launch_kln_table(K, tmax, c->info.kln_dT, c->kln64.p, c->kln32.p, c->st));
   CK(cudaStreamSynchronize(c->st));
+  // the six-point polynomial of every table cell (sixPoint2dInterp,
+  // src/arsenal.cpp:33-54) in FP64, rounded once: the per-cell lookup is
+  // then two loads and five FMAs
+  {
+    std::vector<double> t((size_t)tmax * tmax);
+    CK(cudaMemcpy(t.data(), c->kln64.p, sizeof(double) * t.size(), cudaMemcpyDeviceToHost));
+    std::vector<float4> coef((size_t)tmax * tmax * 2, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int i = 0; i + 2 < tmax; i++)
+      for (int j = 0; j + 2 < tmax; j++) {
+        const double v00 = t[(size_t)i * tmax + j], v01 = t[(size_t)i * tmax + j + 1], v02 = t[(size_t)i * tmax + j + 2];
+        const double v10 = t[(size_t)(i + 1) * tmax + j], v11 = t[(size_t)(i + 1) * tmax + j + 1];
+        const double v20 = t[(size_t)(i + 2) * tmax + j];
+        const double axx = 0.5 * (v00 - 2. * v10 + v20), axy = v00 - v01 - v10 + v11;
+        const double ayy = 0.5 * (v00 - 2. * v01 + v02);
+        const double bx = 0.5 * (-3. * v00 + 4. * v10 - v20), by = 0.5 * (-3. * v00 + 4. * v01 - v02);
+        coef[2 * ((size_t)i * tmax + j)] = make_float4((float)axx, (float)axy, (float)ayy, (float)bx);
+        coef[2 * ((size_t)i * tmax + j) + 1] = make_float4((float)by, (float)v00, 0.f, 0.f);
+      }
+    CK(c->kln_coef.ensure(coef.size()));
+    CK(cudaMemcpy(c->kln_coef.p, coef.data(), sizeof(float4) * coef.size(), cudaMemcpyHostToDevice));
+    c->P.kln_coef = c->kln_coef.p;
+  }
   cudaFree(d_nodes);
   c->P.kln_table = c->kln32.p;
   return SMC_OK;
@@ -837,6 +860,7 @@ void smc_destroy(void *ctx) {
   c->tb.release(); c->scratch.release(); c->status.release(); c->npart.release(); c->ncoll.release();
   c->attempts.release(); c->wounded.release(); c->rho_ev.release(); c->corr_ev.release(); c->cm_ev.release();
   c->mix_sys.release(); c->mix_ev.release(); c->mix_order.release(); c->kln64.release(); c->kln32.release();
+  c->kln_coef.release();
   c->pt64.release(); c->pt32.release(); c->pt_ta.release(); c->pt_tb.release(); c->rho_pt.release();
   c->ev_aux.release();
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();

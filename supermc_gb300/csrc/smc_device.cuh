@@ -120,6 +120,9 @@ struct DevParams {
   // half the smallest nonzero thickness a source adds (its value at the cut)
   float kln_band, kln_tzero;
   const float *kln_table;   // [tmax][tmax] (device)
+  // the six-point interpolation of each table cell (i, j) as polynomial
+  // coefficients (axx, axy, ayy, bx, by, v00, 0, 0), from the FP64 table
+  const float4 *kln_coef;   // [tmax][tmax][2] (device)
   int want_ta, want_tb;     // thickness planes requested
   int splat_mw;             // widest splat window in columns (+ margin)
   int n_planes;             // accumulator planes of the splat (1..3)
