@@ -273,14 +273,26 @@ __device__ __forceinline__ void block_mean2_f(float v0, float v1, int n, float2 
   m1 = out[1];
 }
 
-__device__ __forceinline__ int block_sum_i(int v, int *red, int slot) {
-  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) red[slot * (kNT / 32) + w] = v;
+// three block sums with one barrier (red: 3 * kNT / 32 ints)
+__device__ __forceinline__ void block_sum3_i(int a, int b, int c, int *red, int &sa, int &sb, int &sc) {
+  for (int o = 16; o; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    red[w] = a;
+    red[kNT / 32 + w] = b;
+    red[2 * (kNT / 32) + w] = c;
+  }
   __syncthreads();
-  int s = 0;
-  for (int i = 0; i < kNT / 32; i++) s += red[slot * (kNT / 32) + i];
-  return s;
+  sa = sb = sc = 0;
+  for (int i = 0; i < kNT / 32; i++) {
+    sa += red[i];
+    sb += red[kNT / 32 + i];
+    sc += red[2 * (kNT / 32) + i];
+  }
 }
 
 // Samples one nucleus into sm.ax/ay/az[w] (nucleus frame, centre of mass
@@ -527,9 +539,8 @@ __device__ void place_sorted(SampleSmem &sm, int w, int A, double xc, const doub
       ry = (float)y;
     }
   } else {
-    double mxa, mya;   // centre of mass
+    double mxa, mya;   // centre of mass (block_mean2_f ends with a barrier)
     block_mean2_f(tid < A ? sm.ax[w][tid] : 0.f, tid < A ? sm.ay[w][tid] : 0.f, A, sm.red2, sm.bmean, mxa, mya);
-    __syncthreads();
     if (tid < A) {
       rx = sm.ax[w][tid];
       ry = sm.ay[w][tid];
@@ -886,9 +897,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
         sm.hits[0][tid] = cnt;
       }
       __syncthreads();
-      np1 = block_sum_i(tid < A && sm.hits[0][tid] > 0, sm.ired, 0);
-      np2 = block_sum_i(tid < B && sm.hits[1][tid] > 0, sm.ired, 1);
-      ncoll = block_sum_i(cnt, sm.ired, 2);
+      block_sum3_i(tid < A && sm.hits[0][tid] > 0, tid < B && sm.hits[1][tid] > 0, cnt, sm.ired, np1, np2, ncoll);
       __syncthreads();
       if (inject) break;
       int np = np1 + np2;

@@ -103,6 +103,7 @@ inline double derive_common(const smc_params &p, smc::DevParams &P) {
   P.nx = (int)((p.maxx - (-p.maxx)) / p.dx + 0.1) + 1;   // MCnucl.cpp:39-40
   P.ny = (int)((p.maxy - (-p.maxy)) / p.dy + 0.1) + 1;
   P.xmin = -p.maxx; P.ymin = -p.maxy; P.dx = p.dx; P.dy = p.dy;
+  P.inv_dx = 1.0 / p.dx; P.inv_dy = 1.0 / p.dy;
   P.width = width; P.w2 = width * width; P.quark_width = p.quark_width;
   P.peak = 1 / (2 * M_PI * width * width);
   P.dsq = 0.1 * sigin / M_PI / 1;                       // MCnucl.cpp:120 (overSample = 1)

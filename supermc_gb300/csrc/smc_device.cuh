@@ -100,6 +100,7 @@ struct SystemDev {
 struct DevParams {
   int nx, ny;
   double xmin, ymin, dx, dy;
+  double inv_dx, inv_dy;   // 1 / dx, 1 / dy (the sources' grid offsets)
   double width, w2, quark_width, peak;   // nucleon width, width^2, 1/(2 pi w^2)
   double dsq, sigin, sigma_gg;
   double alpha, final_factor;
@@ -351,15 +352,18 @@ static __device__ __noinline__ float nbd_cell(const DevParams &P, uint64_t ev, u
 // distance (k - cell) - fraction from the position to grid point k then errs
 // by at most 2^-25 + 2^-24 |distance| grid units, where a difference of FP32
 // coordinates errs by 2^-24 of the coordinates' magnitude.
-__device__ __forceinline__ void grid_offset(double v, double vmin, double d, float &cell, float &frac) {
-  const double g = (v - vmin) / d;
+__device__ __forceinline__ void grid_offset(double v, double vmin, double inv_d, float &cell, float &frac) {
+  // a product by the rounded 1/d: within an FP64 ulp or two of the quotient,
+  // far below the FP32 rounding of the fraction (an FP64 division costs
+  // several times more on this part)
+  const double g = (v - vmin) * inv_d;
   const double c = floor(g);
   cell = (float)c;
   frac = (float)(g - c);
 }
 __device__ __forceinline__ void set_grid_offsets(Source &s, const DevParams &P) {
-  grid_offset(s.x, P.xmin, P.dx, s.gi0, s.gfx);
-  grid_offset(s.y, P.ymin, P.dy, s.gj0, s.gfy);
+  grid_offset(s.x, P.xmin, P.inv_dx, s.gi0, s.gfx);
+  grid_offset(s.y, P.ymin, P.inv_dy, s.gj0, s.gfy);
 }
 #endif
 
