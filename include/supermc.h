@@ -179,6 +179,11 @@ smc_status smc_create(const smc_params *params, void **ctx_out);
 void smc_destroy(void *ctx);
 smc_status smc_get_info(void *ctx, smc_info *info);
 const char *smc_status_string(smc_status s);
+/* Name and description of the calling thread's last CUDA runtime error, for
+ * the message of an SMC_ERR_CUDA status (cudaGetLastError: reading it clears
+ * an error that is not sticky; "cudaSuccess: no error" when none is pending).
+ * The string lives until the thread's next call. */
+const char *smc_cuda_error_string(void);
 /* Runs subsequent work on the given cudaStream_t (NULL: the context's own
  * stream). */
 smc_status smc_set_stream(void *ctx, void *cuda_stream);

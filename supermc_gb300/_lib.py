@@ -14,6 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("SUPERMC_GB300_LIB") or os.path.join(HERE, "_build", "libsupermc_gb300.so")
 
 SMC_OK = 0
+SMC_ERR_CUDA = 7
 STATUS_NAMES = {
     0: "SMC_OK", 1: "SMC_ERR_ARGUMENT", 2: "SMC_ERR_CONFIG", 3: "SMC_ERR_RETRY_CAP",
     4: "SMC_ERR_KLN_TABLE", 5: "SMC_ERR_ZERO_DNDY", 6: "SMC_ERR_CAPACITY", 7: "SMC_ERR_CUDA",
@@ -22,7 +23,8 @@ STATUS_NAMES = {
 ECC_LEN = 49
 
 # the entry points include/supermc.h declares (tests/test_capi.py checks the set)
-EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "smc_set_stream",
+EXPORTS = ["smc_create", "smc_destroy", "smc_get_info", "smc_status_string", "smc_cuda_error_string",
+           "smc_set_stream",
            "smc_synchronize", "smc_generate", "smc_inject", "smc_generate_mixed", "smc_generate_plain",
            "smc_set_timing",
            "smc_set_grid_path", "smc_get_stats", "smc_reset_stats", "smc_kln_table", "smc_write_ecc",
@@ -135,6 +137,8 @@ def load() -> ctypes.CDLL:
     lib.smc_get_info.argtypes = [vp, ctypes.POINTER(SmcInfo)]
     lib.smc_status_string.argtypes = [ctypes.c_int]
     lib.smc_status_string.restype = ctypes.c_char_p
+    lib.smc_cuda_error_string.argtypes = []
+    lib.smc_cuda_error_string.restype = ctypes.c_char_p
     lib.smc_set_stream.argtypes = [vp, vp]
     lib.smc_synchronize.argtypes = [vp]
     lib.smc_generate.argtypes = [vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(SmcOutputs)]
@@ -183,6 +187,8 @@ def load() -> ctypes.CDLL:
 
 def check(status: int, what: str) -> None:
     if status != SMC_OK:
+        if status == SMC_ERR_CUDA and _lib is not None:
+            what = f"{what} ({_lib.smc_cuda_error_string().decode()})"
         raise SmcError(status, what)
 
 

@@ -758,6 +758,13 @@ const char *smc_status_string(smc_status s) {
   }
 }
 
+const char *smc_cuda_error_string(void) {
+  thread_local char buf[256];
+  const cudaError_t e = cudaGetLastError();
+  std::snprintf(buf, sizeof buf, "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+  return buf;
+}
+
 smc_status smc_create(const smc_params *params, void **ctx_out) {
   if (!params || !ctx_out) return SMC_ERR_ARGUMENT;
   *ctx_out = nullptr;

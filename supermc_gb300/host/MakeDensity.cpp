@@ -9,7 +9,10 @@
 
 namespace smc {
 
-Error::Error(smc_status s, const std::string &what) : std::runtime_error(what + ": " + smc_status_string(s)), status(s) {}
+Error::Error(smc_status s, const std::string &what)
+    : std::runtime_error(what + ": " + smc_status_string(s) +
+                         (s == SMC_ERR_CUDA ? std::string(" (") + smc_cuda_error_string() + ")" : std::string())),
+      status(s) {}
 
 namespace {
 
