@@ -34,8 +34,7 @@ constexpr int kR = 8;               // rows per strip (held in registers by the 
 constexpr int kGS = 64;             // sources per group
 constexpr int kGW = kGS / 32;       // 32-bit words of a group's source mask
 static_assert(kGS % 32 == 0, "source masks are whole words");
-constexpr int kSplit = 1;           // work units per 32-column block (row slices of the strip)
-constexpr int kRU = kR / kSplit;    // rows of a work unit
+constexpr int kRU = kR;             // rows of a work unit
 static_assert(kRU % 4 == 0, "units are read four rows at a time");
 
 // (source, row) pairs of a strip, structure of arrays [kGS][kR]: the row
@@ -181,6 +180,9 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
     KSum cm0, cm1, cm2, pre;   // pre: the density before NBD fluctuations (the zero-dN/dy test)
     const bool full = out_rho || ta || tb;
     const float kband = kln_event_band(P, rec);
+    // the 32-column blocks of the event's window box: the accumulators
+    // outside them are never written or read
+    const int jb0 = rec.jmin >> 5, nunits = rec.jmax > rec.jmin ? (((rec.jmax + 31) >> 5) - jb0) * np : 0;
     __syncthreads();
 
     for (int r0 = 0; r0 < nx; r0 += kR) {
@@ -245,35 +247,34 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
             }
             __syncthreads();
             // accumulation: lane owns column j of the strip; the work units are
-            // (32-column block, slice of kRU rows), dealt to the warps round
-            // robin so that the busy central blocks spread over them; each
-            // unit visits only the sources that reach its block, in order
-            for (int u = wid; u < (nyp / 32) * kSplit; u += kWarps) {
-              const int jb = u / kSplit, j = jb * 32 + lane, rh = (u - jb * kSplit) * kRU;
+            // (32-column block of the event's box, plane), dealt to the warps
+            // round robin so that the busy central blocks and the two planes
+            // spread over them; each unit visits only the sources of its
+            // plane that reach its block, in order
+            for (int u = wid; u < nunits; u += kWarps) {
+              const int ub = np == 1 ? u : u / np, pl = u - ub * np;
+              const int jb = jb0 + ub, j = jb * 32 + lane;
               const float jf = (float)j;
               // the group's sources whose window reaches this block: lane q
               // of word h tests source 32 h + q
-              int qpl[kGW];
               bool qin[kGW];
 #pragma unroll
               for (int h = 0; h < kGW; h++) {
                 const int q = h * 32 + lane;
                 qin[h] = false;
-                qpl[h] = 0;
                 if (q < gn) {
                   const GroupSrc &g = grp[q];
-                  qin[h] = g.yr > jb * 32 && g.yl < jb * 32 + 32 && g.yr > g.yl;
-                  qpl[h] = g.plane;
+                  qin[h] = g.yr > jb * 32 && g.yl < jb * 32 + 32 && g.yr > g.yl && g.plane == pl;
                 }
               }
-              for (int pl = 0; pl < np; pl++) {
-                float *ab = acc + ((size_t)pl * kR + rh) * nyp + j;
+              {
+                float *ab = acc + (size_t)pl * kR * nyp + j;
                 float a[kRU];
 #pragma unroll
                 for (int r = 0; r < kRU; r++) a[r] = fresh ? 0.f : ab[r * nyp];
 #pragma unroll
                 for (int h = 0; h < kGW; h++) {
-                  uint32_t m = __ballot_sync(0xffffffffu, qin[h] && qpl[h] == pl);
+                  uint32_t m = __ballot_sync(0xffffffffu, qin[h]);
                   while (m) {
                     const int q = h * 32 + __ffs(m) - 1;
                     m &= m - 1u;
@@ -281,7 +282,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
                     const float ey = (g.kind & 16) ? 1.f : gauss_grid(jf, g.gj0, g.gfy, cy);
 #pragma unroll
                     for (int r4 = 0; r4 < kRU; r4 += 4) {
-                      const int o = q * kR + rh + r4;
+                      const int o = q * kR + r4;
                       const float4 w4 = *reinterpret_cast<const float4 *>(p_exw + o);
                       const int4 a4 = *reinterpret_cast<const int4 *>(p_ja + o);
                       const int4 l4 = *reinterpret_cast<const int4 *>(p_len + o);
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
             float p0 = 0.f, p1 = 0.f, p2 = 0.f, pp = 0.f;
             for (int j = s0 + lane; j < s1; j += 32) {
               float v = 0.f, t1 = 0.f, t2 = 0.f;
-              if (active && !fresh) {
+              if (active && !fresh && j >= rec.jmin && j < rec.jmax) {
                 const float a0 = acc[rr * nyp + j];
                 const float a1 = np > 1 ? acc[(kR + rr) * nyp + j] : 0.f;
                 const float a2 = np > 2 ? acc[(2 * kR + rr) * nyp + j] : 0.f;
