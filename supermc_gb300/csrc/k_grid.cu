@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(kGT, 5) k_grid(DevParams P, int n_events, cons
             uint64_t pend = 0;
             // the lane's sums over the segment's cells in FP32 (at most
             // kPendSteps terms), added to the compensated sums after it
-            float p0 = 0.f, p1 = 0.f, p2 = 0.f, pp = 0.f;
+            float p0 = 0.f, p2 = 0.f, pp = 0.f;
             for (int j = s0 + lane; j < s1; j += 32) {
               float v = 0.f, t1 = 0.f, t2 = 0.f;
               if (active && !fresh && j >= rec.jmin && j < rec.jmax) {
