@@ -29,3 +29,19 @@ def test_status_strings_without_device():
     lib = _lib.load()
     for s in range(9):
         assert lib.smc_status_string(s)
+
+
+def test_cuda_error_string_format():
+    """smc_cuda_error_string names the pending CUDA runtime error as
+    "<name>: <description>" (here, without a device, whatever the runtime
+    reports), and an SMC_ERR_CUDA raised by the Python layer carries it."""
+    from supermc_gb300 import _lib
+    lib = _lib.load()
+    text = lib.smc_cuda_error_string().decode()
+    assert text.startswith("cuda") and ": " in text
+    try:
+        _lib.check(_lib.SMC_ERR_CUDA, "probe")
+    except _lib.SmcError as e:
+        assert "probe (cuda" in str(e) and e.status == _lib.SMC_ERR_CUDA
+    else:
+        raise AssertionError("SMC_ERR_CUDA did not raise")
