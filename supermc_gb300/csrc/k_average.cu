@@ -93,23 +93,40 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
   __shared__ float2 red[kAT / 32];
   __shared__ double s_par[4];   // X, Y, cos, sin
   __shared__ int s_box[4];      // the event's new window bounds: imin, imax, jmin, jmax
+  extern __shared__ float s_xy[];   // the cells' coordinates (float)(xmin + i dx), then y
   const int tid = threadIdx.x;
   const int nx = P.nx, ny = P.ny;
   const float inv_dx = (float)(1.0 / P.dx), inv_dy = (float)(1.0 / P.dy);
   const double d_max = P.shape_of_nucleons == 1 ? 2. * sqrt(P.dsq) : 5. * P.width;
+  float *xg = s_xy, *yg = s_xy + nx;
+  for (int i = tid; i < nx; i += kAT) xg[i] = (float)(P.xmin + i * P.dx);
+  for (int j = tid; j < ny; j += kAT) yg[j] = (float)(P.ymin + j * P.dy);
+  __syncthreads();
+  // The density is zero outside the event's window box, and zero cells add
+  // nothing: each thread visits the cells c = tid (mod kAT) of the full grid
+  // in increasing order, as a walk over the whole grid would, but only those
+  // inside the box (its first column of row i: jmin + ((tid - i ny - jmin)
+  // mod kAT)), so the sums are those of the full walk.
+  auto for_box = [&](const EventRec &r, auto &&f) {
+    if (r.imax <= r.imin || r.jmax <= r.jmin) return;
+    for (int i = r.imin; i < r.imax; i++) {
+      const int row0 = i * ny + r.jmin;
+      for (int j = r.jmin + ((tid - row0) & (kAT - 1)); j < r.jmax; j += kAT) f(i, j);
+    }
+  };
+  static_assert((kAT & (kAT - 1)) == 0, "cells are dealt by a power-of-two stride");
   for (int e = blockIdx.x; e < n_events; e += gridDim.x) {
     const EventRec rec = recs[e];
     const float *g = rho + (size_t)e * nx * ny;
     // ---- centre of mass over the full grid (weights rho dx dy; dx dy cancels)
     Kahan sw, sx, sy;
-    for (int c = tid; c < nx * ny; c += kAT) {
-      const float v = g[c];
-      if (v == 0.f) continue;
-      const int i = c / ny, j = c - i * ny;
+    for_box(rec, [&](int i, int j) {
+      const float v = g[(size_t)i * ny + j];
+      if (v == 0.f) return;
       sw.add(v);
-      sx.add((float)(P.xmin + i * P.dx) * v);
-      sy.add((float)(P.ymin + j * P.dy) * v);
-    }
+      sx.add(xg[i] * v);
+      sy.add(yg[j] * v);
+    });
     const double W = block_sum_df(sw.s, sw.c, red);
     const double SX = block_sum_df(sx.s, sx.c, red);
     const double SY = block_sum_df(sy.s, sy.c, red);
@@ -121,11 +138,10 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
     // ---- order-n angle: sum r^n e^{in theta} rho about the centre (full grid)
     Kahan sr, si;
     const float Xf = (float)X, Yf = (float)Y;
-    for (int c = tid; c < nx * ny; c += kAT) {
-      const float v = g[c];
-      if (v == 0.f) continue;
-      const int i = c / ny, j = c - i * ny;
-      const float x = (float)(P.xmin + i * P.dx) - Xf, y = (float)(P.ymin + j * P.dy) - Yf;
+    for_box(rec, [&](int i, int j) {
+      const float v = g[(size_t)i * ny + j];
+      if (v == 0.f) return;
+      const float x = xg[i] - Xf, y = yg[j] - Yf;
       float zr = x, zi = y;
       for (int k = 1; k < order; k++) {
         const float t = zr * x - zi * y;
@@ -134,7 +150,7 @@ __global__ void __launch_bounds__(kAT) k_avg_transform(DevParams P, int n_events
       }
       sr.add(zr * v);
       si.add(zi * v);
-    }
+    });
     const double NR = block_sum_df(sr.s, sr.c, red);
     const double NI = block_sum_df(si.s, si.c, red);
     if (tid == 0) {
@@ -308,20 +324,63 @@ __global__ void k_avg_accum(const float *rho, int n_events, size_t cells, double
 // ---------------------------------------------------- centrality bins
 // Events of the chunk in bin order (bin k: edges[k] <= Npart < edges[k+1]);
 // seg[k] .. seg[k+1] delimit bin k in order[], events outside every bin are
-// left out.  One thread: deterministic order, m is a chunk.
-__global__ void k_avg_bins(const EventRec *recs, int n, const int *edges, int nbins, int *order, int *seg,
-                           int *counts) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int pos = 0;
-  for (int b = 0; b < nbins; b++) {
-    seg[b] = pos;
-    for (int e = 0; e < n; e++) {
-      const int np = recs[e].npart1 + recs[e].npart2;
-      if (recs[e].ncoll > 0 && np >= edges[b] && np < edges[b + 1]) order[pos++] = e;
-    }
-    counts[b] += pos - seg[b];
+// left out; within a bin the events keep their order (the bin sums are
+// taken in that order).
+__global__ void __launch_bounds__(1024) k_avg_bins(const EventRec *recs, int n, const int *edges, int nbins,
+                                                   int *order, int *seg, int *counts) {
+  // one CTA per bin b: the events of the bins before it give seg[b]; its own
+  // events are then compacted in event order (bins are disjoint: the edges
+  // do not decrease)
+  __shared__ int s_w[32], s_v[32];
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int lo0 = edges[0], lob = edges[b], hib = edges[b + 1];
+  auto npart = [&](int e, bool &in) {
+    const EventRec &r = recs[e];
+    in = r.ncoll > 0;
+    return r.npart1 + r.npart2;
+  };
+  int before = 0, mine = 0;
+  for (int e = tid; e < n; e += 1024) {
+    bool in;
+    const int np = npart(e, in);
+    before += in && np >= lo0 && np < lob;
+    mine += in && np >= lob && np < hib;
   }
-  seg[nbins] = pos;
+  for (int o = 16; o; o >>= 1) {
+    before += __shfl_xor_sync(0xffffffffu, before, o);
+    mine += __shfl_xor_sync(0xffffffffu, mine, o);
+  }
+  if (lane == 0) { s_w[wid] = before; s_v[wid] = mine; }
+  __syncthreads();
+  int base = 0, total = 0;
+  for (int q = 0; q < 32; q++) { base += s_w[q]; total += s_v[q]; }
+  __syncthreads();
+  if (tid == 0) {
+    seg[b] = base;
+    counts[b] += total;
+    if (b == nbins - 1) seg[nbins] = base + total;
+  }
+  for (int e0 = 0; e0 < n; e0 += 1024) {
+    const int e = e0 + tid;
+    bool f = false;
+    if (e < n) {
+      bool in;
+      const int np = npart(e, in);
+      f = in && np >= lob && np < hib;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) s_w[wid] = __popc(bal);
+    __syncthreads();
+    int off = 0, tot = 0;
+    for (int q = 0; q < 32; q++) {
+      const int c = s_w[q];
+      off += q < wid ? c : 0;
+      tot += c;
+    }
+    if (f) order[base + off + __popc(bal & ((1u << lane) - 1u))] = e;
+    base += tot;
+    __syncthreads();
+  }
 }
 
 // acc[b][cell] (FP32 sum, compensation) += the chunk's bin-b events at the
@@ -445,7 +504,7 @@ __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const EventRec 
 
 cudaError_t launch_avg_bins(const EventRec *recs, int n, const int *edges, int nbins, int *order, int *seg,
                             int *counts, cudaStream_t st) {
-  k_avg_bins<<<1, 32, 0, st>>>(recs, n, edges, nbins, order, seg, counts);
+  k_avg_bins<<<nbins, 1024, 0, st>>>(recs, n, edges, nbins, order, seg, counts);
   return cudaGetLastError();
 }
 
@@ -463,7 +522,12 @@ cudaError_t launch_avg_init(const DevParams &P, int n, const EventRec *recs, con
 }
 cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Source *srcs, AvgSrc *state,
                                  const float *rho, int order, int mode, int grid, cudaStream_t st, AvgFrame *frame) {
-  k_avg_transform<<<grid, kAT, 0, st>>>(P, n, recs, srcs, state, rho, order, mode, frame);
+  const size_t smem = sizeof(float) * (size_t)(P.nx + P.ny);
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(k_avg_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  k_avg_transform<<<grid, kAT, smem, st>>>(P, n, recs, srcs, state, rho, order, mode, frame);
   return cudaGetLastError();
 }
 cudaError_t launch_avg_accum(const float *rho, int n, size_t cells, double *acc, cudaStream_t st) {
