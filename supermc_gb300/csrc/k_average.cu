@@ -412,9 +412,14 @@ __device__ __forceinline__ float binned_value(const float *G, int nx, int ny, fl
   return (1.f - tx) * ((1.f - ty) * v00 + ty * v01) + tx * ((1.f - ty) * v10 + ty * v11);
 }
 
+// The events of each bin are split into gridDim.z consecutive slices, one
+// per CTA of the tile (the central tiles see nearly every event: one CTA
+// walking all of them would be the whole kernel's critical path).  One
+// slice: the sums go straight into acc; more: slice s writes its
+// compensated sums to part[s][bin][cell] for k_avg_merge.
 __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const EventRec *recs, const float *rho,
                                                    const AvgFrame *frame, const int *order, const int *seg,
-                                                   int nbins, float2 *acc) {
+                                                   int nbins, float2 *acc, float2 *part) {
   __shared__ float4 s_fr[256];
   __shared__ int s_ev[256];
   __shared__ int s_wc[8];
@@ -428,9 +433,11 @@ __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const EventRec 
   const float inv_dx = (float)(1.0 / P.dx), inv_dy = (float)(1.0 / P.dy);
   const float xmin = (float)P.xmin, ymin = (float)P.ymin;
   const bool resample = frame != nullptr;
+  const int slices = gridDim.z, sl = blockIdx.z;
   for (int b = 0; b < nbins; b++) {
     Kahan k;
-    const int e0 = seg[b], e1 = seg[b + 1];
+    const int b0 = seg[b], n_b = seg[b + 1] - b0;
+    const int e0 = b0 + (int)((long long)n_b * sl / slices), e1 = b0 + (int)((long long)n_b * (sl + 1) / slices);
     for (int q0 = e0; q0 < e1; q0 += 256) {
       // ---- stage: which of the next 256 events can reach this tile
       bool hit = false;
@@ -491,7 +498,9 @@ __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const EventRec 
       }
       __syncthreads();   // the staged events are read before the next stage
     }
-    if (in && e1 > e0) {
+    if (in && slices > 1) {
+      part[((size_t)sl * nbins + b) * g + (size_t)i * ny + j] = make_float2(k.s, k.c);
+    } else if (in && e1 > e0) {
       // merge the chunk's compensated sum into the accumulator's
       float2 a = acc[(size_t)b * g + (size_t)i * ny + j];
       const float y = (k.s - k.c) - a.y, t = a.x + y;
@@ -502,6 +511,27 @@ __global__ void __launch_bounds__(256) k_avg_binned(DevParams P, const EventRec 
   }
 }
 
+// acc[b][cell] += the slices' compensated sums, in slice order (empty
+// slices, exactly zero, are passed over)
+__global__ void k_avg_merge(const float2 *part, int slices, size_t cells_all, float2 *acc) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells_all; c += (size_t)gridDim.x * blockDim.x) {
+    float2 a = acc[c];
+    for (int s = 0; s < slices; s++) {
+      const float2 p = part[(size_t)s * cells_all + c];
+      if (p.x == 0.f && p.y == 0.f) continue;
+      const float y = (p.x - p.y) - a.y, t = a.x + y;
+      a.y = (t - a.x) - y;
+      a.x = t;
+    }
+    acc[c] = a;
+  }
+}
+
+int avg_binned_slices(const DevParams &P) {
+  const int tiles = ((P.nx + 15) / 16) * ((P.ny + 15) / 16);
+  return std::max(1, std::min(8, (4096 + tiles - 1) / tiles));
+}
+
 cudaError_t launch_avg_bins(const EventRec *recs, int n, const int *edges, int nbins, int *order, int *seg,
                             int *counts, cudaStream_t st) {
   k_avg_bins<<<nbins, 1024, 0, st>>>(recs, n, edges, nbins, order, seg, counts);
@@ -509,9 +539,14 @@ cudaError_t launch_avg_bins(const EventRec *recs, int n, const int *edges, int n
 }
 
 cudaError_t launch_avg_binned(const DevParams &P, const EventRec *recs, const float *rho, const AvgFrame *frame,
-                              const int *order, const int *seg, int nbins, float2 *acc, cudaStream_t st) {
-  dim3 grid((P.ny + 15) / 16, (P.nx + 15) / 16);
-  k_avg_binned<<<grid, 256, 0, st>>>(P, recs, rho, frame, order, seg, nbins, acc);
+                              const int *order, const int *seg, int nbins, float2 *acc, float2 *part, cudaStream_t st) {
+  const int slices = part ? avg_binned_slices(P) : 1;
+  dim3 grid((P.ny + 15) / 16, (P.nx + 15) / 16, slices);
+  k_avg_binned<<<grid, 256, 0, st>>>(P, recs, rho, frame, order, seg, nbins, acc, part);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || slices == 1) return e;
+  const size_t all = (size_t)nbins * P.nx * P.ny;
+  k_avg_merge<<<(int)std::min<size_t>((all + 255) / 256, 8192), 256, 0, st>>>(part, slices, all, acc);
   return cudaGetLastError();
 }
 

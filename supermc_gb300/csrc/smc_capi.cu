@@ -208,6 +208,7 @@ struct Ctx {
   DevBuf<smc::AvgFrame> avg_frame;
   DevBuf<int> avg_order, avg_seg, avg_count, avg_edges;
   DevBuf<float2> avg_bins;
+  DevBuf<float2> avg_part;   // per-slice bin sums of a chunk (smc_average_binned)
   DevBuf<float> avg_rho, avg_ta, avg_tb, avg_aux;
   DevBuf<Source> avg_view;
   DevBuf<EventRec> avg_vrecs;   // the view's records (every record may splat)
@@ -873,7 +874,7 @@ void smc_destroy(void *ctx) {
   c->avg_state.release(); c->avg_rho.release(); c->avg_acc.release();
   c->avg_ta.release(); c->avg_tb.release(); c->avg_aux.release(); c->avg_view.release(); c->avg_vrecs.release(); c->avg_status.release();
   c->avg_frame.release(); c->avg_order.release(); c->avg_seg.release(); c->avg_count.release();
-  c->avg_edges.release(); c->avg_bins.release();
+  c->avg_edges.release(); c->avg_bins.release(); c->avg_part.release();
   c->ev_order.release(); c->tickets.release();
   c->adj_rho.release(); c->adj_lam.release(); c->adj_grho.release(); c->adj_geps.release(); c->adj_out.release();
   c->icdf_tab[0].release(); c->icdf_tab[1].release(); c->ntan.release(); c->inj_tp.release(); c->inj_tt.release();
@@ -1343,6 +1344,8 @@ smc_status smc_average_binned(void *ctx, uint64_t first_event, int n, int order,
   P.no_moments = 1;
   const size_t g = (size_t)P.nx * P.ny;
   CK(c->avg_bins.ensure(g * nbins));
+  const int slices = smc::avg_binned_slices(P);
+  if (slices > 1) CK(c->avg_part.ensure(g * nbins * slices));
   CK(c->avg_count.ensure(nbins));
   CK(c->avg_seg.ensure(nbins + 1));
   CK(c->avg_edges.ensure(nbins + 1));
@@ -1382,7 +1385,7 @@ smc_status smc_average_binned(void *ctx, uint64_t first_event, int n, int order,
                             c->st));
     CK(timed(c, 2, [&] {
       return smc::launch_avg_binned(P, c->recs.p, c->avg_rho.p, method == 1 ? c->avg_frame.p : nullptr, c->avg_order.p,
-                                    c->avg_seg.p, nbins, c->avg_bins.p, c->st);
+                                    c->avg_seg.p, nbins, c->avg_bins.p, slices > 1 ? c->avg_part.p : nullptr, c->st);
     }));
     c->stats.launches += method == 0 ? 3 : 2;
     c->h_status.resize(m);

@@ -53,9 +53,13 @@ cudaError_t launch_avg_transform(const DevParams &P, int n, EventRec *recs, Sour
 cudaError_t launch_avg_bins(const EventRec *recs, int n, const int *edges, int nbins, int *order, int *seg,
                             int *counts, cudaStream_t st);
 // per-bin compensated sums acc [nbins][nx][ny] of the chunk's densities,
-// bilinearly resampled in each event's frame (frame != NULL) or as they are
+// bilinearly resampled in each event's frame (frame != NULL) or as they are;
+// part (else NULL: one slice): scratch of avg_binned_slices(P) x nbins x
+// nx x ny float2 for the event slices of each bin, merged in order
+int avg_binned_slices(const DevParams &P);
 cudaError_t launch_avg_binned(const DevParams &P, const EventRec *recs, const float *rho, const AvgFrame *frame,
-                              const int *order, const int *seg, int nbins, float2 *acc, cudaStream_t st);
+                              const int *order, const int *seg, int nbins, float2 *acc, float2 *part,
+                              cudaStream_t st);
 cudaError_t launch_avg_accum(const float *rho, int n, size_t cells, double *acc, cudaStream_t st);
 // averaged mode's derived grids: source views (0: rho_binary, 1: spectators)
 // and the T_A T_B product accumulation
