@@ -19,7 +19,6 @@ namespace smc {
 
 constexpr int kNT = 256;   // threads per CTA; also the candidate batch size
 constexpr int kSlab = 32;  // z slabs of the hard-core search, at most
-static_assert(kSlab * (kNT / 32) == kNT, "one slab-mask word per thread is cleared");
 static_assert(kMaxA <= kNT, "one nucleon per thread");
 static_assert(kMaxA % 4 == 0, "float4 rows");
 
@@ -38,19 +37,31 @@ struct SampleConsts {
   int nXp, nYp, ioff, joff;
 };
 
-struct alignas(16) SampleSmem {
+// Working memory of the Woods-Saxon sampler for a group of NT threads (the
+// whole CTA, or half of it when the two nuclei are sampled at once)
+template <int NT>
+struct alignas(16) SampStore {
   // candidate batch (nucleus frame): x, y, z; before the direction is drawn
   // (r, candidate index bits, 0, 0)
-  float4 cpos[kNT];
+  float4 cpos[NT];
   union {
-    uint32_t cmask[kNT][kNT / 32];           // earlier batch candidates each one conflicts with
-    float4 spos[kMaxA];                      // accepted nucleons ordered by z slab
+    uint32_t cmask[NT][NT / 32];           // earlier batch candidates each one conflicts with
+    float4 spos[kMaxA];                    // accepted nucleons ordered by z slab
   } u;
-  uint32_t smask[kSlab][kNT / 32];           // hard-core survivors of the batch per z slab
+  uint32_t smask[kSlab][NT / 32];          // hard-core survivors of the batch per z slab
   int slab_cnt[kSlab], slab_cur[kSlab], slab_start[kSlab + 1];
-  uint8_t cslab[kNT];                        // z slab of each batch candidate
-  uint32_t vb[kNT / 32];                     // hard-core survivors
-  uint32_t keep[kNT / 32], conf[kNT / 32];   // batch resolution state: kept, undecided
+  uint8_t cslab[NT];                       // z slab of each batch candidate
+  uint32_t vb[NT / 32];                    // hard-core survivors
+  uint32_t keep[NT / 32], conf[NT / 32];   // batch resolution state: kept, undecided
+  int ired[NT / 32];                       // radially accepted candidates per warp
+  static_assert(kSlab * (NT / 32) == NT, "one slab-mask word per thread is cleared");
+};
+
+struct alignas(16) SampleSmem {
+  union {
+    SampStore<kNT> full;         // one nucleus at a time, all threads
+    SampStore<kNT / 2> half[2];  // both nuclei at once, one per half
+  } samp;
   // read four at a time (float4): 16-byte aligned rows of kMaxA (a multiple of 4)
   alignas(16) float ax[2][kMaxA];
   alignas(16) float ay[2][kMaxA];
@@ -313,9 +324,22 @@ __device__ __forceinline__ void block_sum3_i(int a, int b, int c, int *red, int 
 // a candidate is dropped once an earlier conflicting candidate is kept and
 // kept once all of them are dropped (the earliest undecided one is decided
 // every round, so the rounds end).  This reproduces the sequential rule.
-__device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t seed, uint64_t ev, int attempt,
-                          float ctr, float phir) {
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+// the sampler's barriers: the CTA's, or a named barrier of one half
+struct FullSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct HalfSync {
+  int h;
+  __device__ __forceinline__ void operator()() const {
+    if (h == 0) asm volatile("bar.sync 1, %0;" ::"n"(kNT / 2) : "memory");
+    else asm volatile("bar.sync 2, %0;" ::"n"(kNT / 2) : "memory");
+  }
+};
+
+template <int NT, typename Sync>
+__device__ bool sample_ws(SampleSmem &sm, SampStore<NT> &ss, const NucleusDev &n, int w, uint64_t seed, uint64_t ev,
+                          int attempt, float ctr, float phir, Sync sync) {
+  const int tid = threadIdx.x & (NT - 1), lane = tid & 31, wid = tid >> 5;
   const int A = n.A;
   const float dmin2 = n.dmin2_f;
   const uint32_t sid = stream_id(attempt, w == 0 ? ST_PROJ : ST_TARG);
@@ -323,10 +347,10 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
   const float rmax = n.rmax_f, inv_w = n.slab_inv_w;
   const int nslab = n.nslab;
   auto slab_of = [&](float z) { return min(nslab - 1, max(0, (int)floorf((z + rmax) * inv_w))); };
-  if (tid < kSlab) { sm.slab_cnt[tid] = 0; sm.slab_cur[tid] = 0; }
-  __syncthreads();
+  if (tid < kSlab) { ss.slab_cnt[tid] = 0; ss.slab_cur[tid] = 0; }
+  sync();
   int n_acc = 0;
-  for (uint32_t base = 0; n_acc < A; base += kNT) {
+  for (uint32_t base = 0; n_acc < A; base += NT) {
     if (base > (1u << 20)) return false;
     const uint32_t c = base + tid;
     float u0, u1;
@@ -343,115 +367,115 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
       ws = ws_radius(n, u0d, u0, u1, r);
     }
     const unsigned bal = __ballot_sync(0xffffffffu, ws);
-    if (lane == 0) sm.ired[wid] = __popc(bal);
+    if (lane == 0) ss.ired[wid] = __popc(bal);
     // accepted nucleons per slab
-    if (tid < n_acc) atomicAdd(&sm.slab_cnt[slab_of(sm.az[w][tid])], 1);
-    sm.smask[tid >> 3][tid & 7] = 0u;   // kSlab * kNT / 32 == kNT words
-    __syncthreads();
+    for (int k = tid; k < n_acc; k += NT) atomicAdd(&ss.slab_cnt[slab_of(sm.az[w][k])], 1);
+    ss.smask[tid / (NT / 32)][tid & (NT / 32 - 1)] = 0u;   // kSlab * NT / 32 == NT words
+    sync();
     // the radially accepted candidates, compacted in candidate order; the
     // accepted nucleons ordered by slab
     int off = 0, nv = 0;
 #pragma unroll
-    for (int q = 0; q < kNT / 32; q++) {
-      const int cq = sm.ired[q];
+    for (int q = 0; q < NT / 32; q++) {
+      const int cq = ss.ired[q];
       off += q < wid ? cq : 0;
       nv += cq;
     }
     if (ws) {
       const int v = off + __popc(bal & ((1u << lane) - 1u));
-      sm.cpos[v] = n.deformed ? make_float4(x, y, z, 0.f) : make_float4(r, __uint_as_float(c), 0.f, 0.f);
+      ss.cpos[v] = n.deformed ? make_float4(x, y, z, 0.f) : make_float4(r, __uint_as_float(c), 0.f, 0.f);
     }
     if (tid <= nslab) {
       int st = 0;
-      for (int t = 0; t < tid; t++) st += sm.slab_cnt[t];
-      sm.slab_start[tid] = st;
+      for (int t = 0; t < tid; t++) st += ss.slab_cnt[t];
+      ss.slab_start[tid] = st;
     }
-    if (tid < n_acc) {
-      const float ax = sm.ax[w][tid], ay = sm.ay[w][tid], az = sm.az[w][tid];
+    for (int k = tid; k < n_acc; k += NT) {
+      const float ax = sm.ax[w][k], ay = sm.ay[w][k], az = sm.az[w][k];
       const int sl = slab_of(az);
       int st = 0;
-      for (int t = 0; t < sl; t++) st += sm.slab_cnt[t];
-      sm.u.spos[st + atomicAdd(&sm.slab_cur[sl], 1)] = make_float4(ax, ay, az, 0.f);
+      for (int t = 0; t < sl; t++) st += ss.slab_cnt[t];
+      ss.u.spos[st + atomicAdd(&ss.slab_cur[sl], 1)] = make_float4(ax, ay, az, 0.f);
     }
-    __syncthreads();
+    sync();
     // candidate tid (< nv): its direction, then the hard core against the
     // accepted nucleons of the neighbouring slabs
     bool ok = tid < nv;
     int sl = 0;
     if (ok) {
-      const float4 p = sm.cpos[tid];
+      const float4 p = ss.cpos[tid];
       if (n.deformed) {
         x = p.x; y = p.y; z = p.z;
       } else {
         float u2, u3;
         uniform2f(seed, ev, sid, 2 * __float_as_uint(p.y) + 1, u2, u3);
         ws_direction(p.x, u2, u3, x, y, z);
-        sm.cpos[tid] = make_float4(x, y, z, 0.f);
+        ss.cpos[tid] = make_float4(x, y, z, 0.f);
       }
       sl = slab_of(z);
-      const int k1 = sm.slab_start[min(nslab, sl + 2)];
-      for (int k = sm.slab_start[max(0, sl - 1)]; k < k1; k++) {
-        const float4 a = sm.u.spos[k];
+      const int k1 = ss.slab_start[min(nslab, sl + 2)];
+      for (int k = ss.slab_start[max(0, sl - 1)]; k < k1; k++) {
+        const float4 a = ss.u.spos[k];
         const float dx = x - a.x, dy = y - a.y, dz = z - a.z;
         if (dx * dx + dy * dy + dz * dz < dmin2) { ok = false; break; }
       }
-      sm.cslab[tid] = (uint8_t)sl;
+      ss.cslab[tid] = (uint8_t)sl;
     }
     const unsigned vb = __ballot_sync(0xffffffffu, ok);
     if (lane == 0) {
-      sm.vb[wid] = vb;
-      sm.conf[wid] = 0u;
+      ss.vb[wid] = vb;
+      ss.conf[wid] = 0u;
     }
-    if (ok) atomicOr(&sm.smask[sl][wid], 1u << lane);
-    __syncthreads();
+    if (ok) atomicOr(&ss.smask[sl][wid], 1u << lane);
+    sync();
     // conflicts with earlier valid candidates of the batch (neighbouring
     // slabs): block (q, r) holds later candidates q*32+lane against earlier
     // ones r*32+kk
     const int Q = (nv + 31) >> 5;
-    for (int blk = wid; blk < Q * (Q + 1) / 2; blk += kNT / 32) {
+    for (int blk = wid; blk < Q * (Q + 1) / 2; blk += NT / 32) {
       int q = 0, s0 = 0;
       while (s0 + q + 1 <= blk) { s0 += q + 1; q++; }
       const int r = blk - s0, cq = q * 32 + lane;
       uint32_t bits = 0;
-      if ((sm.vb[q] >> lane) & 1u) {
-        const float4 pc = sm.cpos[cq];
-        const int sc = sm.cslab[cq];
-        uint32_t m = sm.smask[sc][r];
-        if (sc > 0) m |= sm.smask[sc - 1][r];
-        if (sc + 1 < nslab) m |= sm.smask[sc + 1][r];
+      if ((ss.vb[q] >> lane) & 1u) {
+        const float4 pc = ss.cpos[cq];
+        const int sc = ss.cslab[cq];
+        uint32_t m = ss.smask[sc][r];
+        if (sc > 0) m |= ss.smask[sc - 1][r];
+        if (sc + 1 < nslab) m |= ss.smask[sc + 1][r];
         if (r == q) m &= (1u << lane) - 1u;
         while (m) {
           const int kk = __ffs(m) - 1;
           m &= m - 1u;
-          const float4 pk = sm.cpos[r * 32 + kk];
+          const float4 pk = ss.cpos[r * 32 + kk];
           const float dx = pc.x - pk.x, dy = pc.y - pk.y, dz = pc.z - pk.z;
           if (dx * dx + dy * dy + dz * dz < dmin2) bits |= 1u << kk;
         }
       }
-      sm.u.cmask[cq][r] = bits;
+      ss.u.cmask[cq][r] = bits;
       const unsigned cf = __ballot_sync(0xffffffffu, bits != 0u);
-      if (lane == 0 && cf) atomicOr(&sm.conf[q], cf);
+      if (lane == 0 && cf) atomicOr(&ss.conf[q], cf);
     }
-    __syncthreads();
+    sync();
     if (wid == 0) {
       // kept / undecided words (lane q < 8 owns word q)
-      if (lane < kNT / 32) {
-        const uint32_t v = lane < Q ? sm.vb[lane] : 0u, u = lane < Q ? sm.conf[lane] : 0u;
-        sm.keep[lane] = v & ~u;
-        sm.conf[lane] = u;
+      if (lane < NT / 32) {
+        const uint32_t v = lane < Q ? ss.vb[lane] : 0u, u = lane < Q ? ss.conf[lane] : 0u;
+        ss.keep[lane] = v & ~u;
+        ss.conf[lane] = u;
       }
       __syncwarp();
-      for (int round = 0; round < kNT; round++) {
-        uint32_t kw = lane < kNT / 32 ? sm.keep[lane] : 0u, uw = lane < kNT / 32 ? sm.conf[lane] : 0u;
+      for (int round = 0; round < NT; round++) {
+        uint32_t kw = lane < NT / 32 ? ss.keep[lane] : 0u, uw = lane < NT / 32 ? ss.conf[lane] : 0u;
         if (!__any_sync(0xffffffffu, uw != 0u)) break;
         for (int q = 0; q < Q; q++) {
           bool kept = false, decided = false;
-          if ((sm.conf[q] >> lane) & 1u) {
+          if ((ss.conf[q] >> lane) & 1u) {
             bool hit = false, pend = false;
             for (int r = 0; r <= q; r++) {
-              const uint32_t m = sm.u.cmask[q * 32 + lane][r];
-              hit |= (m & sm.keep[r]) != 0u;
-              pend |= (m & sm.conf[r]) != 0u;
+              const uint32_t m = ss.u.cmask[q * 32 + lane][r];
+              hit |= (m & ss.keep[r]) != 0u;
+              pend |= (m & ss.conf[r]) != 0u;
             }
             decided = hit || !pend;
             kept = !hit && !pend;
@@ -460,32 +484,32 @@ __device__ bool sample_ws(SampleSmem &sm, const NucleusDev &n, int w, uint64_t s
           if (lane == q) { kw |= kb; uw &= ~db; }
         }
         __syncwarp();
-        if (lane < kNT / 32) { sm.keep[lane] = kw; sm.conf[lane] = uw; }
+        if (lane < NT / 32) { ss.keep[lane] = kw; ss.conf[lane] = uw; }
         __syncwarp();
       }
     }
-    __syncthreads();
+    sync();
     // kept candidates in candidate order, up to the nucleons still missing
     {
-      const uint32_t kw = sm.keep[wid];
+      const uint32_t kw = ss.keep[wid];
       int before = 0, total = 0;
 #pragma unroll
-      for (int q = 0; q < kNT / 32; q++) {
-        const int pq = __popc(sm.keep[q]);
+      for (int q = 0; q < NT / 32; q++) {
+        const int pq = __popc(ss.keep[q]);
         before += q < wid ? pq : 0;
         total += pq;
       }
       before += __popc(kw & ((1u << lane) - 1u));
       if (((kw >> lane) & 1u) && n_acc + before < A) {
-        const float4 p = sm.cpos[tid];
+        const float4 p = ss.cpos[tid];
         sm.ax[w][n_acc + before] = p.x;
         sm.ay[w][n_acc + before] = p.y;
         sm.az[w][n_acc + before] = p.z;
       }
       n_acc += min(total, A - n_acc);
-      if (tid < kSlab) { sm.slab_cnt[tid] = 0; sm.slab_cur[tid] = 0; }
+      if (tid < kSlab) { ss.slab_cnt[tid] = 0; ss.slab_cur[tid] = 0; }
     }
-    __syncthreads();
+    sync();
   }
   return true;
 }
@@ -845,6 +869,41 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
       __syncthreads();
       const double b = sm.b;
       bool ok = true;
+      // the nuclei in their own frames: two Woods-Saxon nuclei at once, one
+      // per half of the CTA (each half's barriers its own); otherwise one
+      // after the other by the whole CTA.  The streams are per nucleus, so
+      // the order does not change them.
+      if (!inject && P.nuc[0].A > 2 && P.nuc[1].A > 2 && !P.nuc[0].conf && !P.nuc[1].conf) {
+        const int h = tid / (kNT / 2);
+        const bool okh = sample_ws<kNT / 2>(sm, sm.samp.half[h], P.nuc[h], h, P.seed, ev, attempt,
+                                            (float)sm.ori[h][0], (float)sm.ori[h][1], HalfSync{h});
+        ok = __syncthreads_and(okh) && ok;
+      } else if (!inject) {
+        for (int w = 0; w < 2; w++) {
+          const NucleusDev &nu = P.nuc[w];
+          // rounded to float for the FP32 samplers
+          const float ctr = (float)sm.ori[w][0], phir = (float)sm.ori[w][1];
+          if (nu.conf) {
+            // placed from the table below
+          } else if (nu.A == 1) {
+            if (tid == 0) { sm.ax[w][0] = 0.f; sm.ay[w][0] = 0.f; sm.az[w][0] = 0.f; }
+            __syncthreads();
+          } else if (nu.A == 2) {
+            if (tid == 0) {
+              double u, unused;
+              uniform2(P.seed, ev, stream_id(attempt, ST_DEUT), (uint32_t)w, u, unused);
+              double d = hulthen_inv(u);
+              float x1 = (float)(d / 2.0), y1 = 0.f, z1 = 0.f;
+              rotate3f(x1, y1, z1, ctr, phir);
+              sm.ax[w][0] = x1; sm.ay[w][0] = y1; sm.az[w][0] = z1;
+              sm.ax[w][1] = -x1; sm.ay[w][1] = -y1; sm.az[w][1] = -z1;
+            }
+            __syncthreads();
+          } else {
+            ok = ok && sample_ws<kNT>(sm, sm.samp.full, nu, w, P.seed, ev, attempt, ctr, phir, FullSync{});
+          }
+        }
+      }
       for (int w = 0; w < 2; w++) {
         const NucleusDev &nu = P.nuc[w];
         const double xc = (w == 0 ? b : -b) / 2.0;
@@ -855,28 +914,7 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
                        itan ? itan + (size_t)e * 4 * nu.A : nullptr, ntan);
           continue;
         }
-        // rounded to float for the FP32 samplers
-        const float ctr = (float)sm.ori[w][0], phir = (float)sm.ori[w][1];
         const double *cfg = nu.conf ? nu.conf + (size_t)sm.cfg_idx[w] * 3 * nu.A : nullptr;
-        if (cfg) {
-          // placed from the table below
-        } else if (nu.A == 1) {
-          if (tid == 0) { sm.ax[w][0] = 0.f; sm.ay[w][0] = 0.f; sm.az[w][0] = 0.f; }
-          __syncthreads();
-        } else if (nu.A == 2) {
-          if (tid == 0) {
-            double u, unused;
-            uniform2(P.seed, ev, stream_id(attempt, ST_DEUT), (uint32_t)w, u, unused);
-            double d = hulthen_inv(u);
-            float x1 = (float)(d / 2.0), y1 = 0.f, z1 = 0.f;
-            rotate3f(x1, y1, z1, ctr, phir);
-            sm.ax[w][0] = x1; sm.ay[w][0] = y1; sm.az[w][0] = z1;
-            sm.ax[w][1] = -x1; sm.ay[w][1] = -y1; sm.az[w][1] = -z1;
-          }
-          __syncthreads();
-        } else {
-          ok = ok && sample_ws(sm, nu, w, P.seed, ev, attempt, ctr, phir);
-        }
         place_sorted(sm, w, nu.A, xc, nullptr, nu, nullptr, ntan, cfg, sm.ori[w][0], sm.ori[w][1]);
       }
       if (!ok) { status = 3; break; }
