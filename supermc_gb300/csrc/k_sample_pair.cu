@@ -869,11 +869,13 @@ __global__ void __launch_bounds__(kNT, 6) k_sample_pair(DevParams P_in, uint64_t
       __syncthreads();
       const double b = sm.b;
       bool ok = true;
-      // the nuclei in their own frames: two Woods-Saxon nuclei at once, one
-      // per half of the CTA (each half's barriers its own); otherwise one
-      // after the other by the whole CTA.  The streams are per nucleus, so
-      // the order does not change them.
-      if (!inject && P.nuc[0].A > 2 && P.nuc[1].A > 2 && !P.nuc[0].conf && !P.nuc[1].conf) {
+      // the nuclei in their own frames: two large Woods-Saxon nuclei at
+      // once, one per half of the CTA (each half's barriers its own);
+      // otherwise one after the other by the whole CTA (a nucleus of up to
+      // ~100 nucleons takes about as many half-size batches as full ones, and
+      // measured slower).  The streams are per nucleus, so the order does not
+      // change them.
+      if (!inject && P.nuc[0].A > 100 && P.nuc[1].A > 100 && !P.nuc[0].conf && !P.nuc[1].conf) {
         const int h = tid / (kNT / 2);
         const bool okh = sample_ws<kNT / 2>(sm, sm.samp.half[h], P.nuc[h], h, P.seed, ev, attempt,
                                             (float)sm.ori[h][0], (float)sm.ori[h][1], HalfSync{h});
