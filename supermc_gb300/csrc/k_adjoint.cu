@@ -55,7 +55,8 @@ __device__ __forceinline__ void block_sums(const float (&v)[NV], float2 *red, do
 // xg [nx], yg [ny rounded up to 32], then the reduction slots (16-byte aligned)
 __host__ __device__ inline size_t red_offset(int nx, int ny) {
   const size_t nyp = (ny + 31) / 32 * 32, nw = (ny + 31) / 32;
-  const size_t b = sizeof(uint32_t) * (size_t)nx * nw + sizeof(float) * (nx + nyp);
+  // mask, xg / yg, then xo / yo (the coordinates about the event's centre of mass)
+  const size_t b = sizeof(uint32_t) * (size_t)nx * nw + 2 * sizeof(float) * (nx + nyp);
   return (b + 15) / 16 * 16;
 }
 
@@ -67,6 +68,7 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
   uint32_t *mask = reinterpret_cast<uint32_t *>(smem);
   float *xg = reinterpret_cast<float *>(smem + sizeof(uint32_t) * (size_t)nx * nw);
   float *yg = xg + nx;
+  float *xo = yg + (ny + 31) / 32 * 32, *yo = xo + nx;
   float2 *red = reinterpret_cast<float2 *>(smem + red_offset(nx, ny));
   __shared__ double s_tot[32];
   __shared__ double s_coef[8];
@@ -107,6 +109,10 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
     }
     const double tot = s_tot[0], xc = s_tot[1] / tot, yc = s_tot[2] / tot;
     const float xcf = (float)xc, ycf = (float)yc;
+    // the box's coordinates about the centre of mass, each rounded once from FP64
+    for (int i = i0 + tid; i < i1; i += kAT) xo[i] = (float)((P.xmin + i * P.dx) - xc);
+    for (int j = j0 + tid; j < j1; j += kAT) yo[j] = (float)((P.ymin + j * P.dy) - yc);
+    __syncthreads();
     // ---- masked moments of orders 2 and 3: Z = sum z^n rho, D = sum |z|^n rho,
     // U = sum n z^(n-1) rho, V = sum n |z|^(n-2) z rho (z about the centre of mass)
     {
@@ -118,7 +124,7 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
         if (!((mask[i * nw + (j >> 5)] >> (j & 31)) & 1u)) continue;
         const float d = rho[(size_t)i * ny + j];
         if (d == 0.f) continue;
-        const Cplx z{(float)((P.xmin + i * P.dx) - xc), (float)((P.ymin + j * P.dy) - yc)};
+        const Cplx z{xo[i], yo[j]};
         const float r2 = z.re * z.re + z.im * z.im, r = sqrtf(r2);
         const Cplx z2 = cmul(z, z), z3 = cmul(z2, z);
         // order 2
@@ -159,20 +165,22 @@ __global__ void __launch_bounds__(kAT) k_adjoint(DevParams P, int n_events, cons
       const double A2 = s_coef[0], B2 = s_coef[1], A3 = s_coef[2], B3 = s_coef[3], Cx = s_coef[4], Cy = s_coef[5];
       const float z2r = (float)s_coef[6], z2i = (float)s_coef[7];
       const float z3r = (float)s_tot[7], z3i = (float)s_tot[8];
-      for (int k = tid; k < ncell; k += kAT) {
-        const int i = i0 + k / bw, j = j0 + k % bw;
-        const float x = xg[i] - xcf, y = yg[j] - ycf;
-        float l = (float)(Cx * x + Cy * y);
-        if ((mask[i * nw + (j >> 5)] >> (j & 31)) & 1u) {
-          const Cplx z{(float)((P.xmin + i * P.dx) - xc), (float)((P.ymin + j * P.dy) - yc)};
-          const float r2 = z.re * z.re + z.im * z.im, r = sqrtf(r2);
-          const Cplx zz2 = cmul(z, z), zz3 = cmul(zz2, z);
-          l += (float)A2 * (z2r * zz2.re + z2i * zz2.im) + (float)B2 * r2;
-          l += (float)A3 * (z3r * zz3.re + z3i * zz3.im) + (float)B3 * r2 * r;
+      const float cxf = (float)Cx, cyf = (float)Cy, a2 = (float)A2, b2 = (float)B2, a3 = (float)A3, b3 = (float)B3;
+      // a warp per row of the box, lanes over its columns (each cell on its own)
+      for (int i = i0 + (tid >> 5); i < i1; i += kAW)
+        for (int j = j0 + (tid & 31); j < j1; j += 32) {
+          const float x = xg[i] - xcf, y = yg[j] - ycf;
+          float l = fmaf(cxf, x, cyf * y);
+          if ((mask[i * nw + (j >> 5)] >> (j & 31)) & 1u) {
+            const Cplx z{xo[i], yo[j]};
+            const float r2 = z.re * z.re + z.im * z.im, r = sqrtf(r2);
+            const Cplx zz2 = cmul(z, z), zz3 = cmul(zz2, z);
+            l += a2 * (z2r * zz2.re + z2i * zz2.im) + b2 * r2;
+            l += a3 * (z3r * zz3.re + z3i * zz3.im) + b3 * r2 * r;
+          }
+          if (gg) l += gg[(size_t)i * ny + j];
+          lam[(size_t)i * ny + j] = l;
         }
-        if (gg) l += gg[(size_t)i * ny + j];
-        lam[(size_t)i * ny + j] = l;
-      }
     }
     __syncthreads();
     // ---- contraction: one (source, row) pair per thread, Gaussians recomputed.
