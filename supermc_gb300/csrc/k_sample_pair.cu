@@ -350,8 +350,16 @@ __device__ bool sample_ws(SampleSmem &sm, SampStore<NT> &ss, const NucleusDev &n
   if (tid < kSlab) { ss.slab_cnt[tid] = 0; ss.slab_cur[tid] = 0; }
   sync();
   int n_acc = 0;
-  for (uint32_t base = 0; n_acc < A; base += NT) {
+  // A batch goes on with the first `cap` radially accepted candidates, a few
+  // more than the nucleons still missing (the hard core rejects a few per
+  // cent): a batch that reaches its cap ends at its last valid candidate and
+  // the next one starts after it, so every candidate is decided once and in
+  // order whatever the batch (a small nucleus's batch then carries about as
+  // many candidates as it needs, not the whole group's worth).
+  for (uint32_t base = 0; n_acc < A;) {
     if (base > (1u << 20)) return false;
+    const int need = A - n_acc;
+    const int cap = min(NT, need + need / 8 + 8);
     const uint32_t c = base + tid;
     float u0, u1;
     uniform2f(seed, ev, sid, 2 * c, u0, u1);
@@ -382,9 +390,16 @@ __device__ bool sample_ws(SampleSmem &sm, SampStore<NT> &ss, const NucleusDev &n
       nv += cq;
     }
     if (ws) {
+      // the candidate number rides in w (the direction's stream slot, the
+      // end of a capped batch)
       const int v = off + __popc(bal & ((1u << lane) - 1u));
-      ss.cpos[v] = n.deformed ? make_float4(x, y, z, 0.f) : make_float4(r, __uint_as_float(c), 0.f, 0.f);
+      if (v < cap)
+        ss.cpos[v] = n.deformed ? make_float4(x, y, z, __uint_as_float(c)) : make_float4(r, 0.f, 0.f, __uint_as_float(c));
     }
+    // where the next batch starts (cpos[cap - 1].w is read after the batch's
+    // last barrier, before the next batch writes cpos)
+    const bool capped = nv > cap;
+    nv = min(nv, cap);
     if (tid <= nslab) {
       int st = 0;
       for (int t = 0; t < tid; t++) st += ss.slab_cnt[t];
@@ -408,9 +423,9 @@ __device__ bool sample_ws(SampleSmem &sm, SampStore<NT> &ss, const NucleusDev &n
         x = p.x; y = p.y; z = p.z;
       } else {
         float u2, u3;
-        uniform2f(seed, ev, sid, 2 * __float_as_uint(p.y) + 1, u2, u3);
+        uniform2f(seed, ev, sid, 2 * __float_as_uint(p.w) + 1, u2, u3);
         ws_direction(p.x, u2, u3, x, y, z);
-        ss.cpos[tid] = make_float4(x, y, z, 0.f);
+        ss.cpos[tid] = make_float4(x, y, z, p.w);
       }
       sl = slab_of(z);
       const int k1 = ss.slab_start[min(nslab, sl + 2)];
@@ -510,6 +525,7 @@ __device__ bool sample_ws(SampleSmem &sm, SampStore<NT> &ss, const NucleusDev &n
       if (tid < kSlab) { ss.slab_cnt[tid] = 0; ss.slab_cur[tid] = 0; }
     }
     sync();
+    base = capped ? __float_as_uint(ss.cpos[cap - 1].w) + 1u : base + NT;
   }
   return true;
 }
